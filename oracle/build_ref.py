@@ -1,0 +1,93 @@
+"""Build recipe for the reference engine harness (test infrastructure only).
+
+Compiles the reference's own engine sources where they lie (no copy into this
+repository) together with ``oracle/ref_harness.cpp`` into ``oracle/_ref/``:
+
+    oracle/_ref/ref_harness64   reference built with PE_USE_DOUBLE (its default, CMakeLists.txt:28)
+    oracle/_ref/ref_harness32   reference built with pe::Real = float
+
+Sources follow the reference's own target lists (src/CMakeLists.txt:4-11): the
+PEngine library (intf/world.cpp, rigid/**, cloth/**) plus the four PEUtils
+sources.  The viewer and its prebuilt GL binaries are never touched.  Flags follow
+CMakeLists.txt:6-29 (-DPE_MULTI_THREAD, -DAMGCL_NO_BOOST, aligned storage on),
+compiled with g++ -std=c++14 -O2 like the reference's default build.
+
+Run:  python oracle/build_ref.py [--ref /path/to/reference] [--jobs N]
+Only this container has the reference sources; the GPU host never runs this.
+"""
+import argparse
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+
+
+def sources(ref: Path):
+    src = ref / "src"
+    files = [src / "intf" / "world.cpp"]
+    for sub in ("rigid", "cloth"):
+        files += sorted((src / sub).rglob("*.cpp"))
+    for u in ("logger", "thread_pool", "bvh", "file_system"):
+        files.append(src / "utils" / f"{u}.cpp")
+    return files
+
+
+def flags(ref: Path, bits: int):
+    f = ["-std=c++14", "-O2", "-DPE_MULTI_THREAD", "-DAMGCL_NO_BOOST",
+         "-D_ENABLE_EXTENDED_ALIGNED_STORAGE", f"-DPE_DATA_PATH=\"{ref}/data/\"",
+         f"-I{ref / 'src'}", f"-I{ref / 'ThirdParty'}", f"-I{ref / 'SimpleViewer' / 'include'}",
+         "-w"]
+    if bits == 64:
+        f.append("-DPE_USE_DOUBLE")
+    return f
+
+
+def build(ref: Path, jobs: int, bits_list=(64, 32)):
+    if not (ref / "src" / "intf" / "world.cpp").exists():
+        print(f"reference sources not found under {ref}; skipping reference build")
+        return False
+    OUT.mkdir(exist_ok=True)
+    for bits in bits_list:
+        obj_dir = OUT / f"obj{bits}"
+        obj_dir.mkdir(exist_ok=True)
+        fl = flags(ref, bits)
+        jobs_list = []
+        for s in sources(ref) + [HERE / "ref_harness.cpp"]:
+            rel = s.relative_to(ref) if str(s).startswith(str(ref)) else Path(s.name)
+            o = obj_dir / (str(rel).replace(os.sep, "__") + ".o")
+            if o.exists() and o.stat().st_mtime >= s.stat().st_mtime:
+                jobs_list.append((None, o))
+                continue
+            jobs_list.append((["g++", *fl, "-c", str(s), "-o", str(o)], o))
+
+        def run(cmd):
+            if cmd is None:
+                return 0, ""
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            return r.returncode, r.stderr
+
+        with cf.ThreadPoolExecutor(jobs) as ex:
+            for (cmd, o), (rc, err) in zip(jobs_list, ex.map(lambda j: run(j[0]), jobs_list)):
+                if rc != 0:
+                    sys.stderr.write(err)
+                    raise SystemExit(f"compile failed: {cmd}")
+        exe = OUT / f"ref_harness{bits}"
+        cmd = ["g++", "-O2", "-o", str(exe)] + [str(o) for _, o in jobs_list] + ["-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stderr)
+            raise SystemExit("link failed")
+        print(f"built {exe}")
+    return True
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
+    a = ap.parse_args()
+    build(Path(a.ref), a.jobs)

@@ -1,0 +1,371 @@
+"""Scene description, the ``.pescene`` file format, and seeded synthetic scene generators.
+
+A scene is what a caller hands to ``pe_intf::World`` before stepping it
+(src/intf/world.h:68 addRigidBody, :24-25 gravity/dt, solver iteration
+src/rigid/constraint/constraint_solver/constraint_solver.h:72): a list of collision
+shapes and a list of rigid bodies referencing them.  Shape type codes follow the
+reference's ``ShapeType`` enum order (src/rigid/shape/shape.h:7-9):
+0 box (full size), 1 sphere (radius), 2 cylinder (radius, height), 3 convex mesh.
+
+Body fields mirror the reference's RigidBody setters (src/rigid/object/rigidbody.h):
+mass, friction, restitution, linear/angular damping, kinematic flag, transform
+(origin + row-major 3x3 basis) and linear/angular velocity.
+
+All reals are stored as float64.  A scene meant for the single-precision build is
+generated with every real rounded to float32 first, so that loading it into a
+``float`` world is exact.
+
+Generators (all seeded, all synthetic; no dataset is involved):
+  * ``tower``      - boxes stacked in a grid on a static ground box, hit by a sphere.
+  * ``random_cube``- bodies of mixed shapes scattered uniformly in a cube (one-step stress).
+  * ``pile``       - a jittered pile of mixed shapes (incl. convex hulls) dropped on a ground box.
+  * ``pair_zoo``   - many isolated body pairs of one shape pairing, for narrowphase coverage.
+"""
+from __future__ import annotations
+
+import dataclasses
+import struct
+from pathlib import Path
+
+import numpy as np
+
+BOX, SPHERE, CYLINDER, HULL = 0, 1, 2, 3
+KINEMATIC = 1
+
+MAGIC = b"PESCENE1"
+
+
+@dataclasses.dataclass
+class Scene:
+    dt: float = 0.01
+    gravity: tuple = (0.0, -9.8, 0.0)
+    iterations: int = 10
+    real_bits: int = 64
+    # shapes
+    shape_type: np.ndarray = None      # int32 [S]
+    shape_param: np.ndarray = None     # float64 [S,3]
+    hull_vbeg: np.ndarray = None       # int32 [S]
+    hull_vcnt: np.ndarray = None
+    hull_fbeg: np.ndarray = None
+    hull_fcnt: np.ndarray = None
+    hull_verts: np.ndarray = None      # float64 [HV,3]
+    hull_face_off: np.ndarray = None   # int32 [HF+1]
+    hull_face_idx: np.ndarray = None   # int32 [HI]
+    # bodies
+    body_shape: np.ndarray = None      # int32 [N]
+    body_flags: np.ndarray = None      # int32 [N]
+    mass: np.ndarray = None            # float64 [N]
+    friction: np.ndarray = None
+    restitution: np.ndarray = None
+    lin_damp: np.ndarray = None
+    ang_damp: np.ndarray = None
+    origin: np.ndarray = None          # float64 [N,3]
+    basis: np.ndarray = None           # float64 [N,3,3]
+    lin_vel: np.ndarray = None         # float64 [N,3]
+    ang_vel: np.ndarray = None         # float64 [N,3]
+
+    @property
+    def n_bodies(self) -> int:
+        return int(self.body_shape.shape[0])
+
+    @property
+    def n_shapes(self) -> int:
+        return int(self.shape_type.shape[0])
+
+    def rounded(self, real_bits: int) -> "Scene":
+        """Copy with every real rounded to the given precision (exact load into that build)."""
+        s = dataclasses.replace(self)
+        s.real_bits = real_bits
+        if real_bits == 32:
+            r = lambda a: np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+            s.dt = float(np.float32(self.dt))
+            s.gravity = tuple(float(np.float32(g)) for g in self.gravity)
+            for f in ("shape_param", "hull_verts", "mass", "friction", "restitution", "lin_damp",
+                      "ang_damp", "origin", "basis", "lin_vel", "ang_vel"):
+                setattr(s, f, r(getattr(self, f)))
+        return s
+
+    # ------------------------------------------------------------------ file format
+    def write(self, path) -> None:
+        """Write the little-endian ``.pescene`` layout read by every consumer of a scene."""
+        S, N = self.n_shapes, self.n_bodies
+        with open(path, "wb") as f:
+            f.write(MAGIC)
+            f.write(struct.pack("<6i", S, N, len(self.hull_verts), len(self.hull_face_off) - 1,
+                                len(self.hull_face_idx), int(self.iterations)))
+            f.write(struct.pack("<4d", float(self.dt), *map(float, self.gravity)))
+            for a, t in ((self.shape_type, "<i4"), (self.shape_param, "<f8"), (self.hull_vbeg, "<i4"),
+                         (self.hull_vcnt, "<i4"), (self.hull_fbeg, "<i4"), (self.hull_fcnt, "<i4"),
+                         (self.hull_verts, "<f8"), (self.hull_face_off, "<i4"), (self.hull_face_idx, "<i4"),
+                         (self.body_shape, "<i4"), (self.body_flags, "<i4"), (self.mass, "<f8"),
+                         (self.friction, "<f8"), (self.restitution, "<f8"), (self.lin_damp, "<f8"),
+                         (self.ang_damp, "<f8"), (self.origin, "<f8"), (self.basis, "<f8"),
+                         (self.lin_vel, "<f8"), (self.ang_vel, "<f8")):
+                f.write(np.ascontiguousarray(a, dtype=t).tobytes())
+
+    @staticmethod
+    def read(path, real_bits: int = 64) -> "Scene":
+        b = Path(path).read_bytes()
+        if b[:8] != MAGIC:
+            raise ValueError("not a .pescene file")
+        S, N, HV, HF, HI, iters = struct.unpack_from("<6i", b, 8)
+        dt, gx, gy, gz = struct.unpack_from("<4d", b, 32)
+        off = 64
+        s = Scene(dt=dt, gravity=(gx, gy, gz), iterations=iters, real_bits=real_bits)
+
+        def take(n, t, shape=None):
+            nonlocal off
+            a = np.frombuffer(b, dtype=t, count=n, offset=off).copy()
+            off += a.nbytes
+            return a.reshape(shape) if shape else a
+
+        s.shape_type = take(S, "<i4")
+        s.shape_param = take(S * 3, "<f8", (S, 3))
+        s.hull_vbeg, s.hull_vcnt, s.hull_fbeg, s.hull_fcnt = (take(S, "<i4") for _ in range(4))
+        s.hull_verts = take(HV * 3, "<f8", (HV, 3))
+        s.hull_face_off = take(HF + 1, "<i4")
+        s.hull_face_idx = take(HI, "<i4")
+        s.body_shape = take(N, "<i4")
+        s.body_flags = take(N, "<i4")
+        s.mass, s.friction, s.restitution, s.lin_damp, s.ang_damp = (take(N, "<f8") for _ in range(5))
+        s.origin = take(N * 3, "<f8", (N, 3))
+        s.basis = take(N * 9, "<f8", (N, 3, 3))
+        s.lin_vel = take(N * 3, "<f8", (N, 3))
+        s.ang_vel = take(N * 3, "<f8", (N, 3))
+        return s
+
+
+# ---------------------------------------------------------------------- builders
+class SceneBuilder:
+    """Incremental construction of a Scene (shapes are deduplicated by parameters)."""
+
+    def __init__(self, dt=0.01, gravity=(0.0, -9.8, 0.0), iterations=10):
+        self.dt, self.gravity, self.iterations = dt, gravity, iterations
+        self.shapes = []          # (type, (p0,p1,p2), hull index or -1)
+        self.shape_key = {}
+        self.hulls = []           # (verts [V,3], faces list[list[int]])
+        self.bodies = []
+
+    def shape(self, kind, params=(0.0, 0.0, 0.0), hull=None):
+        params = tuple(float(p) for p in params) + (0.0,) * (3 - len(params))
+        if kind == HULL:
+            self.hulls.append(hull)
+            self.shapes.append((HULL, (0.0, 0.0, 0.0), len(self.hulls) - 1))
+            return len(self.shapes) - 1
+        key = (kind, params)
+        if key not in self.shape_key:
+            self.shapes.append((kind, params, -1))
+            self.shape_key[key] = len(self.shapes) - 1
+        return self.shape_key[key]
+
+    def body(self, shape, origin, basis=None, mass=1.0, v=(0, 0, 0), w=(0, 0, 0), friction=0.5,
+             restitution=0.5, kinematic=False, lin_damp=0.0, ang_damp=0.0):
+        basis = np.eye(3) if basis is None else np.asarray(basis, np.float64)
+        self.bodies.append((shape, KINEMATIC if kinematic else 0, float(mass), float(friction),
+                            float(restitution), float(lin_damp), float(ang_damp),
+                            np.asarray(origin, np.float64), basis, np.asarray(v, np.float64),
+                            np.asarray(w, np.float64)))
+        return len(self.bodies) - 1
+
+    def build(self, real_bits=64) -> Scene:
+        S = len(self.shapes)
+        s = Scene(dt=self.dt, gravity=tuple(self.gravity), iterations=self.iterations, real_bits=64)
+        s.shape_type = np.array([t for t, _, _ in self.shapes], np.int32)
+        s.shape_param = np.array([p for _, p, _ in self.shapes], np.float64).reshape(S, 3)
+        vbeg, vcnt, fbeg, fcnt = (np.zeros(S, np.int32) for _ in range(4))
+        verts, face_off, face_idx = [], [0], []
+        nv = nf = 0
+        for i, (t, _, h) in enumerate(self.shapes):
+            if t != HULL:
+                continue
+            hv, hf = self.hulls[h]
+            vbeg[i], vcnt[i], fbeg[i], fcnt[i] = nv, len(hv), nf, len(hf)
+            verts.append(np.asarray(hv, np.float64))
+            for face in hf:
+                face_idx.extend(int(k) for k in face)
+                face_off.append(len(face_idx))
+            nv += len(hv)
+            nf += len(hf)
+        s.hull_vbeg, s.hull_vcnt, s.hull_fbeg, s.hull_fcnt = vbeg, vcnt, fbeg, fcnt
+        s.hull_verts = np.concatenate(verts) if verts else np.zeros((0, 3))
+        s.hull_face_off = np.array(face_off, np.int32)
+        s.hull_face_idx = np.array(face_idx, np.int32)
+        B = self.bodies
+        s.body_shape = np.array([b[0] for b in B], np.int32)
+        s.body_flags = np.array([b[1] for b in B], np.int32)
+        s.mass, s.friction, s.restitution, s.lin_damp, s.ang_damp = (
+            np.array([b[k] for b in B], np.float64) for k in range(2, 7))
+        s.origin = np.array([b[7] for b in B]).reshape(-1, 3)
+        s.basis = np.array([b[8] for b in B]).reshape(-1, 3, 3)
+        s.lin_vel = np.array([b[9] for b in B]).reshape(-1, 3)
+        s.ang_vel = np.array([b[10] for b in B]).reshape(-1, 3)
+        return s.rounded(real_bits) if real_bits == 32 else s
+
+
+# ---------------------------------------------------------------------- geometry helpers
+def quat_to_basis(q):
+    """Row-major rotation matrices from unit quaternions (w, x, y, z), shape [...,4] -> [...,3,3]."""
+    q = np.asarray(q, np.float64)
+    w, x, y, z = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    m = np.empty(q.shape[:-1] + (3, 3))
+    m[..., 0, 0] = 1 - 2 * (y * y + z * z)
+    m[..., 0, 1] = 2 * (x * y - z * w)
+    m[..., 0, 2] = 2 * (x * z + y * w)
+    m[..., 1, 0] = 2 * (x * y + z * w)
+    m[..., 1, 1] = 1 - 2 * (x * x + z * z)
+    m[..., 1, 2] = 2 * (y * z - x * w)
+    m[..., 2, 0] = 2 * (x * z - y * w)
+    m[..., 2, 1] = 2 * (y * z + x * w)
+    m[..., 2, 2] = 1 - 2 * (x * x + y * y)
+    return m
+
+
+def random_rotations(rng, n):
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return quat_to_basis(q)
+
+
+def random_hull(rng, nverts, scale):
+    """Convex hull of ``nverts`` points on the unit sphere scaled by ``scale``.
+
+    Faces are triangles wound counter-clockwise seen from outside, which is the
+    winding the reference's per-face normal ((p2-p1)x(p3-p1), common/mesh.cpp:1-10)
+    expects for outward normals.
+    """
+    from scipy.spatial import ConvexHull
+
+    while True:
+        p = rng.normal(size=(nverts, 3))
+        p /= np.linalg.norm(p, axis=1, keepdims=True)
+        p *= scale
+        h = ConvexHull(p)
+        if len(h.vertices) == nverts:
+            break
+    remap = {int(v): i for i, v in enumerate(sorted(h.vertices))}
+    verts = p[sorted(h.vertices)]
+    faces = []
+    centre = verts.mean(axis=0)
+    for simplex in h.simplices:
+        a, b, c = (remap[int(k)] for k in simplex)
+        n = np.cross(verts[b] - verts[a], verts[c] - verts[a])
+        if np.dot(n, verts[a] - centre) < 0:
+            b, c = c, b
+        faces.append([a, b, c])
+    return verts, faces
+
+
+def hull_volume(verts, faces):
+    v = 0.0
+    for f in faces:
+        a, b, c = verts[f[0]], verts[f[1]], verts[f[2]]
+        v += np.dot(a, np.cross(b, c)) / 6.0
+    return v
+
+
+# ---------------------------------------------------------------------- generators
+def tower(nx=10, ny=10, nz=10, half=0.5, gap=0.001, density=1000.0, sphere_r=1.0, sphere_mass=50.0,
+          sphere_speed=30.0, dt=1.0 / 60.0, iterations=20, friction=0.5, restitution=0.0,
+          real_bits=64, ground=(100.0, 1.0, 100.0)) -> Scene:
+    """Boxes stacked as an nx x ny x nz tower with ``gap`` spacing on a static ground box,
+    and a sphere fired horizontally (+x) into the tower at mid-height."""
+    sb = SceneBuilder(dt=dt, gravity=(0.0, -9.8, 0.0), iterations=iterations)
+    g = sb.shape(BOX, ground)
+    sb.body(g, (0.0, -ground[1] / 2, 0.0), mass=0.0, friction=friction, restitution=restitution,
+            kinematic=True)
+    size = 2 * half
+    bshape = sb.shape(BOX, (size, size, size))
+    m = density * size ** 3
+    pitch = size + gap
+    x0 = -(nx - 1) * pitch / 2
+    z0 = -(nz - 1) * pitch / 2
+    for j in range(ny):
+        for i in range(nx):
+            for k in range(nz):
+                sb.body(bshape, (x0 + i * pitch, half + gap + j * pitch, z0 + k * pitch), mass=m,
+                        friction=friction, restitution=restitution)
+    s = sb.shape(SPHERE, (sphere_r,))
+    sb.body(s, (x0 - 10.0, ny * pitch / 2, 0.0), mass=sphere_mass, v=(sphere_speed, 0.0, 0.0),
+            friction=friction, restitution=restitution)
+    return sb.build(real_bits)
+
+
+def _random_body(sb, rng, kind, origin, density, basis, v, w, friction=0.5, restitution=0.0, hull_range=(8, 64)):
+    if kind == BOX:
+        he = rng.uniform(0.2, 1.0, size=3)
+        sh = sb.shape(BOX, 2 * he)
+        vol = np.prod(2 * he)
+    elif kind == SPHERE:
+        r = rng.uniform(0.2, 1.0)
+        sh = sb.shape(SPHERE, (r,))
+        vol = 4.0 / 3.0 * np.pi * r ** 3
+    elif kind == CYLINDER:
+        r = rng.uniform(0.2, 0.8)
+        h = rng.uniform(0.4, 2.0)
+        sh = sb.shape(CYLINDER, (r, h))
+        vol = np.pi * r * r * h
+    else:
+        nv = int(rng.integers(hull_range[0], hull_range[1] + 1))
+        verts, faces = random_hull(rng, nv, rng.uniform(0.3, 1.0))
+        sh = sb.shape(HULL, hull=(verts, faces))
+        vol = hull_volume(verts, faces)
+    return sb.body(sh, origin, basis, mass=density * vol, v=v, w=w, friction=friction, restitution=restitution)
+
+
+def random_cube(n=65536, seed=0, extent=100.0, mix=(0.60, 0.25, 0.15, 0.0), density=1000.0,
+                vel_sigma=2.0, dt=1.0 / 60.0, iterations=10, real_bits=32) -> Scene:
+    """Bodies with mixed shapes, uniform positions in a cube, uniform random rotations and
+    N(0, vel_sigma) linear velocities (broad/narrowphase stress)."""
+    rng = np.random.default_rng(seed)
+    sb = SceneBuilder(dt=dt, iterations=iterations)
+    kinds = rng.choice(4, size=n, p=np.asarray(mix) / np.sum(mix))
+    pos = rng.uniform(0.0, extent, size=(n, 3))
+    rot = random_rotations(rng, n)
+    vel = rng.normal(0.0, vel_sigma, size=(n, 3))
+    for i in range(n):
+        _random_body(sb, rng, int(kinds[i]), pos[i], density, rot[i], vel[i], (0.0, 0.0, 0.0))
+    return sb.build(real_bits)
+
+
+def pile(n, seed=0, mix=(0.5, 0.2, 0.1, 0.2), density=1000.0, drop=(0.0, 5.0), dt=1.0 / 60.0,
+         iterations=10, real_bits=32, hull_range=(8, 64)) -> Scene:
+    """A jittered pile of mixed shapes (box/sphere/cylinder/convex hull) above a static ground
+    box, lowest layer between drop[0] and drop[1] metres above the ground."""
+    rng = np.random.default_rng(seed)
+    sb = SceneBuilder(dt=dt, iterations=iterations)
+    side = max(2, int(np.ceil(np.sqrt(n / 2.0))))
+    pitch = 2.2
+    ground = (side * pitch + 10.0, 1.0, side * pitch + 10.0)
+    g = sb.shape(BOX, ground)
+    sb.body(g, (0.0, -0.5, 0.0), mass=0.0, kinematic=True)
+    kinds = rng.choice(4, size=n, p=np.asarray(mix) / np.sum(mix))
+    rot = random_rotations(rng, n)
+    base = rng.uniform(*drop)
+    for i in range(n):
+        layer, cell = divmod(i, side * side)
+        gx, gz = divmod(cell, side)
+        org = ((gx - side / 2) * pitch + rng.uniform(-0.1, 0.1), 1.2 + base + layer * pitch,
+               (gz - side / 2) * pitch + rng.uniform(-0.1, 0.1))
+        _random_body(sb, rng, int(kinds[i]), org, density, rot[i], (0.0, 0.0, 0.0), (0.0, 0.0, 0.0),
+                     hull_range=hull_range)
+    return sb.build(real_bits)
+
+
+def pair_zoo(kind_a, kind_b, m=64, seed=0, spacing=20.0, real_bits=64, hull_range=(8, 32)) -> Scene:
+    """``m`` isolated body pairs of one shape pairing, each placed in its own cell with random
+    rotations and a random offset that mostly overlaps (narrowphase coverage, zero gravity)."""
+    rng = np.random.default_rng(seed)
+    sb = SceneBuilder(dt=1.0 / 60.0, gravity=(0.0, 0.0, 0.0), iterations=10)
+    side = int(np.ceil(m ** (1 / 3)))
+    for i in range(m):
+        cx, rem = divmod(i, side * side)
+        cy, cz = divmod(rem, side)
+        c = np.array([cx, cy, cz], np.float64) * spacing
+        rot = random_rotations(rng, 2)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        off = d * rng.uniform(0.3, 1.6)
+        for k, (kind, o) in enumerate(((kind_a, c), (kind_b, c + off))):
+            _random_body(sb, rng, kind, o, 1000.0, rot[k], (0.0, 0.0, 0.0), (0.0, 0.0, 0.0),
+                         friction=0.5, restitution=0.2, hull_range=hull_range)
+    return sb.build(real_bits)
