@@ -1,0 +1,320 @@
+"""Benchmark of the rigid-body step on the GPU (and of the reference's CPU step).
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload stress|tower|batched]
+
+Workloads (all synthetic, seeded):
+  stress   65,536 bodies (60% boxes, 25% spheres, 15% cylinders, sizes as in the one-step stress
+           configuration) scattered in a 100 m cube with N(0,2) m/s velocities; FP32; dt 1/60;
+           10 solver iterations; coloured Gauss-Seidel.  Default.
+  tower    1,000 boxes stacked 10x10x10 with 1 mm gaps on a static ground box, hit by a 50 kg
+           sphere at 30 m/s; FP64; dt 1/60; 20 iterations; serial-order solver.
+  batched  4,096 independent piles of 8..512 bodies (log-uniform; boxes, spheres, cylinders,
+           convex hulls of 8..64 vertices) dropped on ground boxes; FP32; 10 iterations;
+           coloured Gauss-Seidel; one batched step for all scenes.
+
+One "step" is one full World::step (integrate, broadphase, narrowphase, solver) of the whole
+workload.  `value` = body-steps per second of device time with the state resident in HBM
+(CUDA events on the library's stream, L2 flushed between steps); `e2e` = the same metric
+through the C ABI with host buffers: every step uploads body poses and velocities from host
+memory and reads them back.  `--impl reference` times the reference's CPU step (its
+algorithm restated in oracle/, multithreaded over the host cores like the reference's thread
+pool) on the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "physics-engine_gb300"))
+
+METRIC = "body-steps/s batched vs per-scene GPU step at oracle tol; p50/p99 step latency"
+UNIT = "body-steps/s"
+
+
+def make_workload(name):
+    from pe_gb300 import scene as sc
+    if name == "stress":
+        s = sc.random_cube(n=65536, seed=2024, real_bits=32)
+        return s, 32, 1, None, dict(workload="65,536 mixed bodies (box/sphere/cylinder 60/25/15) in a 100 m cube, "
+                                             "full step, FP32, 10 SI iterations, coloured Gauss-Seidel",
+                                    bodies=65536, scenes=1, solver="coloured")
+    if name == "tower":
+        s = sc.tower(real_bits=64)
+        return s, 64, 0, None, dict(workload="1,000-box 10x10x10 tower + ground + sphere at 30 m/s, full step, FP64, "
+                                             "20 SI iterations, serial-order solver", bodies=s.n_bodies, scenes=1,
+                                    solver="serial-order")
+    if name == "batched":
+        rng = np.random.default_rng(4096)
+        sizes = np.exp(rng.uniform(np.log(8), np.log(512), size=4096)).astype(int)
+        parts = [sc.pile(int(n), seed=1000 + i, real_bits=32, hull_range=(8, 64)) for i, n in enumerate(sizes)]
+        merged, offs = sc.concat(parts)
+        return merged, 32, 1, offs, dict(workload="4,096 independent piles of 8..512 bodies (log-uniform) incl. convex "
+                                                  "hulls, one batched step, FP32, 10 SI iterations, coloured",
+                                         bodies=merged.n_bodies, scenes=4096, solver="coloured")
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ------------------------------------------------------------------ measurement helpers
+class L2Flush:
+    """Writes a buffer larger than L2 (129 MB) between timed steps."""
+
+    def __init__(self, nbytes=256 << 20):
+        try:
+            self.rt = ctypes.CDLL("libcudart.so")
+        except OSError:
+            self.rt = ctypes.CDLL("/usr/local/cuda/lib64/libcudart.so")
+        self.p = ctypes.c_void_p()
+        self.n = nbytes
+        if self.rt.cudaMalloc(ctypes.byref(self.p), ctypes.c_size_t(nbytes)) != 0:
+            raise RuntimeError("cudaMalloc for the L2 flush buffer failed")
+
+    def __call__(self):
+        self.rt.cudaMemset(self.p, 1, ctypes.c_size_t(self.n))
+        self.rt.cudaDeviceSynchronize()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        if not getattr(self, "lines", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of kernel groups from the committed ncu summary (if any)."""
+    p = ROOT / "profiles" / "ncu_traffic.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            f = line.split()
+            if len(f) >= 2 and not line.startswith("#"):
+                try:
+                    out[f[0]] = float(f[1])
+                except ValueError:
+                    pass
+    return out
+
+
+def algorithmic_bytes(counts, n_bodies, iters, real_bytes):
+    """Algorithmic HBM bytes of one step (per kernel group), from the per-unit figures:
+    body 268 B, pair 104 B (+12 B per hull vertex), manifold 8 B, contact point 184 B plus
+    200 B per point and solver iteration (FP32; FP64 doubles every real field)."""
+    k = real_bytes / 4.0
+    P, M, C = counts["pairs"], counts["active"], counts["rows"]
+    return {
+        "integrate": n_bodies * 124 * k,                   # read state 72 + write pose 28 + write AABB 24
+        "bp_sort": n_bodies * (8 + 64),                    # keys/indices + 4-pass radix of 8 B records
+        "bp_sweep": n_bodies * 24 * k + P * 8,             # sorted AABB gather reads + pair writes
+        "narrowphase": P * 104 * k + C * 52 * k + M * 8,   # pair + two bodies' pose/shape; point writes
+        "si_setup": C * (52 + 80) * k,                     # point reads + row writes
+        "si_colored": C * iters * 200 * k,                 # row 80 + accumulators 24 + two bodies' v,w 96
+        "si_serial": C * iters * 200 * k,
+        "step": (n_bodies * 268 + P * 104 + M * 8 + C * (184 + iters * 200)) * k,
+    }
+
+
+KERNEL_BYTES_KEY = {"integrate": "integrate", "radix_sort": "bp_sort", "bp_sweep": "bp_sweep", "narrowphase": "narrowphase",
+                    "si_setup": "si_setup", "si_colored": "si_colored", "si_serial": "si_serial"}
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, rank, world, device):
+    import pe_gb300 as pg
+    scene, bits, mode, offs, cfg = make_workload(args.workload)
+    g = pg.GpuWorld(scene, bits, device=device, scenes=offs)
+    flush = L2Flush()
+    N = scene.n_bodies
+    for _ in range(args.warmup):
+        g.step(1, mode)
+    # device-resident timed region
+    g.phase_times(reset=True)
+    per_step, launches = [], 0
+    with ClockSampler(device) as clk:
+        for _ in range(args.steps):
+            flush()
+            before = g.phase_times()["step"]
+            g.step(1, mode)
+            per_step.append(g.phase_times()["step"] - before)
+            launches += g.last_counts()["launches"]
+    counts = g.last_counts()
+    dev_ms = float(sum(per_step))
+    # dominant kernel: one profiled step (events around every launch; not part of the timed region)
+    g.set_profiling(True)
+    flush()
+    g.step(1, mode)
+    g.set_profiling(False)
+    ks = g.kernel_stats()
+    dom = max((k for k in ks if k in KERNEL_BYTES_KEY), key=lambda k: ks[k][0])
+    dom_ms, dom_n = ks[dom]
+    alg = algorithmic_bytes(counts, N, scene.iterations, bits // 8)
+    dom_bytes = alg[KERNEL_BYTES_KEY[dom]]   # bytes of the whole group in one step
+    peak, peak_kind = measured_peak()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = ncu_traffic().get(dom)
+    # end to end through the C ABI with host buffers
+    st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
+    e2e_times = []
+    for _ in range(max(2, args.steps // 2)):
+        t0 = time.perf_counter()
+        g.set_state(st)
+        g.step(1, mode)
+        st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
+        e2e_times.append(time.perf_counter() - t0)
+    io_bytes = N * 18 * (bits // 8)
+    res = dict(dev_ms=dev_ms, per_step=per_step, N=N, launches=launches, counts=counts, cfg=cfg, bits=bits, clk=clk.summary(),
+               roofline=dict(kernel=dom, bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
+                             traffic=traffic, algorithmic_bytes=dom_bytes, launches=dom_n, avg_launch_ms=dom_ms / max(dom_n, 1),
+                             peak_source=peak_kind, step_frac=alg["step"] / (dev_ms / args.steps * 1e-3) / 1e9 / peak),
+               e2e=dict(value=N * len(e2e_times) / sum(e2e_times), unit=UNIT, h2d_bytes_per_step=io_bytes,
+                        d2h_bytes_per_step=io_bytes),
+               kernels={k: round(v[0], 4) for k, v in ks.items() if v[1]})
+    return res, scene, bits
+
+
+def cpu_baseline(scene, bits, budget_s=20.0):
+    """The reference's CPU step (restated in oracle/) on a bounded number of steps, all host threads."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import orc
+    threads = os.cpu_count() or 1
+    w = orc.OracleWorld(scene, bits, threads=threads)
+    t = w.time_steps(1)
+    steps = 1
+    while t < budget_s and steps < 64:
+        k = max(1, min(int((budget_s - t) / max(t / steps, 1e-3)), 8))
+        t += w.time_steps(k)
+        steps += k
+    return dict(value=scene.n_bodies * steps / t, unit=UNIT, cores=threads, kind="port",
+                sample=f"{steps} full steps of the same workload from its initial state ({t:.1f} s, {threads} threads)")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="stress", choices=["stress", "tower", "batched"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        scene, bits, mode, offs, cfg = make_workload(args.workload)
+        if offs is not None:   # independent scenes: the reference steps one World per scene
+            pass
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import orc
+        threads = os.cpu_count() or 1
+        w = orc.OracleWorld(scene, bits, threads=threads)
+        for _ in range(min(args.warmup, 1)):
+            w.time_steps(1)
+        k = max(1, min(args.steps, 8))
+        t = w.time_steps(k)
+        v = scene.n_bodies * k / t
+        cfg = dict(cfg, solver="serial (the reference's sequential impulse order)")
+        print(json.dumps(dict(metric=METRIC, value=v, unit=UNIT, n_gpus=args.gpus, steps=k, warmup=min(args.warmup, 1),
+                              ms_per_step=t / k * 1e3, higher_is_better=True, scaling="weak", vs_baseline=None,
+                              dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg, impl="reference",
+                              cpu_baseline=dict(value=v, unit=UNIT, cores=threads, kind="port",
+                                                sample=f"{k} full steps from the initial state, {threads} host threads"),
+                              e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))))
+        return 0
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        dist.barrier()
+    res, scene, bits = run_ours(args, rank, world, local)
+    dev_ms = res["dev_ms"]
+    if dist is not None:
+        import torch
+        t = torch.tensor([dev_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        dist.barrier()
+    if rank != 0:
+        return 0
+    per = sorted(res["per_step"])
+    value = res["N"] * args.steps * world / (dev_ms * 1e-3)
+    cfg = dict(res["cfg"], l2="flushed between timed steps (256 MiB memset)", pairs_last_step=res["counts"]["pairs"],
+               contact_points_last_step=res["counts"]["rows"], colors_last_step=res["counts"]["colors"],
+               p50_step_ms=per[len(per) // 2], p99_step_ms=per[min(len(per) - 1, int(0.99 * len(per)))],
+               contacts_per_s=res["counts"]["rows"] * args.steps * world / (dev_ms * 1e-3), parallelism=f"replicas x{world}")
+    out = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
+               ms_per_step=dev_ms / args.steps, higher_is_better=True, scaling="weak", vs_baseline=None,
+               dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg, roofline=res["roofline"],
+               e2e=res["e2e"], gpu_launches=res["launches"], clocks=res["clk"], kernels_ms_one_step=res["kernels"])
+    if not args.no_cpu_baseline and world == 1:
+        out["cpu_baseline"] = cpu_baseline(scene, bits)
+    print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,139 @@
+/*
+ * pe_gpu.h - C ABI of the GB300 rigid-body step.
+ *
+ * One handle = one device-resident world (or a batch of independent scenes) on one GPU.
+ * All functions return an int status (PE_GPU_OK = 0, negative on error; the message is
+ * available from pe_gpu_last_error).  No exception crosses this boundary.  A handle is
+ * not thread-safe, like the reference World ("NOT thread-safe", src/intf/world.h:17-21):
+ * callers serialise calls on one handle.
+ *
+ * Reals cross the boundary as double (the reference's default pe::Real, PE_USE_DOUBLE in
+ * CMakeLists.txt:28); a world created with real_bits = 32 computes in float and rounds on
+ * the way in.  Matrices are row-major 3x3.  Body / shape / pair indices are 0-based
+ * positions in the arrays the caller supplied.
+ *
+ * Each entry point names the reference interface it replaces.
+ */
+#ifndef PE_GPU_H
+#define PE_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PE_GPU_OK 0
+#define PE_GPU_ERR_ARG (-1)
+#define PE_GPU_ERR_CUDA (-2)
+#define PE_GPU_ERR_CAPACITY (-3)
+#define PE_GPU_ERR_STATE (-4)
+
+/* shape types, in the order of pe_phys_shape::ShapeType (src/rigid/shape/shape.h:7-9) */
+#define PE_GPU_SHAPE_BOX 0
+#define PE_GPU_SHAPE_SPHERE 1
+#define PE_GPU_SHAPE_CYLINDER 2
+#define PE_GPU_SHAPE_CONVEX_MESH 3
+
+/* body flags */
+#define PE_GPU_BODY_KINEMATIC 1        /* RigidBody::setKinematic (rigidbody.h:14) */
+#define PE_GPU_BODY_IGNORE_COLLISION 2 /* RigidBody::setIgnoreCollision (rigidbody.h:15) */
+
+/* solver modes */
+#define PE_GPU_SOLVER_SERIAL_ORDER 0   /* the reference's constraint order, one thread per scene */
+#define PE_GPU_SOLVER_COLORED 1        /* graph-coloured Gauss-Seidel */
+
+typedef struct pe_gpu_world pe_gpu_world;
+
+typedef struct pe_gpu_config {
+    int real_bits; /* 32 or 64 */
+    int device;    /* CUDA device ordinal */
+} pe_gpu_config;
+
+/* Creates / destroys a world.  Replaces constructing pe_intf::World (src/intf/world.cpp:10-27). */
+int pe_gpu_create(const pe_gpu_config* cfg, pe_gpu_world** out);
+int pe_gpu_destroy(pe_gpu_world* w);
+const char* pe_gpu_last_error(const pe_gpu_world* w);
+
+/* Collision shapes.  Replaces new BoxShape(size) / SphereShape(r) / CylinderShape(r, h) /
+ * ConvexMeshShape::setMesh(mesh) (box_shape.cpp:7, sphere_shape.cpp:5, cylinder_shape.cpp:6,
+ * convex_mesh_shape.cpp:12).  param[3*i..]: box size xyz; sphere radius; cylinder radius, height.
+ * Convex meshes: hull_vbeg/vcnt index hull_verts (3 doubles per vertex), hull_fbeg/fcnt index
+ * hull_face_off (n_hull_faces+1 offsets into hull_face_idx, indices local to the shape).  Faces
+ * are wound counter-clockwise seen from outside; normals are computed like Mesh::perFaceNormal. */
+int pe_gpu_set_shapes(pe_gpu_world* w, int n_shapes, const int* type, const double* param, const int* hull_vbeg,
+                      const int* hull_vcnt, const int* hull_fbeg, const int* hull_fcnt, int n_hull_verts,
+                      const double* hull_verts, int n_hull_faces, const int* hull_face_off, const int* hull_face_idx);
+
+/* Rigid bodies, all at once.  Replaces RigidBody::setMass / setCollisionShape / setTransform /
+ * setLinearVelocity / setAngularVelocity / setFrictionCoeff / setRestitutionCoeff /
+ * setLinearDamping / setAngularDamping / setKinematic followed by World::addRigidBody
+ * (rigidbody.cpp:11-67, world.cpp:218-221). */
+int pe_gpu_set_bodies(pe_gpu_world* w, int n, const int* shape, const int* flags, const double* mass,
+                      const double* friction, const double* restitution, const double* lin_damp, const double* ang_damp,
+                      const double* origin, const double* basis, const double* lin_vel, const double* ang_vel);
+
+/* Independent scenes in one world: bodies [body_off[s], body_off[s+1]) form scene s.  Each scene
+ * behaves as its own pe_intf::World (own sweep axis, own contact-result pool).  Default: one scene. */
+int pe_gpu_set_scenes(pe_gpu_world* w, int n_scenes, const int* body_off);
+
+/* World::setDt / setGravity (world.h:24-25) and ConstraintSolver::setIteration (constraint_solver.h:72). */
+int pe_gpu_set_params(pe_gpu_world* w, double dt, double gx, double gy, double gz, int iterations);
+
+/* World::step (world.cpp:267-300): n_steps full steps on the device without host round trips
+ * of body state. */
+int pe_gpu_step(pe_gpu_world* w, int n_steps, int solver_mode);
+
+/* ---- per-phase entry points (the reference's phase interfaces) ---- */
+/* World::updateObjectStatus + applyExternalForce (world.cpp:35-127). */
+int pe_gpu_integrate(pe_gpu_world* w);
+/* BroadPhaseBase::calcCollisionPairs (broad_phase_base.h:15-17); *n_pairs receives the count. */
+int pe_gpu_broadphase(pe_gpu_world* w, int* n_pairs);
+/* NarrowPhaseBase::calcContactResults (narrow_phase_base.h:16) on the current pair list. */
+int pe_gpu_narrowphase(pe_gpu_world* w);
+/* ConstraintSolver::setupSolver + solve (constraint_solver.h:14-28) on the current results. */
+int pe_gpu_solve(pe_gpu_world* w, int solver_mode);
+
+/* ---- state transfer (host arrays, doubles) ---- */
+int pe_gpu_n_bodies(const pe_gpu_world* w);
+int pe_gpu_get_state(pe_gpu_world* w, double* origin, double* basis, double* lin_vel, double* ang_vel, double* aabb_min,
+                     double* aabb_max, double* world_inv_inertia);
+int pe_gpu_set_state(pe_gpu_world* w, const double* origin, const double* basis, const double* lin_vel,
+                     const double* ang_vel, const double* aabb_min, const double* aabb_max,
+                     const double* world_inv_inertia);
+/* sweep axis of each scene (BroadPhaseSweepAndPrune::_target_axis) */
+int pe_gpu_get_axes(pe_gpu_world* w, int* axes);
+int pe_gpu_set_axes(pe_gpu_world* w, const int* axes);
+/* pairs as (body A, body B) in broadphase order; set_pairs replaces the list fed to the narrowphase */
+int pe_gpu_n_pairs(const pe_gpu_world* w);
+int pe_gpu_get_pairs(pe_gpu_world* w, int* pairs);
+int pe_gpu_set_pairs(pe_gpu_world* w, int n, const int* pairs);
+/* contact results, one per pair: bodies, point count, combined friction / restitution and the 8
+ * cache slots x 19 reals (world_pos 3, world_normal 3, local_a 3, local_b 3, distance 1,
+ * tangent0 3, tangent1 3).  Slots at or beyond point_size carry only their distance (the value a
+ * pooled ContactResult keeps in an empty slot); their other fields are zero. */
+int pe_gpu_n_results(const pe_gpu_world* w);
+int pe_gpu_get_results(pe_gpu_world* w, int* a, int* b, int* point_size, double* friction, double* restitution,
+                       double* slots);
+int pe_gpu_set_results(pe_gpu_world* w, int n, const int* a, const int* b, const int* point_size,
+                       const double* friction, const double* restitution, const double* slots);
+
+/* Per-phase device time accumulated since the last reset, in milliseconds, measured with CUDA
+ * events on the world's stream (the GPU counterpart of World's update_status_time /
+ * broad_phase_time / narrow_phase_time / constraint_solver_time, world.h:58-61).
+ * ms[0] integrate, ms[1] broadphase, ms[2] narrowphase, ms[3] solver, ms[4] whole steps. */
+int pe_gpu_phase_times(pe_gpu_world* w, double* ms, int reset);
+/* counts6: pairs, non-empty results, contact points (solver rows), colours, kernel launches of the
+ * last pe_gpu_step step, 0 */
+int pe_gpu_last_counts(pe_gpu_world* w, int* counts6);
+/* Per-kernel-group device time: with profiling on, every kernel launch is bracketed by CUDA events
+ * on the world's stream.  ms[k] / launches[k] for k < pe_gpu_kernel_count() (cumulative). */
+int pe_gpu_set_profiling(pe_gpu_world* w, int on);
+int pe_gpu_kernel_count(void);
+const char* pe_gpu_kernel_name(int k);
+int pe_gpu_kernel_stats(pe_gpu_world* w, double* ms, long long* launches);
+/* blocks until all work on the world's stream finished */
+int pe_gpu_sync(pe_gpu_world* w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PE_GPU_H */

@@ -24,6 +24,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
+OBJ = Path(os.environ.get("TMPDIR", "/tmp")) / "pe_ref_obj"   # objects stay outside the repository
 
 
 def sources(ref: Path):
@@ -52,8 +53,8 @@ def build(ref: Path, jobs: int, bits_list=(64, 32)):
         return False
     OUT.mkdir(exist_ok=True)
     for bits in bits_list:
-        obj_dir = OUT / f"obj{bits}"
-        obj_dir.mkdir(exist_ok=True)
+        obj_dir = OBJ / f"obj{bits}"
+        obj_dir.mkdir(parents=True, exist_ok=True)
         fl = flags(ref, bits)
         jobs_list = []
         for s in sources(ref) + [HERE / "ref_harness.cpp"]:

@@ -1,0 +1,154 @@
+// C ABI (include/pe_gpu.h): status codes, argument checks, exception barrier.
+#include <cuda_runtime.h>
+#include <new>
+#include <string>
+#include "../../include/pe_gpu.h"
+#include "pe_world.cuh"
+
+struct pe_gpu_world {
+    pe::WorldBase* w = nullptr;
+    std::string err;
+};
+
+namespace {
+template <class F> int guard(pe_gpu_world* h, F&& f) {
+    if (!h || !h->w) return PE_GPU_ERR_ARG;
+    try {
+        h->err.clear();
+        return f(*h->w);
+    } catch (const pe::CudaError& e) {
+        h->err = e.what();
+        return PE_GPU_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        h->err = "host allocation failed";
+        return PE_GPU_ERR_CAPACITY;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return PE_GPU_ERR_STATE;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int pe_gpu_create(const pe_gpu_config* cfg, pe_gpu_world** out) {
+    if (!cfg || !out || (cfg->real_bits != 32 && cfg->real_bits != 64)) return PE_GPU_ERR_ARG;
+    *out = nullptr;
+    auto* h = new (std::nothrow) pe_gpu_world();
+    if (!h) return PE_GPU_ERR_CAPACITY;
+    try {
+        if (cfg->real_bits == 32) h->w = new pe::World<float>(cfg->device);
+        else h->w = new pe::World<double>(cfg->device);
+    } catch (const std::exception& e) {
+        delete h;
+        return PE_GPU_ERR_CUDA;
+    }
+    *out = h;
+    return PE_GPU_OK;
+}
+
+int pe_gpu_destroy(pe_gpu_world* h) {
+    if (!h) return PE_GPU_ERR_ARG;
+    delete h->w;
+    delete h;
+    return PE_GPU_OK;
+}
+
+const char* pe_gpu_last_error(const pe_gpu_world* h) { return h ? h->err.c_str() : "null handle"; }
+
+int pe_gpu_set_shapes(pe_gpu_world* h, int n, const int* type, const double* param, const int* vbeg, const int* vcnt,
+                      const int* fbeg, const int* fcnt, int hv_n, const double* hv, int hf_n, const int* foff, const int* fidx) {
+    if (n < 0 || (n > 0 && (!type || !param || !vbeg || !vcnt || !fbeg || !fcnt))) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_shapes(n, type, param, vbeg, vcnt, fbeg, fcnt, hv_n, hv, hf_n, foff, fidx); return PE_GPU_OK; });
+}
+
+int pe_gpu_set_bodies(pe_gpu_world* h, int n, const int* shape, const int* flags, const double* mass, const double* fr,
+                      const double* re, const double* ld, const double* ad, const double* o, const double* b, const double* v,
+                      const double* w) {
+    if (n < 0 || (n > 0 && (!shape || !flags || !mass || !fr || !re || !ld || !ad || !o || !b || !v || !w))) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& W) { W.set_bodies(n, shape, flags, mass, fr, re, ld, ad, o, b, v, w); return PE_GPU_OK; });
+}
+
+int pe_gpu_set_scenes(pe_gpu_world* h, int n, const int* off) {
+    if (n < 1 || !off) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_scenes(n, off); return PE_GPU_OK; });
+}
+
+int pe_gpu_set_params(pe_gpu_world* h, double dt, double gx, double gy, double gz, int iterations) {
+    if (!(dt > 0) || iterations < 0) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_params(dt, gx, gy, gz, iterations); return PE_GPU_OK; });
+}
+
+int pe_gpu_step(pe_gpu_world* h, int n_steps, int mode) {
+    if (n_steps < 0 || (mode != PE_GPU_SOLVER_SERIAL_ORDER && mode != PE_GPU_SOLVER_COLORED)) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.step(n_steps, mode); return PE_GPU_OK; });
+}
+
+int pe_gpu_integrate(pe_gpu_world* h) { return guard(h, [&](pe::WorldBase& w) { w.integrate(); w.sync(); return PE_GPU_OK; }); }
+
+int pe_gpu_broadphase(pe_gpu_world* h, int* n_pairs) {
+    return guard(h, [&](pe::WorldBase& w) { const int p = w.broadphase(); w.sync(); if (n_pairs) *n_pairs = p; return PE_GPU_OK; });
+}
+
+int pe_gpu_narrowphase(pe_gpu_world* h) { return guard(h, [&](pe::WorldBase& w) { w.narrowphase(); w.sync(); return PE_GPU_OK; }); }
+
+int pe_gpu_solve(pe_gpu_world* h, int mode) {
+    if (mode != PE_GPU_SOLVER_SERIAL_ORDER && mode != PE_GPU_SOLVER_COLORED) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.solve(mode); w.sync(); return PE_GPU_OK; });
+}
+
+int pe_gpu_n_bodies(const pe_gpu_world* h) { return h && h->w ? h->w->n_bodies() : PE_GPU_ERR_ARG; }
+int pe_gpu_n_pairs(const pe_gpu_world* h) { return h && h->w ? h->w->n_pairs() : PE_GPU_ERR_ARG; }
+int pe_gpu_n_results(const pe_gpu_world* h) { return h && h->w ? h->w->n_results() : PE_GPU_ERR_ARG; }
+
+int pe_gpu_get_state(pe_gpu_world* h, double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) {
+    return guard(h, [&](pe::WorldBase& W) { W.get_state(o, b, v, w, mn, mx, iw); return PE_GPU_OK; });
+}
+int pe_gpu_set_state(pe_gpu_world* h, const double* o, const double* b, const double* v, const double* w, const double* mn,
+                     const double* mx, const double* iw) {
+    return guard(h, [&](pe::WorldBase& W) { W.set_state(o, b, v, w, mn, mx, iw); return PE_GPU_OK; });
+}
+int pe_gpu_get_axes(pe_gpu_world* h, int* a) {
+    if (!a) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.get_axes(a); return PE_GPU_OK; });
+}
+int pe_gpu_set_axes(pe_gpu_world* h, const int* a) {
+    if (!a) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_axes(a); return PE_GPU_OK; });
+}
+int pe_gpu_get_pairs(pe_gpu_world* h, int* p) {
+    if (!p) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.get_pairs(p); return PE_GPU_OK; });
+}
+int pe_gpu_set_pairs(pe_gpu_world* h, int n, const int* p) {
+    if (n < 0 || (n > 0 && !p)) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_pairs(n, p); return PE_GPU_OK; });
+}
+int pe_gpu_get_results(pe_gpu_world* h, int* a, int* b, int* ps, double* fr, double* re, double* slots) {
+    return guard(h, [&](pe::WorldBase& w) { w.get_results(a, b, ps, fr, re, slots); return PE_GPU_OK; });
+}
+int pe_gpu_set_results(pe_gpu_world* h, int n, const int* a, const int* b, const int* ps, const double* fr, const double* re,
+                       const double* slots) {
+    if (n < 0 || (n > 0 && (!a || !b || !ps || !fr || !re || !slots))) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_results(n, a, b, ps, fr, re, slots); return PE_GPU_OK; });
+}
+int pe_gpu_phase_times(pe_gpu_world* h, double* ms, int reset) {
+    if (!ms) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.phase_times(ms, reset != 0); return PE_GPU_OK; });
+}
+int pe_gpu_last_counts(pe_gpu_world* h, int* c) {
+    if (!c) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.last_counts(c); return PE_GPU_OK; });
+}
+int pe_gpu_set_profiling(pe_gpu_world* h, int on) {
+    return guard(h, [&](pe::WorldBase& w) { w.set_profiling(on != 0); return PE_GPU_OK; });
+}
+int pe_gpu_kernel_count(void) { return pe::K_COUNT; }
+const char* pe_gpu_kernel_name(int k) { return pe::kernel_name(k); }
+int pe_gpu_kernel_stats(pe_gpu_world* h, double* ms, long long* launches) {
+    if (!ms || !launches) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.kernel_stats(ms, launches); return PE_GPU_OK; });
+}
+int pe_gpu_sync(pe_gpu_world* h) { return guard(h, [&](pe::WorldBase& w) { w.sync(); return PE_GPU_OK; }); }
+
+}  // extern "C"

@@ -1,0 +1,33 @@
+// Host-side preprocessing shared by the world implementations: unit meshes, convex-mesh
+// preparation and per-body mass properties.  Runs once per scene upload, never per step.
+#pragma once
+#include <vector>
+#include "pe_math.cuh"
+
+namespace pe {
+
+struct UnitMeshes;
+
+// Fills the reference's unit box and 20-gon cylinder meshes (default_mesh.h:7-273).
+void build_unit_meshes(UnitMeshes& u);
+
+// A convex mesh after ConvexMeshShape::setMesh (convex_mesh_shape.cpp:12-131): vertices
+// recentred on the centre of mass, faces in the order the face tree leaves them, per-face
+// bounding boxes, unique edges, unit-density inertia about the centre of mass.
+template <class R> struct HullPrep {
+    std::vector<R> v;                 // [nv*3]
+    std::vector<int> f_off, f_idx;    // [nf+1], local vertex indices
+    std::vector<R> f_n, f_min, f_max; // [nf*3]
+    std::vector<R> e_a, e_b;          // [ne*3]
+    M3<R> inertia;                    // per unit mass (divided by the volume)
+    R volume = 0;
+};
+template <class R> HullPrep<R> prepare_hull(const double* verts, int nv, const int* face_off, const int* face_idx, int nf);
+
+// unit-mass local inertia of the analytic shapes (box_shape.cpp:16-23, sphere_shape.cpp:7-11,
+// cylinder_shape.cpp:25-31)
+template <class R> M3<R> box_inertia(const V3<R>& size);
+template <class R> M3<R> sphere_inertia(R r);
+template <class R> M3<R> cylinder_inertia(R r, R h);
+
+} // namespace pe

@@ -1,0 +1,166 @@
+// Precision-independent device utilities: exclusive scan, stable LSD radix sort passes,
+// pair bucketing, and the constant-memory unit meshes.
+#include "pe_kernels.cuh"
+
+namespace pe {
+
+// ---------------------------------------------------------------- scan
+// tile = kBlock * 4 elements
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kBlock * kScanItems;
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+
+// block-wide exclusive scan of one value per thread; returns the block total in *total
+__device__ int block_excl_scan(int v, int* total) {
+    __shared__ int warp_sums[kBlock / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int incl = warp_incl_scan(v);
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < kBlock / 32 ? warp_sums[lane] : 0;
+        w = warp_incl_scan(w);
+        if (lane < kBlock / 32) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int before = warp == 0 ? 0 : warp_sums[warp - 1];
+    *total = warp_sums[kBlock / 32 - 1];
+    __syncthreads();
+    return before + incl - v;
+}
+
+__global__ void k_scan_tiles(int* data, int n, int* aux) {
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems], s = 0;
+    for (int k = 0; k < kScanItems; k++) { v[k] = base + k < n ? data[base + k] : 0; s += v[k]; }
+    int total;
+    int run = block_excl_scan(s, &total);
+    for (int k = 0; k < kScanItems; k++) { if (base + k < n) data[base + k] = run; run += v[k]; }
+    if (threadIdx.x == 0) aux[blockIdx.x] = total;
+}
+
+// single block: exclusive scan of the m tile totals, grand total into *total
+__global__ void k_scan_aux(int* aux, int m, int* total) {
+    int carry = 0;
+    for (int base = 0; base < m; base += kBlock) {
+        const int i = base + threadIdx.x;
+        const int v = i < m ? aux[i] : 0;
+        int t;
+        const int ex = block_excl_scan(v, &t);
+        if (i < m) aux[i] = carry + ex;
+        carry += t;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(int* data, int n, const int* aux) {
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const int add = aux[blockIdx.x];
+    for (int k = 0; k < kScanItems; k++) if (base + k < n) data[base + k] += add;
+}
+
+// ---------------------------------------------------------------- radix sort
+__device__ __forceinline__ int digit_of(const uint64_t* key, const uint32_t* key2, int i, int shift, int use2) {
+    return use2 ? (int)((key2[i] >> shift) & 0xffu) : (int)((key[i] >> shift) & 0xffull);
+}
+
+// per-tile digit histogram, stored digit-major: hist[d * n_tiles + tile]
+__global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n, int shift, int use2, int* hist, int n_tiles) {
+    __shared__ int cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kRadixTile;
+    for (int r = 0; r < kRadixItems; r++) {
+        const int i = base + r * kBlock + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[digit_of(key, key2, i, shift, use2)], 1);
+    }
+    __syncthreads();
+    hist[threadIdx.x * n_tiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// stable scatter: items of a tile keep their order within each digit
+__global__ void k_radix_scatter(const uint64_t* key_in, const uint32_t* key2_in, const uint32_t* val_in, uint64_t* key_out,
+                                uint32_t* key2_out, uint32_t* val_out, int n, int shift, int use2, const int* hist, int n_tiles) {
+    __shared__ int base_d[256];          // running output position of each digit for this tile
+    __shared__ int warp_cnt[kBlock / 32][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    base_d[threadIdx.x] = hist[threadIdx.x * n_tiles + blockIdx.x];
+    const int tile = blockIdx.x * kRadixTile;
+    for (int r = 0; r < kRadixItems; r++) {
+        for (int w = 0; w < kBlock / 32; w++) warp_cnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        const int i = tile + r * kBlock + threadIdx.x;
+        const bool live = i < n;
+        const int d = live ? digit_of(key_in, key2_in, i, shift, use2) : 256 + lane;   // dead lanes never match live ones
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (live && rank == 0) warp_cnt[warp][d] = __popc(peers);
+        __syncthreads();
+        // exclusive prefix over warps for each digit (thread = digit)
+        {
+            int run = 0;
+            for (int w = 0; w < kBlock / 32; w++) { const int c = warp_cnt[w][threadIdx.x]; warp_cnt[w][threadIdx.x] = run; run += c; }
+            // stash the round total in the digit base after use below
+            __syncthreads();
+            if (live) {
+                const int pos = base_d[d] + warp_cnt[warp][d] + rank;
+                key_out[pos] = key_in[i];
+                key2_out[pos] = key2_in[i];
+                val_out[pos] = val_in[i];
+            }
+            __syncthreads();
+            base_d[threadIdx.x] += run;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- narrowphase bucketing
+__global__ void k_np_bucket(int P, const int* cls, int* cursor, int* order) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int slot = atomicAdd(&cursor[cls[p]], 1);
+    order[slot] = p;
+}
+
+} // namespace pe
+
+namespace pe {
+
+__global__ void k_scene_pair_off(int n_scenes, const int* scene_off, const int* pair_scan, int n, int* pair_scene_off) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > n_scenes) return;
+    pair_scene_off[s] = pair_scan[scene_off[s]];
+}
+
+__global__ void k_active_flags(int P, const int* npts, int* flag) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P) flag[p] = npts[p] > 0 ? 1 : 0;
+    else if (p == P) flag[p] = 0;
+}
+
+__global__ void k_active_compact(int P, const int* npts, const int* scan, int* active) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P && npts[p] > 0) active[scan[p]] = p;
+}
+
+__global__ void k_color_count(int n_active, const int* color, int* cnt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n_active) atomicAdd(&cnt[color[t]], 1);
+}
+
+__global__ void k_color_bucket(int n_active, const int* active, const int* color, int* cursor, int* by_color) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_active) return;
+    by_color[atomicAdd(&cursor[color[t]], 1)] = active[t];
+}
+
+} // namespace pe

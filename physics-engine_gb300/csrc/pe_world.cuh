@@ -1,0 +1,231 @@
+// Host orchestration of the device-resident world (the GB300 counterpart of pe_intf::World).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include "pe_host.h"
+#include "pe_kernels.cuh"
+
+namespace pe {
+
+struct CudaError : std::runtime_error {
+    explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+#define PE_CK(x)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (x);                                                                        \
+        if (e_ != cudaSuccess) throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));    \
+    } while (0)
+
+template <class T> struct DBuf {   // device array that grows on demand
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    void ensure(size_t want, bool keep = false) {
+        if (want <= n && p) return;
+        size_t cap = want < 16 ? 16 : want;
+        T* q = nullptr;
+        PE_CK(cudaMalloc(&q, cap * sizeof(T)));
+        if (keep && p && n) PE_CK(cudaMemcpy(q, p, n * sizeof(T), cudaMemcpyDeviceToDevice));
+        if (p) cudaFree(p);
+        p = q;
+        n = cap;
+    }
+};
+
+// kernel groups for per-kernel device time (profiling mode)
+enum KernelId { K_INTEGRATE = 0, K_BP_KEYS, K_RADIX, K_SCAN, K_BP_GATHER, K_BP_SWEEP, K_BP_AXIS, K_NP_BUCKET, K_NP,
+                K_SI_SETUP, K_SI_SERIAL, K_COLOR, K_SI_COLOR, K_SI_MISC, K_MISC, K_COUNT };
+inline const char* kernel_name(int k) {
+    static const char* n[K_COUNT] = {"integrate", "bp_keys", "radix_sort", "scan", "bp_gather", "bp_sweep", "bp_axis",
+                                     "np_bucket", "narrowphase", "si_setup", "si_serial", "coloring", "si_colored",
+                                     "si_misc", "misc"};
+    return k >= 0 && k < K_COUNT ? n[k] : "";
+}
+
+class WorldBase {
+public:
+    virtual void set_profiling(bool on) = 0;
+    virtual void kernel_stats(double* ms, long long* launches) = 0;
+    virtual ~WorldBase() {}
+    virtual int real_bits() const = 0;
+    virtual void set_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
+                            const int* fcnt, int HV, const double* hv, int HF, const int* foff, const int* fidx) = 0;
+    virtual void set_bodies(int n, const int* shape, const int* flags, const double* mass, const double* fr,
+                            const double* re, const double* ld, const double* ad, const double* o, const double* b,
+                            const double* v, const double* w) = 0;
+    virtual void set_scenes(int n, const int* off) = 0;
+    virtual void set_params(double dt, double gx, double gy, double gz, int iters) = 0;
+    virtual void step(int n, int mode) = 0;
+    virtual void integrate() = 0;
+    virtual int broadphase() = 0;
+    virtual void narrowphase() = 0;
+    virtual void solve(int mode) = 0;
+    virtual int n_bodies() const = 0;
+    virtual void get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) = 0;
+    virtual void set_state(const double* o, const double* b, const double* v, const double* w, const double* mn,
+                           const double* mx, const double* iw) = 0;
+    virtual void get_axes(int* a) = 0;
+    virtual void set_axes(const int* a) = 0;
+    virtual int n_pairs() const = 0;
+    virtual void get_pairs(int* p) = 0;
+    virtual void set_pairs(int n, const int* p) = 0;
+    virtual int n_results() const = 0;
+    virtual void get_results(int* a, int* b, int* ps, double* fr, double* re, double* slots) = 0;
+    virtual void set_results(int n, const int* a, const int* b, const int* ps, const double* fr, const double* re,
+                             const double* slots) = 0;
+    virtual void phase_times(double* ms, bool reset) = 0;
+    virtual void last_counts(int* c) = 0;
+    virtual void sync() = 0;
+    std::string err;
+};
+
+template <class R> class World : public WorldBase {
+public:
+    explicit World(int device);
+    ~World() override;
+    using WorldBase::set_profiling;
+    int real_bits() const override { return sizeof(R) * 8; }
+    void set_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
+                    const int* fcnt, int HV, const double* hv, int HF, const int* foff, const int* fidx) override;
+    void set_bodies(int n, const int* shape, const int* flags, const double* mass, const double* fr, const double* re,
+                    const double* ld, const double* ad, const double* o, const double* b, const double* v,
+                    const double* w) override;
+    void set_scenes(int n, const int* off) override;
+    void set_params(double dt, double gx, double gy, double gz, int iters) override;
+    void step(int n, int mode) override;
+    void integrate() override;
+    int broadphase() override;
+    void narrowphase() override;
+    void solve(int mode) override;
+    int n_bodies() const override { return N_; }
+    void get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) override;
+    void set_state(const double* o, const double* b, const double* v, const double* w, const double* mn, const double* mx,
+                   const double* iw) override;
+    void get_axes(int* a) override;
+    void set_axes(const int* a) override;
+    int n_pairs() const override { return P_; }
+    void get_pairs(int* p) override;
+    void set_pairs(int n, const int* p) override;
+    int n_results() const override { return R_; }
+    void get_results(int* a, int* b, int* ps, double* fr, double* re, double* slots) override;
+    void set_results(int n, const int* a, const int* b, const int* ps, const double* fr, const double* re,
+                     const double* slots) override;
+    void phase_times(double* ms, bool reset) override;
+    void last_counts(int* c) override;
+    void sync() override { PE_CK(cudaStreamSynchronize(st_)); }
+    void set_profiling(bool on) override { resolve_prof(); prof_ = on; }
+    void kernel_stats(double* ms, long long* launches) override {
+        resolve_prof();
+        for (int k = 0; k < K_COUNT; k++) { ms[k] = kms_[k]; launches[k] = klaunch_[k]; }
+    }
+
+private:
+    // every kernel of the step goes through here: counts launches, and in profiling mode
+    // brackets the launch with events on the world's stream
+    template <class Kern, class... A> void launch(int id, int g, Kern kern, A... args) {
+        if (g <= 0) return;
+        klaunch_[id]++;
+        step_launches_++;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (prof_) {
+            if (ev_pool_.size() < 2) { cudaEvent_t a, b; PE_CK(cudaEventCreate(&a)); PE_CK(cudaEventCreate(&b)); ev_pool_.push_back(a); ev_pool_.push_back(b); }
+            e0 = ev_pool_.back(); ev_pool_.pop_back();
+            e1 = ev_pool_.back(); ev_pool_.pop_back();
+            PE_CK(cudaEventRecord(e0, st_));
+        }
+        kern<<<g, kBlock, 0, st_>>>(args...);
+        if (prof_) {
+            PE_CK(cudaEventRecord(e1, st_));
+            pending_.push_back({id, e0, e1});
+        }
+    }
+    struct Pending { int id; cudaEvent_t e0, e1; };
+    void resolve_prof() {
+        if (pending_.empty()) return;
+        PE_CK(cudaStreamSynchronize(st_));
+        for (auto& q : pending_) {
+            float ms = 0;
+            PE_CK(cudaEventElapsedTime(&ms, q.e0, q.e1));
+            kms_[q.id] += ms;
+            ev_pool_.push_back(q.e0);
+            ev_pool_.push_back(q.e1);
+        }
+        pending_.clear();
+    }
+    bool prof_ = false;
+    std::vector<Pending> pending_;
+    std::vector<cudaEvent_t> ev_pool_;
+    double kms_[K_COUNT] = {};
+    long long klaunch_[K_COUNT] = {};
+    long long step_launches_ = 0, last_step_launches_ = 0;
+
+    Bodies<R> bodies() {
+        Bodies<R> b;
+        b.f = bf_.p; b.cap = bcap_; b.n = N_; b.shape = bshape_.p; b.flags = bflags_.p; b.scene = bscene_.p;
+        return b;
+    }
+    ShapeTable<R> shapes() const;
+    Results<R> results();
+    Rows<R> rows();
+    int scan(int* data, int n);   // exclusive scan in place; returns the total (synchronises)
+    R* staging(size_t n);         // pinned host buffer of at least n reals
+    R* stage_ = nullptr;
+    size_t stage_n_ = 0;
+    void radix_sort(int n, int n_scene_passes);
+    void ensure_pair_capacity(int P);
+    void check_status();
+    void ev_begin(int phase);
+    void ev_end(int phase);
+    int grid(int n) const { return (n + kBlock - 1) / kBlock; }
+
+    int dev_;
+    cudaStream_t st_ = nullptr;
+    cudaEvent_t ev_[5][2];
+    bool ev_open_[5] = {false, false, false, false, false};
+    double ms_[5] = {0, 0, 0, 0, 0};
+    StepParams prm_{0.01, {0, -9.8, 0}, 10};
+    // shapes
+    int S_ = 0;
+    DBuf<int> stype_, shull_, hvbeg_, hvcnt_, hfbeg_, hfcnt_, hebeg_, hecnt_, hfoff_, hfidx_;
+    DBuf<R> sparam_, hv_, hfn_, hfmin_, hfmax_, hea_, heb_;
+    std::vector<int> h_stype_;
+    std::vector<R> h_sparam_;
+    std::vector<M3<R>> h_sinertia_;
+    // bodies
+    int N_ = 0, bcap_ = 0;
+    DBuf<R> bf_;
+    DBuf<int> bshape_, bflags_, bscene_;
+    // scenes
+    int NS_ = 1;
+    std::vector<int> h_scene_off_;
+    DBuf<int> scene_off_, scene_axis_, pair_scene_off_, res_scene_off_, prev_res_off_;
+    // broadphase
+    DBuf<uint64_t> key_[2];
+    DBuf<uint32_t> key2_[2], val_[2];
+    DBuf<int> hist_, aux_, total_, count_, status_;
+    DBuf<R> smn_, smx_;
+    DBuf<int> sflag_, ssc_;
+    uint32_t* order_ = nullptr;   // sorted body order (points into val_)
+    DBuf<int2> pairs_;
+    int P_ = 0, pair_cap_ = 0;
+    // narrowphase
+    DBuf<int> cls_, cls_count_, order_np_;
+    DBuf<int> res_a_, res_b_, res_np_;
+    DBuf<R> res_fr_, res_re_, res_pts_, res_dist_[2];
+    int cur_dist_ = 0;
+    int R_ = 0;
+    std::vector<int> h_pair_scene_off_;
+    // solver
+    DBuf<int> row_off_, active_, color_, claim_, by_color_, color_cnt_, remaining_;
+    DBuf<R> rows_;
+    int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0;
+};
+
+} // namespace pe

@@ -1,0 +1,586 @@
+// World<R> member definitions; included by exactly one translation unit per precision.
+#pragma once
+#include <algorithm>
+#include "pe_world.cuh"
+
+namespace pe {
+
+template <class R> World<R>::World(int device) : dev_(device) {
+    PE_CK(cudaSetDevice(dev_));
+    PE_CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    for (auto& e : ev_) { PE_CK(cudaEventCreate(&e[0])); PE_CK(cudaEventCreate(&e[1])); }
+    UnitMeshes u;
+    std::memset(&u, 0, sizeof(u));
+    build_unit_meshes(u);
+    PE_CK(cudaMemcpyToSymbol(g_unit, &u, sizeof(u)));
+    status_.ensure(1);
+    PE_CK(cudaMemset(status_.p, 0, sizeof(int)));
+    total_.ensure(1);
+    set_scenes(1, nullptr);
+}
+
+template <class R> World<R>::~World() {
+    if (st_) cudaStreamSynchronize(st_);
+    if (stage_) cudaFreeHost(stage_);
+    for (auto& q : pending_) { cudaEventDestroy(q.e0); cudaEventDestroy(q.e1); }
+    for (auto e : ev_pool_) cudaEventDestroy(e);
+    for (auto& e : ev_) { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+    if (st_) cudaStreamDestroy(st_);
+}
+
+template <class R> void World<R>::ev_begin(int k) {
+    PE_CK(cudaEventRecord(ev_[k][0], st_));
+    ev_open_[k] = true;
+}
+template <class R> void World<R>::ev_end(int k) {
+    PE_CK(cudaEventRecord(ev_[k][1], st_));
+    PE_CK(cudaEventSynchronize(ev_[k][1]));
+    float ms = 0;
+    PE_CK(cudaEventElapsedTime(&ms, ev_[k][0], ev_[k][1]));
+    ms_[k] += ms;
+    ev_open_[k] = false;
+}
+template <class R> void World<R>::phase_times(double* ms, bool reset) {
+    for (int k = 0; k < 5; k++) ms[k] = ms_[k];
+    if (reset) for (double& m : ms_) m = 0;
+}
+template <class R> void World<R>::last_counts(int* c) {
+    c[0] = P_; c[1] = n_active_; c[2] = n_rows_; c[3] = n_colors_; c[4] = (int)last_step_launches_; c[5] = 0;
+}
+
+template <class R> void World<R>::check_status() {
+    int s = 0;
+    PE_CK(cudaMemcpyAsync(&s, status_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+    if (s) {
+        PE_CK(cudaMemsetAsync(status_.p, 0, sizeof(int), st_));
+        throw std::runtime_error("device capacity overflow (status " + std::to_string(s) + ")");
+    }
+}
+
+template <class R> ShapeTable<R> World<R>::shapes() const {
+    ShapeTable<R> t;
+    t.type = stype_.p; t.param = sparam_.p; t.hull = shull_.p;
+    t.h_vbeg = hvbeg_.p; t.h_vcnt = hvcnt_.p; t.h_fbeg = hfbeg_.p; t.h_fcnt = hfcnt_.p; t.h_ebeg = hebeg_.p; t.h_ecnt = hecnt_.p;
+    t.hv = hv_.p; t.f_off = hfoff_.p; t.f_idx = hfidx_.p; t.f_n = hfn_.p; t.f_min = hfmin_.p; t.f_max = hfmax_.p;
+    t.e_a = hea_.p; t.e_b = heb_.p;
+    return t;
+}
+
+template <class R> Results<R> World<R>::results() {
+    Results<R> r;
+    r.cap = pair_cap_;
+    r.a = res_a_.p; r.b = res_b_.p; r.npts = res_np_.p; r.fr = res_fr_.p; r.re = res_re_.p; r.pts = res_pts_.p;
+    r.dist = res_dist_[cur_dist_].p;
+    r.prev_dist = res_dist_[cur_dist_ ^ 1].p;
+    return r;
+}
+
+template <class R> Rows<R> World<R>::rows() {
+    Rows<R> r;
+    r.cap = rows_cap_;
+    r.f = rows_.p;
+    return r;
+}
+
+template <class T> static void upload(DBuf<T>& d, const std::vector<T>& h, cudaStream_t st) {
+    d.ensure(h.size() + 1);
+    if (!h.empty()) PE_CK(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+// ------------------------------------------------------------------ scene upload
+template <class R>
+void World<R>::set_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
+                          const int* fcnt, int HV, const double* hv, int HF, const int* foff, const int* fidx) {
+    (void)HV; (void)HF;
+    std::vector<int> t(S), hull(S, -1), hvb, hvc, hfb, hfc, heb, hec, f_off, f_idx;
+    std::vector<R> prm(S * 3), v, fn, fmn, fmx, ea, eb;
+    h_sinertia_.assign(S, M3<R>());
+    for (int s = 0; s < S; s++) {
+        t[s] = type[s];
+        for (int k = 0; k < 3; k++) prm[s * 3 + k] = R(param[s * 3 + k]);
+        if (t[s] == ST_BOX) h_sinertia_[s] = box_inertia(V3<R>(prm[s * 3], prm[s * 3 + 1], prm[s * 3 + 2]));
+        else if (t[s] == ST_SPHERE) h_sinertia_[s] = sphere_inertia(prm[s * 3]);
+        else if (t[s] == ST_CYLINDER) h_sinertia_[s] = cylinder_inertia(prm[s * 3], prm[s * 3 + 1]);
+        else if (t[s] == ST_HULL) {
+            // local face offsets of this shape
+            std::vector<int> lo(fcnt[s] + 1);
+            for (int f = 0; f <= fcnt[s]; f++) lo[f] = foff[fbeg[s] + f] - foff[fbeg[s]];
+            if (fcnt[s] >= 16382) throw std::runtime_error("convex mesh with more than 16381 faces is not supported");
+            HullPrep<R> h = prepare_hull<R>(hv + (size_t)vbeg[s] * 3, vcnt[s], lo.data(), fidx + foff[fbeg[s]], fcnt[s]);
+            h_sinertia_[s] = h.inertia;
+            hull[s] = (int)hvb.size();
+            hvb.push_back((int)v.size() / 3); hvc.push_back(vcnt[s]);
+            hfb.push_back((int)fn.size() / 3); hfc.push_back(fcnt[s]);
+            heb.push_back((int)ea.size() / 3); hec.push_back((int)h.e_a.size() / 3);
+            const int ibase = (int)f_idx.size();
+            if (f_off.empty()) f_off.push_back(0);
+            for (int f = 0; f < fcnt[s]; f++) f_off.push_back(ibase + h.f_off[f + 1]);
+            f_idx.insert(f_idx.end(), h.f_idx.begin(), h.f_idx.end());
+            v.insert(v.end(), h.v.begin(), h.v.end());
+            fn.insert(fn.end(), h.f_n.begin(), h.f_n.end());
+            fmn.insert(fmn.end(), h.f_min.begin(), h.f_min.end());
+            fmx.insert(fmx.end(), h.f_max.begin(), h.f_max.end());
+            ea.insert(ea.end(), h.e_a.begin(), h.e_a.end());
+            eb.insert(eb.end(), h.e_b.begin(), h.e_b.end());
+        } else {
+            throw std::runtime_error("unsupported shape type " + std::to_string(t[s]));
+        }
+    }
+    // hull face offsets are global per face: face f of hull h sits at hfb[h] + f, its offsets at
+    // f_off[hfb[h] + f] .. f_off[hfb[h] + f + 1]
+    S_ = S;
+    h_stype_ = t;
+    h_sparam_ = prm;
+    upload(stype_, t, st_); upload(sparam_, prm, st_); upload(shull_, hull, st_);
+    upload(hvbeg_, hvb, st_); upload(hvcnt_, hvc, st_); upload(hfbeg_, hfb, st_); upload(hfcnt_, hfc, st_);
+    upload(hebeg_, heb, st_); upload(hecnt_, hec, st_);
+    upload(hv_, v, st_); upload(hfoff_, f_off, st_); upload(hfidx_, f_idx, st_); upload(hfn_, fn, st_);
+    upload(hfmin_, fmn, st_); upload(hfmax_, fmx, st_); upload(hea_, ea, st_); upload(heb_, eb, st_);
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
+template <class R>
+void World<R>::set_bodies(int n, const int* shape, const int* flags, const double* mass, const double* fr, const double* re,
+                          const double* ld, const double* ad, const double* o, const double* b, const double* v,
+                          const double* w) {
+    N_ = n;
+    bcap_ = std::max(n, 1);
+    std::vector<R> f((size_t)NBF * bcap_, R(0));
+    auto F = [&](int k, int i) -> R& { return f[(size_t)k * bcap_ + i]; };
+    for (int i = 0; i < n; i++) {
+        if (shape[i] < 0 || shape[i] >= S_) throw std::runtime_error("body " + std::to_string(i) + ": bad shape index");
+        const R m = R(mass[i]);
+        // RigidBody::setMass + setCollisionShape (rigidbody.cpp:11-41)
+        const R inv_m = m > eps<R>() ? R(1.0) / m : R(0);
+        M3<R> li;
+        for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) li.m[r][c] = h_sinertia_[shape[i]].m[r][c] * m;
+        const M3<R> lii = m > eps<R>() ? inverse3(li) : M3<R>();
+        M3<R> basis;
+        for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) basis.m[r][c] = R(b[i * 9 + r * 3 + c]);
+        const M3<R> wi = world_inertia(basis, lii);
+        for (int k = 0; k < 3; k++) {
+            F(OX + k, i) = R(o[i * 3 + k]);
+            F(VX + k, i) = R(v[i * 3 + k]);
+            F(WX + k, i) = R(w[i * 3 + k]);
+        }
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                F(B00 + r * 3 + c, i) = basis.m[r][c];
+                F(I00 + r * 3 + c, i) = wi.m[r][c];
+                F(L00 + r * 3 + c, i) = lii.m[r][c];
+            }
+        F(INVM, i) = inv_m;
+        F(MASS, i) = m;
+        F(FRIC, i) = R(fr[i]);
+        F(REST, i) = R(re[i]);
+        F(LDAMP, i) = R(ld[i]);
+        F(ADAMP, i) = R(ad[i]);
+    }
+    upload(bf_, f, st_);
+    upload(bshape_, std::vector<int>(shape, shape + n), st_);
+    upload(bflags_, std::vector<int>(flags, flags + n), st_);
+    claim_.ensure(n + 1);
+    set_scenes(1, nullptr);
+}
+
+template <class R> void World<R>::set_scenes(int ns, const int* off) {
+    std::vector<int> so(ns + 1);
+    if (off) for (int s = 0; s <= ns; s++) so[s] = off[s];
+    else { so[0] = 0; so[1] = N_; }
+    if (so[0] != 0 || so[ns] != N_) throw std::runtime_error("scene offsets must start at 0 and end at the body count");
+    for (int s = 0; s < ns; s++) if (so[s + 1] < so[s]) throw std::runtime_error("scene offsets must not decrease");
+    NS_ = ns;
+    h_scene_off_ = so;
+    std::vector<int> sc(std::max(N_, 1), 0);
+    for (int s = 0; s < ns; s++) for (int i = so[s]; i < so[s + 1]; i++) sc[i] = s;
+    upload(bscene_, sc, st_);
+    upload(scene_off_, so, st_);
+    upload(scene_axis_, std::vector<int>(ns, 0), st_);
+    std::vector<int> zero(ns + 1, 0);
+    upload(pair_scene_off_, zero, st_);
+    upload(res_scene_off_, zero, st_);
+    upload(prev_res_off_, zero, st_);
+    h_pair_scene_off_ = zero;
+    P_ = 0;
+    R_ = 0;
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
+template <class R> void World<R>::set_params(double dt, double gx, double gy, double gz, int iters) {
+    prm_.dt = dt; prm_.g[0] = gx; prm_.g[1] = gy; prm_.g[2] = gz; prm_.iterations = iters;
+}
+
+// ------------------------------------------------------------------ utilities
+template <class R> int World<R>::scan(int* data, int n) {
+    const int tiles = (n + 1023) / 1024;
+    aux_.ensure(tiles + 1);
+    launch(K_SCAN, tiles, k_scan_tiles, data, n, aux_.p);
+    launch(K_SCAN, 1, k_scan_aux, aux_.p, tiles, total_.p);
+    launch(K_SCAN, tiles, k_scan_add, data, n, aux_.p);
+    int tot = 0;
+    PE_CK(cudaMemcpyAsync(&tot, total_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+    return tot;
+}
+
+template <class R> void World<R>::radix_sort(int n, int scene_passes) {
+    const int tiles = (n + kRadixTile - 1) / kRadixTile;
+    hist_.ensure((size_t)256 * tiles + 1);
+    aux_.ensure((256 * tiles + 1023) / 1024 + 1);
+    const int key_bits = sizeof(R) * 8;
+    int cur = 0;
+    auto pass = [&](int shift, int use2) {
+        launch(K_RADIX, tiles, k_radix_hist, key_[cur].p, key2_[cur].p, n, shift, use2, hist_.p, tiles);
+        const int m = 256 * tiles;
+        const int st = (m + 1023) / 1024;
+        launch(K_SCAN, st, k_scan_tiles, hist_.p, m, aux_.p);
+        launch(K_SCAN, 1, k_scan_aux, aux_.p, st, total_.p);
+        launch(K_SCAN, st, k_scan_add, hist_.p, m, aux_.p);
+        launch(K_RADIX, tiles, k_radix_scatter, key_[cur].p, key2_[cur].p, val_[cur].p, key_[cur ^ 1].p, key2_[cur ^ 1].p,
+                                                  val_[cur ^ 1].p, n, shift, use2, hist_.p, tiles);
+        cur ^= 1;
+    };
+    for (int s = 0; s < key_bits; s += 8) pass(s, 0);
+    for (int s = 0; s < scene_passes * 8; s += 8) pass(s, 1);
+    order_ = val_[cur].p;
+}
+
+template <class R> void World<R>::ensure_pair_capacity(int P) {
+    if (P <= pair_cap_) return;
+    const int cap = std::max(P + P / 2, 1024);
+    pairs_.ensure(cap);
+    cls_.ensure(cap); order_np_.ensure(cap);
+    res_a_.ensure(cap); res_b_.ensure(cap); res_np_.ensure(cap + 1);
+    res_fr_.ensure(cap); res_re_.ensure(cap);
+    res_pts_.ensure((size_t)NPF * cap * kSlots);
+    // result slot distances survive between steps: grow both generations keeping contents
+    res_dist_[0].ensure((size_t)cap * kSlots, true);
+    res_dist_[1].ensure((size_t)cap * kSlots, true);
+    row_off_.ensure(cap + 1); active_.ensure(cap + 1); color_.ensure(cap); by_color_.ensure(cap);
+    // the point buffer is field-major over the capacity: re-layout requires no copy because
+    // points are only meaningful within one step
+    pair_cap_ = cap;
+}
+
+// ------------------------------------------------------------------ phases
+template <class R> void World<R>::integrate() {
+    if (N_ == 0) return;
+    launch(K_INTEGRATE, grid(N_), k_integrate<R>, bodies(), shapes(), prm_, 1);
+    PE_CK(cudaGetLastError());
+}
+
+template <class R> int World<R>::broadphase() {
+    const int n = N_;
+    if (n < 2) return P_;   // the reference leaves the pair list untouched below two bodies
+    for (int k = 0; k < 2; k++) { key_[k].ensure(n); key2_[k].ensure(n); val_[k].ensure(n); }
+    smn_.ensure((size_t)3 * n); smx_.ensure((size_t)3 * n); sflag_.ensure(n); ssc_.ensure(n);
+    count_.ensure(n + 1);
+    launch(K_BP_KEYS, grid(n), k_bp_keys<R>, bodies(), scene_axis_.p, key_[0].p, key2_[0].p, val_[0].p);
+    int scene_passes = 0;
+    for (int m = NS_ - 1; m > 0; m >>= 8) scene_passes++;
+    radix_sort(n, scene_passes);
+    launch(K_BP_GATHER, grid(n), k_bp_gather<R>, bodies(), order_, smn_.p, smx_.p, sflag_.p, ssc_.p);
+    launch(K_BP_SWEEP, grid(n), k_bp_sweep<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, nullptr,
+                                               nullptr, 0, status_.p);
+    PE_CK(cudaMemsetAsync(count_.p + n, 0, sizeof(int), st_));
+    const int P = scan(count_.p, n + 1);
+    ensure_pair_capacity(P);
+    launch(K_BP_SWEEP, grid(n), k_bp_sweep<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, nullptr, count_.p,
+                                               pairs_.p, pair_cap_, status_.p);
+    launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
+    launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
+    PE_CK(cudaGetLastError());
+    P_ = P;
+    return P;
+}
+
+template <class R> void World<R>::narrowphase() {
+    const int P = P_;
+    ensure_pair_capacity(std::max(P, 1));
+    // the results of the previous step become the pool the new step draws stale slots from
+    PE_CK(cudaMemcpyAsync(prev_res_off_.p, res_scene_off_.p, (NS_ + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
+    cur_dist_ ^= 1;
+    if (P > 0) {
+        cls_count_.ensure(2 * PC_COUNT);
+        PE_CK(cudaMemsetAsync(cls_count_.p, 0, 2 * PC_COUNT * sizeof(int), st_));
+        launch(K_NP_BUCKET, grid(P), k_np_classify<R>, P, pairs_.p, bodies(), stype_.p, cls_.p, cls_count_.p);
+        int cnt[PC_COUNT];
+        PE_CK(cudaMemcpyAsync(cnt, cls_count_.p, sizeof(cnt), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaStreamSynchronize(st_));
+        int cur[PC_COUNT], run = 0;
+        for (int c = 0; c < PC_COUNT; c++) { cur[c] = run; run += cnt[c]; }
+        PE_CK(cudaMemcpyAsync(cls_count_.p + PC_COUNT, cur, sizeof(cur), cudaMemcpyHostToDevice, st_));
+        launch(K_NP_BUCKET, grid(P), k_np_bucket, P, cls_.p, cls_count_.p + PC_COUNT, order_np_.p);
+        launch(K_NP, grid(P), k_np<R>, P, order_np_.p, cls_.p, pairs_.p, bodies(), shapes(), results(),
+                                             pair_scene_off_.p, prev_res_off_.p, 0, PC_COUNT - 1);
+        PE_CK(cudaGetLastError());
+    }
+    PE_CK(cudaMemcpyAsync(res_scene_off_.p, pair_scene_off_.p, (NS_ + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
+    R_ = P;
+}
+
+template <class R> void World<R>::solve(int mode) {
+    const int P = R_;
+    if (N_ == 0) return;
+    launch(K_SI_MISC, grid(N_), k_si_clear<R>, bodies());
+    if (P > 0) {
+        PE_CK(cudaMemcpyAsync(row_off_.p, res_np_.p, P * sizeof(int), cudaMemcpyDeviceToDevice, st_));
+        PE_CK(cudaMemsetAsync(row_off_.p + P, 0, sizeof(int), st_));
+        n_rows_ = scan(row_off_.p, P + 1);
+        if (n_rows_ > rows_cap_) {
+            rows_cap_ = std::max(n_rows_ + n_rows_ / 2, 1024);
+            rows_.ensure((size_t)NRF * rows_cap_);
+        }
+        launch(K_SI_SETUP, grid(P), k_si_setup<R>, P, results(), bodies(), rows(), row_off_.p, prm_, status_.p);
+        if (mode == 0) {
+            launch(K_SI_SERIAL, grid(NS_), k_si_serial<R>, NS_, res_scene_off_.p, results(), bodies(), rows(), row_off_.p,
+                                                         prm_.iterations);
+            n_colors_ = 0;
+        } else {
+            // results with points
+            launch(K_SI_MISC, grid(P + 1), k_active_flags, P, res_np_.p, active_.p);
+            color_.ensure(P + 1);
+            int* flags = color_.p;   // reuse as scan scratch
+            PE_CK(cudaMemcpyAsync(flags, active_.p, (P + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
+            n_active_ = scan(flags, P + 1);
+            launch(K_SI_MISC, grid(P), k_active_compact, P, res_np_.p, flags, active_.p);
+            const int A = n_active_;
+            PE_CK(cudaMemsetAsync(color_.p, 0xff, (A + 1) * sizeof(int), st_));   // -1 = uncoloured
+            remaining_.ensure(1);
+            int c = 0;
+            for (; A > 0; c++) {
+                PE_CK(cudaMemsetAsync(remaining_.p, 0, sizeof(int), st_));
+                launch(K_COLOR, grid(A), k_color_reset<R>, A, active_.p, color_.p, results(), claim_.p);
+                launch(K_COLOR, grid(A), k_color_claim<R>, A, active_.p, color_.p, results(), bodies(), claim_.p);
+                launch(K_COLOR, grid(A), k_color_take<R>, A, active_.p, color_.p, results(), bodies(), claim_.p, c,
+                                                             remaining_.p);
+                int rem = 0;
+                PE_CK(cudaMemcpyAsync(&rem, remaining_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+                PE_CK(cudaStreamSynchronize(st_));
+                if (rem == 0) break;
+                if (c > 4096) throw std::runtime_error("colouring did not converge");
+            }
+            n_colors_ = A ? c + 1 : 0;
+            color_cnt_.ensure(2 * n_colors_ + 2);
+            PE_CK(cudaMemsetAsync(color_cnt_.p, 0, (2 * n_colors_ + 2) * sizeof(int), st_));
+            launch(K_COLOR, grid(A), k_color_count, A, color_.p, color_cnt_.p);
+            std::vector<int> cnt(n_colors_ + 1), off(n_colors_ + 1, 0);
+            if (n_colors_) PE_CK(cudaMemcpyAsync(cnt.data(), color_cnt_.p, n_colors_ * sizeof(int), cudaMemcpyDeviceToHost, st_));
+            PE_CK(cudaStreamSynchronize(st_));
+            for (int k = 0; k < n_colors_; k++) off[k + 1] = off[k] + cnt[k];
+            if (n_colors_) PE_CK(cudaMemcpyAsync(color_cnt_.p + n_colors_ + 1, off.data(), n_colors_ * sizeof(int),
+                                                 cudaMemcpyHostToDevice, st_));
+            launch(K_COLOR, grid(A), k_color_bucket, A, active_.p, color_.p, color_cnt_.p + n_colors_ + 1, by_color_.p);
+            for (int it = 0; it < prm_.iterations; it++)
+                for (int k = 0; k < n_colors_; k++) {
+                    const int lo = off[k], hi = off[k + 1];
+                    launch(K_SI_COLOR, grid(hi - lo), k_si_color<R>, lo, hi, by_color_.p, results(), bodies(), rows(), row_off_.p);
+                }
+        }
+    }
+    launch(K_SI_MISC, grid(N_), k_si_sync<R>, bodies());
+    PE_CK(cudaGetLastError());
+}
+
+template <class R> void World<R>::step(int n, int mode) {
+    for (int s = 0; s < n; s++) {
+        step_launches_ = 0;
+        ev_begin(4);
+        ev_begin(0); integrate(); ev_end(0);
+        ev_begin(1); broadphase(); ev_end(1);
+        ev_begin(2); narrowphase(); ev_end(2);
+        ev_begin(3); solve(mode); ev_end(3);
+        ev_end(4);
+        last_step_launches_ = step_launches_;
+        check_status();
+    }
+    resolve_prof();
+}
+
+// ------------------------------------------------------------------ transfers
+// column-wise transfers: each requested field is one contiguous column of the field-major body
+// array, staged through pinned host memory (these are the host<->device copies a drop-in caller pays)
+template <class R> R* World<R>::staging(size_t n) {
+    if (n > stage_n_) {
+        if (stage_) cudaFreeHost(stage_);
+        stage_ = nullptr;
+        PE_CK(cudaMallocHost(&stage_, n * sizeof(R)));
+        stage_n_ = n;
+    }
+    return stage_;
+}
+
+template <class R>
+void World<R>::get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) {
+    struct G { double* dst; int k0; int nk; };
+    const G groups[7] = {{o, OX, 3}, {b, B00, 9}, {v, VX, 3}, {w, WX, 3}, {mn, MNX, 3}, {mx, MXX, 3}, {iw, I00, 9}};
+    int cols = 0;
+    for (const G& g : groups) if (g.dst) cols += g.nk;
+    if (!N_ || !cols) return;
+    R* h = staging((size_t)cols * N_);
+    int c = 0;
+    for (const G& g : groups) {
+        if (!g.dst) continue;
+        PE_CK(cudaMemcpyAsync(h + (size_t)c * N_, bf_.p + (size_t)g.k0 * bcap_, (size_t)g.nk * N_ * sizeof(R), cudaMemcpyDeviceToHost, st_));
+        c += g.nk;
+    }
+    PE_CK(cudaStreamSynchronize(st_));
+    c = 0;
+    for (const G& g : groups) {
+        if (!g.dst) continue;
+        for (int k = 0; k < g.nk; k++) {
+            const R* col = h + (size_t)(c + k) * N_;
+            for (int i = 0; i < N_; i++) g.dst[(size_t)i * g.nk + k] = (double)col[i];
+        }
+        c += g.nk;
+    }
+}
+
+template <class R>
+void World<R>::set_state(const double* o, const double* b, const double* v, const double* w, const double* mn, const double* mx,
+                         const double* iw) {
+    struct G { const double* src; int k0; int nk; };
+    const G groups[7] = {{o, OX, 3}, {b, B00, 9}, {v, VX, 3}, {w, WX, 3}, {mn, MNX, 3}, {mx, MXX, 3}, {iw, I00, 9}};
+    const bool scale = mn && mx && o;
+    int cols = scale ? 1 : 0;
+    for (const G& g : groups) if (g.src) cols += g.nk;
+    if (!N_ || !cols) return;
+    R* h = staging((size_t)cols * N_);
+    int c = 0;
+    for (const G& g : groups) {
+        if (!g.src) continue;
+        for (int k = 0; k < g.nk; k++) {
+            R* col = h + (size_t)(c + k) * N_;
+            for (int i = 0; i < N_; i++) col[i] = R(g.src[(size_t)i * g.nk + k]);
+        }
+        PE_CK(cudaMemcpyAsync(bf_.p + (size_t)g.k0 * bcap_, h + (size_t)c * N_, (size_t)g.nk * N_ * sizeof(R), cudaMemcpyHostToDevice, st_));
+        c += g.nk;
+    }
+    if (scale) {   // RigidBody::getAABBScale of the injected box
+        R* col = h + (size_t)c * N_;
+        for (int i = 0; i < N_; i++) {
+            const V3<R> a = V3<R>(R(mn[i * 3]), R(mn[i * 3 + 1]), R(mn[i * 3 + 2]));
+            const V3<R> d = V3<R>(R(mx[i * 3]), R(mx[i * 3 + 1]), R(mx[i * 3 + 2]));
+            const V3<R> org = V3<R>(R(o[i * 3]), R(o[i * 3 + 1]), R(o[i * 3 + 2]));
+            const R sc = norm(d - a), df = norm(d + a - org * R(2));
+            col[i] = (sc + df) * R(0.5);
+        }
+        PE_CK(cudaMemcpyAsync(bf_.p + (size_t)SCALE * bcap_, col, (size_t)N_ * sizeof(R), cudaMemcpyHostToDevice, st_));
+    }
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
+template <class R> void World<R>::get_axes(int* a) {
+    PE_CK(cudaMemcpyAsync(a, scene_axis_.p, NS_ * sizeof(int), cudaMemcpyDeviceToHost, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+}
+template <class R> void World<R>::set_axes(const int* a) {
+    PE_CK(cudaMemcpyAsync(scene_axis_.p, a, NS_ * sizeof(int), cudaMemcpyHostToDevice, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
+template <class R> void World<R>::get_pairs(int* p) {
+    if (P_) PE_CK(cudaMemcpyAsync(p, pairs_.p, (size_t)P_ * sizeof(int2), cudaMemcpyDeviceToHost, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
+// per-scene offsets of a list grouped by scene (scene of its first body)
+static std::vector<int> scene_offsets(int n, const int* a, const std::vector<int>& scene_off) {
+    const int ns = (int)scene_off.size() - 1;
+    std::vector<int> off(ns + 1, 0);
+    int s = 0;
+    for (int i = 0; i < n; i++) {
+        const int b = a[i * 2];
+        const int sb = (int)(std::upper_bound(scene_off.begin(), scene_off.end(), b) - scene_off.begin()) - 1;
+        if (sb < s) throw std::runtime_error("list must be grouped by scene in scene order");
+        while (s < sb) off[++s] = i;
+    }
+    while (s < ns) off[++s] = n;
+    return off;
+}
+
+template <class R> void World<R>::set_pairs(int n, const int* p) {
+    for (int i = 0; i < 2 * n; i++) if (p[i] < 0 || p[i] >= N_) throw std::runtime_error("pair body index out of range");
+    ensure_pair_capacity(std::max(n, 1));
+    if (n) PE_CK(cudaMemcpyAsync(pairs_.p, p, (size_t)n * sizeof(int2), cudaMemcpyHostToDevice, st_));
+    h_pair_scene_off_ = scene_offsets(n, p, h_scene_off_);
+    PE_CK(cudaMemcpyAsync(pair_scene_off_.p, h_pair_scene_off_.data(), (NS_ + 1) * sizeof(int), cudaMemcpyHostToDevice, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+    P_ = n;
+}
+
+template <class R> void World<R>::get_results(int* a, int* b, int* ps, double* fr, double* re, double* slots) {
+    const int P = R_;
+    std::vector<int> ha(P), hb(P), hn(P);
+    std::vector<R> hfr(P), hre(P), hd((size_t)P * kSlots), pts((size_t)NPF * pair_cap_ * kSlots);
+    if (P) {
+        PE_CK(cudaMemcpyAsync(ha.data(), res_a_.p, P * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaMemcpyAsync(hb.data(), res_b_.p, P * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaMemcpyAsync(hn.data(), res_np_.p, P * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaMemcpyAsync(hfr.data(), res_fr_.p, P * sizeof(R), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaMemcpyAsync(hre.data(), res_re_.p, P * sizeof(R), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaMemcpyAsync(hd.data(), res_dist_[cur_dist_].p, hd.size() * sizeof(R), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaMemcpyAsync(pts.data(), res_pts_.p, pts.size() * sizeof(R), cudaMemcpyDeviceToHost, st_));
+    }
+    PE_CK(cudaStreamSynchronize(st_));
+    const size_t stride = (size_t)pair_cap_ * kSlots;
+    for (int p = 0; p < P; p++) {
+        if (a) a[p] = ha[p];
+        if (b) b[p] = hb[p];
+        if (ps) ps[p] = hn[p];
+        if (fr) fr[p] = hfr[p];
+        if (re) re[p] = hre[p];
+        if (!slots) continue;
+        for (int k = 0; k < kSlots; k++) {
+            double* o = slots + ((size_t)p * kSlots + k) * 19;
+            for (int q = 0; q < 19; q++) o[q] = 0;
+            o[12] = hd[(size_t)p * kSlots + k];
+            if (k >= hn[p]) continue;
+            const size_t s = (size_t)p * kSlots + k;
+            for (int g = 0; g < 4; g++) for (int d = 0; d < 3; d++) o[g * 3 + d] = pts[(size_t)(g * 3 + d) * stride + s];
+            for (int g = 4; g < 6; g++) for (int d = 0; d < 3; d++) o[13 + (g - 4) * 3 + d] = pts[(size_t)(g * 3 + d) * stride + s];
+        }
+    }
+}
+
+template <class R>
+void World<R>::set_results(int n, const int* a, const int* b, const int* ps, const double* fr, const double* re,
+                           const double* slots) {
+    ensure_pair_capacity(std::max(n, 1));
+    std::vector<int> ab(2 * n);
+    for (int i = 0; i < n; i++) {
+        if (a[i] < 0 || a[i] >= N_ || b[i] < 0 || b[i] >= N_ || ps[i] < 0 || ps[i] > kSlots)
+            throw std::runtime_error("result " + std::to_string(i) + " out of range");
+        ab[2 * i] = a[i];
+        ab[2 * i + 1] = b[i];
+    }
+    std::vector<int> off = scene_offsets(n, ab.data(), h_scene_off_);
+    std::vector<R> hfr(n), hre(n), hd((size_t)n * kSlots), pts((size_t)NPF * pair_cap_ * kSlots, R(0));
+    const size_t stride = (size_t)pair_cap_ * kSlots;
+    for (int p = 0; p < n; p++) {
+        hfr[p] = R(fr[p]);
+        hre[p] = R(re[p]);
+        for (int k = 0; k < kSlots; k++) {
+            const double* o = slots + ((size_t)p * kSlots + k) * 19;
+            const size_t s = (size_t)p * kSlots + k;
+            hd[s] = R(o[12]);
+            for (int g = 0; g < 4; g++) for (int d = 0; d < 3; d++) pts[(size_t)(g * 3 + d) * stride + s] = R(o[g * 3 + d]);
+            for (int g = 4; g < 6; g++) for (int d = 0; d < 3; d++) pts[(size_t)(g * 3 + d) * stride + s] = R(o[13 + (g - 4) * 3 + d]);
+        }
+    }
+    if (n) {
+        PE_CK(cudaMemcpyAsync(res_a_.p, a, n * sizeof(int), cudaMemcpyHostToDevice, st_));
+        PE_CK(cudaMemcpyAsync(res_b_.p, b, n * sizeof(int), cudaMemcpyHostToDevice, st_));
+        PE_CK(cudaMemcpyAsync(res_np_.p, ps, n * sizeof(int), cudaMemcpyHostToDevice, st_));
+        PE_CK(cudaMemcpyAsync(res_fr_.p, hfr.data(), n * sizeof(R), cudaMemcpyHostToDevice, st_));
+        PE_CK(cudaMemcpyAsync(res_re_.p, hre.data(), n * sizeof(R), cudaMemcpyHostToDevice, st_));
+        PE_CK(cudaMemcpyAsync(res_dist_[cur_dist_].p, hd.data(), hd.size() * sizeof(R), cudaMemcpyHostToDevice, st_));
+        PE_CK(cudaMemcpyAsync(res_pts_.p, pts.data(), pts.size() * sizeof(R), cudaMemcpyHostToDevice, st_));
+    }
+    PE_CK(cudaMemcpyAsync(res_scene_off_.p, off.data(), (NS_ + 1) * sizeof(int), cudaMemcpyHostToDevice, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+    R_ = n;
+}
+
+} // namespace pe

@@ -1,0 +1,253 @@
+"""Python binding of the GB300 rigid-body step (ctypes over include/pe_gpu.h).
+
+``GpuWorld`` mirrors pe_intf::World (src/intf/world.h): it is built from a ``Scene``
+(shapes + bodies, see ``scene.py``), stepped with ``step()``, and exposes the reference's
+phase boundaries (integrate / broadphase / narrowphase / solve) for phase-by-phase use.
+The CUDA library is required: loading fails loudly when it is missing or no GPU is present.
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .scene import Scene  # noqa: F401
+
+PKG = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG / "lib" / "libpe_gpu.so"
+HEADER = PKG.parent / "include" / "pe_gpu.h"
+
+SERIAL_ORDER, COLORED = 0, 1
+_lib = None
+
+
+class PeGpuError(RuntimeError):
+    pass
+
+
+def load(build_if_missing: bool = True):
+    """Load libpe_gpu.so (building it in-tree first when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        if not build_if_missing:
+            raise PeGpuError(f"{LIB_PATH} is missing; run physics-engine_gb300/pe_gb300/build.py")
+        from .build import build
+        build()
+    lib = C.CDLL(str(LIB_PATH))
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    sig = {
+        "pe_gpu_create": (I, [C.c_void_p, C.POINTER(P)]),
+        "pe_gpu_destroy": (I, [P]),
+        "pe_gpu_last_error": (C.c_char_p, [P]),
+        "pe_gpu_set_shapes": (I, [P, I, ip, dp, ip, ip, ip, ip, I, dp, I, ip, ip]),
+        "pe_gpu_set_bodies": (I, [P, I, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, dp]),
+        "pe_gpu_set_scenes": (I, [P, I, ip]),
+        "pe_gpu_set_params": (I, [P, D, D, D, D, I]),
+        "pe_gpu_step": (I, [P, I, I]),
+        "pe_gpu_integrate": (I, [P]),
+        "pe_gpu_broadphase": (I, [P, C.POINTER(I)]),
+        "pe_gpu_narrowphase": (I, [P]),
+        "pe_gpu_solve": (I, [P, I]),
+        "pe_gpu_n_bodies": (I, [P]), "pe_gpu_n_pairs": (I, [P]), "pe_gpu_n_results": (I, [P]),
+        "pe_gpu_get_state": (I, [P] + [P] * 7),
+        "pe_gpu_set_state": (I, [P] + [P] * 7),
+        "pe_gpu_get_axes": (I, [P, ip]), "pe_gpu_set_axes": (I, [P, ip]),
+        "pe_gpu_get_pairs": (I, [P, ip]), "pe_gpu_set_pairs": (I, [P, I, ip]),
+        "pe_gpu_get_results": (I, [P, ip, ip, ip, dp, dp, dp]),
+        "pe_gpu_set_results": (I, [P, I, ip, ip, ip, dp, dp, dp]),
+        "pe_gpu_phase_times": (I, [P, dp, I]),
+        "pe_gpu_last_counts": (I, [P, ip]),
+        "pe_gpu_sync": (I, [P]),
+        "pe_gpu_set_profiling": (I, [P, I]),
+        "pe_gpu_kernel_count": (I, []),
+        "pe_gpu_kernel_name": (C.c_char_p, [I]),
+        "pe_gpu_kernel_stats": (I, [P, dp, np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+    _lib = lib
+    return lib
+
+
+class _Config(C.Structure):
+    _fields_ = [("real_bits", C.c_int), ("device", C.c_int)]
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, np.float64)
+    return a.reshape(shape) if shape is not None else a
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, np.int32)
+
+
+class GpuWorld:
+    """A device-resident world (or batch of independent scenes) on one GPU."""
+
+    def __init__(self, scene, real_bits=64, device=0, scenes=None):
+        self.lib = load()
+        self.h = C.c_void_p()
+        cfg = _Config(real_bits, device)
+        rc = self.lib.pe_gpu_create(C.byref(cfg), C.byref(self.h))
+        if rc != 0:
+            raise PeGpuError(f"pe_gpu_create failed ({rc}): no usable CUDA device?")
+        self.real_bits = real_bits
+        s = scene
+        self._ck(self.lib.pe_gpu_set_shapes(
+            self.h, s.n_shapes, _i32(s.shape_type), _f64(s.shape_param).ravel(), _i32(s.hull_vbeg), _i32(s.hull_vcnt),
+            _i32(s.hull_fbeg), _i32(s.hull_fcnt), len(s.hull_verts), _f64(s.hull_verts).ravel() if len(s.hull_verts) else np.zeros(1),
+            len(s.hull_face_off) - 1, _i32(s.hull_face_off), _i32(s.hull_face_idx) if len(s.hull_face_idx) else np.zeros(1, np.int32)))
+        self._ck(self.lib.pe_gpu_set_bodies(
+            self.h, s.n_bodies, _i32(s.body_shape), _i32(s.body_flags), _f64(s.mass), _f64(s.friction), _f64(s.restitution),
+            _f64(s.lin_damp), _f64(s.ang_damp), _f64(s.origin).ravel(), _f64(s.basis).ravel(), _f64(s.lin_vel).ravel(),
+            _f64(s.ang_vel).ravel()))
+        self._ck(self.lib.pe_gpu_set_params(self.h, float(s.dt), *map(float, s.gravity), int(s.iterations)))
+        if scenes is not None:
+            self.set_scenes(scenes)
+
+    def _ck(self, rc):
+        if rc != 0:
+            msg = self.lib.pe_gpu_last_error(self.h)
+            raise PeGpuError(f"pe_gpu call failed ({rc}): {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.pe_gpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- stepping
+    def set_scenes(self, body_off):
+        off = _i32(body_off)
+        self._ck(self.lib.pe_gpu_set_scenes(self.h, len(off) - 1, off))
+
+    def step(self, k=1, mode=COLORED):
+        self._ck(self.lib.pe_gpu_step(self.h, int(k), int(mode)))
+
+    def integrate(self):
+        self._ck(self.lib.pe_gpu_integrate(self.h))
+
+    def broadphase(self):
+        n = C.c_int(0)
+        self._ck(self.lib.pe_gpu_broadphase(self.h, C.byref(n)))
+        return n.value
+
+    def narrowphase(self):
+        self._ck(self.lib.pe_gpu_narrowphase(self.h))
+
+    def solve(self, mode=SERIAL_ORDER):
+        self._ck(self.lib.pe_gpu_solve(self.h, int(mode)))
+
+    def sync(self):
+        self._ck(self.lib.pe_gpu_sync(self.h))
+
+    # ---------------------------------------------------------------- state
+    @property
+    def n(self):
+        return self.lib.pe_gpu_n_bodies(self.h)
+
+    STATE_FIELDS = (("origin", 3), ("basis", 9), ("lin_vel", 3), ("ang_vel", 3), ("aabb_min", 3), ("aabb_max", 3),
+                    ("world_inv_inertia", 9))
+
+    def state(self, fields=None):
+        """Body state as float64 arrays; ``fields`` limits the transfer to the named fields."""
+        N = self.n
+        out, ptrs = {}, []
+        for name, k in self.STATE_FIELDS:
+            if fields is None or name in fields:
+                a = np.zeros((N, 3, 3) if k == 9 else (N, 3))
+                out[name] = a
+                ptrs.append(a.ctypes.data_as(C.c_void_p))
+            else:
+                ptrs.append(None)
+        self._ck(self.lib.pe_gpu_get_state(self.h, *ptrs))
+        return out
+
+    def set_state(self, d):
+        """Overwrite the given body-state fields (missing keys are left untouched)."""
+        keep, ptrs = [], []
+        for name, k in self.STATE_FIELDS:
+            if name in d and d[name] is not None:
+                a = _f64(d[name]).reshape(-1)
+                keep.append(a)
+                ptrs.append(a.ctypes.data_as(C.c_void_p))
+            else:
+                ptrs.append(None)
+        self._ck(self.lib.pe_gpu_set_state(self.h, *ptrs))
+
+    def axes(self, n_scenes=1):
+        out = np.zeros(n_scenes, np.int32)
+        self._ck(self.lib.pe_gpu_get_axes(self.h, out))
+        return out
+
+    def set_axes(self, axes):
+        self._ck(self.lib.pe_gpu_set_axes(self.h, _i32(np.atleast_1d(axes))))
+
+    @property
+    def axis(self):
+        return int(self.axes(1)[0])
+
+    @axis.setter
+    def axis(self, a):
+        self.set_axes([a])
+
+    def pairs(self):
+        P = self.lib.pe_gpu_n_pairs(self.h)
+        out = np.zeros((max(P, 1), 2), np.int32)
+        self._ck(self.lib.pe_gpu_get_pairs(self.h, out.reshape(-1)))
+        return out[:P]
+
+    def set_pairs(self, p):
+        p = _i32(p).reshape(-1, 2)
+        self._ck(self.lib.pe_gpu_set_pairs(self.h, len(p), p.reshape(-1) if len(p) else np.zeros(2, np.int32)))
+
+    def results(self):
+        R = self.lib.pe_gpu_n_results(self.h)
+        n = max(R, 1)
+        a, b, ps = (np.zeros(n, np.int32) for _ in range(3))
+        fr, re = np.zeros(n), np.zeros(n)
+        slots = np.zeros((n, 8, 19))
+        self._ck(self.lib.pe_gpu_get_results(self.h, a, b, ps, fr, re, slots.reshape(-1)))
+        valid = np.array([(1 << k) - 1 for k in ps[:R]], np.int32) if R else np.zeros(0, np.int32)
+        return dict(res_a=a[:R], res_b=b[:R], point_size=ps[:R], friction=fr[:R], restitution=re[:R], slots=slots[:R],
+                    valid_mask=valid)
+
+    def set_results(self, d):
+        R = len(d["res_a"])
+        if R == 0:
+            z = np.zeros(1, np.int32)
+            self._ck(self.lib.pe_gpu_set_results(self.h, 0, z, z, z, np.zeros(1), np.zeros(1), np.zeros(19 * 8)))
+            return
+        self._ck(self.lib.pe_gpu_set_results(self.h, R, _i32(d["res_a"]), _i32(d["res_b"]), _i32(d["point_size"]),
+                                             _f64(d["friction"]), _f64(d["restitution"]), _f64(d["slots"]).reshape(-1)))
+
+    def phase_times(self, reset=False):
+        ms = np.zeros(5)
+        self._ck(self.lib.pe_gpu_phase_times(self.h, ms, int(reset)))
+        return dict(integrate=ms[0], broadphase=ms[1], narrowphase=ms[2], solver=ms[3], step=ms[4])
+
+    def last_counts(self):
+        c = np.zeros(6, np.int32)
+        self._ck(self.lib.pe_gpu_last_counts(self.h, c))
+        return dict(pairs=int(c[0]), active=int(c[1]), rows=int(c[2]), colors=int(c[3]), launches=int(c[4]))
+
+    def set_profiling(self, on=True):
+        self._ck(self.lib.pe_gpu_set_profiling(self.h, int(bool(on))))
+
+    def kernel_stats(self):
+        """{kernel group: (device ms, launches)} accumulated while profiling was on."""
+        n = self.lib.pe_gpu_kernel_count()
+        ms = np.zeros(n)
+        cnt = np.zeros(n, np.int64)
+        self._ck(self.lib.pe_gpu_kernel_stats(self.h, ms, cnt))
+        return {self.lib.pe_gpu_kernel_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(n)}

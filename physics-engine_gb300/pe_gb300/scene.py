@@ -369,3 +369,42 @@ def pair_zoo(kind_a, kind_b, m=64, seed=0, spacing=20.0, real_bits=64, hull_rang
             _random_body(sb, rng, kind, o, 1000.0, rot[k], (0.0, 0.0, 0.0), (0.0, 0.0, 0.0),
                          friction=0.5, restitution=0.2, hull_range=hull_range)
     return sb.build(real_bits)
+
+
+def concat(scenes):
+    """Scenes side by side in one Scene (bodies of scene i at [off[i], off[i+1])); shapes are
+    concatenated and re-indexed.  Used for batched stepping of independent scenes."""
+    first = scenes[0]
+    out = Scene(dt=first.dt, gravity=first.gravity, iterations=first.iterations, real_bits=first.real_bits)
+    sh_base = vb = fb = ib = 0
+    cols = {k: [] for k in ("shape_type", "shape_param", "hull_vbeg", "hull_vcnt", "hull_fbeg", "hull_fcnt", "hull_verts",
+                            "hull_face_idx", "body_shape", "body_flags", "mass", "friction", "restitution", "lin_damp",
+                            "ang_damp", "origin", "basis", "lin_vel", "ang_vel")}
+    face_off = [0]
+    offs = [0]
+    for s in scenes:
+        if (s.dt, tuple(s.gravity), s.iterations) != (first.dt, tuple(first.gravity), first.iterations):
+            raise ValueError("batched scenes must share dt, gravity and iterations")
+        cols["shape_type"].append(s.shape_type)
+        cols["shape_param"].append(s.shape_param)
+        cols["hull_vbeg"].append(s.hull_vbeg + vb)
+        cols["hull_vcnt"].append(s.hull_vcnt)
+        cols["hull_fbeg"].append(s.hull_fbeg + fb)
+        cols["hull_fcnt"].append(s.hull_fcnt)
+        cols["hull_verts"].append(s.hull_verts)
+        cols["hull_face_idx"].append(s.hull_face_idx)
+        face_off.extend((s.hull_face_off[1:] + ib).tolist())
+        cols["body_shape"].append(s.body_shape + sh_base)
+        for k in ("body_flags", "mass", "friction", "restitution", "lin_damp", "ang_damp", "origin", "basis", "lin_vel",
+                  "ang_vel"):
+            cols[k].append(getattr(s, k))
+        sh_base += s.n_shapes
+        vb += len(s.hull_verts)
+        fb += len(s.hull_face_off) - 1
+        ib += len(s.hull_face_idx)
+        offs.append(offs[-1] + s.n_bodies)
+    for k, v in cols.items():
+        setattr(out, k, np.concatenate(v))
+    out.hull_verts = out.hull_verts.reshape(-1, 3)
+    out.hull_face_off = np.array(face_off, np.int32)
+    return out, np.array(offs, np.int32)

@@ -1,0 +1,71 @@
+"""Generate the golden fixtures of tests/golden/ by running the reference engine itself.
+
+The reference is compiled from its own sources by oracle/build_ref.py (only possible where
+those sources exist); each fixture stores a seeded synthetic scene and the reference's
+phase records (state seen by the broadphase, ordered pairs, all contact-result cache slots,
+post-solve velocities) for chosen steps.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT / "physics-engine_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+from pe_gb300 import scene as sc  # noqa: E402
+import pedump  # noqa: E402
+import build_ref  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+FIELDS = ["origin", "basis", "lin_vel", "ang_vel", "aabb_min", "aabb_max", "world_inv_inertia", "pairs", "res_a",
+          "res_b", "point_size", "valid_mask", "friction", "restitution", "slots", "lin_vel_post", "ang_vel_post"]
+
+# name -> (scene factory, real bits, steps to run, steps to record)
+CASES = {
+    "tower3_f64": (lambda: sc.tower(nx=3, ny=3, nz=3, real_bits=64), 64, 60, [0, 1, 2, 20, 21, 58, 59]),
+    "tower3_f32": (lambda: sc.tower(nx=3, ny=3, nz=3, real_bits=32), 32, 60, [0, 1, 2, 20, 21, 58, 59]),
+    "cube_f32": (lambda: sc.random_cube(n=400, seed=11, extent=12.0, real_bits=32), 32, 2, [0, 1]),
+    "cube_f64": (lambda: sc.random_cube(n=400, seed=12, extent=12.0, real_bits=64), 64, 2, [0, 1]),
+    "pile_f64": (lambda: sc.pile(48, seed=5, real_bits=64, hull_range=(8, 24), drop=(0.0, 0.3)), 64, 40,
+                 [0, 1, 24, 25, 38, 39]),
+    "pile_f32": (lambda: sc.pile(48, seed=6, real_bits=32, hull_range=(8, 24), drop=(0.0, 0.3)), 32, 40,
+                 [0, 1, 24, 25, 38, 39]),
+}
+for a in range(4):
+    for b in range(a, 4):
+        CASES[f"zoo_{a}{b}_f64"] = (lambda a=a, b=b: sc.pair_zoo(a, b, m=48, seed=100 + 4 * a + b, real_bits=64), 64, 2, [0, 1])
+for a, b in ((0, 0), (0, 2), (2, 2), (2, 3), (3, 3)):
+    CASES[f"zoo_{a}{b}_f32"] = (lambda a=a, b=b: sc.pair_zoo(a, b, m=48, seed=200 + 4 * a + b, real_bits=32), 32, 2, [0, 1])
+
+
+def make(name, ref_dir):
+    factory, bits, steps, rec = CASES[name]
+    scene = factory()
+    with tempfile.TemporaryDirectory() as td:
+        sp = Path(td) / "s.pescene"
+        dp = Path(td) / "d.pedump"
+        scene.write(sp)
+        exe = ref_dir / f"ref_harness{bits}"
+        subprocess.run([str(exe), str(sp), str(dp), str(steps), "2", *map(str, rec)], check=True, capture_output=True)
+        dumps = pedump.read(dp)
+        arrays = {"scene": np.frombuffer(sp.read_bytes(), np.uint8), "bits": np.array(bits), "steps": np.array(steps),
+                  "recorded": np.array([d["step"] for d in dumps])}
+        for d in dumps:
+            for f in FIELDS:
+                arrays[f"s{d['step']}_{f}"] = d[f]
+            arrays[f"s{d['step']}_axis"] = np.array([d["axis_before"], d["axis_after"]])
+        np.savez_compressed(OUT / f"{name}.npz", **arrays)
+    return sum(len(d["pairs"]) for d in dumps), sum(int(d["point_size"].sum()) for d in dumps)
+
+
+if __name__ == "__main__":
+    build_ref.build(Path("/root/reference"), 8)
+    for name in sorted(CASES):
+        p, c = make(name, build_ref.OUT)
+        print(f"{name}: pairs {p} contact points {c}")

@@ -1,0 +1,72 @@
+"""Shared helpers of the test-suite: golden fixtures and result comparison."""
+import io
+from pathlib import Path
+
+import numpy as np
+
+from pe_gb300.scene import Scene
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+STATE_KEYS = ["origin", "basis", "lin_vel", "ang_vel", "aabb_min", "aabb_max", "world_inv_inertia"]
+RESULT_KEYS = ["res_a", "res_b", "point_size", "valid_mask", "friction", "restitution", "slots"]
+
+
+def golden_names():
+    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+
+
+def load_golden(name):
+    z = np.load(GOLDEN / f"{name}.npz")
+    bits = int(z["bits"])
+    import tempfile, os
+    fd, path = tempfile.mkstemp(suffix=".pescene")
+    os.close(fd)
+    try:
+        Path(path).write_bytes(z["scene"].tobytes())
+        scene = Scene.read(path, real_bits=bits)
+    finally:
+        os.unlink(path)
+    steps = {}
+    for k in z["recorded"]:
+        d = {f: z[f"s{k}_{f}"] for f in STATE_KEYS + RESULT_KEYS + ["pairs", "lin_vel_post", "ang_vel_post"]}
+        d["axis_before"], d["axis_after"] = (int(x) for x in z[f"s{k}_axis"])
+        steps[int(k)] = d
+    return scene, bits, int(z["steps"]), steps
+
+
+def results_of(d):
+    return {k: d[k] for k in RESULT_KEYS}
+
+
+def slot_masks(point_size):
+    full = np.arange(8)[None, :] < np.asarray(point_size)[:, None]
+    return full
+
+
+def compare_results(got, ref, rtol=0.0, atol=0.0, what=""):
+    """Contact results: bodies, counts, point slots (all fields below point_size, the carried
+    distance of the remaining slots).  rtol = atol = 0 means bitwise equality."""
+    assert len(got["res_a"]) == len(ref["res_a"]), f"{what}: result count {len(got['res_a'])} != {len(ref['res_a'])}"
+    assert np.array_equal(got["res_a"], ref["res_a"]) and np.array_equal(got["res_b"], ref["res_b"]), f"{what}: bodies differ"
+    bad = np.nonzero(got["point_size"] != ref["point_size"])[0]
+    assert len(bad) == 0, f"{what}: point counts differ at results {bad[:10]}: {got['point_size'][bad[:10]]} vs {ref['point_size'][bad[:10]]}"
+    m = slot_masks(ref["point_size"])
+    g, r = got["slots"][m], ref["slots"][m]
+    if rtol == 0 and atol == 0:
+        diff = np.argwhere(g != r)
+        assert len(diff) == 0, f"{what}: {len(diff)} slot values differ; first at {diff[:3]}: {g[tuple(diff[0])]} vs {r[tuple(diff[0])]}"
+        assert np.array_equal(got["slots"][~m][:, 12], ref["slots"][~m][:, 12]), f"{what}: carried slot distances differ"
+    else:
+        np.testing.assert_allclose(g, r, rtol=rtol, atol=atol, err_msg=what)
+    np.testing.assert_array_equal(got["friction"], ref["friction"])
+    np.testing.assert_array_equal(got["restitution"], ref["restitution"])
+
+
+def compare_state(got, ref, keys=STATE_KEYS, what=""):
+    for k in keys:
+        diff = np.argwhere(np.asarray(got[k]) != np.asarray(ref[k]))
+        assert len(diff) == 0, f"{what}: {k} differs at {diff[:3]} ({np.asarray(got[k])[tuple(diff[0])]} vs {np.asarray(ref[k])[tuple(diff[0])]})"
+
+
+def dump_state(d):
+    return {k: d[k] for k in STATE_KEYS}

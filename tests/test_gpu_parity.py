@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's recorded outputs
+(golden fixtures) and against the oracle on seeded scenes, phase by phase and step by step.
+Integer outputs (pair sets, contact counts) must match exactly; the arithmetic reproduces the
+reference's operation order, so real-valued outputs are compared bit for bit as well, with
+the documented tolerance (1e-5 relative for contact geometry, 1e-6 for solved velocities)
+used only where an operation order differs by design."""
+import numpy as np
+import pytest
+
+import orc
+import pe_gb300 as pg
+from pe_gb300 import scene as sc
+from pe_testlib import compare_results, compare_state, dump_state, golden_names, load_golden, results_of
+
+pytestmark = pytest.mark.gpu
+
+
+def keys_tie_free(d, axis):
+    k = d["aabb_min"][:, axis]
+    return len(np.unique(k)) == len(k)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_gpu_phases_match_reference(name):
+    scene, bits, steps, rec = load_golden(name)
+    g = pg.GpuWorld(scene, bits)
+    for k in sorted(rec):
+        d = rec[k]
+        # broadphase: the pair set exactly; the order too when no two sort keys tie
+        g.set_state(dump_state(d))
+        g.axis = d["axis_before"]
+        g.broadphase()
+        got = g.pairs()
+        ref = d["pairs"]
+        assert sorted(map(tuple, np.sort(got, axis=1))) == sorted(map(tuple, np.sort(ref, axis=1))), f"{name} step {k}: pair sets differ"
+        if keys_tie_free(d, d["axis_before"]):
+            np.testing.assert_array_equal(got, ref)
+        # narrowphase on the reference's pairs with the previous step's pooled results
+        if k - 1 in rec:
+            g.set_results(results_of(rec[k - 1]))
+            g.set_pairs(ref)
+            g.narrowphase()
+            compare_results(g.results(), results_of(d), what=f"{name} narrowphase step {k}")
+        # serial-order solver on the reference's contact results
+        g.set_state(dump_state(d))
+        g.set_results(results_of(d))
+        g.solve(pg.SERIAL_ORDER)
+        st = g.state()
+        np.testing.assert_array_equal(st["lin_vel"], d["lin_vel_post"], err_msg=f"{name} solve step {k}")
+        np.testing.assert_array_equal(st["ang_vel"], d["ang_vel_post"], err_msg=f"{name} solve step {k}")
+        # integration from the previous step's end state
+        if k - 1 in rec:
+            p = rec[k - 1]
+            s0 = dump_state(p)
+            s0["lin_vel"], s0["ang_vel"] = p["lin_vel_post"], p["ang_vel_post"]
+            g.set_state(s0)
+            g.integrate()
+            compare_state(g.state(), dump_state(d), what=f"{name} integrate step {k}")
+
+
+@pytest.mark.parametrize("name", ["cube_f32", "cube_f64", "zoo_22_f64", "zoo_23_f32", "zoo_33_f64", "pile_f64"])
+def test_gpu_full_steps_serial_order_match_reference(name):
+    """Whole steps on the device in serial-order mode reproduce the reference trajectory
+    (scenes whose sort keys never tie, so the broadphase order is the reference's)."""
+    scene, bits, steps, rec = load_golden(name)
+    g = pg.GpuWorld(scene, bits)
+    done = 0
+    for k in sorted(rec):
+        g.step(k + 1 - done, pg.SERIAL_ORDER)
+        done = k + 1
+        d = rec[k]
+        st = g.state()
+        compare_state(st, dump_state(d), keys=["origin", "basis", "aabb_min", "aabb_max", "world_inv_inertia"], what=f"{name} step {k}")
+        np.testing.assert_array_equal(st["lin_vel"], d["lin_vel_post"])
+        np.testing.assert_array_equal(g.pairs(), d["pairs"])
+        compare_results(g.results(), results_of(d), what=f"{name} step {k}")
+
+
+def test_gpu_stress_scene_broadphase_and_narrowphase_match_oracle():
+    """65,536 mixed bodies in a 100 m cube (one-step stress): integration bit-exact, the
+    pair set exact, and every contact result exact given the oracle's pair order."""
+    scene = sc.random_cube(n=65536, seed=7, real_bits=32)
+    o = orc.OracleWorld(scene, 32, threads=8)
+    g = pg.GpuWorld(scene, 32)
+    o.integrate()
+    g.integrate()
+    compare_state(g.state(), o.state(), what="integrate")
+    o.broadphase()
+    g.broadphase()
+    po, pgpu = o.pairs(), g.pairs()
+    assert len(po) > 50000
+    so = np.sort(np.sort(po, axis=1).view([("a", np.int32), ("b", np.int32)]).ravel(), order=["a", "b"])
+    sg = np.sort(np.sort(pgpu, axis=1).view([("a", np.int32), ("b", np.int32)]).ravel(), order=["a", "b"])
+    np.testing.assert_array_equal(so, sg)
+    assert o.axis == g.axis
+    o.narrowphase()
+    g.set_pairs(po)
+    g.narrowphase()
+    ro = o.results()
+    assert ro["point_size"].sum() > 30000
+    compare_results(g.results(), ro, what="stress narrowphase")
+    o.solve()
+    g.solve(pg.SERIAL_ORDER)
+    so_, sg_ = o.state(), g.state()
+    np.testing.assert_array_equal(sg_["lin_vel"], so_["lin_vel"])
+    np.testing.assert_array_equal(sg_["ang_vel"], so_["ang_vel"])
+
+
+def test_gpu_tower_serial_order_per_step_replay():
+    """The 1,002-body tower in double precision: from identical state, one GPU step with the
+    oracle's pair order (ties among the sort keys make the order a property of the host
+    sort) gives the oracle's state after the step."""
+    scene = sc.tower(real_bits=64)
+    o = orc.OracleWorld(scene, 64)
+    g = pg.GpuWorld(scene, 64)
+    o.step(5)
+    g.set_state(o.state())
+    g.set_results(o.results())
+    g.axis = o.axis
+    for _ in range(3):
+        g.integrate()
+        o.integrate()
+        compare_state(g.state(), o.state(), what="tower integrate")
+        g.axis = o.axis
+        g.broadphase()
+        o.broadphase()
+        assert sorted(map(tuple, np.sort(g.pairs(), axis=1))) == sorted(map(tuple, np.sort(o.pairs(), axis=1)))
+        g.set_pairs(o.pairs())
+        g.narrowphase()
+        o.narrowphase()
+        compare_results(g.results(), o.results(), what="tower narrowphase")
+        g.solve(pg.SERIAL_ORDER)
+        o.solve()
+        compare_state(g.state(), o.state(), keys=["lin_vel", "ang_vel"], what="tower solve")
+
+
+def test_gpu_batched_scenes_equal_scenes_alone():
+    """Independent scenes stepped in one batch give, per scene, exactly what each scene gives
+    alone (serial-order and coloured modes)."""
+    parts = [sc.pile(n, seed=s, real_bits=32, hull_range=(8, 16), drop=(0.0, 0.5)) for n, s in ((20, 1), (35, 2), (9, 3))]
+    merged, offs = sc.concat(parts)
+    for mode in (pg.SERIAL_ORDER, pg.COLORED):
+        g = pg.GpuWorld(merged, 32, scenes=offs)
+        g.step(40, mode)
+        big = g.state()
+        for i, p in enumerate(parts):
+            a = pg.GpuWorld(p, 32)
+            a.step(40, mode)
+            alone = a.state()
+            sl = slice(offs[i], offs[i + 1])
+            for k in ("origin", "basis", "lin_vel", "ang_vel"):
+                np.testing.assert_array_equal(big[k][sl], alone[k], err_msg=f"scene {i} {k} mode {mode}")
+
+
+def test_gpu_colored_tower_stays_physical():
+    """Coloured Gauss-Seidel on the tower hit by the sphere: contacts stay resolved (max
+    penetration bounded like the serial solver's) and nothing gains energy from nowhere."""
+    scene = sc.tower(real_bits=32)
+    g = pg.GpuWorld(scene, 32)
+    g.step(60, pg.COLORED)
+    st = g.state()
+    boxes = slice(1, 1001)
+    assert np.all(np.isfinite(st["origin"]))
+    # resting boxes below the impact height keep their layer height (no sinking, no jumping)
+    y = st["origin"][boxes, 1]
+    assert y.min() > 0.45
+    assert np.abs(st["lin_vel"][boxes]).max() < 40.0
+    r = g.results()
+    depth = [r["slots"][i, :n, 12].min() for i, n in enumerate(r["point_size"]) if n]
+    assert min(depth) > -0.05
