@@ -68,10 +68,7 @@ class L2Flush:
     """Writes a buffer larger than L2 (129 MB) between timed steps."""
 
     def __init__(self, nbytes=256 << 20):
-        try:
-            self.rt = ctypes.CDLL("libcudart.so")
-        except OSError:
-            self.rt = ctypes.CDLL("/usr/local/cuda/lib64/libcudart.so")
+        self.rt = _cudart()
         self.p = ctypes.c_void_p()
         self.n = nbytes
         if self.rt.cudaMalloc(ctypes.byref(self.p), ctypes.c_size_t(nbytes)) != 0:
@@ -82,18 +79,69 @@ class L2Flush:
         self.rt.cudaDeviceSynchronize()
 
 
+def _cudart():
+    try:
+        return ctypes.CDLL("libcudart.so")
+    except OSError:
+        return ctypes.CDLL("/usr/local/cuda/lib64/libcudart.so")
+
+
+def _pci_bus_id(device):
+    """PCI bus id of a CUDA device (so that NVML samples the GPU this process runs on)."""
+    buf = ctypes.create_string_buffer(64)
+    if _cudart().cudaDeviceGetPCIBusId(buf, 64, device) != 0:
+        return b""
+    return buf.value
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+    """SM clocks and clock-event (throttle) reasons sampled while the timed region runs.
+
+    Reads NVML directly (libnvidia-ml, read-only queries) every 10 ms from a thread, so that a
+    timed region of a few tens of milliseconds still gets samples; falls back to
+    `nvidia-smi -lms 200` when NVML cannot be loaded."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
 
-    def __init__(self, device):
+    def __init__(self, device, period_s=0.01):
         self.device = device
+        self.period = period_s
         self.proc = None
+        self.nvml = None
+        self.samples = []
+        self.lines = []
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() == 0:
+                h = ctypes.c_void_p()
+                if lib.nvmlDeviceGetHandleByPciBusId_v2(_pci_bus_id(device), ctypes.byref(h)) == 0 or \
+                        lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device), ctypes.byref(h)) == 0:
+                    self.nvml, self.handle = lib, h
+        except (OSError, AttributeError):
+            self.nvml = None
+
+    def _poll(self):
+        lib, h = self.nvml, self.handle
+        clk, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and get_reasons(h, ctypes.byref(rs)) == 0:
+                self.samples.append((clk.value, mx.value, rs.value))
+            self.stop.wait(self.period)
 
     def __enter__(self):
+        if self.nvml is not None:
+            self.stop = threading.Event()
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
@@ -102,7 +150,10 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
-        self.lines = []
+        if self.nvml is not None:
+            self.stop.set()
+            self.thread.join()
+            return
         if self.proc:
             self.proc.terminate()
             try:
@@ -113,22 +164,30 @@ class ClockSampler:
             self.lines = [l for l in out.splitlines() if l.strip()]
 
     def summary(self):
-        if not getattr(self, "lines", None):
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
-            f = [x.strip() for x in l.split(",")]
-            try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
-            except (ValueError, IndexError):
-                continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        if self.samples:
+            for c, m, r in self.samples:
+                sm.append(float(c))
+                smax.append(float(m))
+                reasons.update(n for bit, n in self.REASONS.items() if r & bit)
+            src = "nvml, 10 ms"
+        else:
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for l in self.lines:
+                f = [x.strip() for x in l.split(",")]
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                except (ValueError, IndexError):
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+            src = "nvidia-smi, 200 ms"
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "source": src}
 
 
 def measured_peak():
@@ -172,8 +231,11 @@ def algorithmic_bytes(counts, n_bodies, iters, real_bytes):
     }
 
 
-KERNEL_BYTES_KEY = {"integrate": "integrate", "radix_sort": "bp_sort", "bp_sweep": "bp_sweep", "narrowphase": "narrowphase",
-                    "si_setup": "si_setup", "si_colored": "si_colored", "si_serial": "si_serial"}
+# kernel groups (as reported by pe_gpu_kernel_stats) whose algorithmic bytes are one entry above;
+# the narrowphase's per-class thread kernels and its warp-per-pair SAT kernel share the pair bytes
+KERNEL_GROUPS = {"integrate": ("integrate",), "bp_sort": ("radix_sort",), "bp_sweep": ("bp_sweep",),
+                 "narrowphase": ("narrowphase", "np_sat"), "si_setup": ("si_setup",), "si_colored": ("si_colored",),
+                 "si_serial": ("si_serial",)}
 
 
 # ------------------------------------------------------------------ our arm
@@ -203,13 +265,16 @@ def run_ours(args, rank, world, device):
     g.step(1, mode)
     g.set_profiling(False)
     ks = g.kernel_stats()
-    dom = max((k for k in ks if k in KERNEL_BYTES_KEY), key=lambda k: ks[k][0])
-    dom_ms, dom_n = ks[dom]
+    grp = {g: (sum(ks.get(k, (0.0, 0))[0] for k in m), sum(ks.get(k, (0.0, 0))[1] for k in m))
+           for g, m in KERNEL_GROUPS.items()}
+    dom = max(grp, key=lambda g: grp[g][0])
+    dom_ms, dom_n = grp[dom]
     alg = algorithmic_bytes(counts, N, scene.iterations, bits // 8)
-    dom_bytes = alg[KERNEL_BYTES_KEY[dom]]   # bytes of the whole group in one step
+    dom_bytes = alg[dom]   # bytes of the whole group in one step
     peak, peak_kind = measured_peak()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = ncu_traffic().get(dom)
+    tr = ncu_traffic()
+    traffic = sum(tr[k] for k in KERNEL_GROUPS[dom] if k in tr) if any(k in tr for k in KERNEL_GROUPS[dom]) else None
     # end to end through the C ABI with host buffers
     st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
     e2e_times = []

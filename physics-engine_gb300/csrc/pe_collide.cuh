@@ -655,27 +655,10 @@ template <class R> __device__ bool find_sep_axis(Pair<R>& c, V3<R>& sep) {
 
 constexpr int kMaxClip = 64;   // clipped polygon capacity (incident face vertices + one per clip plane)
 
-// clipHullAgainstHull + clipFaceAgainstHull (:63-170)
-template <class R> __device__ void clip_hull_hull(Pair<R>& c, const V3<R>& sep, R min_dist, R max_dist) {
+// clipFaceAgainstHull (:63-131): the incident face fb of B clipped against the side planes of
+// the reference face fa of A; points whose depth under fa lies in [min_dist, max_dist] are kept
+template <class R> __device__ void clip_faces(Pair<R>& c, const V3<R>& sep, R min_dist, R max_dist, int fb, int fa) {
     const R margin = 0;
-    int fb = -1;
-    {
-        R dmax = Lim<R>::min();
-        for (int f = 0; f < c.sb.face_count(); f++) {
-            const R d = dot(mv(c.tb().b, c.sb.face_normal(f)), sep);
-            if (d > dmax) { dmax = d; fb = f; }
-        }
-    }
-    if (fb < 0) return;
-    int fa = -1;
-    {
-        R dmin = Lim<R>::max();
-        for (int f = 0; f < c.sa.face_count(); f++) {
-            const R d = dot(mv(c.ta().b, c.sa.face_normal(f)), sep);
-            if (d < dmin) { dmin = d; fa = f; }
-        }
-    }
-    if (fa < 0) return;
     V3<R> buf[2][kMaxClip];
     int n_in = 0;
     const int nbv = c.sb.face_size(fb);
@@ -721,6 +704,30 @@ template <class R> __device__ void clip_hull_hull(Pair<R>& c, const V3<R>& sep, 
         const R depth = dot(lpn, c.ta().inv_apply(v) - pv);
         if (depth <= max_dist && depth >= min_dist) c.add(sep, v - sep * margin, depth + margin * 2);
     }
+}
+
+// clipHullAgainstHull (:133-170): incident face = first maximum of n_B.sep, reference face =
+// first minimum of n_A.sep
+template <class R> __device__ void clip_hull_hull(Pair<R>& c, const V3<R>& sep, R min_dist, R max_dist) {
+    int fb = -1;
+    {
+        R dmax = Lim<R>::min();
+        for (int f = 0; f < c.sb.face_count(); f++) {
+            const R d = dot(mv(c.tb().b, c.sb.face_normal(f)), sep);
+            if (d > dmax) { dmax = d; fb = f; }
+        }
+    }
+    if (fb < 0) return;
+    int fa = -1;
+    {
+        R dmin = Lim<R>::max();
+        for (int f = 0; f < c.sa.face_count(); f++) {
+            const R d = dot(mv(c.ta().b, c.sa.face_normal(f)), sep);
+            if (d < dmin) { dmin = d; fa = f; }
+        }
+    }
+    if (fa < 0) return;
+    clip_faces(c, sep, min_dist, max_dist, fb, fa);
 }
 
 template <class R> __device__ bool convex_convex(Pair<R>& c) {   // :408-432

@@ -110,12 +110,12 @@ __global__ void k_bp_gather(Bodies<R> B, const uint32_t* order, R* smn, R* smx, 
 
 // BroadPhaseSweepAndPrune::calcCollisionPairs sweep (broad_phase_sweep_and_prune.cpp:24-35)
 // with BroadPhaseBase::validateCollisionPair (broad_phase_base.cpp:5-19).  Pass 0 counts the
-// pairs of each sorted position, pass 1 writes them at the scanned offsets.
+// pairs of each sorted position and keeps the first kStage partners; pass 1 writes the pairs at
+// the scanned offsets, re-sweeping only positions with more than kStage partners.
+constexpr int kStage = 4;
 template <class R>
-__global__ void k_bp_sweep(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
-                           const uint32_t* order, int* count, const int* offset, int2* pairs, int pair_cap, int* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ int sweep_one(int i, int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag,
+                                         const int* sscene, int* stage, int2* out, const uint32_t* order, int pair_cap, int* status) {
     const int sc = sscene[i];
     const int ax = scene_axis[sc];
     const R* amin = smn + (size_t)ax * n;
@@ -123,38 +123,63 @@ __global__ void k_bp_sweep(int n, const int* scene_axis, const R* smn, const R* 
     const R mnx = smn[i], mny = smn[n + i], mnz = smn[2 * (size_t)n + i];
     const R mxx = smx[i], mxy = smx[n + i], mxz = smx[2 * (size_t)n + i];
     const int fi = sflag[i];
-    const bool write = offset != nullptr;
+    if (fi & BF_IGNORE) return 0;
     int c = 0;
-    int base = write ? offset[i] : 0;
-    if (fi & BF_IGNORE) { if (!write) count[i] = 0; return; }
     for (int j = i + 1; j < n; j++) {
-        if (sscene[j] != sc) break;
         if (amin[j] > maxi_ax) break;
+        if (sscene[j] != sc) break;
         const int fj = sflag[j];
         if (fj & BF_IGNORE) continue;
         if ((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) continue;
-        const R jmnx = smn[j], jmny = smn[n + j], jmnz = smn[2 * (size_t)n + j];
-        const R jmxx = smx[j], jmxy = smx[n + j], jmxz = smx[2 * (size_t)n + j];
-        if (mnx > jmxx || jmnx > mxx) continue;
-        if (mny > jmxy || jmny > mxy) continue;
-        if (mnz > jmxz || jmnz > mxz) continue;
-        if (write) {
-            const int p = base + c;
-            if (p < pair_cap) pairs[p] = make_int2((int)order[i], (int)order[j]);
+        if (mnx > smx[j] || smn[j] > mxx) continue;
+        if (mny > smx[n + j] || smn[n + j] > mxy) continue;
+        if (mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz) continue;
+        if (stage && c < kStage) stage[(size_t)i * kStage + c] = j;
+        if (out) {
+            if (c < pair_cap) out[c] = make_int2((int)order[i], (int)order[j]);
             else atomicOr(status, ST_PAIR_OVERFLOW);
         }
         c++;
     }
-    if (!write) count[i] = c;
+    return c;
+}
+
+template <class R>
+__global__ void k_bp_count(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene, int* count,
+                           int* stage) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    count[i] = sweep_one<R>(i, n, scene_axis, smn, smx, sflag, sscene, stage, nullptr, nullptr, 0, nullptr);
+}
+
+template <class R>
+__global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                           const uint32_t* order, const int* offset, const int* stage, int2* pairs, int pair_cap, int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int base = offset[i], c = offset[i + 1] - base;
+    if (c == 0) return;
+    if (base + c > pair_cap) { atomicOr(status, ST_PAIR_OVERFLOW); return; }
+    if (c <= kStage) {
+        const int a = (int)order[i];
+        for (int k = 0; k < c; k++) pairs[base + k] = make_int2(a, (int)order[stage[(size_t)i * kStage + k]]);
+    } else {
+        sweep_one<R>(i, n, scene_axis, smn, smx, sflag, sscene, nullptr, pairs + base, order, c, status);
+    }
 }
 
 // next sweep axis of each scene: the axis of largest AABB-centre variance (sweep_and_prune.cpp:37-40).
-// One block per scene, sums in a fixed tree order.
+// Sums in double in a fixed order (deterministic run to run): per-tile partial sums of the sorted
+// centres, then one thread per scene adds its tiles in order.  A scene below two bodies keeps its
+// axis, as the reference returns before updating it.
+constexpr int kAxisTile = 1024;
 template <class R>
-__global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, int* scene_axis) {
-    const int s = blockIdx.x;
-    const int lo = scene_off[s], hi = scene_off[s + 1];
+__global__ void k_bp_axis_partial(const R* smn, const R* smx, int n, const int* sscene, double* part) {
+    const int t = blockIdx.x;
+    const int lo = t * kAxisTile, hi = min(n, lo + kAxisTile);
     __shared__ double red[6][kBlock];
+    // tiles never mix scenes in the partial: positions are assigned to the scene of the tile's
+    // first element only when the whole tile is one scene; otherwise the combine step rescans
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
         for (int d = 0; d < 3; d++) {
@@ -169,16 +194,37 @@ __global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_of
         if ((int)threadIdx.x < w) for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        const int cnt = hi - lo;
-        if (cnt < 2) return;   // the reference returns before touching the axis
-        double v[3];
-        for (int d = 0; d < 3; d++) v[d] = red[3 + d][0] - red[d][0] * red[d][0] / (double)cnt;
-        int ax = 0;
-        if (v[1] > v[0]) ax = 1;
-        if (v[2] > v[ax]) ax = 2;
-        scene_axis[s] = ax;
+    if (threadIdx.x < 6) part[t * 6 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+template <class R>
+__global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, const double* part, int* scene_axis, int n_scenes) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_scenes) return;
+    const int lo = scene_off[s], hi = scene_off[s + 1];
+    const int cnt = hi - lo;
+    if (cnt < 2) return;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    int k = lo;
+    while (k < hi) {
+        if (k % kAxisTile == 0 && k + kAxisTile <= hi) {   // a whole tile of this scene
+            for (int q = 0; q < 6; q++) acc[q] += part[(k / kAxisTile) * 6 + q];
+            k += kAxisTile;
+        } else {
+            for (int d = 0; d < 3; d++) {
+                const double c = (double)((smn[(size_t)d * n + k] + smx[(size_t)d * n + k]) * R(0.5));
+                acc[d] += c;
+                acc[3 + d] += c * c;
+            }
+            k++;
+        }
     }
+    double v[3];
+    for (int d = 0; d < 3; d++) v[d] = acc[3 + d] - acc[d] * acc[d] / (double)cnt;
+    int ax = 0;
+    if (v[1] > v[0]) ax = 1;
+    if (v[2] > v[ax]) ax = 2;
+    scene_axis[s] = ax;
 }
 
 // ===================================================================== narrowphase
@@ -194,45 +240,39 @@ __global__ void k_np_classify(int P, const int2* pairs, Bodies<R> B, const int* 
 }
 __global__ void k_np_bucket(int P, const int* cls, int* cursor, int* order);
 
-// One thread per pair: SimpleNarrowPhase::calcContactResults body (simple_narrow_phase.cpp:24-41):
-// reset the pooled result, combine materials, dispatch, sort the cache, write the result out.
-// Slot distances of a pooled result persist between steps: slot k of result p starts with
-// the distance that slot had after the previous step's sort when the same (scene-local)
-// result index existed then, and the "fresh result" maximum otherwise.
+// Pair setup of SimpleNarrowPhase::calcContactResults (simple_narrow_phase.cpp:24-38): the pooled
+// result is reset, keeping the distances its slots had after the previous step's sort when the
+// same (scene-local) result index existed then, the "fresh result" maximum otherwise.
 template <class R>
-__global__ void k_np(int P, const int* order, const int* cls, const int2* pairs, Bodies<R> B, ShapeTable<R> S,
-                     Results<R> res, const int* pair_scene_off, const int* prev_off, int cls_lo, int cls_hi) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P) return;
-    const int p = order[t];
-    const int c = cls[p];
-    if (c < cls_lo || c > cls_hi) return;
+__device__ __forceinline__ void np_setup(int p, const int2* pairs, const Bodies<R>& B, const ShapeTable<R>& S, const Results<R>& res,
+                                         const int* pair_scene_off, const int* prev_off, Cache<R>& cache, Pair<R>& pr) {
     const int2 q = pairs[p];
     const int ia = q.x, ib = q.y;
-    Cache<R> cache;
     cache.valid = 0;
     cache.swap = false;
-    {   // stale slot distances of the pooled result
-        const int sc = B.scene[ia];
-        const int local = p - pair_scene_off[sc];
-        if (local < prev_off[sc + 1] - prev_off[sc]) {
-            const int src = (prev_off[sc] + local) * kSlots;
-            for (int k = 0; k < kSlots; k++) cache.dist[k] = res.prev_dist[src + k];
-        } else {
-            for (int k = 0; k < kSlots; k++) cache.dist[k] = Lim<R>::max();
-        }
+    const int sc = B.scene[ia];
+    const int local = p - pair_scene_off[sc];
+    if (local < prev_off[sc + 1] - prev_off[sc]) {
+        const int src = (prev_off[sc] + local) * kSlots;
+        for (int k = 0; k < kSlots; k++) cache.dist[k] = res.prev_dist[src + k];
+    } else {
+        for (int k = 0; k < kSlots; k++) cache.dist[k] = Lim<R>::max();
     }
     cache.ta = B.xf(ia);
     cache.tb = B.xf(ib);
     cache.scale_a = B.at(SCALE, ia);
     cache.scale_b = B.at(SCALE, ib);
-    Pair<R> pr;
     pr.sa = S.view(B.shape[ia]);
     pr.sb = S.view(B.shape[ib]);
     pr.ref_scale = (cache.scale_a + cache.scale_b) * R(0.05);
     pr.c = &cache;
-    collide(pr, c);
-    // ContactResult::sortContactPoints: stable order by distance over all 8 slots
+}
+
+// ContactResult::sortContactPoints (stable order by distance over all 8 slots, size = first
+// invalid slot) and write-out of result p
+template <class R>
+__device__ __forceinline__ void np_finish(int p, const int2* pairs, const Bodies<R>& B, const Results<R>& res, const Cache<R>& cache) {
+    const int2 q = pairs[p];
     int perm[kSlots];
     for (int k = 0; k < kSlots; k++) {
         int j = k;
@@ -242,11 +282,11 @@ __global__ void k_np(int P, const int* order, const int* cls, const int2* pairs,
     }
     int np = kSlots;
     for (int k = 0; k < kSlots; k++) if (!((cache.valid >> perm[k]) & 1u)) { np = k; break; }
-    res.a[p] = ia;
-    res.b[p] = ib;
+    res.a[p] = q.x;
+    res.b[p] = q.y;
     res.npts[p] = np;
-    res.fr[p] = rsqrt_(B.at(FRIC, ia) * B.at(FRIC, ib));
-    res.re[p] = rsqrt_(B.at(REST, ia) * B.at(REST, ib));
+    res.fr[p] = rsqrt_(B.at(FRIC, q.x) * B.at(FRIC, q.y));     // ContactResult::setObjects (contact_result.cpp:80-86)
+    res.re[p] = rsqrt_(B.at(REST, q.x) * B.at(REST, q.y));
     for (int k = 0; k < kSlots; k++) res.dist[p * kSlots + k] = cache.dist[perm[k]];
     for (int k = 0; k < np; k++) {
         const int s = perm[k];
@@ -256,6 +296,383 @@ __global__ void k_np(int P, const int* order, const int* cls, const int2* pairs,
         const V3<R> f[6] = {cache.pos[s], cache.nrm[s], cache.la[s], cache.lb[s], t0, t1};
         for (int g = 0; g < 6; g++) { res.pt(g * 3, o) = f[g].x; res.pt(g * 3 + 1, o) = f[g].y; res.pt(g * 3 + 2, o) = f[g].z; }
     }
+}
+
+// one thread per pair of one algorithm class; `order[lo..hi)` holds that class's pairs
+template <class R, int CLS>
+__global__ void k_np_class(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                           const int* pair_scene_off, const int* prev_off) {
+    const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= hi) return;
+    const int p = order[t];
+    Cache<R> cache;
+    Pair<R> pr;
+    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
+    collide(pr, CLS);
+    np_finish(p, pairs, B, res, cache);
+}
+
+// ---------------------------------------------------------------- warp-cooperative SAT
+// (convex_convex_collision_algorithm.cpp:251-432) for cylinder-cylinder, box-hull and hull-hull:
+// one warp per pair, lanes over candidate axes.  The reference scans axes in order and keeps
+// the first strictly smaller depth; that is the lexicographic minimum of (depth, axis index),
+// which the warp reduces.  Any separating axis ends the test (the reference returns at the
+// first one it meets; what it computed before that is discarded except the corner point).
+template <class R> __device__ __forceinline__ void warp_argmin(R& d, int& idx) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const R od = __shfl_xor_sync(0xffffffffu, d, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (od < d || (od == d && oi < idx)) { d = od; idx = oi; }
+    }
+}
+template <class R> __device__ __forceinline__ void warp_argmax(R& d, int& idx) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const R od = __shfl_xor_sync(0xffffffffu, d, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (od > d || (od == d && oi < idx)) { d = od; idx = oi; }
+    }
+}
+template <class R> __device__ __forceinline__ V3<R> shfl3(const V3<R>& v, int src) {
+    return V3<R>(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src), __shfl_sync(0xffffffffu, v.z, src));
+}
+
+// ---- SAT with per-pair staging: world face normals, world unit edge directions and local hull
+// vertices of both shapes are computed once into shared memory; support intervals are computed
+// first and witness points only for an axis that becomes the current best.  Same formulas as
+// Shape::project (so the same bits); only the order of evaluation across axes differs.
+constexpr int kSatF = 128, kSatE = 192, kSatV = 64;
+constexpr int kSatWarps = 4;
+template <class R> constexpr int sat_stage_reals() { return 3 * (2 * kSatF + 2 * kSatE + 2 * kSatV); }
+
+template <class R> struct SatStage {
+    R* nA; R* nB; R* dA; R* dB; R* vA; R* vB;
+    __device__ void bind(R* base) {
+        nA = base; nB = nA + 3 * kSatF; dA = nB + 3 * kSatF; dB = dA + 3 * kSatE; vA = dB + 3 * kSatE; vB = vA + 3 * kSatV;
+    }
+};
+template <class R> __device__ __forceinline__ V3<R> ld3(const R* p, int i) { return V3<R>(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
+template <class R> __device__ __forceinline__ void st3(R* p, int i, const V3<R>& v) { p[3 * i] = v.x; p[3 * i + 1] = v.y; p[3 * i + 2] = v.z; }
+
+template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& s) {
+    return s.face_count() <= kSatF && s.edge_count() <= kSatE && (s.type != ST_HULL || s.nv <= kSatV);
+}
+
+// support interval of a shape along a world axis (Shape::project without the witness points);
+// for hulls the indices of the witness vertices are returned (the first vertex never becomes
+// the maximum, like convex_mesh_shape.cpp:171-175)
+template <class R>
+__device__ __forceinline__ void shape_interval(const ShapeView<R>& s, const Xf<R>& t, const V3<R>& axis, const R* lv, R& mnp, R& mxp,
+                                               int& imn, int& imx) {
+    if (s.type == ST_SPHERE) {
+        const R off = dot(t.o, axis);
+        mnp = off - s.radius; mxp = off + s.radius;
+        return;
+    }
+    const V3<R> la = mtv(t.b, axis);
+    const R off = dot(t.o, axis);
+    if (s.type == ST_BOX) {
+        const V3<R> ext(la.x > 0 ? s.half.x : -s.half.x, la.y > 0 ? s.half.y : -s.half.y, la.z > 0 ? s.half.z : -s.half.z);
+        const R he = dot(ext, la);
+        mnp = off - he; mxp = off + he;
+        return;
+    }
+    if (s.type == ST_CYLINDER) {
+        const R hh = s.height * R(0.5);
+        if (rabs(la.x - 0) < eps<R>() && rabs(la.z - 0) < eps<R>()) { mnp = off - hh; mxp = off + hh; }
+        else if (rabs(la.y - 0) < eps<R>()) { mnp = off - s.radius; mxp = off + s.radius; }
+        else {
+            const R r = rsqrt_(la.x * la.x + la.z * la.z);
+            const R x = s.radius * la.x / r, z = s.radius * la.z / r;
+            const R y = hh * (la.y > 0 ? 1 : -1);
+            const R el = dot(V3<R>(x, y, z), la);
+            mnp = off - el; mxp = off + el;
+        }
+        return;
+    }
+    mnp = Lim<R>::max();
+    mxp = Lim<R>::min();
+    imn = -1; imx = -1;
+    for (int i = 0; i < s.nv; i++) {
+        const R v = dot(ld3(lv, i), la);
+        if (v < mnp) { mnp = v; imn = i; }
+        else if (v > mxp) { mxp = v; imx = i; }
+    }
+    mnp += off;
+    mxp += off;
+}
+
+// witness point of Shape::project on the min (want_max = false) or max side
+template <class R>
+__device__ V3<R> shape_witness(const ShapeView<R>& s, const Xf<R>& t, const V3<R>& axis, bool want_max, int idx, const R* lv) {
+    R a, b;
+    V3<R> pmin, pmax;
+    if (s.type == ST_HULL) {
+        // an index never set leaves the reference's witness undefined; that only happens on a
+        // separating axis, whose witness is never used
+        const V3<R> p = idx >= 0 ? ld3(lv, idx) : V3<R>(0, 0, 0);
+        return t.apply(p);
+    }
+    shape_project(s, t, axis, a, b, pmin, pmax);
+    return want_max ? pmax : pmin;
+}
+
+template <class R>
+__device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
+    const R margin = 0;
+    SatStage<R> st;
+    st.bind(smem);
+    const int fa = c.sa.face_count(), fb = c.sb.face_count();
+    const int na = c.sa.edge_count(), nb = c.sb.edge_count();
+    for (int f = lane; f < fa; f += 32) st3(st.nA, f, mv(c.ta().b, c.sa.face_normal(f)));
+    for (int f = lane; f < fb; f += 32) st3(st.nB, f, mv(c.tb().b, c.sb.face_normal(f)));
+    for (int e = lane; e < na; e += 32) { V3<R> a0, a1; c.sa.edge(e, a0, a1); st3(st.dA, e, mv(c.ta().b, normalized(a0 - a1))); }
+    for (int e = lane; e < nb; e += 32) { V3<R> b0, b1; c.sb.edge(e, b0, b1); st3(st.dB, e, mv(c.tb().b, normalized(b0 - b1))); }
+    if (c.sa.type == ST_HULL) for (int i = lane; i < c.sa.nv; i += 32) st3(st.vA, i, c.sa.vert(i));
+    if (c.sb.type == ST_HULL) for (int i = lane; i < c.sb.nv; i += 32) st3(st.vB, i, c.sb.vert(i));
+    __syncwarp();
+    const V3<R> dc = c.ta().o - c.tb().o;
+    // ---- face axes of A, then of B (findSeparatingAxis :265-308)
+    R bd = Lim<R>::max();
+    int bf = 0x7fffffff, bside = 0, bia = -1, bib = -1;
+    bool sep_found = false;
+    for (int f = lane; f < fa + fb; f += 32) {
+        V3<R> n = f < fa ? ld3(st.nA, f) : ld3(st.nB, f - fa);
+        if (dot(dc, n) < 0) n = n * R(-1.0);
+        R min0, max0, min1, max1;
+        int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
+        shape_interval(c.sa, c.ta(), n, st.vA, min0, max0, a0, a1);
+        shape_interval(c.sb, c.tb(), n, st.vB, min1, max1, b0, b1);
+        if (max0 < min1 || max1 < min0) { sep_found = true; break; }
+        const R d0 = max0 - min1, d1 = max1 - min0;
+        const R d = d0 < d1 ? d0 : d1;
+        if (d < bd) { bd = d; bf = f; bside = d0 < d1; bia = d0 < d1 ? a1 : a0; bib = d0 < d1 ? b0 : b1; }
+    }
+    if (__any_sync(0xffffffffu, sep_found)) return false;
+    R dmin = bd;
+    int wf = bf;
+    warp_argmin(dmin, wf);
+    V3<R> sep, dpt;
+    const bool on_a = wf >= fa;
+    if (wf < 0x7fffffff) {
+        const int sl = wf % 32;
+        if (lane == sl) {
+            V3<R> n = wf < fa ? ld3(st.nA, wf) : ld3(st.nB, wf - fa);
+            if (dot(dc, n) < 0) n = n * R(-1.0);
+            sep = n;
+            // testSepAxis witnesses: d0 < d1 -> (max of A, min of B), else (min of A, max of B)
+            if (!on_a) dpt = shape_witness(c.sb, c.tb(), n, !bside, bib, st.vB);
+            else dpt = shape_witness(c.sa, c.ta(), n, bside, bia, st.vA) + n * bd;
+        }
+        sep = shfl3(sep, sl);
+        dpt = shfl3(dpt, sl);
+        if (lane == 0 &&
+            ((on_a && shape_inside(c.sb, c.tb().inv_apply(dpt))) || (!on_a && shape_inside(c.sa, c.ta().inv_apply(dpt)))))
+            c.add(sep, dpt - sep * margin, -dmin + margin * 2);
+    }
+    // ---- edge-pair axes (:323-361)
+    R ed = dmin;
+    int ep = 0x7fffffff;
+    V3<R> ewa, ewb, en;
+    sep_found = false;
+    for (int q = lane; q < na * nb; q += 32) {
+        const int e0 = q / nb, e1 = q - e0 * nb;
+        const V3<R> w0 = ld3(st.dA, e0), w1 = ld3(st.dB, e1);
+        V3<R> cr = cross(w0, w1);
+        if (rabs(norm(cr) - 0) < eps<R>()) continue;
+        cr = normalized(cr);
+        if (dot(dc, cr) < 0) cr = cr * R(-1.0);
+        R min0, max0, min1, max1;
+        int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
+        shape_interval(c.sa, c.ta(), cr, st.vA, min0, max0, a0, a1);
+        shape_interval(c.sb, c.tb(), cr, st.vB, min1, max1, b0, b1);
+        if (max0 < min1 || max1 < min0) { sep_found = true; break; }
+        const R d0 = max0 - min1, d1 = max1 - min0;
+        const R dist = d0 < d1 ? d0 : d1;
+        if (dist < ed) {
+            const bool side = d0 < d1;
+            const V3<R> wa = shape_witness(c.sa, c.ta(), cr, side, side ? a1 : a0, st.vA);
+            const V3<R> wb = shape_witness(c.sb, c.tb(), cr, !side, side ? b0 : b1, st.vB);
+            V3<R> p0, p1, q0, q1;
+            c.sa.edge(e0, p0, p1);
+            c.sb.edge(e1, q0, q1);
+            if (!on_line(p0, p1, c.ta().inv_apply(wa)) || !on_line(q0, q1, c.tb().inv_apply(wb))) continue;
+            ed = dist; ep = q; ewa = wa; ewb = wb; en = cr;
+        }
+    }
+    if (__any_sync(0xffffffffu, sep_found)) return false;
+    R emin = ed;
+    int wq = ep;
+    warp_argmin(emin, wq);
+    if (wq < 0x7fffffff) {
+        const int sl = wq % 32;
+        const V3<R> wpa = shfl3(ewa, sl), wpb = shfl3(ewb, sl);
+        sep = shfl3(en, sl);
+        if (lane == 0) {   // segmentsClosestPoints with unbounded half-lengths (:172-214, :363-395)
+            const int e0 = wq / nb, e1 = wq - e0 * nb;
+            const V3<R> wea = ld3(st.dA, e0), web = ld3(st.dB, e1);
+            const V3<R> tr = wpb - wpa;
+            const R ab = dot(wea, web), at = dot(wea, tr), bt = dot(web, tr);
+            const R d = R(1.0) - ab * ab;
+            const R ha = Lim<R>::max(), hb = Lim<R>::max();
+            R ta, tb;
+            if (d == 0) ta = 0;
+            else { ta = (at - bt * ab) / d; if (ta < -ha) ta = -ha; else if (ta > ha) ta = ha; }
+            tb = ta * ab - bt;
+            if (tb < -hb) { tb = -hb; ta = tb * ab + at; if (ta < -ha) ta = -ha; else if (ta > ha) ta = ha; }
+            else if (tb > hb) { tb = hb; ta = tb * ab + at; if (ta < -ha) ta = -ha; else if (ta > ha) ta = ha; }
+            const V3<R> oa = wea * ta, ob = web * tb;
+            V3<R> pts = tr - oa + ob;
+            const R nl2 = sqnorm(pts);
+            if (nl2 > eps<R>()) {
+                const R nl = rsqrt_(nl2);
+                pts = pts * (R(1.0) / nl);
+                if (dot(pts, dc) < 0) pts = pts * R(-1.0);
+                c.add(pts, wpb + ob - pts * margin, -nl + margin * 2);
+            }
+        }
+    }
+    if (dot(dc, sep) < 0) sep = -sep;
+    // ---- clipping (:63-170): incident face of B (first maximum), reference face of A (first minimum)
+    R dmax = Lim<R>::min();
+    int fbest = 0x7fffffff;
+    for (int f = lane; f < fb; f += 32) {
+        const R d = dot(ld3(st.nB, f), sep);
+        if (d > dmax) { dmax = d; fbest = f; }
+    }
+    warp_argmax(dmax, fbest);
+    R dmn = Lim<R>::max();
+    int fabest = 0x7fffffff;
+    for (int f = lane; f < fa; f += 32) {
+        const R d = dot(ld3(st.nA, f), sep);
+        if (d < dmn) { dmn = d; fabest = f; }
+    }
+    warp_argmin(dmn, fabest);
+    if (lane == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) clip_faces(c, sep, -c.ref_scale, R(0), fbest, fabest);
+    return true;
+}
+
+template <class R>
+__device__ bool sat_warp(Pair<R>& c, int lane) {
+    const R margin = 0;
+    const V3<R> dc = c.ta().o - c.tb().o;
+    const int fa = c.sa.face_count(), fb = c.sb.face_count();
+    // face axes of A, then of B
+    R bd = Lim<R>::max();
+    int bf = 0x7fffffff;
+    V3<R> bn, bpt;
+    bool sep_found = false;
+    for (int f = lane; f < fa + fb; f += 32) {
+        const bool is_a = f < fa;
+        V3<R> n = is_a ? mv(c.ta().b, c.sa.face_normal(f)) : mv(c.tb().b, c.sb.face_normal(f - fa));
+        if (dot(dc, n) < 0) n = n * R(-1.0);
+        R d;
+        V3<R> wa, wb;
+        if (!sep_test(c, n, d, wa, wb)) { sep_found = true; break; }
+        if (d < bd) { bd = d; bf = f; bn = n; bpt = is_a ? wb : wa + n * d; }
+    }
+    if (__any_sync(0xffffffffu, sep_found)) return false;
+    R dmin = bd;
+    int wf = bf;
+    warp_argmin(dmin, wf);
+    const int src_lane = wf < 0x7fffffff ? wf % 32 : 0;
+    V3<R> sep = shfl3(bn, src_lane);
+    const V3<R> dpt = shfl3(bpt, src_lane);
+    const bool on_a = wf >= fa;
+    if (wf < 0x7fffffff && lane == 0) {
+        if ((on_a && shape_inside(c.sb, c.tb().inv_apply(dpt))) || (!on_a && shape_inside(c.sa, c.ta().inv_apply(dpt))))
+            c.add(sep, dpt - sep * margin, -dmin + margin * 2);
+    }
+    // edge-pair axes
+    const int na = c.sa.edge_count(), nb = c.sb.edge_count();
+    const int ne = na * nb;
+    R ed = dmin;
+    int ep = 0x7fffffff;
+    V3<R> ewa, ewb, ew0, ew1, en;
+    sep_found = false;
+    for (int q = lane; q < ne; q += 32) {
+        const int e0 = q / nb, e1 = q - e0 * nb;
+        V3<R> a0, a1, b0, b1;
+        c.sa.edge(e0, a0, a1);
+        c.sb.edge(e1, b0, b1);
+        const V3<R> w0 = mv(c.ta().b, normalized(a0 - a1));
+        const V3<R> w1 = mv(c.tb().b, normalized(b0 - b1));
+        V3<R> cr = cross(w0, w1);
+        if (rabs(norm(cr) - 0) < eps<R>()) continue;
+        cr = normalized(cr);
+        if (dot(dc, cr) < 0) cr = cr * R(-1.0);
+        R dist;
+        V3<R> wa, wb;
+        if (!sep_test(c, cr, dist, wa, wb)) { sep_found = true; break; }
+        if (dist < ed) {
+            if (!on_line(a0, a1, c.ta().inv_apply(wa)) || !on_line(b0, b1, c.tb().inv_apply(wb))) continue;
+            ed = dist; ep = q; ewa = wa; ewb = wb; ew0 = w0; ew1 = w1; en = cr;
+        }
+    }
+    if (__any_sync(0xffffffffu, sep_found)) return false;
+    R emin = ed;
+    int wq = ep;
+    warp_argmin(emin, wq);
+    if (wq < 0x7fffffff) {
+        const int sl = wq % 32;
+        const V3<R> wpa = shfl3(ewa, sl), wpb = shfl3(ewb, sl), wea = shfl3(ew0, sl), web = shfl3(ew1, sl);
+        sep = shfl3(en, sl);
+        if (lane == 0) {   // segmentsClosestPoints with unbounded half-lengths (:172-214, :363-395)
+            const V3<R> tr = wpb - wpa;
+            const R ab = dot(wea, web), at = dot(wea, tr), bt = dot(web, tr);
+            const R d = R(1.0) - ab * ab;
+            const R ha = Lim<R>::max(), hb = Lim<R>::max();
+            R ta, tb;
+            if (d == 0) ta = 0;
+            else { ta = (at - bt * ab) / d; if (ta < -ha) ta = -ha; else if (ta > ha) ta = ha; }
+            tb = ta * ab - bt;
+            if (tb < -hb) { tb = -hb; ta = tb * ab + at; if (ta < -ha) ta = -ha; else if (ta > ha) ta = ha; }
+            else if (tb > hb) { tb = hb; ta = tb * ab + at; if (ta < -ha) ta = -ha; else if (ta > ha) ta = ha; }
+            const V3<R> oa = wea * ta, ob = web * tb;
+            V3<R> pts = tr - oa + ob;
+            const R nl2 = sqnorm(pts);
+            if (nl2 > eps<R>()) {
+                const R nl = rsqrt_(nl2);
+                pts = pts * (R(1.0) / nl);
+                if (dot(pts, dc) < 0) pts = pts * R(-1.0);
+                c.add(pts, wpb + ob - pts * margin, -nl + margin * 2);
+            }
+        }
+    }
+    if (dot(dc, sep) < 0) sep = -sep;
+    // clipping (:63-170): incident face of B (first maximum), reference face of A (first minimum)
+    R dmax = Lim<R>::min();
+    int fbest = 0x7fffffff;
+    for (int f = lane; f < fb; f += 32) {
+        const R d = dot(mv(c.tb().b, c.sb.face_normal(f)), sep);
+        if (d > dmax) { dmax = d; fbest = f; }
+    }
+    warp_argmax(dmax, fbest);
+    R dmn = Lim<R>::max();
+    int fabest = 0x7fffffff;
+    for (int f = lane; f < fa; f += 32) {
+        const R d = dot(mv(c.ta().b, c.sa.face_normal(f)), sep);
+        if (d < dmn) { dmn = d; fabest = f; }
+    }
+    warp_argmin(dmn, fabest);
+    if (lane == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) clip_faces(c, sep, -c.ref_scale, R(0), fbest, fabest);
+    return true;
+}
+
+template <class R>
+__global__ void k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                         const int* pair_scene_off, const int* prev_off) {
+    extern __shared__ __align__(16) unsigned char sat_smem[];
+    const int warp = threadIdx.x >> 5;
+    const int t = lo + blockIdx.x * kSatWarps + warp;
+    const int lane = threadIdx.x & 31;
+    if (t >= hi) return;   // whole warps leave together
+    const int p = order[t];
+    Cache<R> cache;
+    Pair<R> pr;
+    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
+    if (sat_fits(pr.sa) && sat_fits(pr.sb)) sat_staged(pr, lane, reinterpret_cast<R*>(sat_smem) + (size_t)warp * sat_stage_reals<R>());
+    else sat_warp(pr, lane);
+    if (lane == 0) np_finish(p, pairs, B, res, cache);
 }
 
 // ===================================================================== solver
@@ -346,61 +763,157 @@ __device__ __forceinline__ void si_iterate_result(const Bodies<R>& B, const Rows
     if (!kb) { B.set_vec(TVX, ib, tvb); B.set_vec(TWX, ib, twb); }
 }
 
-// serial-order mode: one thread per scene replays SequentialImpulseSolver::solve's loop
-// (sequential_impulse_solver.cpp:60-69) over that scene's results in order
+// ---------------------------------------------------------------- contact islands
+// Islands: connected components of dynamic bodies linked by contact results (a kinematic body
+// links nothing: its temporary velocity never changes).  Results of different islands touch
+// disjoint dynamic bodies, so running each island's results in the reference's global order
+// (SequentialImpulseSolver::solve, sequential_impulse_solver.cpp:60-69) yields exactly the
+// reference's velocities while islands proceed in parallel.
+__device__ __forceinline__ int uf_find(const int* parent, int x) {
+    int p = parent[x];
+    while (p != x) { x = p; p = parent[x]; }   // parents always point to smaller indices
+    return x;
+}
+__device__ __forceinline__ void uf_union(int* parent, int a, int b) {
+    for (;;) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return;
+        if (a < b) { const int t = a; a = b; b = t; }
+        // hook the larger root below the smaller one; retry if another thread moved it first
+        if (atomicCAS(&parent[a], a, b) == a) return;
+    }
+}
+
+__global__ void k_isl_init(int n, int* parent);
 template <class R>
-__global__ void k_si_serial(int n_scenes, const int* scene_pair_off, Results<R> res, Bodies<R> B, Rows<R> rows, const int* row_off,
-                            int iterations) {
+__global__ void k_isl_union(int A, const int* active, Results<R> res, Bodies<R> B, int* parent) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A) return;
+    const int p = active[t];
+    const int ia = res.a[p], ib = res.b[p];
+    if ((B.flags[ia] & BF_KINEMATIC) || (B.flags[ib] & BF_KINEMATIC)) return;
+    uf_union(parent, ia, ib);
+}
+// sort keys: island label (smallest body index of the island) of each active result
+template <class R>
+__global__ void k_isl_keys(int A, const int* active, Results<R> res, Bodies<R> B, const int* parent, uint64_t* key, uint32_t* key2,
+                           uint32_t* val) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A) return;
+    const int p = active[t];
+    const int ia = res.a[p], ib = res.b[p];
+    const int dyn = (B.flags[ia] & BF_KINEMATIC) ? ib : ia;
+    key[t] = (uint64_t)uf_find(parent, dyn);
+    key2[t] = 0;
+    val[t] = (uint32_t)p;
+}
+__global__ void k_isl_flags(int A, const uint64_t* key, int* flag);
+__global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out);
+
+// serial order inside each island: one thread per island (all islands in serial-order mode,
+// islands up to `max_len` results in coloured mode)
+template <class R>
+__global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Bodies<R> B, Rows<R> rows,
+                             const int* row_off, int iterations, int max_len) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n_scenes) return;
-    const int lo = scene_pair_off[s], hi = scene_pair_off[s + 1];
+    if (s >= *n_isl) return;
+    const int lo = isl_off[s], hi = isl_off[s + 1];
+    if (hi - lo > max_len) return;
     for (int it = 0; it < iterations; it++)
-        for (int p = lo; p < hi; p++) {
-            const int np = res.npts[p];
-            if (np) si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], np);
+        for (int k = lo; k < hi; k++) {
+            const int p = (int)order[k];
+            si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
         }
 }
 
-// greedy colouring in rounds: an uncoloured result takes colour c when it holds the smallest
-// index among the uncoloured results touching each of its dynamic bodies
+// coloured Gauss-Seidel of one island per block: greedy colouring in rounds (a result takes
+// colour c when it holds the smallest position among the uncoloured results on each of its
+// dynamic bodies), then every iteration runs the colours in turn, all results of a colour in
+// parallel.  Results still uncoloured after kMaxColors - 1 rounds form a last colour that one
+// thread runs in order.
+constexpr int kMaxColors = 64;
 template <class R>
-__global__ void k_color_claim(int n_active, const int* active, const int* color, Results<R> res, Bodies<R> B, int* claim) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_active) return;
-    if (color[t] >= 0) return;
-    const int p = active[t];
-    const int ia = res.a[p], ib = res.b[p];
-    if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], t);
-    if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], t);
-}
-template <class R>
-__global__ void k_color_take(int n_active, const int* active, int* color, Results<R> res, Bodies<R> B, int* claim, int c, int* remaining) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_active) return;
-    if (color[t] >= 0) return;
-    const int p = active[t];
-    const int ia = res.a[p], ib = res.b[p];
-    const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
-    const bool win = (!da || claim[ia] == t) && (!db || claim[ib] == t);
-    if (win) color[t] = c;
-    else atomicAdd(remaining, 1);
-}
-template <class R>
-__global__ void k_color_reset(int n_active, const int* active, const int* color, Results<R> res, int* claim) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_active) return;
-    const int p = active[t];
-    claim[res.a[p]] = 0x7fffffff;
-    claim[res.b[p]] = 0x7fffffff;
-}
-
-// coloured Gauss-Seidel: all results of one colour in parallel (no shared dynamic body)
-template <class R>
-__global__ void k_si_color(int lo, int hi, const int* by_color, Results<R> res, Bodies<R> B, Rows<R> rows, const int* row_off) {
-    const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= hi) return;
-    const int p = by_color[t];
-    si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
+__global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Bodies<R> B, Rows<R> rows,
+                              const int* row_off, int iterations, int min_len, int* claim, int* color, uint32_t* corder,
+                              int* n_colors_out) {
+    const int s = blockIdx.x;
+    if (s >= *n_isl) return;
+    const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
+    if (m <= min_len) return;
+    __shared__ int cnt[kMaxColors + 1];
+    __shared__ int remaining;
+    __shared__ int ncol;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) color[lo + j] = -1;
+    if (threadIdx.x == 0) ncol = 0;
+    __syncthreads();
+    for (int c = 0; c < kMaxColors - 1; c++) {
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            if (color[lo + j] >= 0) continue;
+            const int p = (int)order[lo + j];
+            claim[res.a[p]] = 0x7fffffff;
+            claim[res.b[p]] = 0x7fffffff;
+        }
+        if (threadIdx.x == 0) remaining = 0;
+        __syncthreads();
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            if (color[lo + j] >= 0) continue;
+            const int p = (int)order[lo + j];
+            const int ia = res.a[p], ib = res.b[p];
+            if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
+            if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            if (color[lo + j] >= 0) continue;
+            const int p = (int)order[lo + j];
+            const int ia = res.a[p], ib = res.b[p];
+            const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
+            if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) color[lo + j] = c;
+            else atomicAdd(&remaining, 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) ncol = c + 1;
+        const int rem = remaining;
+        __syncthreads();
+        if (rem == 0) break;
+    }
+    // leftovers (pathological degree): one last colour, run in order by one thread
+    for (int j = threadIdx.x; j < m; j += blockDim.x)
+        if (color[lo + j] < 0) color[lo + j] = kMaxColors - 1;
+    for (int k = threadIdx.x; k <= kMaxColors; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) atomicAdd(&cnt[color[lo + j] + 1], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kMaxColors; k++) cnt[k + 1] += cnt[k];   // cnt[c] = first slot of colour c
+        atomicMax(n_colors_out, ncol + (cnt[kMaxColors] > cnt[kMaxColors - 1] ? 1 : 0));
+    }
+    __syncthreads();
+    // placement by colour keeping the island order within each colour
+    if (threadIdx.x == 0) {
+        int fill[kMaxColors];
+        for (int k = 0; k < kMaxColors; k++) fill[k] = cnt[k];
+        for (int j = 0; j < m; j++) corder[lo + fill[color[lo + j]]++] = order[lo + j];
+    }
+    __syncthreads();
+    for (int it = 0; it < iterations; it++) {
+        for (int c = 0; c < kMaxColors - 1; c++) {
+            const int a = cnt[c], b = cnt[c + 1];
+            if (a == b) continue;
+            for (int j = a + threadIdx.x; j < b; j += blockDim.x) {
+                const int p = (int)corder[lo + j];
+                si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0)
+            for (int j = cnt[kMaxColors - 1]; j < cnt[kMaxColors]; j++) {
+                const int p = (int)corder[lo + j];
+                si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
+            }
+        __syncthreads();
+    }
 }
 
 // RigidBody::clearTempVelocity (rigidbody.cpp:160-164) at SequentialImpulseSolver::setupSolver
@@ -418,8 +931,6 @@ __global__ void k_scene_pair_off(int n_scenes, const int* scene_off, const int* 
 // results with at least one point, compacted
 __global__ void k_active_flags(int P, const int* npts, int* flag);
 __global__ void k_active_compact(int P, const int* npts, const int* scan, int* active);
-__global__ void k_color_count(int n_active, const int* color, int* cnt);
-__global__ void k_color_bucket(int n_active, const int* active, const int* color, int* cursor, int* by_color);
 
 // RigidBody::syncTempVelocity (rigidbody.cpp:154-158)
 template <class R>

@@ -152,15 +152,22 @@ __global__ void k_active_compact(int P, const int* npts, const int* scan, int* a
     if (p < P && npts[p] > 0) active[scan[p]] = p;
 }
 
-__global__ void k_color_count(int n_active, const int* color, int* cnt) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n_active) atomicAdd(&cnt[color[t]], 1);
+__global__ void k_isl_init(int n, int* parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) parent[i] = i;
 }
 
-__global__ void k_color_bucket(int n_active, const int* active, const int* color, int* cursor, int* by_color) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n_active) return;
-    by_color[atomicAdd(&cursor[color[t]], 1)] = active[t];
+__global__ void k_isl_flags(int A, const uint64_t* key, int* flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < A) flag[k] = (k == 0 || key[k] != key[k - 1]) ? 1 : 0;
+    else if (k == A) flag[k] = 0;
+}
+
+// after an exclusive scan of the flags: island id = scan value at each island's first slot
+__global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < A && (k == 0 || key[k] != key[k - 1])) isl_off[scan[k]] = k;
+    if (k == A) { isl_off[scan[A]] = A; *n_isl_out = scan[A]; }
 }
 
 } // namespace pe

@@ -40,11 +40,11 @@ template <class T> struct DBuf {   // device array that grows on demand
 };
 
 // kernel groups for per-kernel device time (profiling mode)
-enum KernelId { K_INTEGRATE = 0, K_BP_KEYS, K_RADIX, K_SCAN, K_BP_GATHER, K_BP_SWEEP, K_BP_AXIS, K_NP_BUCKET, K_NP,
-                K_SI_SETUP, K_SI_SERIAL, K_COLOR, K_SI_COLOR, K_SI_MISC, K_MISC, K_COUNT };
+enum KernelId { K_INTEGRATE = 0, K_BP_KEYS, K_RADIX, K_SCAN, K_BP_GATHER, K_BP_SWEEP, K_BP_AXIS, K_NP_BUCKET, K_NP, K_NP_SAT,
+                K_SI_SETUP, K_ISLAND, K_SI_SERIAL, K_SI_COLOR, K_SI_MISC, K_MISC, K_COUNT };
 inline const char* kernel_name(int k) {
     static const char* n[K_COUNT] = {"integrate", "bp_keys", "radix_sort", "scan", "bp_gather", "bp_sweep", "bp_axis",
-                                     "np_bucket", "narrowphase", "si_setup", "si_serial", "coloring", "si_colored",
+                                     "np_bucket", "narrowphase", "np_sat", "si_setup", "islands", "si_serial", "si_colored",
                                      "si_misc", "misc"};
     return k >= 0 && k < K_COUNT ? n[k] : "";
 }
@@ -120,7 +120,11 @@ public:
     void phase_times(double* ms, bool reset) override;
     void last_counts(int* c) override;
     void sync() override { PE_CK(cudaStreamSynchronize(st_)); }
-    void set_profiling(bool on) override { resolve_prof(); prof_ = on; }
+    void set_profiling(bool on) override {
+        resolve_prof();
+        if (on && !prof_) for (int k = 0; k < K_COUNT; k++) { kms_[k] = 0; klaunch_[k] = 0; }
+        prof_ = on;
+    }
     void kernel_stats(double* ms, long long* launches) override {
         resolve_prof();
         for (int k = 0; k < K_COUNT; k++) { ms[k] = kms_[k]; launches[k] = klaunch_[k]; }
@@ -129,7 +133,11 @@ public:
 private:
     // every kernel of the step goes through here: counts launches, and in profiling mode
     // brackets the launch with events on the world's stream
-    template <class Kern, class... A> void launch(int id, int g, Kern kern, A... args) {
+    template <class Kern, class... A> void launch(int id, int g, Kern kern, A... args) { launch_smem(id, g, kBlock, 0, kern, args...); }
+    template <class Kern, class... A> void launch_block(int id, int g, int block, Kern kern, A... args) {
+        launch_smem(id, g, block, 0, kern, args...);
+    }
+    template <class Kern, class... A> void launch_smem(int id, int g, int block, size_t smem, Kern kern, A... args) {
         if (g <= 0) return;
         klaunch_[id]++;
         step_launches_++;
@@ -140,7 +148,7 @@ private:
             e1 = ev_pool_.back(); ev_pool_.pop_back();
             PE_CK(cudaEventRecord(e0, st_));
         }
-        kern<<<g, kBlock, 0, st_>>>(args...);
+        kern<<<g, block, smem, st_>>>(args...);
         if (prof_) {
             PE_CK(cudaEventRecord(e1, st_));
             pending_.push_back({id, e0, e1});
@@ -179,6 +187,7 @@ private:
     R* stage_ = nullptr;
     size_t stage_n_ = 0;
     void radix_sort(int n, int n_scene_passes);
+    int radix_sort_keys(int n, int key_passes, int scene_passes);   // returns the buffer holding the result
     void ensure_pair_capacity(int P);
     void check_status();
     void ev_begin(int phase);
@@ -211,7 +220,8 @@ private:
     DBuf<uint32_t> key2_[2], val_[2];
     DBuf<int> hist_, aux_, total_, count_, status_;
     DBuf<R> smn_, smx_;
-    DBuf<int> sflag_, ssc_;
+    DBuf<int> sflag_, ssc_, bp_stage_;
+    DBuf<double> axis_part_;
     uint32_t* order_ = nullptr;   // sorted body order (points into val_)
     DBuf<int2> pairs_;
     int P_ = 0, pair_cap_ = 0;
@@ -223,9 +233,12 @@ private:
     int R_ = 0;
     std::vector<int> h_pair_scene_off_;
     // solver
-    DBuf<int> row_off_, active_, color_, claim_, by_color_, color_cnt_, remaining_;
+    DBuf<int> row_off_, active_, color_, claim_, parent_, isl_flag_, isl_off_, isl_n_, ncol_;
+    DBuf<uint32_t> isl_corder_;
     DBuf<R> rows_;
-    int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0;
+    int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0, n_islands_ = 0;
+    int small_island_ = 8;
+    bool sat_attr_ = false;   // islands with at most this many results run serially in one thread
 };
 
 } // namespace pe

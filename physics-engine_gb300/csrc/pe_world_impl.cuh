@@ -45,7 +45,7 @@ template <class R> void World<R>::phase_times(double* ms, bool reset) {
     if (reset) for (double& m : ms_) m = 0;
 }
 template <class R> void World<R>::last_counts(int* c) {
-    c[0] = P_; c[1] = n_active_; c[2] = n_rows_; c[3] = n_colors_; c[4] = (int)last_step_launches_; c[5] = 0;
+    c[0] = P_; c[1] = n_active_; c[2] = n_rows_; c[3] = n_colors_; c[4] = (int)last_step_launches_; c[5] = n_islands_;
 }
 
 template <class R> void World<R>::check_status() {
@@ -225,10 +225,13 @@ template <class R> int World<R>::scan(int* data, int n) {
 }
 
 template <class R> void World<R>::radix_sort(int n, int scene_passes) {
+    order_ = val_[radix_sort_keys(n, (int)sizeof(R), scene_passes)].p;
+}
+
+template <class R> int World<R>::radix_sort_keys(int n, int key_passes, int scene_passes) {
     const int tiles = (n + kRadixTile - 1) / kRadixTile;
     hist_.ensure((size_t)256 * tiles + 1);
     aux_.ensure((256 * tiles + 1023) / 1024 + 1);
-    const int key_bits = sizeof(R) * 8;
     int cur = 0;
     auto pass = [&](int shift, int use2) {
         launch(K_RADIX, tiles, k_radix_hist, key_[cur].p, key2_[cur].p, n, shift, use2, hist_.p, tiles);
@@ -241,9 +244,9 @@ template <class R> void World<R>::radix_sort(int n, int scene_passes) {
                                                   val_[cur ^ 1].p, n, shift, use2, hist_.p, tiles);
         cur ^= 1;
     };
-    for (int s = 0; s < key_bits; s += 8) pass(s, 0);
+    for (int s = 0; s < key_passes * 8; s += 8) pass(s, 0);
     for (int s = 0; s < scene_passes * 8; s += 8) pass(s, 1);
-    order_ = val_[cur].p;
+    return cur;
 }
 
 template <class R> void World<R>::ensure_pair_capacity(int P) {
@@ -257,9 +260,8 @@ template <class R> void World<R>::ensure_pair_capacity(int P) {
     // result slot distances survive between steps: grow both generations keeping contents
     res_dist_[0].ensure((size_t)cap * kSlots, true);
     res_dist_[1].ensure((size_t)cap * kSlots, true);
-    row_off_.ensure(cap + 1); active_.ensure(cap + 1); color_.ensure(cap); by_color_.ensure(cap);
-    // the point buffer is field-major over the capacity: re-layout requires no copy because
-    // points are only meaningful within one step
+    row_off_.ensure(cap + 1); active_.ensure(cap + 1); color_.ensure(cap + 1);
+    // point buffer: field-major over the capacity; its contents live for one step only
     pair_cap_ = cap;
 }
 
@@ -281,15 +283,18 @@ template <class R> int World<R>::broadphase() {
     for (int m = NS_ - 1; m > 0; m >>= 8) scene_passes++;
     radix_sort(n, scene_passes);
     launch(K_BP_GATHER, grid(n), k_bp_gather<R>, bodies(), order_, smn_.p, smx_.p, sflag_.p, ssc_.p);
-    launch(K_BP_SWEEP, grid(n), k_bp_sweep<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, nullptr,
-                                               nullptr, 0, status_.p);
+    bp_stage_.ensure((size_t)n * kStage);
+    launch(K_BP_SWEEP, grid(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p);
     PE_CK(cudaMemsetAsync(count_.p + n, 0, sizeof(int), st_));
     const int P = scan(count_.p, n + 1);
     ensure_pair_capacity(P);
-    launch(K_BP_SWEEP, grid(n), k_bp_sweep<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, nullptr, count_.p,
-                                               pairs_.p, pair_cap_, status_.p);
+    launch(K_BP_SWEEP, grid(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
+           pairs_.p, pair_cap_, status_.p);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
-    launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
+    const int tiles = (n + kAxisTile - 1) / kAxisTile;
+    axis_part_.ensure((size_t)tiles * 6);
+    launch(K_BP_AXIS, tiles, k_bp_axis_partial<R>, smn_.p, smx_.p, n, ssc_.p, axis_part_.p);
+    launch(K_BP_AXIS, grid(NS_), k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, axis_part_.p, scene_axis_.p, NS_);
     PE_CK(cudaGetLastError());
     P_ = P;
     return P;
@@ -312,8 +317,33 @@ template <class R> void World<R>::narrowphase() {
         for (int c = 0; c < PC_COUNT; c++) { cur[c] = run; run += cnt[c]; }
         PE_CK(cudaMemcpyAsync(cls_count_.p + PC_COUNT, cur, sizeof(cur), cudaMemcpyHostToDevice, st_));
         launch(K_NP_BUCKET, grid(P), k_np_bucket, P, cls_.p, cls_count_.p + PC_COUNT, order_np_.p);
-        launch(K_NP, grid(P), k_np<R>, P, order_np_.p, cls_.p, pairs_.p, bodies(), shapes(), results(),
-                                             pair_scene_off_.p, prev_res_off_.p, 0, PC_COUNT - 1);
+        const Results<R> rs = results();
+        const Bodies<R> bd = bodies();
+        const ShapeTable<R> sh = shapes();
+        for (int c = 0; c < PC_COUNT; c++) {
+            const int lo = cur[c], hi = cur[c] + cnt[c];
+            if (hi == lo) continue;
+            const int g = grid(hi - lo);
+            switch (c) {
+                case PC_BOX_BOX: launch(K_NP, g, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_SPHERE: launch(K_NP, g, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_SPHERE: launch(K_NP, g, k_np_class<R, PC_SPHERE_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_CYL: launch(K_NP, g, k_np_class<R, PC_SPHERE_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_CYL: launch(K_NP, g, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_HULL: launch(K_NP, g, k_np_class<R, PC_SPHERE_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_CYL_HULL: launch(K_NP, g, k_np_class<R, PC_CYL_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                default: {
+                    const size_t smem = (size_t)kSatWarps * sat_stage_reals<R>() * sizeof(R);
+                    if (!sat_attr_) {
+                        PE_CK(cudaFuncSetAttribute(k_np_sat<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                        sat_attr_ = true;
+                    }
+                    launch_smem(K_NP_SAT, (hi - lo + kSatWarps - 1) / kSatWarps, 32 * kSatWarps, smem, k_np_sat<R>, lo, hi, order_np_.p,
+                                pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
+                    break;
+                }
+            }
+        }
         PE_CK(cudaGetLastError());
     }
     PE_CK(cudaMemcpyAsync(res_scene_off_.p, pair_scene_off_.p, (NS_ + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
@@ -324,7 +354,11 @@ template <class R> void World<R>::solve(int mode) {
     const int P = R_;
     if (N_ == 0) return;
     launch(K_SI_MISC, grid(N_), k_si_clear<R>, bodies());
+    n_active_ = 0;
+    n_colors_ = 0;
+    n_islands_ = 0;
     if (P > 0) {
+        // rows: one per contact point, results' rows contiguous in result order
         PE_CK(cudaMemcpyAsync(row_off_.p, res_np_.p, P * sizeof(int), cudaMemcpyDeviceToDevice, st_));
         PE_CK(cudaMemsetAsync(row_off_.p + P, 0, sizeof(int), st_));
         n_rows_ = scan(row_off_.p, P + 1);
@@ -333,50 +367,45 @@ template <class R> void World<R>::solve(int mode) {
             rows_.ensure((size_t)NRF * rows_cap_);
         }
         launch(K_SI_SETUP, grid(P), k_si_setup<R>, P, results(), bodies(), rows(), row_off_.p, prm_, status_.p);
-        if (mode == 0) {
-            launch(K_SI_SERIAL, grid(NS_), k_si_serial<R>, NS_, res_scene_off_.p, results(), bodies(), rows(), row_off_.p,
-                                                         prm_.iterations);
-            n_colors_ = 0;
-        } else {
-            // results with points
-            launch(K_SI_MISC, grid(P + 1), k_active_flags, P, res_np_.p, active_.p);
-            color_.ensure(P + 1);
-            int* flags = color_.p;   // reuse as scan scratch
-            PE_CK(cudaMemcpyAsync(flags, active_.p, (P + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
-            n_active_ = scan(flags, P + 1);
-            launch(K_SI_MISC, grid(P), k_active_compact, P, res_np_.p, flags, active_.p);
-            const int A = n_active_;
-            PE_CK(cudaMemsetAsync(color_.p, 0xff, (A + 1) * sizeof(int), st_));   // -1 = uncoloured
-            remaining_.ensure(1);
-            int c = 0;
-            for (; A > 0; c++) {
-                PE_CK(cudaMemsetAsync(remaining_.p, 0, sizeof(int), st_));
-                launch(K_COLOR, grid(A), k_color_reset<R>, A, active_.p, color_.p, results(), claim_.p);
-                launch(K_COLOR, grid(A), k_color_claim<R>, A, active_.p, color_.p, results(), bodies(), claim_.p);
-                launch(K_COLOR, grid(A), k_color_take<R>, A, active_.p, color_.p, results(), bodies(), claim_.p, c,
-                                                             remaining_.p);
-                int rem = 0;
-                PE_CK(cudaMemcpyAsync(&rem, remaining_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-                PE_CK(cudaStreamSynchronize(st_));
-                if (rem == 0) break;
-                if (c > 4096) throw std::runtime_error("colouring did not converge");
+        // results with points, in result order
+        launch(K_SI_MISC, grid(P + 1), k_active_flags, P, res_np_.p, active_.p);
+        color_.ensure(P + 1);
+        PE_CK(cudaMemcpyAsync(color_.p, active_.p, (P + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
+        n_active_ = scan(color_.p, P + 1);
+        launch(K_SI_MISC, grid(P), k_active_compact, P, res_np_.p, color_.p, active_.p);
+        const int A = n_active_;
+        if (A > 0) {
+            // contact islands: union-find over dynamic bodies, results grouped by island keeping order
+            parent_.ensure(N_ + 1);
+            launch(K_ISLAND, grid(N_), k_isl_init, N_, parent_.p);
+            launch(K_ISLAND, grid(A), k_isl_union<R>, A, active_.p, results(), bodies(), parent_.p);
+            for (int k = 0; k < 2; k++) { key_[k].ensure(A); key2_[k].ensure(A); val_[k].ensure(A); }
+            launch(K_ISLAND, grid(A), k_isl_keys<R>, A, active_.p, results(), bodies(), parent_.p, key_[0].p, key2_[0].p, val_[0].p);
+            int label_passes = 0;
+            for (int m = N_ - 1; m > 0; m >>= 8) label_passes++;
+            const int cur = radix_sort_keys(A, label_passes, 0);
+            const uint64_t* skey = key_[cur].p;
+            const uint32_t* order = val_[cur].p;
+            isl_flag_.ensure(A + 1);
+            isl_off_.ensure(A + 1);
+            isl_n_.ensure(1);
+            launch(K_ISLAND, grid(A + 1), k_isl_flags, A, skey, isl_flag_.p);
+            n_islands_ = scan(isl_flag_.p, A + 1);
+            launch(K_ISLAND, grid(A + 1), k_isl_offsets, A, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
+            const int NI = n_islands_;
+            if (mode == 0) {
+                launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
+                       prm_.iterations, 0x7fffffff);
+            } else {
+                isl_corder_.ensure(A);
+                ncol_.ensure(1);
+                PE_CK(cudaMemsetAsync(ncol_.p, 0, sizeof(int), st_));
+                launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
+                       prm_.iterations, small_island_);
+                launch_block(K_SI_COLOR, NI, 256, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
+                             prm_.iterations, small_island_, claim_.p, color_.p, isl_corder_.p, ncol_.p);
+                PE_CK(cudaMemcpyAsync(&n_colors_, ncol_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
             }
-            n_colors_ = A ? c + 1 : 0;
-            color_cnt_.ensure(2 * n_colors_ + 2);
-            PE_CK(cudaMemsetAsync(color_cnt_.p, 0, (2 * n_colors_ + 2) * sizeof(int), st_));
-            launch(K_COLOR, grid(A), k_color_count, A, color_.p, color_cnt_.p);
-            std::vector<int> cnt(n_colors_ + 1), off(n_colors_ + 1, 0);
-            if (n_colors_) PE_CK(cudaMemcpyAsync(cnt.data(), color_cnt_.p, n_colors_ * sizeof(int), cudaMemcpyDeviceToHost, st_));
-            PE_CK(cudaStreamSynchronize(st_));
-            for (int k = 0; k < n_colors_; k++) off[k + 1] = off[k] + cnt[k];
-            if (n_colors_) PE_CK(cudaMemcpyAsync(color_cnt_.p + n_colors_ + 1, off.data(), n_colors_ * sizeof(int),
-                                                 cudaMemcpyHostToDevice, st_));
-            launch(K_COLOR, grid(A), k_color_bucket, A, active_.p, color_.p, color_cnt_.p + n_colors_ + 1, by_color_.p);
-            for (int it = 0; it < prm_.iterations; it++)
-                for (int k = 0; k < n_colors_; k++) {
-                    const int lo = off[k], hi = off[k + 1];
-                    launch(K_SI_COLOR, grid(hi - lo), k_si_color<R>, lo, hi, by_color_.p, results(), bodies(), rows(), row_off_.p);
-                }
         }
     }
     launch(K_SI_MISC, grid(N_), k_si_sync<R>, bodies());
