@@ -109,13 +109,19 @@ __global__ void k_bp_gather(Bodies<R> B, const uint32_t* order, R* smn, R* smx, 
 }
 
 // BroadPhaseSweepAndPrune::calcCollisionPairs sweep (broad_phase_sweep_and_prune.cpp:24-35)
-// with BroadPhaseBase::validateCollisionPair (broad_phase_base.cpp:5-19).  Pass 0 counts the
-// pairs of each sorted position and keeps the first kStage partners; pass 1 writes the pairs at
-// the scanned offsets, re-sweeping only positions with more than kStage partners.
+// with BroadPhaseBase::validateCollisionPair (broad_phase_base.cpp:5-19).
+//
+// One warp per sorted position i; the lanes test candidates j = i+1+lane, i+33+lane, ... with
+// coalesced loads of the sorted AABBs.  The reference stops at the first j whose minimum along
+// the axis exceeds i's maximum; minima are sorted, so the lanes still in range form a prefix and
+// the warp stops after the first chunk that is not full.  Overlapping partners are compacted in
+// ascending j with a ballot and a prefix popcount, which is the reference's pair order.
+// Pass 0 counts the pairs of each position and keeps its first kStage partners; pass 1 writes the
+// pairs at the scanned offsets, copying staged partners and re-sweeping only crowded positions.
 constexpr int kStage = 4;
-template <class R>
-__device__ __forceinline__ int sweep_one(int i, int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag,
-                                         const int* sscene, int* stage, int2* out, const uint32_t* order, int pair_cap, int* status) {
+template <class R, bool WRITE>
+__device__ __forceinline__ int sweep_warp(int i, int n, int lane, const int* scene_axis, const R* smn, const R* smx,
+                                          const int* sflag, const int* sscene, int* stage, int2* out, const uint32_t* order) {
     const int sc = sscene[i];
     const int ax = scene_axis[sc];
     const R* amin = smn + (size_t)ax * n;
@@ -124,22 +130,28 @@ __device__ __forceinline__ int sweep_one(int i, int n, const int* scene_axis, co
     const R mxx = smx[i], mxy = smx[n + i], mxz = smx[2 * (size_t)n + i];
     const int fi = sflag[i];
     if (fi & BF_IGNORE) return 0;
+    const int a = WRITE ? (int)order[i] : 0;
+    const unsigned lt = (1u << lane) - 1u;
     int c = 0;
-    for (int j = i + 1; j < n; j++) {
-        if (amin[j] > maxi_ax) break;
-        if (sscene[j] != sc) break;
-        const int fj = sflag[j];
-        if (fj & BF_IGNORE) continue;
-        if ((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) continue;
-        if (mnx > smx[j] || smn[j] > mxx) continue;
-        if (mny > smx[n + j] || smn[n + j] > mxy) continue;
-        if (mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz) continue;
-        if (stage && c < kStage) stage[(size_t)i * kStage + c] = j;
-        if (out) {
-            if (c < pair_cap) out[c] = make_int2((int)order[i], (int)order[j]);
-            else atomicOr(status, ST_PAIR_OVERFLOW);
+    for (int j0 = i + 1; j0 < n; j0 += 32) {
+        const int j = j0 + lane;
+        const bool in = j < n && !(amin[j] > maxi_ax) && sscene[j] == sc;
+        const unsigned live = __ballot_sync(0xffffffffu, in);
+        bool hit = false;
+        if (in) {
+            const int fj = sflag[j];
+            hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
+                  !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
+                  !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
         }
-        c++;
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int k = c + __popc(m & lt);
+            if (WRITE) out[k] = make_int2(a, (int)order[j]);
+            else if (k < kStage) stage[(size_t)i * kStage + k] = j;
+        }
+        c += __popc(m);
+        if (live != 0xffffffffu) break;
     }
     return c;
 }
@@ -147,24 +159,29 @@ __device__ __forceinline__ int sweep_one(int i, int n, const int* scene_axis, co
 template <class R>
 __global__ void k_bp_count(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene, int* count,
                            int* stage) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (i >= n) return;
-    count[i] = sweep_one<R>(i, n, scene_axis, smn, smx, sflag, sscene, stage, nullptr, nullptr, 0, nullptr);
+    const int c = sweep_warp<R, false>(i, n, lane, scene_axis, smn, smx, sflag, sscene, stage, nullptr, nullptr);
+    if (lane == 0) count[i] = c;
 }
 
 template <class R>
 __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
                            const uint32_t* order, const int* offset, const int* stage, int2* pairs, int pair_cap, int* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (i >= n) return;
     const int base = offset[i], c = offset[i + 1] - base;
     if (c == 0) return;
-    if (base + c > pair_cap) { atomicOr(status, ST_PAIR_OVERFLOW); return; }
+    if (base + c > pair_cap) {
+        if (lane == 0) atomicOr(status, ST_PAIR_OVERFLOW);
+        return;
+    }
     if (c <= kStage) {
-        const int a = (int)order[i];
-        for (int k = 0; k < c; k++) pairs[base + k] = make_int2(a, (int)order[stage[(size_t)i * kStage + k]]);
+        if (lane < c) pairs[base + lane] = make_int2((int)order[i], (int)order[stage[(size_t)i * kStage + lane]]);
     } else {
-        sweep_one<R>(i, n, scene_axis, smn, smx, sflag, sscene, nullptr, pairs + base, order, c, status);
+        sweep_warp<R, true>(i, n, lane, scene_axis, smn, smx, sflag, sscene, nullptr, pairs + base, order);
     }
 }
 

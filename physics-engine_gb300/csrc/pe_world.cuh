@@ -193,6 +193,7 @@ private:
     void ev_begin(int phase);
     void ev_end(int phase);
     int grid(int n) const { return (n + kBlock - 1) / kBlock; }
+    int grid_warps(int n) const { return (int)(((size_t)n * 32 + kBlock - 1) / kBlock); }   // one warp per item
 
     int dev_;
     cudaStream_t st_ = nullptr;

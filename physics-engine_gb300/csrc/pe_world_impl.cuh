@@ -284,11 +284,11 @@ template <class R> int World<R>::broadphase() {
     radix_sort(n, scene_passes);
     launch(K_BP_GATHER, grid(n), k_bp_gather<R>, bodies(), order_, smn_.p, smx_.p, sflag_.p, ssc_.p);
     bp_stage_.ensure((size_t)n * kStage);
-    launch(K_BP_SWEEP, grid(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p);
+    launch(K_BP_SWEEP, grid_warps(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p);
     PE_CK(cudaMemsetAsync(count_.p + n, 0, sizeof(int), st_));
     const int P = scan(count_.p, n + 1);
     ensure_pair_capacity(P);
-    launch(K_BP_SWEEP, grid(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
+    launch(K_BP_SWEEP, grid_warps(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
            pairs_.p, pair_cap_, status_.p);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
     const int tiles = (n + kAxisTile - 1) / kAxisTile;
