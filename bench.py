@@ -53,13 +53,11 @@ def make_workload(name):
                                              "20 SI iterations, serial-order solver", bodies=s.n_bodies, scenes=1,
                                     solver="serial-order")
     if name == "batched":
-        rng = np.random.default_rng(4096)
-        sizes = np.exp(rng.uniform(np.log(8), np.log(512), size=4096)).astype(int)
-        parts = [sc.pile(int(n), seed=1000 + i, real_bits=32, hull_range=(8, 64)) for i, n in enumerate(sizes)]
-        merged, offs = sc.concat(parts)
-        return merged, 32, 1, offs, dict(workload="4,096 independent piles of 8..512 bodies (log-uniform) incl. convex "
-                                                  "hulls, one batched step, FP32, 10 SI iterations, coloured",
-                                         bodies=merged.n_bodies, scenes=4096, solver="coloured")
+        s, offs = sc.batched_piles(n_scenes=4096, seed=4096, real_bits=32)
+        return s, 32, 1, offs, dict(workload="4,096 independent piles of 8..512 bodies (log-uniform; box/sphere/cylinder/"
+                                             "convex hull 50/20/10/20, hulls of 8..64 vertices from a 512-shape pool) "
+                                             "on static ground boxes, one batched step, FP32, 10 SI iterations, coloured",
+                                    bodies=s.n_bodies, scenes=4096, solver="coloured", preroll_steps=120)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -245,6 +243,8 @@ def run_ours(args, rank, world, device):
     g = pg.GpuWorld(scene, bits, device=device, scenes=offs)
     flush = L2Flush()
     N = scene.n_bodies
+    for _ in range(cfg.get("preroll_steps", 0)):   # untimed settling (part of the workload definition)
+        g.step(1, mode)
     for _ in range(args.warmup):
         g.step(1, mode)
     # device-resident timed region
@@ -284,31 +284,86 @@ def run_ours(args, rank, world, device):
         g.step(1, mode)
         st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
         e2e_times.append(time.perf_counter() - t0)
-    io_bytes = N * 18 * (bits // 8)
+    io_bytes = N * 18 * 8   # float64 poses and velocities through the C ABI, each way
+    per_scene = per_scene_gpu(pg, scene, offs, g.state(fields=("origin", "basis", "lin_vel", "ang_vel")), bits, mode,
+                              device, args.steps) if offs is not None else None
     res = dict(dev_ms=dev_ms, per_step=per_step, N=N, launches=launches, counts=counts, cfg=cfg, bits=bits, clk=clk.summary(),
                roofline=dict(kernel=dom, bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
                              traffic=traffic, algorithmic_bytes=dom_bytes, launches=dom_n, avg_launch_ms=dom_ms / max(dom_n, 1),
                              peak_source=peak_kind, step_frac=alg["step"] / (dev_ms / args.steps * 1e-3) / 1e9 / peak),
                e2e=dict(value=N * len(e2e_times) / sum(e2e_times), unit=UNIT, h2d_bytes_per_step=io_bytes,
                         d2h_bytes_per_step=io_bytes),
-               kernels={k: round(v[0], 4) for k, v in ks.items() if v[1]})
-    return res, scene, bits
+               kernels={k: round(v[0], 4) for k, v in ks.items() if v[1]}, per_scene=per_scene)
+    return res, scene, bits, offs
 
 
-def cpu_baseline(scene, bits, budget_s=20.0):
-    """The reference's CPU step (restated in oracle/) on a bounded number of steps, all host threads."""
+def per_scene_gpu(pg, scene, offs, state, bits, mode, device, steps, sample=64, warmup=3):
+    """The plain one-scene-per-launch GPU path: a stratified sample of the batch's scenes, each
+    stepped alone in its own world (same state as in the batch), timed with device events."""
+    from pe_gb300 import scene as sc
+    S = len(offs) - 1
+    picks = np.unique(np.linspace(0, S - 1, min(sample, S)).astype(int))
+    bodies, ms, per_step = 0, 0.0, []
+    for k in picks:
+        b0, b1 = int(offs[k]), int(offs[k + 1])
+        w = pg.GpuWorld(sc.extract(scene, offs, k), bits, device=device)
+        w.set_state({f: v[b0:b1] for f, v in state.items()})
+        for _ in range(warmup):
+            w.step(1, mode)
+        t0 = w.phase_times()["step"]
+        for _ in range(steps):
+            w.step(1, mode)
+        t = w.phase_times()["step"] - t0
+        bodies += (b1 - b0) * steps
+        ms += t
+        per_step.append(t / steps)
+        w.close()
+    per_step.sort()
+    return dict(value=bodies / (ms * 1e-3), unit=UNIT, scenes=len(picks),
+                sample=f"{len(picks)} scenes spread over the batch, each stepped alone {steps} times after {warmup} warm-up steps",
+                p50_step_ms=per_step[len(per_step) // 2], p99_step_ms=per_step[min(len(per_step) - 1, int(0.99 * len(per_step)))])
+
+
+def _cpu_scene_worker(job):
+    """One scene on one host thread: untimed pre-roll, then timed steps (oracle process pool)."""
+    scene, bits, preroll, steps = job
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import orc
+    w = orc.OracleWorld(scene, bits, threads=1)
+    if preroll:
+        w.time_steps(preroll)
+    return scene.n_bodies * steps, w.time_steps(steps)
+
+
+def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, steps=5):
+    """The reference's CPU step (its algorithm restated in oracle/) on a bounded sample, all host
+    threads.  One scene: the reference's thread pool inside one world.  Independent scenes: one
+    scene per host thread (a spawn process pool), a spread sample of the batch."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import orc
     threads = os.cpu_count() or 1
-    w = orc.OracleWorld(scene, bits, threads=threads)
-    t = w.time_steps(1)
-    steps = 1
-    while t < budget_s and steps < 64:
-        k = max(1, min(int((budget_s - t) / max(t / steps, 1e-3)), 8))
-        t += w.time_steps(k)
-        steps += k
-    return dict(value=scene.n_bodies * steps / t, unit=UNIT, cores=threads, kind="port",
-                sample=f"{steps} full steps of the same workload from its initial state ({t:.1f} s, {threads} threads)")
+    if offs is None:
+        w = orc.OracleWorld(scene, bits, threads=threads)
+        t = w.time_steps(1)
+        n = 1
+        while t < budget_s and n < 64:
+            k = max(1, min(int((budget_s - t) / max(t / n, 1e-3)), 8))
+            t += w.time_steps(k)
+            n += k
+        return dict(value=scene.n_bodies * n / t, unit=UNIT, cores=threads, kind="port",
+                    sample=f"{n} full steps of the same workload from its initial state ({t:.1f} s, {threads} threads)")
+    import multiprocessing as mp
+    from pe_gb300 import scene as sc
+    S = len(offs) - 1
+    picks = np.unique(np.linspace(0, S - 1, min(sample, S)).astype(int))
+    jobs = [(sc.extract(scene, offs, int(k)), bits, preroll, steps) for k in picks]
+    with mp.get_context("spawn").Pool(threads) as pool:
+        out = pool.map(_cpu_scene_worker, jobs, chunksize=1)
+    body_steps = sum(o[0] for o in out)
+    t = sum(o[1] for o in out)
+    return dict(value=body_steps / (t / threads), unit=UNIT, cores=threads, kind="port",
+                sample=f"{len(picks)} scenes spread over the batch, one per host thread, {steps} timed steps each after "
+                       f"{preroll} untimed; summed per-scene time / {threads} threads ({t:.1f} s of CPU time)")
 
 
 def main():
@@ -330,21 +385,25 @@ def main():
         scene, bits, mode, offs, cfg = make_workload(args.workload)
         if offs is not None:   # independent scenes: the reference steps one World per scene
             pass
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import orc
-        threads = os.cpu_count() or 1
-        w = orc.OracleWorld(scene, bits, threads=threads)
-        for _ in range(min(args.warmup, 1)):
-            w.time_steps(1)
-        k = max(1, min(args.steps, 8))
-        t = w.time_steps(k)
-        v = scene.n_bodies * k / t
         cfg = dict(cfg, solver="serial (the reference's sequential impulse order)")
+        k = max(1, min(args.steps, 8))
+        if offs is None:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import orc
+            threads = os.cpu_count() or 1
+            w = orc.OracleWorld(scene, bits, threads=threads)
+            for _ in range(min(args.warmup, 1)):
+                w.time_steps(1)
+            t = w.time_steps(k)
+            cb = dict(value=scene.n_bodies * k / t, unit=UNIT, cores=threads, kind="port",
+                      sample=f"{k} full steps from the initial state, {threads} host threads")
+        else:
+            cb = cpu_baseline(scene, bits, offs, preroll=cfg.get("preroll_steps", 0), steps=k)
+        v = cb["value"]
         print(json.dumps(dict(metric=METRIC, value=v, unit=UNIT, n_gpus=args.gpus, steps=k, warmup=min(args.warmup, 1),
-                              ms_per_step=t / k * 1e3, higher_is_better=True, scaling="weak", vs_baseline=None,
-                              dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg, impl="reference",
-                              cpu_baseline=dict(value=v, unit=UNIT, cores=threads, kind="port",
-                                                sample=f"{k} full steps from the initial state, {threads} host threads"),
+                              ms_per_step=scene.n_bodies / v * 1e3, higher_is_better=True, scaling="weak",
+                              vs_baseline=None, dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg,
+                              impl="reference", cpu_baseline=cb,
                               e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))))
         return 0
 
@@ -355,7 +414,7 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
         dist.barrier()
-    res, scene, bits = run_ours(args, rank, world, local)
+    res, scene, bits, offs = run_ours(args, rank, world, local)
     dev_ms = res["dev_ms"]
     if dist is not None:
         import torch
@@ -371,12 +430,15 @@ def main():
                contact_points_last_step=res["counts"]["rows"], colors_last_step=res["counts"]["colors"],
                p50_step_ms=per[len(per) // 2], p99_step_ms=per[min(len(per) - 1, int(0.99 * len(per)))],
                contacts_per_s=res["counts"]["rows"] * args.steps * world / (dev_ms * 1e-3), parallelism=f"replicas x{world}")
+    if res["per_scene"] is not None:
+        cfg["per_scene_gpu"] = res["per_scene"]
+        cfg["batched_over_per_scene"] = value / world / res["per_scene"]["value"]
     out = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
                ms_per_step=dev_ms / args.steps, higher_is_better=True, scaling="weak", vs_baseline=None,
                dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg, roofline=res["roofline"],
                e2e=res["e2e"], gpu_launches=res["launches"], clocks=res["clk"], kernels_ms_one_step=res["kernels"])
     if not args.no_cpu_baseline and world == 1:
-        out["cpu_baseline"] = cpu_baseline(scene, bits)
+        out["cpu_baseline"] = cpu_baseline(scene, bits, offs, preroll=res["cfg"].get("preroll_steps", 0))
     print(json.dumps(out))
     return 0
 

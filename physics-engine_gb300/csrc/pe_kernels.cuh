@@ -359,16 +359,28 @@ template <class R> __device__ __forceinline__ V3<R> shfl3(const V3<R>& v, int sr
 // Shape::project (so the same bits); only the order of evaluation across axes differs.
 constexpr int kSatF = 128, kSatE = 192, kSatV = 64;
 constexpr int kSatWarps = 4;
-template <class R> constexpr int sat_stage_reals() { return 3 * (2 * kSatF + 2 * kSatE + 2 * kSatV); }
+template <class R> constexpr int sat_stage_reals() { return 3 * (2 * kSatF + 2 * kSatE) + 4 * 2 * kSatV; }
 
 template <class R> struct SatStage {
-    R* nA; R* nB; R* dA; R* dB; R* vA; R* vB;
+    R* nA; R* nB; R* dA; R* dB; R* vA; R* vB;   // vertices padded to 4 reals (16-byte aligned rows)
     __device__ void bind(R* base) {
-        nA = base; nB = nA + 3 * kSatF; dA = nB + 3 * kSatF; dB = dA + 3 * kSatE; vA = dB + 3 * kSatE; vB = vA + 3 * kSatV;
+        nA = base; nB = nA + 3 * kSatF; dA = nB + 3 * kSatF; dB = dA + 3 * kSatE; vA = dB + 3 * kSatE; vB = vA + 4 * kSatV;
     }
 };
 template <class R> __device__ __forceinline__ V3<R> ld3(const R* p, int i) { return V3<R>(p[3 * i], p[3 * i + 1], p[3 * i + 2]); }
 template <class R> __device__ __forceinline__ void st3(R* p, int i, const V3<R>& v) { p[3 * i] = v.x; p[3 * i + 1] = v.y; p[3 * i + 2] = v.z; }
+__device__ __forceinline__ V3<float> ldv(const float* p, int i) {
+    const float4 f = reinterpret_cast<const float4*>(p)[i];
+    return V3<float>(f.x, f.y, f.z);
+}
+__device__ __forceinline__ V3<double> ldv(const double* p, int i) {
+    const double2* q = reinterpret_cast<const double2*>(p) + 2 * i;
+    const double2 a = q[0], b = q[1];
+    return V3<double>(a.x, a.y, b.x);
+}
+template <class R> __device__ __forceinline__ void stv(R* p, int i, const V3<R>& v) {
+    p[4 * i] = v.x; p[4 * i + 1] = v.y; p[4 * i + 2] = v.z; p[4 * i + 3] = R(0);
+}
 
 template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& s) {
     return s.face_count() <= kSatF && s.edge_count() <= kSatE && (s.type != ST_HULL || s.nv <= kSatV);
@@ -410,12 +422,37 @@ __device__ __forceinline__ void shape_interval(const ShapeView<R>& s, const Xf<R
     mxp = Lim<R>::min();
     imn = -1; imx = -1;
     for (int i = 0; i < s.nv; i++) {
-        const R v = dot(ld3(lv, i), la);
+        const R v = dot(ldv(lv, i), la);
         if (v < mnp) { mnp = v; imn = i; }
         else if (v > mxp) { mxp = v; imx = i; }
     }
     mnp += off;
     mxp += off;
+}
+
+// two axes at once: a hull's vertices are loaded once for both (same arithmetic per axis)
+template <class R>
+__device__ __forceinline__ void shape_interval2(const ShapeView<R>& s, const Xf<R>& t, const V3<R>* axis, const R* lv, R* mnp, R* mxp,
+                                                int* imn, int* imx) {
+    if (s.type != ST_HULL) {
+        shape_interval(s, t, axis[0], lv, mnp[0], mxp[0], imn[0], imx[0]);
+        shape_interval(s, t, axis[1], lv, mnp[1], mxp[1], imn[1], imx[1]);
+        return;
+    }
+    const V3<R> l0 = mtv(t.b, axis[0]), l1 = mtv(t.b, axis[1]);
+    R n0 = Lim<R>::max(), x0 = Lim<R>::min(), n1 = Lim<R>::max(), x1 = Lim<R>::min();
+    int in0 = -1, ix0 = -1, in1 = -1, ix1 = -1;
+    for (int i = 0; i < s.nv; i++) {
+        const V3<R> p = ldv(lv, i);
+        const R v0 = dot(p, l0), v1 = dot(p, l1);
+        if (v0 < n0) { n0 = v0; in0 = i; }
+        else if (v0 > x0) { x0 = v0; ix0 = i; }
+        if (v1 < n1) { n1 = v1; in1 = i; }
+        else if (v1 > x1) { x1 = v1; ix1 = i; }
+    }
+    const R o0 = dot(t.o, axis[0]), o1 = dot(t.o, axis[1]);
+    mnp[0] = n0 + o0; mxp[0] = x0 + o0; imn[0] = in0; imx[0] = ix0;
+    mnp[1] = n1 + o1; mxp[1] = x1 + o1; imn[1] = in1; imx[1] = ix1;
 }
 
 // witness point of Shape::project on the min (want_max = false) or max side
@@ -426,7 +463,7 @@ __device__ V3<R> shape_witness(const ShapeView<R>& s, const Xf<R>& t, const V3<R
     if (s.type == ST_HULL) {
         // an index never set leaves the reference's witness undefined; that only happens on a
         // separating axis, whose witness is never used
-        const V3<R> p = idx >= 0 ? ld3(lv, idx) : V3<R>(0, 0, 0);
+        const V3<R> p = idx >= 0 ? ldv(lv, idx) : V3<R>(0, 0, 0);
         return t.apply(p);
     }
     shape_project(s, t, axis, a, b, pmin, pmax);
@@ -444,27 +481,40 @@ __device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
     for (int f = lane; f < fb; f += 32) st3(st.nB, f, mv(c.tb().b, c.sb.face_normal(f)));
     for (int e = lane; e < na; e += 32) { V3<R> a0, a1; c.sa.edge(e, a0, a1); st3(st.dA, e, mv(c.ta().b, normalized(a0 - a1))); }
     for (int e = lane; e < nb; e += 32) { V3<R> b0, b1; c.sb.edge(e, b0, b1); st3(st.dB, e, mv(c.tb().b, normalized(b0 - b1))); }
-    if (c.sa.type == ST_HULL) for (int i = lane; i < c.sa.nv; i += 32) st3(st.vA, i, c.sa.vert(i));
-    if (c.sb.type == ST_HULL) for (int i = lane; i < c.sb.nv; i += 32) st3(st.vB, i, c.sb.vert(i));
+    if (c.sa.type == ST_HULL) for (int i = lane; i < c.sa.nv; i += 32) stv(st.vA, i, c.sa.vert(i));
+    if (c.sb.type == ST_HULL) for (int i = lane; i < c.sb.nv; i += 32) stv(st.vB, i, c.sb.vert(i));
     __syncwarp();
     const V3<R> dc = c.ta().o - c.tb().o;
-    // ---- face axes of A, then of B (findSeparatingAxis :265-308)
+    // ---- face axes of A, then of B (findSeparatingAxis :265-308); each lane takes axes f and
+    // f + 32 of a 64-axis chunk, and the warp stops at the first chunk holding a separating axis
     R bd = Lim<R>::max();
     int bf = 0x7fffffff, bside = 0, bia = -1, bib = -1;
-    bool sep_found = false;
-    for (int f = lane; f < fa + fb; f += 32) {
-        V3<R> n = f < fa ? ld3(st.nA, f) : ld3(st.nB, f - fa);
-        if (dot(dc, n) < 0) n = n * R(-1.0);
-        R min0, max0, min1, max1;
-        int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
-        shape_interval(c.sa, c.ta(), n, st.vA, min0, max0, a0, a1);
-        shape_interval(c.sb, c.tb(), n, st.vB, min1, max1, b0, b1);
-        if (max0 < min1 || max1 < min0) { sep_found = true; break; }
-        const R d0 = max0 - min1, d1 = max1 - min0;
-        const R d = d0 < d1 ? d0 : d1;
-        if (d < bd) { bd = d; bf = f; bside = d0 < d1; bia = d0 < d1 ? a1 : a0; bib = d0 < d1 ? b0 : b1; }
+    for (int base = 0; base < fa + fb; base += 64) {
+        V3<R> n[2];
+        bool ok[2];
+        for (int k = 0; k < 2; k++) {
+            const int f = base + 32 * k + lane;
+            ok[k] = f < fa + fb;
+            n[k] = !ok[k] ? V3<R>(0, 0, 0) : f < fa ? ld3(st.nA, f) : ld3(st.nB, f - fa);
+            if (ok[k] && dot(dc, n[k]) < 0) n[k] = n[k] * R(-1.0);
+        }
+        R min0[2], max0[2], min1[2], max1[2];
+        int a0[2], a1[2], b0[2], b1[2];
+        shape_interval2(c.sa, c.ta(), n, st.vA, min0, max0, a0, a1);
+        shape_interval2(c.sb, c.tb(), n, st.vB, min1, max1, b0, b1);
+        bool sep = false;
+        for (int k = 0; k < 2; k++) sep |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
+        if (__any_sync(0xffffffffu, sep)) return false;
+        for (int k = 0; k < 2; k++) {
+            if (!ok[k]) continue;
+            const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
+            const R d = d0 < d1 ? d0 : d1;
+            if (d < bd) {
+                bd = d; bf = base + 32 * k + lane; bside = d0 < d1;
+                bia = d0 < d1 ? a1[k] : a0[k]; bib = d0 < d1 ? b0[k] : b1[k];
+            }
+        }
     }
-    if (__any_sync(0xffffffffu, sep_found)) return false;
     R dmin = bd;
     int wf = bf;
     warp_argmin(dmin, wf);
@@ -490,33 +540,49 @@ __device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
     R ed = dmin;
     int ep = 0x7fffffff;
     V3<R> ewa, ewb, en;
-    sep_found = false;
-    for (int q = lane; q < na * nb; q += 32) {
-        const int e0 = q / nb, e1 = q - e0 * nb;
-        const V3<R> w0 = ld3(st.dA, e0), w1 = ld3(st.dB, e1);
-        V3<R> cr = cross(w0, w1);
-        if (rabs(norm(cr) - 0) < eps<R>()) continue;
-        cr = normalized(cr);
-        if (dot(dc, cr) < 0) cr = cr * R(-1.0);
-        R min0, max0, min1, max1;
-        int a0 = -1, a1 = -1, b0 = -1, b1 = -1;
-        shape_interval(c.sa, c.ta(), cr, st.vA, min0, max0, a0, a1);
-        shape_interval(c.sb, c.tb(), cr, st.vB, min1, max1, b0, b1);
-        if (max0 < min1 || max1 < min0) { sep_found = true; break; }
-        const R d0 = max0 - min1, d1 = max1 - min0;
-        const R dist = d0 < d1 ? d0 : d1;
-        if (dist < ed) {
-            const bool side = d0 < d1;
-            const V3<R> wa = shape_witness(c.sa, c.ta(), cr, side, side ? a1 : a0, st.vA);
-            const V3<R> wb = shape_witness(c.sb, c.tb(), cr, !side, side ? b0 : b1, st.vB);
-            V3<R> p0, p1, q0, q1;
-            c.sa.edge(e0, p0, p1);
-            c.sb.edge(e1, q0, q1);
-            if (!on_line(p0, p1, c.ta().inv_apply(wa)) || !on_line(q0, q1, c.tb().inv_apply(wb))) continue;
-            ed = dist; ep = q; ewa = wa; ewb = wb; en = cr;
+    const int ne = na * nb;
+    for (int base = 0; base < ne; base += 64) {
+        V3<R> cr[2];
+        bool ok[2];
+        for (int k = 0; k < 2; k++) {
+            const int q = base + 32 * k + lane;
+            ok[k] = false;
+            cr[k] = V3<R>(0, 0, 0);
+            if (q < ne) {
+                const int e0 = q / nb, e1 = q - e0 * nb;
+                const V3<R> x = cross(ld3(st.dA, e0), ld3(st.dB, e1));
+                if (!(rabs(norm(x) - 0) < eps<R>())) {
+                    ok[k] = true;
+                    cr[k] = normalized(x);
+                    if (dot(dc, cr[k]) < 0) cr[k] = cr[k] * R(-1.0);
+                }
+            }
+        }
+        R min0[2], max0[2], min1[2], max1[2];
+        int a0[2], a1[2], b0[2], b1[2];
+        shape_interval2(c.sa, c.ta(), cr, st.vA, min0, max0, a0, a1);
+        shape_interval2(c.sb, c.tb(), cr, st.vB, min1, max1, b0, b1);
+        bool sep = false;
+        for (int k = 0; k < 2; k++) sep |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
+        if (__any_sync(0xffffffffu, sep)) return false;
+        for (int k = 0; k < 2; k++) {
+            if (!ok[k]) continue;
+            const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
+            const R dist = d0 < d1 ? d0 : d1;
+            if (dist < ed) {
+                const int q = base + 32 * k + lane;
+                const int e0 = q / nb, e1 = q - e0 * nb;
+                const bool side = d0 < d1;
+                const V3<R> wa = shape_witness(c.sa, c.ta(), cr[k], side, side ? a1[k] : a0[k], st.vA);
+                const V3<R> wb = shape_witness(c.sb, c.tb(), cr[k], !side, side ? b0[k] : b1[k], st.vB);
+                V3<R> p0, p1, q0, q1;
+                c.sa.edge(e0, p0, p1);
+                c.sb.edge(e1, q0, q1);
+                if (!on_line(p0, p1, c.ta().inv_apply(wa)) || !on_line(q0, q1, c.tb().inv_apply(wb))) continue;
+                ed = dist; ep = q; ewa = wa; ewb = wb; en = cr[k];
+            }
         }
     }
-    if (__any_sync(0xffffffffu, sep_found)) return false;
     R emin = ed;
     int wq = ep;
     warp_argmin(emin, wq);
@@ -676,7 +742,7 @@ __device__ bool sat_warp(Pair<R>& c, int lane) {
 }
 
 template <class R>
-__global__ void k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+__global__ void __launch_bounds__(32 * kSatWarps, 4) k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
                          const int* pair_scene_off, const int* prev_off) {
     extern __shared__ __align__(16) unsigned char sat_smem[];
     const int warp = threadIdx.x >> 5;

@@ -408,3 +408,151 @@ def concat(scenes):
     out.hull_verts = out.hull_verts.reshape(-1, 3)
     out.hull_face_off = np.array(face_off, np.int32)
     return out, np.array(offs, np.int32)
+
+
+def _hull_volumes(verts, faces):
+    f = np.asarray(faces, np.int64)
+    a, b, c = verts[f[:, 0]], verts[f[:, 1]], verts[f[:, 2]]
+    return float(np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6.0)
+
+
+def batched_piles(n_scenes=4096, seed=0, size_range=(8, 512), mix=(0.5, 0.2, 0.1, 0.2), hull_pool=512,
+                  hull_range=(8, 64), drop=(0.0, 5.0), density=1000.0, dt=1.0 / 60.0, iterations=10,
+                  real_bits=32):
+    """``n_scenes`` independent piles, each laid out like ``pile`` (a jittered grid of mixed shapes
+    above its own static ground box, lowest layer drop[0]..drop[1] m up), with body counts
+    log-uniform in ``size_range``.  Box/sphere/cylinder sizes follow ``random_cube``; convex hulls
+    have 8..64 vertices on a sphere scaled U[0.3, 1.0] and are drawn from a seeded pool of
+    ``hull_pool`` shapes shared by all scenes (bodies may share a shape, as RigidBody shape
+    pointers may in the reference).  Returns (Scene, body offsets [n_scenes + 1]); the bodies of
+    scene k are [off[k], off[k+1]), its ground box first.  Vectorised: ~500k bodies in seconds."""
+    rng = np.random.default_rng(seed)
+    lo, hi = size_range
+    sizes = np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), n_scenes))).astype(np.int64).clip(lo, hi)
+    # hull pool
+    pool_v, pool_f, pool_vol = [], [], []
+    for _ in range(hull_pool):
+        nv = int(rng.integers(hull_range[0], hull_range[1] + 1))
+        v, f = random_hull(rng, nv, rng.uniform(0.3, 1.0))
+        pool_v.append(v)
+        pool_f.append(f)
+        pool_vol.append(_hull_volumes(v, f))
+    pool_vol = np.array(pool_vol)
+    sides = np.maximum(2, np.ceil(np.sqrt(sizes / 2.0))).astype(np.int64)
+    pitch = 2.2
+    n_dyn = int(sizes.sum())
+    N = n_dyn + n_scenes
+    # body -> scene, index inside the scene's pile
+    scene_of = np.repeat(np.arange(n_scenes), sizes)
+    start = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    idx = np.arange(n_dyn) - start[scene_of]
+    kinds = rng.choice(4, size=n_dyn, p=np.asarray(mix) / np.sum(mix))
+    side = sides[scene_of]
+    layer, cell = np.divmod(idx, side * side)
+    gx, gz = np.divmod(cell, side)
+    base = rng.uniform(drop[0], drop[1], n_scenes)[scene_of]
+    org = np.stack([(gx - side / 2) * pitch + rng.uniform(-0.1, 0.1, n_dyn), 1.2 + base + layer * pitch,
+                    (gz - side / 2) * pitch + rng.uniform(-0.1, 0.1, n_dyn)], axis=1)
+    rot = random_rotations(rng, n_dyn)
+    # shapes: hull pool first, then one ground box per distinct side, then one shape per primitive body
+    he = rng.uniform(0.2, 1.0, size=(n_dyn, 3))
+    rs = rng.uniform(0.2, 1.0, n_dyn)
+    rc = rng.uniform(0.2, 0.8, n_dyn)
+    hc = rng.uniform(0.4, 2.0, n_dyn)
+    pick = rng.integers(0, hull_pool, n_dyn)
+    uniq_sides, side_idx = np.unique(sides, return_inverse=True)
+    prim = kinds != HULL
+    n_prim = int(prim.sum())
+    S = hull_pool + len(uniq_sides) + n_prim
+    shape_type = np.zeros(S, np.int32)
+    shape_param = np.zeros((S, 3))
+    shape_type[:hull_pool] = HULL
+    g0 = hull_pool
+    shape_type[g0:g0 + len(uniq_sides)] = BOX
+    gs = uniq_sides * pitch + 10.0
+    shape_param[g0:g0 + len(uniq_sides)] = np.stack([gs, np.ones_like(gs, dtype=np.float64), gs], axis=1)
+    p0 = g0 + len(uniq_sides)
+    pk = kinds[prim]
+    shape_type[p0:] = pk
+    par = np.zeros((n_prim, 3))
+    par[pk == BOX] = 2 * he[prim][pk == BOX]
+    par[pk == SPHERE, 0] = rs[prim][pk == SPHERE]
+    par[pk == CYLINDER, 0] = rc[prim][pk == CYLINDER]
+    par[pk == CYLINDER, 1] = hc[prim][pk == CYLINDER]
+    shape_param[p0:] = par
+    body_shape_dyn = np.where(prim, 0, pick)
+    body_shape_dyn[prim] = p0 + np.arange(n_prim)
+    vol = np.where(kinds == BOX, np.prod(2 * he, axis=1),
+                   np.where(kinds == SPHERE, 4.0 / 3.0 * np.pi * rs ** 3,
+                            np.where(kinds == CYLINDER, np.pi * rc * rc * hc, pool_vol[pick])))
+    # hull tables
+    vbeg, vcnt, fbeg, fcnt = (np.zeros(S, np.int32) for _ in range(4))
+    vcnt[:hull_pool] = [len(v) for v in pool_v]
+    fcnt[:hull_pool] = [len(f) for f in pool_f]
+    vbeg[:hull_pool] = np.concatenate([[0], np.cumsum(vcnt[:hull_pool])[:-1]])
+    fbeg[:hull_pool] = np.concatenate([[0], np.cumsum(fcnt[:hull_pool])[:-1]])
+    face_idx = np.concatenate([np.asarray(f, np.int32).ravel() for f in pool_f])
+    face_off = np.arange(0, 3 * int(fcnt.sum()) + 1, 3, dtype=np.int32)
+    # interleave: scene k = [ground_k, its bodies]
+    pos = np.arange(n_dyn) + scene_of + 1            # body slot in the merged order
+    gpos = start + np.arange(n_scenes)               # ground slot of each scene
+    s = Scene(dt=dt, gravity=(0.0, -9.8, 0.0), iterations=iterations, real_bits=64)
+    s.shape_type, s.shape_param = shape_type, shape_param
+    s.hull_vbeg, s.hull_vcnt, s.hull_fbeg, s.hull_fcnt = vbeg, vcnt, fbeg, fcnt
+    s.hull_verts = np.concatenate(pool_v).reshape(-1, 3)
+    s.hull_face_off, s.hull_face_idx = face_off, face_idx
+    s.body_shape = np.zeros(N, np.int32)
+    s.body_shape[pos] = body_shape_dyn
+    s.body_shape[gpos] = g0 + side_idx
+    s.body_flags = np.zeros(N, np.int32)
+    s.body_flags[gpos] = KINEMATIC
+    s.mass = np.zeros(N)
+    s.mass[pos] = density * vol
+    s.friction = np.full(N, 0.5)
+    s.restitution = np.zeros(N)
+    s.lin_damp = np.zeros(N)
+    s.ang_damp = np.zeros(N)
+    s.origin = np.zeros((N, 3))
+    s.origin[pos] = org
+    s.origin[gpos] = (0.0, -0.5, 0.0)
+    s.basis = np.tile(np.eye(3), (N, 1, 1))
+    s.basis[pos] = rot
+    s.lin_vel = np.zeros((N, 3))
+    s.ang_vel = np.zeros((N, 3))
+    offs = np.concatenate([[0], np.cumsum(sizes + 1)]).astype(np.int32)
+    return (s.rounded(real_bits) if real_bits == 32 else s), offs
+
+
+def extract(scene, offs, k):
+    """Scene k of a batch as a standalone Scene (its bodies and the shapes they use)."""
+    b0, b1 = int(offs[k]), int(offs[k + 1])
+    used = np.unique(scene.body_shape[b0:b1])
+    remap = np.full(scene.n_shapes, -1, np.int64)
+    remap[used] = np.arange(len(used))
+    s = Scene(dt=scene.dt, gravity=scene.gravity, iterations=scene.iterations, real_bits=scene.real_bits)
+    s.shape_type = scene.shape_type[used].copy()
+    s.shape_param = scene.shape_param[used].copy()
+    vbeg, vcnt, fbeg, fcnt = (np.zeros(len(used), np.int32) for _ in range(4))
+    verts, face_off, face_idx = [], [0], []
+    nv = nf = 0
+    for t, sh in enumerate(used):
+        if scene.shape_type[sh] != HULL:
+            continue
+        v0, vc = scene.hull_vbeg[sh], scene.hull_vcnt[sh]
+        f0, fc = scene.hull_fbeg[sh], scene.hull_fcnt[sh]
+        vbeg[t], vcnt[t], fbeg[t], fcnt[t] = nv, vc, nf, fc
+        verts.append(scene.hull_verts[v0:v0 + vc])
+        for f in range(f0, f0 + fc):
+            face_idx.extend(scene.hull_face_idx[scene.hull_face_off[f]:scene.hull_face_off[f + 1]].tolist())
+            face_off.append(len(face_idx))
+        nv += vc
+        nf += fc
+    s.hull_vbeg, s.hull_vcnt, s.hull_fbeg, s.hull_fcnt = vbeg, vcnt, fbeg, fcnt
+    s.hull_verts = np.concatenate(verts).reshape(-1, 3) if verts else np.zeros((0, 3))
+    s.hull_face_off = np.array(face_off, np.int32)
+    s.hull_face_idx = np.array(face_idx, np.int32)
+    s.body_shape = remap[scene.body_shape[b0:b1]].astype(np.int32)
+    for f in ("body_flags", "mass", "friction", "restitution", "lin_damp", "ang_damp", "origin", "basis", "lin_vel",
+              "ang_vel"):
+        setattr(s, f, getattr(scene, f)[b0:b1].copy())
+    return s

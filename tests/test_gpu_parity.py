@@ -152,6 +152,24 @@ def test_gpu_batched_scenes_equal_scenes_alone():
                 np.testing.assert_array_equal(big[k][sl], alone[k], err_msg=f"scene {i} {k} mode {mode}")
 
 
+def test_gpu_batched_piles_equal_scenes_alone():
+    """The batched-pile workload generator (shared hull pool, uneven scene sizes): a batch of 48
+    scenes stepped together equals, per scene, the scene extracted and stepped alone."""
+    merged, offs = sc.batched_piles(n_scenes=48, seed=7, size_range=(8, 96), hull_pool=16, real_bits=32)
+    picks = (0, 5, 17, 47)
+    for mode in (pg.SERIAL_ORDER, pg.COLORED):
+        g = pg.GpuWorld(merged, 32, scenes=offs)
+        g.step(30, mode)
+        big = g.state()
+        for k in picks:
+            a = pg.GpuWorld(sc.extract(merged, offs, k), 32)
+            a.step(30, mode)
+            alone = a.state()
+            sl = slice(offs[k], offs[k + 1])
+            for f in ("origin", "basis", "lin_vel", "ang_vel"):
+                np.testing.assert_array_equal(big[f][sl], alone[f], err_msg=f"scene {k} {f} mode {mode}")
+
+
 def test_gpu_colored_tower_stays_physical():
     """Coloured Gauss-Seidel on the tower hit by the sphere: contacts stay resolved (max
     penetration bounded like the serial solver's) and nothing gains energy from nowhere."""

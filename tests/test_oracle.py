@@ -137,3 +137,20 @@ def test_oracle_stale_slot_distances_truncate_results():
     w.set_results(seeded)
     w.narrowphase()
     assert w.results()["point_size"][0] == 0   # all new points sort behind invalid slots
+
+
+def test_batched_piles_extract_round_trip():
+    """Scenes extracted from a generated batch carry exactly the batch's bodies and shapes."""
+    merged, offs = sc.batched_piles(n_scenes=12, seed=3, size_range=(8, 40), hull_pool=6, real_bits=32)
+    assert offs[-1] == merged.n_bodies and len(offs) == 13
+    parts = [sc.extract(merged, offs, k) for k in range(12)]
+    again, offs2 = sc.concat(parts)
+    np.testing.assert_array_equal(offs, offs2)
+    for f in ("body_flags", "mass", "origin", "basis", "lin_vel"):
+        np.testing.assert_array_equal(getattr(again, f), getattr(merged, f))
+    for k, p in enumerate(parts):
+        assert p.body_flags[0] == sc.KINEMATIC and p.mass[0] == 0.0   # ground first
+        for i in range(p.n_bodies):
+            t0, t1 = merged.shape_type[merged.body_shape[offs[k] + i]], p.shape_type[p.body_shape[i]]
+            assert t0 == t1
+            np.testing.assert_array_equal(merged.shape_param[merged.body_shape[offs[k] + i]], p.shape_param[p.body_shape[i]])
