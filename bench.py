@@ -40,7 +40,7 @@ METRIC = "body-steps/s batched vs per-scene GPU step at oracle tol; p50/p99 step
 UNIT = "body-steps/s"
 
 
-def make_workload(name):
+def make_workload(name, n_scenes=4096):
     from pe_gb300 import scene as sc
     if name == "stress":
         s = sc.random_cube(n=65536, seed=2024, real_bits=32)
@@ -53,11 +53,11 @@ def make_workload(name):
                                              "20 SI iterations, serial-order solver", bodies=s.n_bodies, scenes=1,
                                     solver="serial-order")
     if name == "batched":
-        s, offs = sc.batched_piles(n_scenes=4096, seed=4096, real_bits=32)
-        return s, 32, 1, offs, dict(workload="4,096 independent piles of 8..512 bodies (log-uniform; box/sphere/cylinder/"
+        s, offs = sc.batched_piles(n_scenes=n_scenes, seed=4096, real_bits=32)
+        return s, 32, 1, offs, dict(workload=f"{n_scenes:,} independent piles of 8..512 bodies (log-uniform; box/sphere/cylinder/"
                                              "convex hull 50/20/10/20, hulls of 8..64 vertices from a 512-shape pool) "
                                              "on static ground boxes, one batched step, FP32, 10 SI iterations, coloured",
-                                    bodies=s.n_bodies, scenes=4096, solver="coloured", preroll_steps=120)
+                                    bodies=s.n_bodies, scenes=n_scenes, solver="coloured", preroll_steps=120)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -239,7 +239,7 @@ KERNEL_GROUPS = {"integrate": ("integrate",), "bp_sort": ("radix_sort",), "bp_sw
 # ------------------------------------------------------------------ our arm
 def run_ours(args, rank, world, device):
     import pe_gb300 as pg
-    scene, bits, mode, offs, cfg = make_workload(args.workload)
+    scene, bits, mode, offs, cfg = make_workload(args.workload, args.scenes)
     g = pg.GpuWorld(scene, bits, device=device, scenes=offs)
     flush = L2Flush()
     N = scene.n_bodies
@@ -286,7 +286,7 @@ def run_ours(args, rank, world, device):
         e2e_times.append(time.perf_counter() - t0)
     io_bytes = N * 18 * 8   # float64 poses and velocities through the C ABI, each way
     per_scene = per_scene_gpu(pg, scene, offs, g.state(fields=("origin", "basis", "lin_vel", "ang_vel")), bits, mode,
-                              device, args.steps) if offs is not None else None
+                              device, args.steps) if offs is not None and not args.no_per_scene else None
     res = dict(dev_ms=dev_ms, per_step=per_step, N=N, launches=launches, counts=counts, cfg=cfg, bits=bits, clk=clk.summary(),
                roofline=dict(kernel=dom, bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
                              traffic=traffic, algorithmic_bytes=dom_bytes, launches=dom_n, avg_launch_ms=dom_ms / max(dom_n, 1),
@@ -374,6 +374,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="stress", choices=["stress", "tower", "batched"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scenes", type=int, default=4096, help="scene count of the batched workload")
+    ap.add_argument("--no-per-scene", action="store_true", help="skip the one-scene-per-launch comparison")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -382,7 +384,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        scene, bits, mode, offs, cfg = make_workload(args.workload)
+        scene, bits, mode, offs, cfg = make_workload(args.workload, args.scenes)
         if offs is not None:   # independent scenes: the reference steps one World per scene
             pass
         cfg = dict(cfg, solver="serial (the reference's sequential impulse order)")

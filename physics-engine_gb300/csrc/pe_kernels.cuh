@@ -246,12 +246,31 @@ __global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_of
 
 // ===================================================================== narrowphase
 // bucket pairs by algorithm class
+// Shared-memory staging limits of the SAT kernels (faces, unique edges, hull vertices per shape),
+// and the scheduling split of ConvexConvexCollisionAlgorithm pairs by estimated work: candidate
+// axes x projection cost (hull vertices; a box or cylinder projects in closed form).
+constexpr int kSatF = 128, kSatE = 192, kSatV = 64;
+constexpr int kSatWarps = 4;                 // pairs (one warp each) per block, light pairs
+constexpr int kSatGroup = 8;                 // warps per pair, heavy pairs (one block each)
+constexpr long long kSatHeavyCost = 200000;
+template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& s) {
+    return s.face_count() <= kSatF && s.edge_count() <= kSatE && (s.type != ST_HULL || s.nv <= kSatV);
+}
+template <class R> __device__ __forceinline__ int sat_class(const ShapeView<R>& a, const ShapeView<R>& b) {
+    if (!sat_fits(a) || !sat_fits(b)) return PC_CONVEX_BIG;
+    auto w = [](const ShapeView<R>& s) { return s.type == ST_HULL ? s.nv : s.type == ST_CYLINDER ? 12 : s.type == ST_BOX ? 8 : 2; };
+    const long long axes = (long long)a.face_count() + b.face_count() + (long long)a.edge_count() * b.edge_count();
+    return axes * (w(a) + w(b)) >= kSatHeavyCost ? PC_CONVEX_HEAVY : PC_CONVEX;
+}
+
 template <class R>
-__global__ void k_np_classify(int P, const int2* pairs, Bodies<R> B, const int* shape_type, int* cls, int* cls_count) {
+__global__ void k_np_classify(int P, const int2* pairs, Bodies<R> B, ShapeTable<R> S, int* cls, int* cls_count) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
     const int2 q = pairs[p];
-    const int c = pair_class(shape_type[B.shape[q.x]], shape_type[B.shape[q.y]]);
+    const ShapeView<R> sa = S.view(B.shape[q.x]), sb = S.view(B.shape[q.y]);
+    int c = pair_class(sa.type, sb.type);
+    if (c == PC_CONVEX) c = sat_class(sa, sb);
     cls[p] = c;
     atomicAdd(&cls_count[c], 1);
 }
@@ -262,14 +281,16 @@ __global__ void k_np_bucket(int P, const int* cls, int* cursor, int* order);
 // same (scene-local) result index existed then, the "fresh result" maximum otherwise.
 template <class R>
 __device__ __forceinline__ void np_setup(int p, const int2* pairs, const Bodies<R>& B, const ShapeTable<R>& S, const Results<R>& res,
-                                         const int* pair_scene_off, const int* prev_off, Cache<R>& cache, Pair<R>& pr) {
+                                         const int* pair_scene_off, const int* prev_off, Cache<R>& cache, Pair<R>& pr,
+                                         bool load_cache = true) {
     const int2 q = pairs[p];
     const int ia = q.x, ib = q.y;
     cache.valid = 0;
     cache.swap = false;
     const int sc = B.scene[ia];
     const int local = p - pair_scene_off[sc];
-    if (local < prev_off[sc + 1] - prev_off[sc]) {
+    if (!load_cache) {
+    } else if (local < prev_off[sc + 1] - prev_off[sc]) {
         const int src = (prev_off[sc] + local) * kSlots;
         for (int k = 0; k < kSlots; k++) cache.dist[k] = res.prev_dist[src + k];
     } else {
@@ -342,6 +363,12 @@ template <class R> __device__ __forceinline__ void warp_argmin(R& d, int& idx) {
         if (od < d || (od == d && oi < idx)) { d = od; idx = oi; }
     }
 }
+template <class R> __device__ __forceinline__ void warp_min(R& d) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const R od = __shfl_xor_sync(0xffffffffu, d, o);
+        if (od < d) d = od;
+    }
+}
 template <class R> __device__ __forceinline__ void warp_argmax(R& d, int& idx) {
     for (int o = 16; o > 0; o >>= 1) {
         const R od = __shfl_xor_sync(0xffffffffu, d, o);
@@ -357,8 +384,6 @@ template <class R> __device__ __forceinline__ V3<R> shfl3(const V3<R>& v, int sr
 // vertices of both shapes are computed once into shared memory; support intervals are computed
 // first and witness points only for an axis that becomes the current best.  Same formulas as
 // Shape::project (so the same bits); only the order of evaluation across axes differs.
-constexpr int kSatF = 128, kSatE = 192, kSatV = 64;
-constexpr int kSatWarps = 4;
 template <class R> constexpr int sat_stage_reals() { return 3 * (2 * kSatF + 2 * kSatE) + 4 * 2 * kSatV; }
 
 template <class R> struct SatStage {
@@ -382,9 +407,6 @@ template <class R> __device__ __forceinline__ void stv(R* p, int i, const V3<R>&
     p[4 * i] = v.x; p[4 * i + 1] = v.y; p[4 * i + 2] = v.z; p[4 * i + 3] = R(0);
 }
 
-template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& s) {
-    return s.face_count() <= kSatF && s.edge_count() <= kSatE && (s.type != ST_HULL || s.nv <= kSatV);
-}
 
 // support interval of a shape along a world axis (Shape::project without the witness points);
 // for hulls the indices of the witness vertices are returned (the first vertex never becomes
@@ -455,6 +477,60 @@ __device__ __forceinline__ void shape_interval2(const ShapeView<R>& s, const Xf<
     mnp[1] = n1 + o1; mxp[1] = x1 + o1; imn[1] = in1; imx[1] = ix1;
 }
 
+// Intervals of both shapes along two axes.  The larger hull's vertex loop may stop early: its
+// running minimum only falls and its (first-vertex-excluding) running maximum only rises, so the
+// overlap depths min(maxA - minB, maxB - minA) computed from a prefix of its vertices are lower
+// bounds of the final ones (IEEE rounding is monotone).  Once both depths of an axis exceed `best`
+// (an upper bound of the pair's minimum depth) the axis can neither separate nor be the minimum;
+// when that holds for both axes the loop ends and both are reported not live.
+template <class R>
+__device__ __forceinline__ void pair_intervals2(const Pair<R>& c, const V3<R>* ax, bool* live, R best, const R* vA, const R* vB,
+                                                R* min0, R* max0, R* min1, R* max1, int* a0, int* a1, int* b0, int* b1) {
+    const bool part_b = c.sb.type == ST_HULL && (c.sa.type != ST_HULL || c.sb.nv >= c.sa.nv);
+    const bool part_a = !part_b && c.sa.type == ST_HULL;
+    if (!part_a && !part_b) {
+        shape_interval2(c.sa, c.ta(), ax, vA, min0, max0, a0, a1);
+        shape_interval2(c.sb, c.tb(), ax, vB, min1, max1, b0, b1);
+        return;
+    }
+    // the complete side first
+    const ShapeView<R>& sp = part_b ? c.sb : c.sa;
+    const Xf<R>& tp = part_b ? c.tb() : c.ta();
+    const R* lv = part_b ? vB : vA;
+    R cmn[2], cmx[2];
+    if (part_b) { shape_interval2(c.sa, c.ta(), ax, vA, min0, max0, a0, a1); cmn[0] = min0[0]; cmn[1] = min0[1]; cmx[0] = max0[0]; cmx[1] = max0[1]; }
+    else { shape_interval2(c.sb, c.tb(), ax, vB, min1, max1, b0, b1); cmn[0] = min1[0]; cmn[1] = min1[1]; cmx[0] = max1[0]; cmx[1] = max1[1]; }
+    const V3<R> l0 = mtv(tp.b, ax[0]), l1 = mtv(tp.b, ax[1]);
+    const R o0 = dot(tp.o, ax[0]), o1 = dot(tp.o, ax[1]);
+    R n0 = Lim<R>::max(), x0 = Lim<R>::min(), n1 = Lim<R>::max(), x1 = Lim<R>::min();
+    int in0 = -1, ix0 = -1, in1 = -1, ix1 = -1;
+    bool done = false;
+    for (int i0 = 0; i0 < sp.nv; i0 += 8) {
+        const int e = i0 + 8 < sp.nv ? i0 + 8 : sp.nv;
+        for (int i = i0; i < e; i++) {
+            const V3<R> p = ldv(lv, i);
+            const R v0 = dot(p, l0), v1 = dot(p, l1);
+            if (v0 < n0) { n0 = v0; in0 = i; }
+            else if (v0 > x0) { x0 = v0; ix0 = i; }
+            if (v1 < n1) { n1 = v1; in1 = i; }
+            else if (v1 > x1) { x1 = v1; ix1 = i; }
+        }
+        if (e == sp.nv) break;
+        // partial depths: d0 = maxA - minB, d1 = maxB - minA with the partial side's running values
+        bool dec[2];
+        const R pn[2] = {n0 + o0, n1 + o1}, px[2] = {x0 + o0, x1 + o1};
+        for (int k = 0; k < 2; k++) {
+            const R d0 = part_b ? cmx[k] - pn[k] : px[k] - cmn[k];
+            const R d1 = part_b ? px[k] - cmn[k] : cmx[k] - pn[k];
+            dec[k] = !live[k] || (d0 > best && d1 > best);
+        }
+        if (dec[0] && dec[1]) { done = true; break; }
+    }
+    if (done) { live[0] = live[1] = false; return; }
+    if (part_b) { min1[0] = n0 + o0; max1[0] = x0 + o0; b0[0] = in0; b1[0] = ix0; min1[1] = n1 + o1; max1[1] = x1 + o1; b0[1] = in1; b1[1] = ix1; }
+    else { min0[0] = n0 + o0; max0[0] = x0 + o0; a0[0] = in0; a1[0] = ix0; min0[1] = n1 + o1; max0[1] = x1 + o1; a0[1] = in1; a1[1] = ix1; }
+}
+
 // witness point of Shape::project on the min (want_max = false) or max side
 template <class R>
 __device__ V3<R> shape_witness(const ShapeView<R>& s, const Xf<R>& t, const V3<R>& axis, bool want_max, int idx, const R* lv) {
@@ -470,59 +546,105 @@ __device__ V3<R> shape_witness(const ShapeView<R>& s, const Xf<R>& t, const V3<R
     return want_max ? pmax : pmin;
 }
 
-template <class R>
-__device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
+// Group primitives of the staged SAT: a group is one warp (G = 1) or a whole block of G warps.
+// Reductions are lexicographic (value, axis index) minima/maxima, so their result does not depend
+// on the order lanes and warps are combined in.
+template <int G> __device__ __forceinline__ bool group_any(bool p) {
+    if (G == 1) return __any_sync(0xffffffffu, p);
+    return __syncthreads_or(p) != 0;
+}
+template <class R, int G> __device__ __forceinline__ void group_argmin(R& d, int& idx, int tid, R* rd, int* ri) {
+    warp_argmin(d, idx);
+    if (G == 1) return;
+    if ((tid & 31) == 0) { rd[tid >> 5] = d; ri[tid >> 5] = idx; }
+    __syncthreads();
+    d = rd[0]; idx = ri[0];
+    for (int k = 1; k < G; k++)
+        if (rd[k] < d || (rd[k] == d && ri[k] < idx)) { d = rd[k]; idx = ri[k]; }
+    __syncthreads();
+}
+template <class R, int G> __device__ __forceinline__ void group_argmax(R& d, int& idx, int tid, R* rd, int* ri) {
+    warp_argmax(d, idx);
+    if (G == 1) return;
+    if ((tid & 31) == 0) { rd[tid >> 5] = d; ri[tid >> 5] = idx; }
+    __syncthreads();
+    d = rd[0]; idx = ri[0];
+    for (int k = 1; k < G; k++)
+        if (rd[k] > d || (rd[k] == d && ri[k] < idx)) { d = rd[k]; idx = ri[k]; }
+    __syncthreads();
+}
+// value of the one thread of the group with `mine` set (the thread that evaluated the winning axis)
+template <class R, int G> __device__ __forceinline__ V3<R> group_bcast3(const V3<R>& v, bool mine, R* buf) {
+    if (G == 1) return shfl3(v, __ffs(__ballot_sync(0xffffffffu, mine)) - 1);
+    if (mine) { buf[0] = v.x; buf[1] = v.y; buf[2] = v.z; }
+    __syncthreads();
+    const V3<R> r(buf[0], buf[1], buf[2]);
+    __syncthreads();
+    return r;
+}
+// reals of per-group scratch after the staging area: G reduction values, G indices, 3 broadcast
+template <class R> constexpr int sat_scratch_reals(int G) { return G == 1 ? 0 : 2 * G + 4; }
+
+// Staged SAT of one pair by a group of G warps (tid in [0, 32 G)).  Each thread takes axes
+// f and f + 32 G of every 64 G-axis chunk, so a thread's axes ascend; the group stops at the
+// first chunk holding a separating axis.
+template <class R, int G>
+__device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
+    constexpr int T = 32 * G;
     const R margin = 0;
     SatStage<R> st;
     st.bind(smem);
+    R* rd = smem + sat_stage_reals<R>();
+    int* ri = reinterpret_cast<int*>(rd + G);
+    R* bc = rd + 2 * G;
     const int fa = c.sa.face_count(), fb = c.sb.face_count();
     const int na = c.sa.edge_count(), nb = c.sb.edge_count();
-    for (int f = lane; f < fa; f += 32) st3(st.nA, f, mv(c.ta().b, c.sa.face_normal(f)));
-    for (int f = lane; f < fb; f += 32) st3(st.nB, f, mv(c.tb().b, c.sb.face_normal(f)));
-    for (int e = lane; e < na; e += 32) { V3<R> a0, a1; c.sa.edge(e, a0, a1); st3(st.dA, e, mv(c.ta().b, normalized(a0 - a1))); }
-    for (int e = lane; e < nb; e += 32) { V3<R> b0, b1; c.sb.edge(e, b0, b1); st3(st.dB, e, mv(c.tb().b, normalized(b0 - b1))); }
-    if (c.sa.type == ST_HULL) for (int i = lane; i < c.sa.nv; i += 32) stv(st.vA, i, c.sa.vert(i));
-    if (c.sb.type == ST_HULL) for (int i = lane; i < c.sb.nv; i += 32) stv(st.vB, i, c.sb.vert(i));
-    __syncwarp();
+    for (int f = tid; f < fa; f += T) st3(st.nA, f, mv(c.ta().b, c.sa.face_normal(f)));
+    for (int f = tid; f < fb; f += T) st3(st.nB, f, mv(c.tb().b, c.sb.face_normal(f)));
+    for (int e = tid; e < na; e += T) { V3<R> a0, a1; c.sa.edge(e, a0, a1); st3(st.dA, e, mv(c.ta().b, normalized(a0 - a1))); }
+    for (int e = tid; e < nb; e += T) { V3<R> b0, b1; c.sb.edge(e, b0, b1); st3(st.dB, e, mv(c.tb().b, normalized(b0 - b1))); }
+    if (c.sa.type == ST_HULL) for (int i = tid; i < c.sa.nv; i += T) stv(st.vA, i, c.sa.vert(i));
+    if (c.sb.type == ST_HULL) for (int i = tid; i < c.sb.nv; i += T) stv(st.vB, i, c.sb.vert(i));
+    if (G == 1) __syncwarp(); else __syncthreads();
     const V3<R> dc = c.ta().o - c.tb().o;
-    // ---- face axes of A, then of B (findSeparatingAxis :265-308); each lane takes axes f and
-    // f + 32 of a 64-axis chunk, and the warp stops at the first chunk holding a separating axis
+    // ---- face axes of A, then of B (findSeparatingAxis :265-308)
     R bd = Lim<R>::max();
     int bf = 0x7fffffff, bside = 0, bia = -1, bib = -1;
-    for (int base = 0; base < fa + fb; base += 64) {
+    for (int base = 0; base < fa + fb; base += 2 * T) {
         V3<R> n[2];
         bool ok[2];
         for (int k = 0; k < 2; k++) {
-            const int f = base + 32 * k + lane;
+            const int f = base + T * k + tid;
             ok[k] = f < fa + fb;
             n[k] = !ok[k] ? V3<R>(0, 0, 0) : f < fa ? ld3(st.nA, f) : ld3(st.nB, f - fa);
             if (ok[k] && dot(dc, n[k]) < 0) n[k] = n[k] * R(-1.0);
         }
         R min0[2], max0[2], min1[2], max1[2];
         int a0[2], a1[2], b0[2], b1[2];
-        shape_interval2(c.sa, c.ta(), n, st.vA, min0, max0, a0, a1);
-        shape_interval2(c.sb, c.tb(), n, st.vB, min1, max1, b0, b1);
+        R best = bd;
+        warp_min(best);
+        pair_intervals2(c, n, ok, best, st.vA, st.vB, min0, max0, min1, max1, a0, a1, b0, b1);
         bool sep = false;
         for (int k = 0; k < 2; k++) sep |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
-        if (__any_sync(0xffffffffu, sep)) return false;
+        if (group_any<G>(sep)) return false;
         for (int k = 0; k < 2; k++) {
             if (!ok[k]) continue;
             const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
             const R d = d0 < d1 ? d0 : d1;
             if (d < bd) {
-                bd = d; bf = base + 32 * k + lane; bside = d0 < d1;
+                bd = d; bf = base + T * k + tid; bside = d0 < d1;
                 bia = d0 < d1 ? a1[k] : a0[k]; bib = d0 < d1 ? b0[k] : b1[k];
             }
         }
     }
     R dmin = bd;
     int wf = bf;
-    warp_argmin(dmin, wf);
+    group_argmin<R, G>(dmin, wf, tid, rd, ri);
     V3<R> sep, dpt;
     const bool on_a = wf >= fa;
     if (wf < 0x7fffffff) {
-        const int sl = wf % 32;
-        if (lane == sl) {
+        const bool mine = bf == wf;
+        if (mine) {
             V3<R> n = wf < fa ? ld3(st.nA, wf) : ld3(st.nB, wf - fa);
             if (dot(dc, n) < 0) n = n * R(-1.0);
             sep = n;
@@ -530,9 +652,9 @@ __device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
             if (!on_a) dpt = shape_witness(c.sb, c.tb(), n, !bside, bib, st.vB);
             else dpt = shape_witness(c.sa, c.ta(), n, bside, bia, st.vA) + n * bd;
         }
-        sep = shfl3(sep, sl);
-        dpt = shfl3(dpt, sl);
-        if (lane == 0 &&
+        sep = group_bcast3<R, G>(sep, mine, bc);
+        dpt = group_bcast3<R, G>(dpt, mine, bc);
+        if (tid == 0 &&
             ((on_a && shape_inside(c.sb, c.tb().inv_apply(dpt))) || (!on_a && shape_inside(c.sa, c.ta().inv_apply(dpt)))))
             c.add(sep, dpt - sep * margin, -dmin + margin * 2);
     }
@@ -541,11 +663,11 @@ __device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
     int ep = 0x7fffffff;
     V3<R> ewa, ewb, en;
     const int ne = na * nb;
-    for (int base = 0; base < ne; base += 64) {
+    for (int base = 0; base < ne; base += 2 * T) {
         V3<R> cr[2];
         bool ok[2];
         for (int k = 0; k < 2; k++) {
-            const int q = base + 32 * k + lane;
+            const int q = base + T * k + tid;
             ok[k] = false;
             cr[k] = V3<R>(0, 0, 0);
             if (q < ne) {
@@ -560,17 +682,18 @@ __device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
         }
         R min0[2], max0[2], min1[2], max1[2];
         int a0[2], a1[2], b0[2], b1[2];
-        shape_interval2(c.sa, c.ta(), cr, st.vA, min0, max0, a0, a1);
-        shape_interval2(c.sb, c.tb(), cr, st.vB, min1, max1, b0, b1);
-        bool sep = false;
-        for (int k = 0; k < 2; k++) sep |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
-        if (__any_sync(0xffffffffu, sep)) return false;
+        R best = ed;
+        warp_min(best);
+        pair_intervals2(c, cr, ok, best, st.vA, st.vB, min0, max0, min1, max1, a0, a1, b0, b1);
+        bool sp = false;
+        for (int k = 0; k < 2; k++) sp |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
+        if (group_any<G>(sp)) return false;
         for (int k = 0; k < 2; k++) {
             if (!ok[k]) continue;
             const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
             const R dist = d0 < d1 ? d0 : d1;
             if (dist < ed) {
-                const int q = base + 32 * k + lane;
+                const int q = base + T * k + tid;
                 const int e0 = q / nb, e1 = q - e0 * nb;
                 const bool side = d0 < d1;
                 const V3<R> wa = shape_witness(c.sa, c.ta(), cr[k], side, side ? a1[k] : a0[k], st.vA);
@@ -585,12 +708,12 @@ __device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
     }
     R emin = ed;
     int wq = ep;
-    warp_argmin(emin, wq);
+    group_argmin<R, G>(emin, wq, tid, rd, ri);
     if (wq < 0x7fffffff) {
-        const int sl = wq % 32;
-        const V3<R> wpa = shfl3(ewa, sl), wpb = shfl3(ewb, sl);
-        sep = shfl3(en, sl);
-        if (lane == 0) {   // segmentsClosestPoints with unbounded half-lengths (:172-214, :363-395)
+        const bool mine = ep == wq;
+        const V3<R> wpa = group_bcast3<R, G>(ewa, mine, bc), wpb = group_bcast3<R, G>(ewb, mine, bc);
+        sep = group_bcast3<R, G>(en, mine, bc);
+        if (tid == 0) {   // segmentsClosestPoints with unbounded half-lengths (:172-214, :363-395)
             const int e0 = wq / nb, e1 = wq - e0 * nb;
             const V3<R> wea = ld3(st.dA, e0), web = ld3(st.dB, e1);
             const V3<R> tr = wpb - wpa;
@@ -618,19 +741,19 @@ __device__ bool sat_staged(Pair<R>& c, int lane, R* smem) {
     // ---- clipping (:63-170): incident face of B (first maximum), reference face of A (first minimum)
     R dmax = Lim<R>::min();
     int fbest = 0x7fffffff;
-    for (int f = lane; f < fb; f += 32) {
+    for (int f = tid; f < fb; f += T) {
         const R d = dot(ld3(st.nB, f), sep);
         if (d > dmax) { dmax = d; fbest = f; }
     }
-    warp_argmax(dmax, fbest);
+    group_argmax<R, G>(dmax, fbest, tid, rd, ri);
     R dmn = Lim<R>::max();
     int fabest = 0x7fffffff;
-    for (int f = lane; f < fa; f += 32) {
+    for (int f = tid; f < fa; f += T) {
         const R d = dot(ld3(st.nA, f), sep);
         if (d < dmn) { dmn = d; fabest = f; }
     }
-    warp_argmin(dmn, fabest);
-    if (lane == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) clip_faces(c, sep, -c.ref_scale, R(0), fbest, fabest);
+    group_argmin<R, G>(dmn, fabest, tid, rd, ri);
+    if (tid == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) clip_faces(c, sep, -c.ref_scale, R(0), fbest, fabest);
     return true;
 }
 
@@ -741,20 +864,40 @@ __device__ bool sat_warp(Pair<R>& c, int lane) {
     return true;
 }
 
-template <class R>
-__global__ void __launch_bounds__(32 * kSatWarps, 4) k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
-                         const int* pair_scene_off, const int* prev_off) {
+// SAT pairs (PC_CONVEX, PC_CONVEX_HEAVY): G = 1 runs kSatWarps pairs per block, one warp each;
+// G = kSatGroup runs one pair per block.  Only thread 0 holds the pair's contact cache.
+// per-group stride, a multiple of 4 reals so that every group's vertex rows stay 16-byte aligned
+template <class R> constexpr int sat_group_reals(int G) { return (sat_stage_reals<R>() + sat_scratch_reals<R>(G) + 3) & ~3; }
+static_assert(sat_group_reals<float>(1) % 4 == 0 && (3 * (2 * kSatF + 2 * kSatE)) % 4 == 0, "SAT staging alignment");
+template <class R, int G>
+__global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 4 : 2)
+k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+         const int* pair_scene_off, const int* prev_off) {
     extern __shared__ __align__(16) unsigned char sat_smem[];
-    const int warp = threadIdx.x >> 5;
-    const int t = lo + blockIdx.x * kSatWarps + warp;
+    const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
+    const int tid = G == 1 ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
+    const int t = lo + blockIdx.x * (G == 1 ? kSatWarps : 1) + grp;
+    if (t >= hi) return;   // whole groups leave together
+    const int p = order[t];
+    Cache<R> cache;
+    Pair<R> pr;
+    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr, tid == 0);
+    sat_staged<R, G>(pr, tid, reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G));
+    if (tid == 0) np_finish(p, pairs, B, res, cache);
+}
+
+// SAT pairs with a shape beyond the staging limits (PC_CONVEX_BIG): one warp each, unstaged
+template <class R>
+__global__ void k_np_sat_big(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                             const int* pair_scene_off, const int* prev_off) {
+    const int t = lo + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (t >= hi) return;   // whole warps leave together
+    if (t >= hi) return;
     const int p = order[t];
     Cache<R> cache;
     Pair<R> pr;
     np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
-    if (sat_fits(pr.sa) && sat_fits(pr.sb)) sat_staged(pr, lane, reinterpret_cast<R*>(sat_smem) + (size_t)warp * sat_stage_reals<R>());
-    else sat_warp(pr, lane);
+    sat_warp(pr, lane);
     if (lane == 0) np_finish(p, pairs, B, res, cache);
 }
 

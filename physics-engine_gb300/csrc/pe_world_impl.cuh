@@ -309,7 +309,7 @@ template <class R> void World<R>::narrowphase() {
     if (P > 0) {
         cls_count_.ensure(2 * PC_COUNT);
         PE_CK(cudaMemsetAsync(cls_count_.p, 0, 2 * PC_COUNT * sizeof(int), st_));
-        launch(K_NP_BUCKET, grid(P), k_np_classify<R>, P, pairs_.p, bodies(), stype_.p, cls_.p, cls_count_.p);
+        launch(K_NP_BUCKET, grid(P), k_np_classify<R>, P, pairs_.p, bodies(), shapes(), cls_.p, cls_count_.p);
         int cnt[PC_COUNT];
         PE_CK(cudaMemcpyAsync(cnt, cls_count_.p, sizeof(cnt), cudaMemcpyDeviceToHost, st_));
         PE_CK(cudaStreamSynchronize(st_));
@@ -320,6 +320,13 @@ template <class R> void World<R>::narrowphase() {
         const Results<R> rs = results();
         const Bodies<R> bd = bodies();
         const ShapeTable<R> sh = shapes();
+        if (!sat_attr_) {   // dynamic shared memory of the staged SAT kernels (above the 48 KB default for FP64)
+            PE_CK(cudaFuncSetAttribute(k_np_sat<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(kSatWarps * sat_group_reals<R>(1) * sizeof(R))));
+            PE_CK(cudaFuncSetAttribute(k_np_sat<R, kSatGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sat_group_reals<R>(kSatGroup) * sizeof(R))));
+            sat_attr_ = true;
+        }
         for (int c = 0; c < PC_COUNT; c++) {
             const int lo = cur[c], hi = cur[c] + cnt[c];
             if (hi == lo) continue;
@@ -332,16 +339,22 @@ template <class R> void World<R>::narrowphase() {
                 case PC_BOX_CYL: launch(K_NP, g, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_SPHERE_HULL: launch(K_NP, g, k_np_class<R, PC_SPHERE_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_CYL_HULL: launch(K_NP, g, k_np_class<R, PC_CYL_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                default: {
-                    const size_t smem = (size_t)kSatWarps * sat_stage_reals<R>() * sizeof(R);
-                    if (!sat_attr_) {
-                        PE_CK(cudaFuncSetAttribute(k_np_sat<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-                        sat_attr_ = true;
-                    }
-                    launch_smem(K_NP_SAT, (hi - lo + kSatWarps - 1) / kSatWarps, 32 * kSatWarps, smem, k_np_sat<R>, lo, hi, order_np_.p,
-                                pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
+                case PC_CONVEX: {
+                    const size_t smem = (size_t)kSatWarps * sat_group_reals<R>(1) * sizeof(R);
+                    launch_smem(K_NP_SAT, (hi - lo + kSatWarps - 1) / kSatWarps, 32 * kSatWarps, smem, k_np_sat<R, 1>, lo, hi,
+                                order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
                     break;
                 }
+                case PC_CONVEX_HEAVY: {
+                    const size_t smem = (size_t)sat_group_reals<R>(kSatGroup) * sizeof(R);
+                    launch_smem(K_NP_SAT, hi - lo, 32 * kSatGroup, smem, k_np_sat<R, kSatGroup>, lo, hi, order_np_.p, pairs_.p, bd,
+                                sh, rs, pair_scene_off_.p, prev_res_off_.p);
+                    break;
+                }
+                default:   // PC_CONVEX_BIG
+                    launch(K_NP_SAT, grid_warps(hi - lo), k_np_sat_big<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,
+                           pair_scene_off_.p, prev_res_off_.p);
+                    break;
             }
         }
         PE_CK(cudaGetLastError());
