@@ -133,6 +133,30 @@ int pe_gpu_kernel_stats(pe_gpu_world* w, double* ms, long long* launches);
 /* blocks until all work on the world's stream finished */
 int pe_gpu_sync(pe_gpu_world* w);
 
+/* Sweep-and-prune pairs of caller-supplied AABBs, allocating no memory.  This entry point has
+ * no counterpart in the reference; it is a variant of the broadphase above (the same sort keys,
+ * sweep, validation and pair order as BroadPhaseSweepAndPrune::calcCollisionPairs,
+ * broad_phase_sweep_and_prune.cpp:6-41, for one scene, sorting along `axis`) for callers that may
+ * not allocate device memory at the moment they need pairs: cudaMalloc and cudaFree can block or
+ * synchronise the whole device, which stalls the other streams of a loop that keeps many scenes in
+ * flight, and they are not allowed while a stream is being captured into a graph.
+ *
+ * All temporaries live in one fixed scratch array of about 1.4 MB per device, which limits n to
+ * 16384 bodies; a larger n returns PE_GPU_ERR_CAPACITY with a message.  The first call on a device
+ * looks the scratch up (cudaGetSymbolAddress, the device current) and caches it; make that first
+ * call before any stream capture.  The device's context must already exist.  The scratch is
+ * shared: calls on one device whose work overlaps (other streams, other threads) race on it, so
+ * serialise them.  Nothing needs to start at zero: the call initialises every scratch value it
+ * reads.
+ *
+ * Device pointers: aabb_min / aabb_max [3 n] floats (x, y, z per body), flags [n] PE_GPU_BODY_*
+ * bits or NULL (all dynamic), pairs [2 pair_cap] ints (body indices, lower sweep position first),
+ * n_pairs one int.  The work is queued on `stream` (a cudaStream_t, NULL for the default stream);
+ * *n_pairs holds the pair count when it completes.  If that count exceeds pair_cap the output is
+ * incomplete: call again with a larger buffer.  err (optional) receives a message on failure. */
+int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min, const float* aabb_max, const int* flags, int axis,
+                             int* pairs, int pair_cap, int* n_pairs, void* stream, char* err, int err_cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,181 @@
+// Sweep-and-prune pair query that allocates no device memory (pe_gpu_sap_pairs_noalloc).
+//
+// Same kernels and the same pair order as the world's broadphase (BroadPhaseSweepAndPrune::
+// calcCollisionPairs, broad_phase_sweep_and_prune.cpp:6-41, with validateCollisionPair,
+// broad_phase_base.cpp:5-19) for one scene of at most kSapMaxBodies bodies, but every temporary
+// (sort keys, sorted AABBs, counts, scan totals) lives in one file-scope __device__ array.  The
+// array comes into existence when the CUDA module is loaded into the device's context; its
+// address is looked up once per device with cudaGetSymbolAddress and cached.
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include "../../include/pe_gpu.h"
+#include "pe_kernels.cuh"
+
+namespace pe {
+namespace {
+
+constexpr int kSapMaxBodies = 16384;
+constexpr size_t kAlign = 256;
+constexpr size_t al(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
+constexpr int kSapTiles = (kSapMaxBodies + kRadixTile - 1) / kRadixTile;
+constexpr int kSapAux = (256 * kSapTiles + 1023) / 1024 + (kSapMaxBodies + 1 + 1023) / 1024 + 2;
+
+// byte layout of the scratch array
+struct SapLayout {
+    size_t key[2], key2[2], val[2], hist, aux, total, axis, status, smn, smx, sflag, sscene, count, stage, end;
+};
+constexpr SapLayout sap_layout() {
+    SapLayout L{};
+    size_t o = 0;
+    const size_t n = kSapMaxBodies;
+    for (int k = 0; k < 2; k++) { L.key[k] = o; o += al(n * 8); }
+    for (int k = 0; k < 2; k++) { L.key2[k] = o; o += al(n * 4); }
+    for (int k = 0; k < 2; k++) { L.val[k] = o; o += al(n * 4); }
+    L.hist = o; o += al((256 * kSapTiles + 1) * 4);
+    L.aux = o; o += al(kSapAux * 4);
+    L.total = o; o += al(4);
+    L.axis = o; o += al(4);
+    L.status = o; o += al(4);
+    L.smn = o; o += al(3 * n * 4);
+    L.smx = o; o += al(3 * n * 4);
+    L.sflag = o; o += al(n * 4);
+    L.sscene = o; o += al(n * 4);
+    L.count = o; o += al((n + 1) * 4);
+    L.stage = o; o += al(n * kStage * 4);
+    L.end = o;
+    return L;
+}
+constexpr SapLayout kL = sap_layout();
+constexpr size_t kSapScratchBytes = kL.end;   // about 1.4 MB
+static_assert(kSapScratchBytes <= (size_t)2 << 20, "scratch budget");
+
+__device__ __align__(256) unsigned char g_sap_scratch[kSapScratchBytes];
+
+// sort keys of the bodies (AABB minimum along the axis, as in k_bp_keys); also the per-call
+// values that must start known: the scene axis, one scene id for every key
+__global__ void k_sap_keys(int n, const float* mn, int axis, uint64_t* key, uint32_t* key2, uint32_t* val, int* scene_axis) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) scene_axis[0] = axis;
+    if (i >= n) return;
+    key[i] = order_bits(mn[3 * i + axis]);
+    key2[i] = 0u;
+    val[i] = (uint32_t)i;
+}
+
+// sorted copies of the sweep inputs (as k_bp_gather); zeroes the scan's last count and the status
+__global__ void k_sap_gather(int n, const float* mn, const float* mx, const int* flags, const uint32_t* order, float* smn,
+                             float* smx, int* sflag, int* sscene, int* count, int* status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) { count[n] = 0; *status = 0; }
+    if (k >= n) return;
+    const int i = (int)order[k];
+    for (int d = 0; d < 3; d++) {
+        smn[(size_t)d * n + k] = mn[3 * i + d];
+        smx[(size_t)d * n + k] = mx[3 * i + d];
+    }
+    sflag[k] = flags ? flags[i] : 0;
+    sscene[k] = 0;
+}
+
+__global__ void k_sap_total(const int* total, int* n_pairs) { *n_pairs = *total; }
+
+std::mutex g_setup_mu;
+void* g_scratch[64] = {};
+
+void set_err(char* err, int cap, const char* msg) {
+    if (err && cap > 0) {
+        std::strncpy(err, msg, (size_t)cap - 1);
+        err[cap - 1] = '\0';
+    }
+}
+
+}  // namespace
+}  // namespace pe
+
+extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min, const float* aabb_max, const int* flags, int axis,
+                                        int* pairs, int pair_cap, int* n_pairs, void* stream, char* err, int err_cap) {
+    using namespace pe;
+    char msg[160];
+    if (n < 0 || axis < 0 || axis > 2 || pair_cap < 0 || !n_pairs || (n > 0 && (!aabb_min || !aabb_max)) ||
+        (pair_cap > 0 && !pairs) || device < 0 || device >= 64) {
+        set_err(err, err_cap, "pe_gpu_sap_pairs_noalloc: bad argument");
+        return PE_GPU_ERR_ARG;
+    }
+    if (n > kSapMaxBodies) {
+        std::snprintf(msg, sizeof msg, "pe_gpu_sap_pairs_noalloc: %d bodies exceed the fixed scratch limit of %d", n, kSapMaxBodies);
+        set_err(err, err_cap, msg);
+        return PE_GPU_ERR_CAPACITY;
+    }
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) { set_err(err, err_cap, "cudaGetDevice failed"); return PE_GPU_ERR_CUDA; }
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) { set_err(err, err_cap, "cudaSetDevice failed"); return PE_GPU_ERR_CUDA; }
+    auto done = [&](int rc, const char* what) {
+        if (what) {
+            std::snprintf(msg, sizeof msg, "pe_gpu_sap_pairs_noalloc: %s: %s", what, cudaGetErrorString(cudaGetLastError()));
+            set_err(err, err_cap, msg);
+        }
+        if (prev != device) cudaSetDevice(prev);
+        return rc;
+    };
+    // set-up, once per device, with that device current
+    unsigned char* base;
+    {
+        std::lock_guard<std::mutex> lk(g_setup_mu);
+        if (!g_scratch[device]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_sap_scratch) != cudaSuccess || !p) return done(PE_GPU_ERR_CUDA, "cudaGetSymbolAddress");
+            g_scratch[device] = p;
+        }
+        base = static_cast<unsigned char*>(g_scratch[device]);
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (n < 2) {   // no pair (the world's broadphase returns before sorting below two bodies)
+        if (cudaMemsetAsync(n_pairs, 0, sizeof(int), st) != cudaSuccess) return done(PE_GPU_ERR_CUDA, "cudaMemsetAsync");
+        return done(PE_GPU_OK, nullptr);
+    }
+    uint64_t* key[2] = {reinterpret_cast<uint64_t*>(base + kL.key[0]), reinterpret_cast<uint64_t*>(base + kL.key[1])};
+    uint32_t* key2[2] = {reinterpret_cast<uint32_t*>(base + kL.key2[0]), reinterpret_cast<uint32_t*>(base + kL.key2[1])};
+    uint32_t* val[2] = {reinterpret_cast<uint32_t*>(base + kL.val[0]), reinterpret_cast<uint32_t*>(base + kL.val[1])};
+    int* hist = reinterpret_cast<int*>(base + kL.hist);
+    int* aux = reinterpret_cast<int*>(base + kL.aux);
+    int* total = reinterpret_cast<int*>(base + kL.total);
+    int* scene_axis = reinterpret_cast<int*>(base + kL.axis);
+    int* status = reinterpret_cast<int*>(base + kL.status);
+    float* smn = reinterpret_cast<float*>(base + kL.smn);
+    float* smx = reinterpret_cast<float*>(base + kL.smx);
+    int* sflag = reinterpret_cast<int*>(base + kL.sflag);
+    int* sscene = reinterpret_cast<int*>(base + kL.sscene);
+    int* count = reinterpret_cast<int*>(base + kL.count);
+    int* stage = reinterpret_cast<int*>(base + kL.stage);
+
+    const int g = (n + kBlock - 1) / kBlock;
+    k_sap_keys<<<g, kBlock, 0, st>>>(n, aabb_min, axis, key[0], key2[0], val[0], scene_axis);
+    // stable LSD radix sort of the 32-bit keys (as World::radix_sort_keys)
+    const int tiles = (n + kRadixTile - 1) / kRadixTile;
+    int cur = 0;
+    for (int shift = 0; shift < 32; shift += 8) {
+        k_radix_hist<<<tiles, kBlock, 0, st>>>(key[cur], key2[cur], n, shift, 0, hist, tiles);
+        const int m = 256 * tiles, ht = (m + 1023) / 1024;
+        k_scan_tiles<<<ht, kBlock, 0, st>>>(hist, m, aux);
+        k_scan_aux<<<1, kBlock, 0, st>>>(aux, ht, total);
+        k_scan_add<<<ht, kBlock, 0, st>>>(hist, m, aux);
+        k_radix_scatter<<<tiles, kBlock, 0, st>>>(key[cur], key2[cur], val[cur], key[cur ^ 1], key2[cur ^ 1], val[cur ^ 1], n, shift, 0,
+                                                 hist, tiles);
+        cur ^= 1;
+    }
+    const uint32_t* order = val[cur];
+    k_sap_gather<<<g, kBlock, 0, st>>>(n, aabb_min, aabb_max, flags, order, smn, smx, sflag, sscene, count, status);
+    const int gw = (int)(((size_t)n * 32 + kBlock - 1) / kBlock);
+    k_bp_count<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, stage);
+    const int ct = (n + 1 + 1023) / 1024;
+    k_scan_tiles<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
+    k_scan_aux<<<1, kBlock, 0, st>>>(aux, ct, total);
+    k_scan_add<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
+    k_bp_write<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, order, count, stage, reinterpret_cast<int2*>(pairs),
+                                             pair_cap, status);
+    k_sap_total<<<1, 1, 0, st>>>(total, n_pairs);
+    if (cudaGetLastError() != cudaSuccess) return done(PE_GPU_ERR_CUDA, "kernel launch");
+    return done(PE_GPU_OK, nullptr);
+}

@@ -65,6 +65,8 @@ def load(build_if_missing: bool = True):
         "pe_gpu_kernel_count": (I, []),
         "pe_gpu_kernel_name": (C.c_char_p, [I]),
         "pe_gpu_kernel_stats": (I, [P, dp, np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]),
+        # device pointers throughout (see include/pe_gpu.h)
+        "pe_gpu_sap_pairs_noalloc": (I, [I, I, P, P, P, I, P, I, P, P, C.c_char_p, I]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -18,7 +18,7 @@ OUT = PKG / "lib"
 OBJ = PKG / "_build"
 LIB = OUT / "libpe_gpu.so"
 
-CU_SOURCES = ["pe_util.cu", "pe_world_f32.cu", "pe_world_f64.cu", "pe_capi.cu"]
+CU_SOURCES = ["pe_util.cu", "pe_world_f32.cu", "pe_world_f64.cu", "pe_capi.cu", "pe_noalloc.cu"]
 CPP_SOURCES = ["pe_host_shapes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
