@@ -1,16 +1,22 @@
 """Benchmark of the rigid-body step on the GPU (and of the reference's CPU step).
 
-python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload stress|tower|batched]
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload batched|stress|tower]
 
 Workloads (all synthetic, seeded):
+  batched  4,096 independent piles of 8..512 bodies (log-uniform; box/sphere/cylinder/convex hull
+           50/20/10/20, hulls of 8..64 vertices on a sphere scaled U[0.3, 1.0]) dropped 0..5 m onto
+           their own static ground boxes; FP32; dt 1/60; 10 iterations; coloured Gauss-Seidel; one
+           batched step for all scenes; timed after 120 untimed steps (piles in contact).  Beside
+           it, a sample of the same scenes stepped one world at a time (the per-scene GPU path).
+           Default.
   stress   65,536 bodies (60% boxes, 25% spheres, 15% cylinders, sizes as in the one-step stress
            configuration) scattered in a 100 m cube with N(0,2) m/s velocities; FP32; dt 1/60;
-           10 solver iterations; coloured Gauss-Seidel.  Default.
+           10 solver iterations; coloured Gauss-Seidel.
   tower    1,000 boxes stacked 10x10x10 with 1 mm gaps on a static ground box, hit by a 50 kg
            sphere at 30 m/s; FP64; dt 1/60; 20 iterations; serial-order solver.
-  batched  4,096 independent piles of 8..512 bodies (log-uniform; boxes, spheres, cylinders,
-           convex hulls of 8..64 vertices) dropped on ground boxes; FP32; 10 iterations;
-           coloured Gauss-Seidel; one batched step for all scenes.
+  large    262,144 bodies (box/sphere/convex hull 50/30/20, sizes U[0.1, 0.5] m) poured from a
+           40x40x80 m volume into a 40x40 m walled container; FP32; dt 1/120; 10 iterations;
+           coloured; timed after 240 untimed steps.
 
 One "step" is one full World::step (integrate, broadphase, narrowphase, solver) of the whole
 workload.  `value` = body-steps per second of device time with the state resident in HBM
@@ -58,6 +64,12 @@ def make_workload(name, n_scenes=4096):
                                              "convex hull 50/20/10/20, hulls of 8..64 vertices from a 512-shape pool) "
                                              "on static ground boxes, one batched step, FP32, 10 SI iterations, coloured",
                                     bodies=s.n_bodies, scenes=n_scenes, solver="coloured", preroll_steps=120)
+    if name == "large":
+        s = sc.container_pour(n=262144, seed=5, real_bits=32)
+        return s, 32, 1, None, dict(workload="262,144 bodies (box/sphere/convex hull 50/30/20, sizes U[0.1,0.5] m, hulls of "
+                                             "16..32 vertices from a 256-shape pool) poured from a 40x40x80 m volume into a "
+                                             "40x40 m walled container, FP32, dt 1/120, 10 SI iterations, coloured",
+                                    bodies=s.n_bodies, scenes=1, solver="coloured", preroll_steps=240)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -196,17 +208,19 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM bytes of kernel groups from the committed ncu summary (if any)."""
+def ncu_traffic(workload):
+    """DRAM traffic per algorithmic byte of each kernel group, from the committed ncu summary
+    (`<workload> <group> <dram bytes> <algorithmic bytes>` lines, measured on a smaller case of
+    the same workload); scaled by this run's algorithmic bytes."""
     p = ROOT / "profiles" / "ncu_traffic.txt"
     out = {}
     if p.exists():
         for line in p.read_text().splitlines():
             f = line.split()
-            if len(f) >= 2 and not line.startswith("#"):
+            if len(f) >= 4 and not line.startswith("#") and f[0] == workload:
                 try:
-                    out[f[0]] = float(f[1])
-                except ValueError:
+                    out[f[1]] = float(f[2]) / float(f[3])
+                except (ValueError, ZeroDivisionError):
                     pass
     return out
 
@@ -273,8 +287,8 @@ def run_ours(args, rank, world, device):
     dom_bytes = alg[dom]   # bytes of the whole group in one step
     peak, peak_kind = measured_peak()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    tr = ncu_traffic()
-    traffic = sum(tr[k] for k in KERNEL_GROUPS[dom] if k in tr) if any(k in tr for k in KERNEL_GROUPS[dom]) else None
+    ratio = ncu_traffic(args.workload).get(dom)
+    traffic = ratio * dom_bytes if ratio is not None else None
     # end to end through the C ABI with host buffers
     st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
     e2e_times = []
@@ -372,7 +386,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="stress", choices=["stress", "tower", "batched"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "stress", "tower", "large"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scenes", type=int, default=4096, help="scene count of the batched workload")
     ap.add_argument("--no-per-scene", action="store_true", help="skip the one-scene-per-launch comparison")

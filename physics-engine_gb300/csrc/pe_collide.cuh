@@ -73,13 +73,16 @@ template <class R> struct Cache {
     }
 };
 
+// One pair being collided: shapes and transforms held by value (registers); the contact cache
+// (local memory, only touched by the thread that adds points) is reached through `c`.
 template <class R> struct Pair {
     ShapeView<R> sa, sb;
+    Xf<R> xa, xb;
     R ref_scale;
     Cache<R>* c;
     __device__ void add(const V3<R>& n, const V3<R>& p, R d) { c->add(n, p, d); }
-    __device__ const Xf<R>& ta() const { return c->ta; }
-    __device__ const Xf<R>& tb() const { return c->tb; }
+    __device__ const Xf<R>& ta() const { return xa; }
+    __device__ const Xf<R>& tb() const { return xb; }
 };
 
 // ======================================================================= box-box
@@ -935,10 +938,11 @@ template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_con
 
 // pair classes (narrow_phase_base.cpp:20-29 restricted to the four convex shape types)
 // PC_CONVEX (cylinder-cylinder, box-hull, hull-hull, all run by ConvexConvexCollisionAlgorithm) is
-// split by cost for scheduling: PC_CONVEX_HEAVY pairs get a block of warps each, PC_CONVEX a warp
-// each, and PC_CONVEX_BIG (a shape beyond the shared-memory staging limits) the unstaged warp path.
+// split for scheduling: by shape pairing for the warp-per-pair kernel (so that a launch runs one
+// code path), PC_CONVEX_HEAVY pairs get a block of warps each, and PC_CONVEX_BIG (a shape beyond
+// the shared-memory staging limits) the unstaged warp path.
 enum PairClass { PC_BOX_BOX = 0, PC_BOX_SPHERE, PC_SPHERE_SPHERE, PC_SPHERE_CYL, PC_BOX_CYL, PC_CONVEX, PC_SPHERE_HULL,
-                 PC_CYL_HULL, PC_CONVEX_HEAVY, PC_CONVEX_BIG, PC_COUNT };
+                 PC_CYL_HULL, PC_CONVEX_HEAVY, PC_CONVEX_BIG, PC_CONVEX_HULL_HULL, PC_CONVEX_CYL_CYL, PC_COUNT };
 
 __host__ __device__ inline int pair_class(int ta, int tb) {
     const int lo = ta < tb ? ta : tb, hi = ta < tb ? tb : ta;

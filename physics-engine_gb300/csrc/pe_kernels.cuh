@@ -259,8 +259,12 @@ template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& 
 template <class R> __device__ __forceinline__ int sat_class(const ShapeView<R>& a, const ShapeView<R>& b) {
     if (!sat_fits(a) || !sat_fits(b)) return PC_CONVEX_BIG;
     auto w = [](const ShapeView<R>& s) { return s.type == ST_HULL ? s.nv : s.type == ST_CYLINDER ? 12 : s.type == ST_BOX ? 8 : 2; };
-    const long long axes = (long long)a.face_count() + b.face_count() + (long long)a.edge_count() * b.edge_count();
-    return axes * (w(a) + w(b)) >= kSatHeavyCost ? PC_CONVEX_HEAVY : PC_CONVEX;
+    auto ue = [](const ShapeView<R>& s) { return s.type == ST_BOX ? 3 : s.edge_count(); };   // distinct edge axes
+    const long long axes = (long long)a.face_count() + b.face_count() + (long long)ue(a) * ue(b);
+    if (axes * (w(a) + w(b)) >= kSatHeavyCost) return PC_CONVEX_HEAVY;
+    if (a.type == ST_HULL && b.type == ST_HULL) return PC_CONVEX_HULL_HULL;
+    if (a.type == ST_CYLINDER) return PC_CONVEX_CYL_CYL;
+    return PC_CONVEX;   // box-hull either way round
 }
 
 template <class R>
@@ -285,25 +289,28 @@ __device__ __forceinline__ void np_setup(int p, const int2* pairs, const Bodies<
                                          bool load_cache = true) {
     const int2 q = pairs[p];
     const int ia = q.x, ib = q.y;
+    pr.xa = B.xf(ia);
+    pr.xb = B.xf(ib);
+    const R scale_a = B.at(SCALE, ia), scale_b = B.at(SCALE, ib);
+    pr.sa = S.view(B.shape[ia]);
+    pr.sb = S.view(B.shape[ib]);
+    pr.ref_scale = (scale_a + scale_b) * R(0.05);
+    pr.c = &cache;
+    if (!load_cache) return;
     cache.valid = 0;
     cache.swap = false;
     const int sc = B.scene[ia];
     const int local = p - pair_scene_off[sc];
-    if (!load_cache) {
-    } else if (local < prev_off[sc + 1] - prev_off[sc]) {
+    if (local < prev_off[sc + 1] - prev_off[sc]) {
         const int src = (prev_off[sc] + local) * kSlots;
         for (int k = 0; k < kSlots; k++) cache.dist[k] = res.prev_dist[src + k];
     } else {
         for (int k = 0; k < kSlots; k++) cache.dist[k] = Lim<R>::max();
     }
-    cache.ta = B.xf(ia);
-    cache.tb = B.xf(ib);
-    cache.scale_a = B.at(SCALE, ia);
-    cache.scale_b = B.at(SCALE, ib);
-    pr.sa = S.view(B.shape[ia]);
-    pr.sb = S.view(B.shape[ib]);
-    pr.ref_scale = (cache.scale_a + cache.scale_b) * R(0.05);
-    pr.c = &cache;
+    cache.ta = pr.xa;
+    cache.tb = pr.xb;
+    cache.scale_a = scale_a;
+    cache.scale_b = scale_b;
 }
 
 // ContactResult::sortContactPoints (stable order by distance over all 8 slots, size = first
@@ -658,11 +665,18 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
             ((on_a && shape_inside(c.sb, c.tb().inv_apply(dpt))) || (!on_a && shape_inside(c.sa, c.ta().inv_apply(dpt)))))
             c.add(sep, dpt - sep * margin, -dmin + margin * 2);
     }
-    // ---- edge-pair axes (:323-361)
+    // ---- edge-pair axes (:323-361).  A box's 12 edges come in 3 classes of 4 whose direction
+    // vectors are bit-identical (scaled unit-mesh differences), so they give identical axes,
+    // projections and witnesses: each class is projected once, and a candidate takes the first
+    // edge pair of the class (in the reference's e0-major order) whose lines hold the witnesses.
+    // Candidates compare by (depth, reference axis index), which is the reference's first strict
+    // minimum whatever order the axes are visited in.
     R ed = dmin;
     int ep = 0x7fffffff;
     V3<R> ewa, ewb, en;
-    const int ne = na * nb;
+    const bool boxA = c.sa.type == ST_BOX, boxB = c.sb.type == ST_BOX;
+    const int ua = boxA ? 3 : na, ub = boxB ? 3 : nb;
+    const int ne = ua * ub;
     for (int base = 0; base < ne; base += 2 * T) {
         V3<R> cr[2];
         bool ok[2];
@@ -671,8 +685,8 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
             ok[k] = false;
             cr[k] = V3<R>(0, 0, 0);
             if (q < ne) {
-                const int e0 = q / nb, e1 = q - e0 * nb;
-                const V3<R> x = cross(ld3(st.dA, e0), ld3(st.dB, e1));
+                const int iu = q / ub, ju = q - iu * ub;
+                const V3<R> x = cross(ld3(st.dA, boxA ? 4 * iu : iu), ld3(st.dB, boxB ? 4 * ju : ju));
                 if (!(rabs(norm(x) - 0) < eps<R>())) {
                     ok[k] = true;
                     cr[k] = normalized(x);
@@ -692,18 +706,28 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
             if (!ok[k]) continue;
             const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
             const R dist = d0 < d1 ? d0 : d1;
-            if (dist < ed) {
-                const int q = base + T * k + tid;
-                const int e0 = q / nb, e1 = q - e0 * nb;
-                const bool side = d0 < d1;
-                const V3<R> wa = shape_witness(c.sa, c.ta(), cr[k], side, side ? a1[k] : a0[k], st.vA);
-                const V3<R> wb = shape_witness(c.sb, c.tb(), cr[k], !side, side ? b0[k] : b1[k], st.vB);
-                V3<R> p0, p1, q0, q1;
+            if (!(dist < ed || (dist == ed && ep != 0x7fffffff))) continue;
+            const int q = base + T * k + tid;
+            const int iu = q / ub, ju = q - iu * ub;
+            const bool side = d0 < d1;
+            const V3<R> wa = shape_witness(c.sa, c.ta(), cr[k], side, side ? a1[k] : a0[k], st.vA);
+            const V3<R> wb = shape_witness(c.sb, c.tb(), cr[k], !side, side ? b0[k] : b1[k], st.vB);
+            const V3<R> la = c.ta().inv_apply(wa), lb = c.tb().inv_apply(wb);
+            int qref = 0x7fffffff;
+            for (int m0 = 0; m0 < (boxA ? 4 : 1) && qref == 0x7fffffff; m0++) {
+                const int e0 = boxA ? 4 * iu + m0 : iu;
+                V3<R> p0, p1;
                 c.sa.edge(e0, p0, p1);
-                c.sb.edge(e1, q0, q1);
-                if (!on_line(p0, p1, c.ta().inv_apply(wa)) || !on_line(q0, q1, c.tb().inv_apply(wb))) continue;
-                ed = dist; ep = q; ewa = wa; ewb = wb; en = cr[k];
+                if (!on_line(p0, p1, la)) continue;
+                for (int m1 = 0; m1 < (boxB ? 4 : 1); m1++) {
+                    const int e1 = boxB ? 4 * ju + m1 : ju;
+                    V3<R> q0, q1;
+                    c.sb.edge(e1, q0, q1);
+                    if (on_line(q0, q1, lb)) { qref = e0 * nb + e1; break; }
+                }
             }
+            if (qref == 0x7fffffff || !(dist < ed || qref < ep)) continue;
+            ed = dist; ep = qref; ewa = wa; ewb = wb; en = cr[k];
         }
     }
     R emin = ed;

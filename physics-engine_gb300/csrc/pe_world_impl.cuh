@@ -339,7 +339,9 @@ template <class R> void World<R>::narrowphase() {
                 case PC_BOX_CYL: launch(K_NP, g, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_SPHERE_HULL: launch(K_NP, g, k_np_class<R, PC_SPHERE_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_CYL_HULL: launch(K_NP, g, k_np_class<R, PC_CYL_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_CONVEX: {
+                case PC_CONVEX:
+                case PC_CONVEX_HULL_HULL:
+                case PC_CONVEX_CYL_CYL: {
                     const size_t smem = (size_t)kSatWarps * sat_group_reals<R>(1) * sizeof(R);
                     launch_smem(K_NP_SAT, (hi - lo + kSatWarps - 1) / kSatWarps, 32 * kSatWarps, smem, k_np_sat<R, 1>, lo, hi,
                                 order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);

@@ -556,3 +556,87 @@ def extract(scene, offs, k):
               "ang_vel"):
         setattr(s, f, getattr(scene, f)[b0:b1].copy())
     return s
+
+
+def container_pour(n=262144, seed=0, mix=(0.5, 0.3, 0.0, 0.2), size_range=(0.1, 0.5), floor=(40.0, 40.0),
+                   spawn_height=(1.0, 81.0), wall_height=90.0, hull_pool=256, hull_range=(16, 32), density=1000.0,
+                   dt=1.0 / 120.0, iterations=10, real_bits=32) -> Scene:
+    """One large scene: ``n`` bodies (box/sphere/cylinder/convex hull in ``mix`` proportions; box
+    half-extents, sphere radii and hull scales U[size_range]) at uniform random positions and
+    rotations in a floor[0] x floor[1] x (spawn_height) volume, above a static floor box and
+    inside four static walls.  Hulls (hull_range vertices) come from a seeded pool shared by the
+    bodies.  Bodies 0..4 are the floor and the walls."""
+    rng = np.random.default_rng(seed)
+    fx, fz = floor
+    kinds = rng.choice(4, size=n, p=np.asarray(mix) / np.sum(mix))
+    lo, hi = size_range
+    pool_v, pool_f, pool_vol = [], [], []
+    for _ in range(hull_pool):
+        nv = int(rng.integers(hull_range[0], hull_range[1] + 1))
+        v, f = random_hull(rng, nv, rng.uniform(lo, hi))
+        pool_v.append(v)
+        pool_f.append(f)
+        pool_vol.append(_hull_volumes(v, f))
+    pool_vol = np.array(pool_vol)
+    he = rng.uniform(lo, hi, size=(n, 3))
+    rs = rng.uniform(lo, hi, n)
+    rc = rng.uniform(lo, hi, n)
+    hc = rng.uniform(2 * lo, 2 * hi, n)
+    pick = rng.integers(0, hull_pool, n)
+    org = np.stack([rng.uniform(-fx / 2 + hi, fx / 2 - hi, n), rng.uniform(*spawn_height, n),
+                    rng.uniform(-fz / 2 + hi, fz / 2 - hi, n)], axis=1)
+    rot = random_rotations(rng, n)
+    # shapes: hull pool, floor, x-walls, z-walls, then one shape per primitive body
+    t = 1.0
+    statics = [(BOX, (fx + 2 * t, t, fz + 2 * t), (0.0, -t / 2, 0.0)),
+               (BOX, (t, wall_height, fz + 2 * t), (-fx / 2 - t / 2, wall_height / 2, 0.0)),
+               (BOX, (t, wall_height, fz + 2 * t), (fx / 2 + t / 2, wall_height / 2, 0.0)),
+               (BOX, (fx, wall_height, t), (0.0, wall_height / 2, -fz / 2 - t / 2)),
+               (BOX, (fx, wall_height, t), (0.0, wall_height / 2, fz / 2 + t / 2))]
+    prim = kinds != HULL
+    n_prim = int(prim.sum())
+    H, K = hull_pool, len(statics)
+    S = H + K + n_prim
+    shape_type = np.zeros(S, np.int32)
+    shape_param = np.zeros((S, 3))
+    shape_type[:H] = HULL
+    for k, (ty, p, _) in enumerate(statics):
+        shape_type[H + k] = ty
+        shape_param[H + k] = p
+    pk = kinds[prim]
+    shape_type[H + K:] = pk
+    par = np.zeros((n_prim, 3))
+    par[pk == BOX] = 2 * he[prim][pk == BOX]
+    par[pk == SPHERE, 0] = rs[prim][pk == SPHERE]
+    par[pk == CYLINDER, 0] = rc[prim][pk == CYLINDER]
+    par[pk == CYLINDER, 1] = hc[prim][pk == CYLINDER]
+    shape_param[H + K:] = par
+    body_shape_dyn = np.where(prim, 0, pick)
+    body_shape_dyn[prim] = H + K + np.arange(n_prim)
+    vol = np.where(kinds == BOX, np.prod(2 * he, axis=1),
+                   np.where(kinds == SPHERE, 4.0 / 3.0 * np.pi * rs ** 3,
+                            np.where(kinds == CYLINDER, np.pi * rc * rc * hc, pool_vol[pick])))
+    vbeg, vcnt, fbeg, fcnt = (np.zeros(S, np.int32) for _ in range(4))
+    vcnt[:H] = [len(v) for v in pool_v]
+    fcnt[:H] = [len(f) for f in pool_f]
+    vbeg[:H] = np.concatenate([[0], np.cumsum(vcnt[:H])[:-1]])
+    fbeg[:H] = np.concatenate([[0], np.cumsum(fcnt[:H])[:-1]])
+    N = n + K
+    s = Scene(dt=dt, gravity=(0.0, -9.8, 0.0), iterations=iterations, real_bits=64)
+    s.shape_type, s.shape_param = shape_type, shape_param
+    s.hull_vbeg, s.hull_vcnt, s.hull_fbeg, s.hull_fcnt = vbeg, vcnt, fbeg, fcnt
+    s.hull_verts = np.concatenate(pool_v).reshape(-1, 3)
+    s.hull_face_idx = np.concatenate([np.asarray(f, np.int32).ravel() for f in pool_f])
+    s.hull_face_off = np.arange(0, 3 * int(fcnt.sum()) + 1, 3, dtype=np.int32)
+    s.body_shape = np.concatenate([H + np.arange(K), body_shape_dyn]).astype(np.int32)
+    s.body_flags = np.concatenate([np.full(K, KINEMATIC), np.zeros(n)]).astype(np.int32)
+    s.mass = np.concatenate([np.zeros(K), density * vol])
+    s.friction = np.full(N, 0.5)
+    s.restitution = np.zeros(N)
+    s.lin_damp = np.zeros(N)
+    s.ang_damp = np.zeros(N)
+    s.origin = np.concatenate([np.array([p for _, _, p in statics]), org])
+    s.basis = np.concatenate([np.tile(np.eye(3), (K, 1, 1)), rot])
+    s.lin_vel = np.zeros((N, 3))
+    s.ang_vel = np.zeros((N, 3))
+    return s.rounded(real_bits) if real_bits == 32 else s

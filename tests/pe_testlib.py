@@ -70,3 +70,20 @@ def compare_state(got, ref, keys=STATE_KEYS, what=""):
 
 def dump_state(d):
     return {k: d[k] for k in STATE_KEYS}
+
+
+def mechanical_energy(state, scene, g=9.8):
+    """Kinetic (linear + rotational, world inertia from the stored inverse) plus potential energy
+    of the dynamic bodies."""
+    dyn = scene.mass > 0
+    m = scene.mass[dyn]
+    v, w = state["lin_vel"][dyn], state["ang_vel"][dyn]
+    inertia = np.linalg.inv(state["world_inv_inertia"][dyn])
+    ke = 0.5 * m * np.einsum("ij,ij->i", v, v) + 0.5 * np.einsum("ni,nij,nj->n", w, inertia, w)
+    return float(ke.sum() + (m * g * state["origin"][dyn, 1]).sum())
+
+
+def max_penetration(results):
+    """Deepest contact (positive = penetration) over the valid points of all results."""
+    d = [results["slots"][i, :n, 12].min() for i, n in enumerate(results["point_size"]) if n]
+    return float(max(0.0, -min(d))) if d else 0.0
