@@ -133,6 +133,47 @@ int pe_gpu_kernel_stats(pe_gpu_world* w, double* ms, long long* launches);
 /* blocks until all work on the world's stream finished */
 int pe_gpu_sync(pe_gpu_world* w);
 
+/* Serving (no counterpart in the reference, which steps one World per caller): a request loop over
+ * one device-resident world.  A request is a scene (the arrays of pe_gpu_set_shapes and
+ * pe_gpu_set_bodies, indices local to the scene) and a number of steps.  Requests queue on
+ * submission; each pe_gpu_server_step retires the requests that have run all their steps (their
+ * final state is read back), admits queued requests in arrival order while their estimated device
+ * footprint fits hbm_budget_bytes, and advances every live scene by one step in one batched step.
+ * Live scenes keep their state, sweep axes and contact-result pools on the device between steps,
+ * so a request's result is the one its scene gives stepped alone in a world of its own.  All
+ * requests share dt, gravity, iterations and solver mode. */
+typedef struct pe_gpu_scene {
+    int n_shapes;
+    const int* shape_type;
+    const double* shape_param;                     /* [3 n_shapes] */
+    const int* hull_vbeg; const int* hull_vcnt;    /* [n_shapes] */
+    const int* hull_fbeg; const int* hull_fcnt;    /* [n_shapes] */
+    int n_hull_verts; const double* hull_verts;    /* [3 n_hull_verts] */
+    int n_hull_faces; const int* hull_face_off;    /* [n_hull_faces + 1] */
+    const int* hull_face_idx;
+    int n_bodies;
+    const int* body_shape; const int* body_flags;
+    const double* mass; const double* friction; const double* restitution; const double* lin_damp; const double* ang_damp;
+    const double* origin; const double* basis; const double* lin_vel; const double* ang_vel;
+} pe_gpu_scene;
+
+typedef struct pe_gpu_server pe_gpu_server;
+int pe_gpu_server_create(const pe_gpu_config* cfg, double dt, double gx, double gy, double gz, int iterations, int solver_mode,
+                         double hbm_budget_bytes, pe_gpu_server** out);
+int pe_gpu_server_destroy(pe_gpu_server* s);
+const char* pe_gpu_server_last_error(const pe_gpu_server* s);
+/* copies the scene; *id identifies the request */
+int pe_gpu_server_submit(pe_gpu_server* s, const pe_gpu_scene* scene, int n_steps, long long* id);
+/* retire, admit, one batched step of all live scenes */
+int pe_gpu_server_step(pe_gpu_server* s, int* n_live, int* n_queued);
+/* *state: 0 queued, 1 running, 2 done (final origin / basis / velocities copied to the caller's
+ * arrays of the scene's body count, and the request released), 3 rejected (larger than the budget) */
+int pe_gpu_server_result(pe_gpu_server* s, long long id, int* state, double* origin, double* basis, double* lin_vel,
+                         double* ang_vel);
+/* out10: p50, p99 and mean device time per batched step (ms), batched steps, body-steps, requests
+ * admitted, requests finished, peak charged footprint (bytes), live requests, queued requests */
+int pe_gpu_server_stats(pe_gpu_server* s, double* out10);
+
 /* Sweep-and-prune pairs of caller-supplied AABBs, allocating no memory.  This entry point has
  * no counterpart in the reference; it is a variant of the broadphase above (the same sort keys,
  * sweep, validation and pair order as BroadPhaseSweepAndPrune::calcCollisionPairs,

@@ -24,6 +24,17 @@ template <class R> struct HullPrep {
 };
 template <class R> HullPrep<R> prepare_hull(const double* verts, int nv, const int* face_off, const int* face_idx, int nf);
 
+// A scene as a caller describes it (the arrays of pe_gpu_set_shapes and pe_gpu_set_bodies), owned
+// on the host; shape indices of the bodies and hull indices are local to the scene.
+struct SceneData {
+    std::vector<int> shape_type, hull_vbeg, hull_vcnt, hull_fbeg, hull_fcnt, hull_face_off, hull_face_idx;
+    std::vector<double> shape_param, hull_verts;
+    std::vector<int> body_shape, body_flags;
+    std::vector<double> mass, friction, restitution, lin_damp, ang_damp, origin, basis, lin_vel, ang_vel;
+    int n_shapes() const { return (int)shape_type.size(); }
+    int n_bodies() const { return (int)body_shape.size(); }
+};
+
 // unit-mass local inertia of the analytic shapes (box_shape.cpp:16-23, sphere_shape.cpp:7-11,
 // cylinder_shape.cpp:25-31)
 template <class R> M3<R> box_inertia(const V3<R>& size);

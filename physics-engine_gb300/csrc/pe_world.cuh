@@ -83,6 +83,11 @@ public:
     virtual void phase_times(double* ms, bool reset) = 0;
     virtual void last_counts(int* c) = 0;
     virtual void sync() = 0;
+    // serving: replace the scene list by the kept scenes (old indices, in the new order) followed by
+    // the added ones, keeping the kept scenes' bodies, sweep axes and contact-result pools on the device
+    virtual void repack(const int* keep, int n_keep, const SceneData* const* adds, int n_add) = 0;
+    virtual const std::vector<int>& scene_body_offsets() const = 0;
+    virtual void get_state_range(int first, int count, double* o, double* b, double* v, double* w) = 0;
     std::string err;
 };
 
@@ -120,6 +125,9 @@ public:
     void phase_times(double* ms, bool reset) override;
     void last_counts(int* c) override;
     void sync() override { PE_CK(cudaStreamSynchronize(st_)); }
+    void repack(const int* keep, int n_keep, const SceneData* const* adds, int n_add) override;
+    const std::vector<int>& scene_body_offsets() const override { return h_scene_off_; }
+    void get_state_range(int first, int count, double* o, double* b, double* v, double* w) override;
     void set_profiling(bool on) override {
         resolve_prof();
         if (on && !prof_) for (int k = 0; k < K_COUNT; k++) { kms_[k] = 0; klaunch_[k] = 0; }
@@ -180,6 +188,10 @@ private:
         return b;
     }
     ShapeTable<R> shapes() const;
+    int append_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
+                      const int* fcnt, const double* hv, const int* foff, const int* fidx);   // returns the first new index
+    void fill_body(R* f, size_t stride, int j, int shape, double mass, double fr, double re, double ld, double ad,
+                   const double* o, const double* b, const double* v, const double* w) const;
     Results<R> results();
     Rows<R> rows();
     int scan(int* data, int n);   // exclusive scan in place; returns the total (synchronises)
@@ -208,6 +220,9 @@ private:
     std::vector<int> h_stype_;
     std::vector<R> h_sparam_;
     std::vector<M3<R>> h_sinertia_;
+    // host copies of the shape tables (shapes are only ever appended after set_shapes)
+    std::vector<int> h_shull_, h_hvb_, h_hvc_, h_hfb_, h_hfc_, h_heb_, h_hec_, h_foff_, h_fidx_;
+    std::vector<R> h_hv_, h_fn_, h_fmn_, h_fmx_, h_ea_, h_eb_;
     // bodies
     int N_ = 0, bcap_ = 0;
     DBuf<R> bf_;
@@ -238,8 +253,8 @@ private:
     DBuf<uint32_t> isl_corder_;
     DBuf<R> rows_;
     int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0, n_islands_ = 0;
-    int small_island_ = 8;
-    bool sat_attr_ = false;   // islands with at most this many results run serially in one thread
+    int small_island_ = 8;    // islands with at most this many results run serially in one thread
+    bool sat_attr_ = false;
 };
 
 } // namespace pe

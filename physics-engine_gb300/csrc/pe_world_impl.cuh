@@ -89,55 +89,113 @@ template <class T> static void upload(DBuf<T>& d, const std::vector<T>& h, cudaS
 }
 
 // ------------------------------------------------------------------ scene upload
+// device copy grows geometrically keeping its contents; only the new tail is copied
+template <class T> static void upload_tail(DBuf<T>& d, const std::vector<T>& h, size_t from, cudaStream_t st) {
+    const size_t want = h.size() + 1;
+    if (want > d.n) d.ensure(std::max(want, d.n + d.n / 2), true);
+    if (h.size() > from) PE_CK(cudaMemcpyAsync(d.p + from, h.data() + from, (h.size() - from) * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
 template <class R>
 void World<R>::set_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
                           const int* fcnt, int HV, const double* hv, int HF, const int* foff, const int* fidx) {
     (void)HV; (void)HF;
-    std::vector<int> t(S), hull(S, -1), hvb, hvc, hfb, hfc, heb, hec, f_off, f_idx;
-    std::vector<R> prm(S * 3), v, fn, fmn, fmx, ea, eb;
-    h_sinertia_.assign(S, M3<R>());
+    S_ = 0;
+    h_stype_.clear(); h_sparam_.clear(); h_sinertia_.clear(); h_shull_.clear();
+    h_hvb_.clear(); h_hvc_.clear(); h_hfb_.clear(); h_hfc_.clear(); h_heb_.clear(); h_hec_.clear(); h_foff_.clear(); h_fidx_.clear();
+    h_hv_.clear(); h_fn_.clear(); h_fmn_.clear(); h_fmx_.clear(); h_ea_.clear(); h_eb_.clear();
+    append_shapes(S, type, param, vbeg, vcnt, fbeg, fcnt, hv, foff, fidx);
+}
+
+template <class R>
+int World<R>::append_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
+                            const int* fcnt, const double* hv, const int* foff, const int* fidx) {
+    const int s0 = S_;
+    const size_t o_h = h_hvb_.size(), o_v = h_hv_.size(), o_f = h_fn_.size(), o_e = h_ea_.size(), o_fo = h_foff_.size(),
+                 o_fi = h_fidx_.size();
     for (int s = 0; s < S; s++) {
-        t[s] = type[s];
-        for (int k = 0; k < 3; k++) prm[s * 3 + k] = R(param[s * 3 + k]);
-        if (t[s] == ST_BOX) h_sinertia_[s] = box_inertia(V3<R>(prm[s * 3], prm[s * 3 + 1], prm[s * 3 + 2]));
-        else if (t[s] == ST_SPHERE) h_sinertia_[s] = sphere_inertia(prm[s * 3]);
-        else if (t[s] == ST_CYLINDER) h_sinertia_[s] = cylinder_inertia(prm[s * 3], prm[s * 3 + 1]);
-        else if (t[s] == ST_HULL) {
+        const int t = type[s];
+        V3<R> p;
+        for (int k = 0; k < 3; k++) h_sparam_.push_back(R(param[s * 3 + k]));
+        p = V3<R>(h_sparam_[(size_t)(s0 + s) * 3], h_sparam_[(size_t)(s0 + s) * 3 + 1], h_sparam_[(size_t)(s0 + s) * 3 + 2]);
+        h_stype_.push_back(t);
+        int hull = -1;
+        M3<R> inertia;
+        if (t == ST_BOX) inertia = box_inertia(p);
+        else if (t == ST_SPHERE) inertia = sphere_inertia(p.x);
+        else if (t == ST_CYLINDER) inertia = cylinder_inertia(p.x, p.y);
+        else if (t == ST_HULL) {
             // local face offsets of this shape
             std::vector<int> lo(fcnt[s] + 1);
             for (int f = 0; f <= fcnt[s]; f++) lo[f] = foff[fbeg[s] + f] - foff[fbeg[s]];
             if (fcnt[s] >= 16382) throw std::runtime_error("convex mesh with more than 16381 faces is not supported");
             HullPrep<R> h = prepare_hull<R>(hv + (size_t)vbeg[s] * 3, vcnt[s], lo.data(), fidx + foff[fbeg[s]], fcnt[s]);
-            h_sinertia_[s] = h.inertia;
-            hull[s] = (int)hvb.size();
-            hvb.push_back((int)v.size() / 3); hvc.push_back(vcnt[s]);
-            hfb.push_back((int)fn.size() / 3); hfc.push_back(fcnt[s]);
-            heb.push_back((int)ea.size() / 3); hec.push_back((int)h.e_a.size() / 3);
-            const int ibase = (int)f_idx.size();
-            if (f_off.empty()) f_off.push_back(0);
-            for (int f = 0; f < fcnt[s]; f++) f_off.push_back(ibase + h.f_off[f + 1]);
-            f_idx.insert(f_idx.end(), h.f_idx.begin(), h.f_idx.end());
-            v.insert(v.end(), h.v.begin(), h.v.end());
-            fn.insert(fn.end(), h.f_n.begin(), h.f_n.end());
-            fmn.insert(fmn.end(), h.f_min.begin(), h.f_min.end());
-            fmx.insert(fmx.end(), h.f_max.begin(), h.f_max.end());
-            ea.insert(ea.end(), h.e_a.begin(), h.e_a.end());
-            eb.insert(eb.end(), h.e_b.begin(), h.e_b.end());
+            inertia = h.inertia;
+            hull = (int)h_hvb_.size();
+            h_hvb_.push_back((int)h_hv_.size() / 3); h_hvc_.push_back(vcnt[s]);
+            h_hfb_.push_back((int)h_fn_.size() / 3); h_hfc_.push_back(fcnt[s]);
+            h_heb_.push_back((int)h_ea_.size() / 3); h_hec_.push_back((int)h.e_a.size() / 3);
+            const int ibase = (int)h_fidx_.size();
+            if (h_foff_.empty()) h_foff_.push_back(0);
+            for (int f = 0; f < fcnt[s]; f++) h_foff_.push_back(ibase + h.f_off[f + 1]);
+            h_fidx_.insert(h_fidx_.end(), h.f_idx.begin(), h.f_idx.end());
+            h_hv_.insert(h_hv_.end(), h.v.begin(), h.v.end());
+            h_fn_.insert(h_fn_.end(), h.f_n.begin(), h.f_n.end());
+            h_fmn_.insert(h_fmn_.end(), h.f_min.begin(), h.f_min.end());
+            h_fmx_.insert(h_fmx_.end(), h.f_max.begin(), h.f_max.end());
+            h_ea_.insert(h_ea_.end(), h.e_a.begin(), h.e_a.end());
+            h_eb_.insert(h_eb_.end(), h.e_b.begin(), h.e_b.end());
         } else {
-            throw std::runtime_error("unsupported shape type " + std::to_string(t[s]));
+            throw std::runtime_error("unsupported shape type " + std::to_string(t));
         }
+        h_shull_.push_back(hull);
+        h_sinertia_.push_back(inertia);
     }
     // hull face offsets are global per face: face f of hull h sits at hfb[h] + f, its offsets at
     // f_off[hfb[h] + f] .. f_off[hfb[h] + f + 1]
-    S_ = S;
-    h_stype_ = t;
-    h_sparam_ = prm;
-    upload(stype_, t, st_); upload(sparam_, prm, st_); upload(shull_, hull, st_);
-    upload(hvbeg_, hvb, st_); upload(hvcnt_, hvc, st_); upload(hfbeg_, hfb, st_); upload(hfcnt_, hfc, st_);
-    upload(hebeg_, heb, st_); upload(hecnt_, hec, st_);
-    upload(hv_, v, st_); upload(hfoff_, f_off, st_); upload(hfidx_, f_idx, st_); upload(hfn_, fn, st_);
-    upload(hfmin_, fmn, st_); upload(hfmax_, fmx, st_); upload(hea_, ea, st_); upload(heb_, eb, st_);
+    S_ = s0 + S;
+    PE_CK(cudaStreamSynchronize(st_));   // growth copies below run outside the stream
+    upload_tail(stype_, h_stype_, s0, st_); upload_tail(sparam_, h_sparam_, (size_t)s0 * 3, st_); upload_tail(shull_, h_shull_, s0, st_);
+    upload_tail(hvbeg_, h_hvb_, o_h, st_); upload_tail(hvcnt_, h_hvc_, o_h, st_); upload_tail(hfbeg_, h_hfb_, o_h, st_);
+    upload_tail(hfcnt_, h_hfc_, o_h, st_); upload_tail(hebeg_, h_heb_, o_h, st_); upload_tail(hecnt_, h_hec_, o_h, st_);
+    upload_tail(hv_, h_hv_, o_v, st_); upload_tail(hfoff_, h_foff_, o_fo, st_); upload_tail(hfidx_, h_fidx_, o_fi, st_);
+    upload_tail(hfn_, h_fn_, o_f, st_); upload_tail(hfmin_, h_fmn_, o_f, st_); upload_tail(hfmax_, h_fmx_, o_f, st_);
+    upload_tail(hea_, h_ea_, o_e, st_); upload_tail(heb_, h_eb_, o_e, st_);
     PE_CK(cudaStreamSynchronize(st_));
+    return s0;
+}
+
+// RigidBody::setMass + setCollisionShape (rigidbody.cpp:11-41) and the initial pose: body j of a
+// field-major array with the given stride
+template <class R>
+void World<R>::fill_body(R* f, size_t stride, int j, int shape, double mass, double fr, double re, double ld, double ad,
+                         const double* o, const double* b, const double* v, const double* w) const {
+    auto F = [&](int k) -> R& { return f[(size_t)k * stride + j]; };
+    const R m = R(mass);
+    const R inv_m = m > eps<R>() ? R(1.0) / m : R(0);
+    M3<R> li;
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) li.m[r][c] = h_sinertia_[shape].m[r][c] * m;
+    const M3<R> lii = m > eps<R>() ? inverse3(li) : M3<R>();
+    M3<R> basis;
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) basis.m[r][c] = R(b[r * 3 + c]);
+    const M3<R> wi = world_inertia(basis, lii);
+    for (int k = 0; k < 3; k++) {
+        F(OX + k) = R(o[k]);
+        F(VX + k) = R(v[k]);
+        F(WX + k) = R(w[k]);
+    }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            F(B00 + r * 3 + c) = basis.m[r][c];
+            F(I00 + r * 3 + c) = wi.m[r][c];
+            F(L00 + r * 3 + c) = lii.m[r][c];
+        }
+    F(INVM) = inv_m;
+    F(MASS) = m;
+    F(FRIC) = R(fr);
+    F(REST) = R(re);
+    F(LDAMP) = R(ld);
+    F(ADAMP) = R(ad);
 }
 
 template <class R>
@@ -147,35 +205,9 @@ void World<R>::set_bodies(int n, const int* shape, const int* flags, const doubl
     N_ = n;
     bcap_ = std::max(n, 1);
     std::vector<R> f((size_t)NBF * bcap_, R(0));
-    auto F = [&](int k, int i) -> R& { return f[(size_t)k * bcap_ + i]; };
     for (int i = 0; i < n; i++) {
         if (shape[i] < 0 || shape[i] >= S_) throw std::runtime_error("body " + std::to_string(i) + ": bad shape index");
-        const R m = R(mass[i]);
-        // RigidBody::setMass + setCollisionShape (rigidbody.cpp:11-41)
-        const R inv_m = m > eps<R>() ? R(1.0) / m : R(0);
-        M3<R> li;
-        for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) li.m[r][c] = h_sinertia_[shape[i]].m[r][c] * m;
-        const M3<R> lii = m > eps<R>() ? inverse3(li) : M3<R>();
-        M3<R> basis;
-        for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) basis.m[r][c] = R(b[i * 9 + r * 3 + c]);
-        const M3<R> wi = world_inertia(basis, lii);
-        for (int k = 0; k < 3; k++) {
-            F(OX + k, i) = R(o[i * 3 + k]);
-            F(VX + k, i) = R(v[i * 3 + k]);
-            F(WX + k, i) = R(w[i * 3 + k]);
-        }
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) {
-                F(B00 + r * 3 + c, i) = basis.m[r][c];
-                F(I00 + r * 3 + c, i) = wi.m[r][c];
-                F(L00 + r * 3 + c, i) = lii.m[r][c];
-            }
-        F(INVM, i) = inv_m;
-        F(MASS, i) = m;
-        F(FRIC, i) = R(fr[i]);
-        F(REST, i) = R(re[i]);
-        F(LDAMP, i) = R(ld[i]);
-        F(ADAMP, i) = R(ad[i]);
+        fill_body(f.data(), bcap_, i, shape[i], mass[i], fr[i], re[i], ld[i], ad[i], o + i * 3, b + i * 9, v + i * 3, w + i * 3);
     }
     upload(bf_, f, st_);
     upload(bshape_, std::vector<int>(shape, shape + n), st_);
@@ -625,6 +657,166 @@ void World<R>::set_results(int n, const int* a, const int* b, const int* ps, con
     PE_CK(cudaMemcpyAsync(res_scene_off_.p, off.data(), (NS_ + 1) * sizeof(int), cudaMemcpyHostToDevice, st_));
     PE_CK(cudaStreamSynchronize(st_));
     R_ = n;
+}
+
+// ------------------------------------------------------------------ serving: scene repacking
+namespace {
+// kept bodies: field-major gather from the old layout (stride ocap) into the new one (stride ncap)
+template <class R>
+__global__ void k_repack_bodies(const R* of, int ocap, const int* oshape, const int* oflags, R* nf, int ncap, int* nshape,
+                                int* nflags, const int* src, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int i = src[j];
+    for (int k = 0; k < NBF; k++) nf[(size_t)k * ncap + j] = of[(size_t)k * ocap + i];
+    nshape[j] = oshape[i];
+    nflags[j] = oflags[i];
+}
+// added bodies: a compact field-major block [NBF x n] placed at new index `at`
+template <class R>
+__global__ void k_place_bodies(const R* blk, int n, R* nf, int ncap, int at) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    for (int k = 0; k < NBF; k++) nf[(size_t)k * ncap + at + j] = blk[(size_t)k * n + j];
+}
+// contact-result distance pools: slot t of the new pool comes from the kept scene's old segment
+template <class R>
+__global__ void k_repack_pool(const R* src, R* dst, const int* new_off, const int* old_start, int ns, int n_slots) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_slots) return;
+    const int r = t / kSlots, k = t - r * kSlots;
+    int lo = 0, hi = ns;   // scene s with new_off[s] <= r < new_off[s + 1]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (new_off[mid] <= r) lo = mid;
+        else hi = mid;
+    }
+    dst[t] = src[(size_t)(old_start[lo] + r - new_off[lo]) * kSlots + k];
+}
+}  // namespace
+
+template <class R>
+void World<R>::repack(const int* keep, int n_keep, const SceneData* const* adds, int n_add) {
+    PE_CK(cudaStreamSynchronize(st_));
+    const int ons = NS_;
+    std::vector<int> old_res(ons + 1, 0), old_axis(std::max(ons, 1), 0);
+    PE_CK(cudaMemcpy(old_res.data(), res_scene_off_.p, (ons + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    PE_CK(cudaMemcpy(old_axis.data(), scene_axis_.p, ons * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n_keep; k++)
+        if (keep[k] < 0 || keep[k] >= ons) throw std::runtime_error("repack: kept scene index out of range");
+    // shapes of the added scenes go to the end of the shape tables
+    std::vector<int> sbase(n_add);
+    for (int a = 0; a < n_add; a++) {
+        const SceneData& d = *adds[a];
+        for (int sh : d.body_shape)
+            if (sh < 0 || sh >= d.n_shapes()) throw std::runtime_error("repack: body shape index out of range");
+        sbase[a] = append_shapes(d.n_shapes(), d.shape_type.data(), d.shape_param.data(), d.hull_vbeg.data(), d.hull_vcnt.data(),
+                                 d.hull_fbeg.data(), d.hull_fcnt.data(), d.hull_verts.data(), d.hull_face_off.data(),
+                                 d.hull_face_idx.data());
+    }
+    // new body layout: kept scenes in order, then the added ones
+    std::vector<int> off(1, 0), src;
+    for (int k = 0; k < n_keep; k++) {
+        const int s = keep[k];
+        for (int i = h_scene_off_[s]; i < h_scene_off_[s + 1]; i++) src.push_back(i);
+        off.push_back((int)src.size());
+    }
+    const int n_kept = (int)src.size();
+    int n_new = 0;
+    for (int a = 0; a < n_add; a++) { n_new += adds[a]->n_bodies(); off.push_back(n_kept + n_new); }
+    const int N = n_kept + n_new, ncap = std::max(N, 1);
+    std::vector<R> blk((size_t)NBF * std::max(n_new, 1), R(0));
+    std::vector<int> ashape(std::max(n_new, 1)), aflags(std::max(n_new, 1));
+    for (int a = 0, j = 0; a < n_add; a++) {
+        const SceneData& d = *adds[a];
+        for (int i = 0; i < d.n_bodies(); i++, j++) {
+            ashape[j] = sbase[a] + d.body_shape[i];
+            aflags[j] = d.body_flags[i];
+            fill_body(blk.data(), n_new, j, ashape[j], d.mass[i], d.friction[i], d.restitution[i], d.lin_damp[i], d.ang_damp[i],
+                      &d.origin[(size_t)i * 3], &d.basis[(size_t)i * 9], &d.lin_vel[(size_t)i * 3], &d.ang_vel[(size_t)i * 3]);
+        }
+    }
+    DBuf<R> nf;
+    DBuf<int> nshape, nflags, dsrc;
+    nf.ensure((size_t)NBF * ncap);
+    nshape.ensure(ncap + 1);
+    nflags.ensure(ncap + 1);
+    if (n_kept) {
+        upload(dsrc, src, st_);
+        launch(K_MISC, grid(n_kept), k_repack_bodies<R>, (const R*)bf_.p, bcap_, (const int*)bshape_.p, (const int*)bflags_.p, nf.p,
+               ncap, nshape.p, nflags.p, (const int*)dsrc.p, n_kept);
+    }
+    DBuf<R> dblk;
+    if (n_new) {
+        upload(dblk, blk, st_);
+        launch(K_MISC, grid(n_new), k_place_bodies<R>, (const R*)dblk.p, n_new, nf.p, ncap, n_kept);
+        PE_CK(cudaMemcpyAsync(nshape.p + n_kept, ashape.data(), n_new * sizeof(int), cudaMemcpyHostToDevice, st_));
+        PE_CK(cudaMemcpyAsync(nflags.p + n_kept, aflags.data(), n_new * sizeof(int), cudaMemcpyHostToDevice, st_));
+    }
+    // contact-result pools of the kept scenes (the current generation becomes the next step's "previous")
+    const int ns = n_keep + n_add;
+    std::vector<int> new_res(ns + 1, 0), old_start(std::max(ns, 1), 0), axis(std::max(ns, 1), 0);
+    for (int k = 0; k < n_keep; k++) {
+        const int s = keep[k];
+        new_res[k + 1] = new_res[k] + old_res[s + 1] - old_res[s];
+        old_start[k] = old_res[s];
+        axis[k] = old_axis[s];
+    }
+    for (int a = 0; a < n_add; a++) new_res[n_keep + a + 1] = new_res[n_keep + a];
+    const int T = new_res[ns];
+    ensure_pair_capacity(std::max(T, 1));   // grows both pool generations keeping their contents
+    if (T) {
+        DBuf<int> dnew, dold;
+        upload(dnew, new_res, st_);
+        upload(dold, old_start, st_);
+        launch(K_MISC, grid(T * kSlots), k_repack_pool<R>, (const R*)res_dist_[cur_dist_].p, res_dist_[cur_dist_ ^ 1].p,
+               (const int*)dnew.p, (const int*)dold.p, ns, T * kSlots);
+        PE_CK(cudaStreamSynchronize(st_));
+        cur_dist_ ^= 1;
+    }
+    PE_CK(cudaStreamSynchronize(st_));
+    std::swap(bf_.p, nf.p); std::swap(bf_.n, nf.n);
+    std::swap(bshape_.p, nshape.p); std::swap(bshape_.n, nshape.n);
+    std::swap(bflags_.p, nflags.p); std::swap(bflags_.n, nflags.n);
+    N_ = N;
+    bcap_ = ncap;
+    claim_.ensure(N + 1);
+    // scene tables (as set_scenes), then the kept axes and result offsets
+    NS_ = std::max(ns, 1);
+    if (ns == 0) off = {0, 0};
+    h_scene_off_ = off;
+    std::vector<int> sc(std::max(N, 1), 0);
+    for (int s = 0; s < ns; s++) for (int i = off[s]; i < off[s + 1]; i++) sc[i] = s;
+    upload(bscene_, sc, st_);
+    upload(scene_off_, off, st_);
+    upload(scene_axis_, axis, st_);
+    if (ns == 0) new_res = {0, 0};
+    std::vector<int> zero(NS_ + 1, 0);
+    upload(pair_scene_off_, zero, st_);
+    upload(prev_res_off_, zero, st_);
+    upload(res_scene_off_, new_res, st_);
+    h_pair_scene_off_ = zero;
+    P_ = 0;
+    R_ = 0;
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
+template <class R>
+void World<R>::get_state_range(int first, int count, double* o, double* b, double* v, double* w) {
+    if (first < 0 || count < 0 || first + count > N_) throw std::runtime_error("state range out of bounds");
+    if (!count) return;
+    // fields OX..WZ (origin, basis, linear and angular velocity) are 18 consecutive field rows
+    R* h = staging((size_t)18 * count);
+    PE_CK(cudaMemcpy2DAsync(h, (size_t)count * sizeof(R), bf_.p + first, (size_t)bcap_ * sizeof(R), (size_t)count * sizeof(R), 18,
+                            cudaMemcpyDeviceToHost, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+    struct G { double* dst; int k0; int nk; };
+    const G groups[4] = {{o, OX, 3}, {b, B00, 9}, {v, VX, 3}, {w, WX, 3}};
+    for (const G& g : groups) {
+        if (!g.dst) continue;
+        for (int k = 0; k < g.nk; k++)
+            for (int i = 0; i < count; i++) g.dst[(size_t)i * g.nk + k] = (double)h[(size_t)(g.k0 + k) * count + i];
+    }
 }
 
 } // namespace pe

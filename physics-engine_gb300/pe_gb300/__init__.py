@@ -67,6 +67,13 @@ def load(build_if_missing: bool = True):
         "pe_gpu_kernel_stats": (I, [P, dp, np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]),
         # device pointers throughout (see include/pe_gpu.h)
         "pe_gpu_sap_pairs_noalloc": (I, [I, I, P, P, P, I, P, I, P, P, C.c_char_p, I]),
+        "pe_gpu_server_create": (I, [C.c_void_p, D, D, D, D, I, I, D, C.POINTER(P)]),
+        "pe_gpu_server_destroy": (I, [P]),
+        "pe_gpu_server_last_error": (C.c_char_p, [P]),
+        "pe_gpu_server_submit": (I, [P, C.c_void_p, I, C.POINTER(C.c_longlong)]),
+        "pe_gpu_server_step": (I, [P, C.POINTER(I), C.POINTER(I)]),
+        "pe_gpu_server_result": (I, [P, C.c_longlong, C.POINTER(I), P, P, P, P]),
+        "pe_gpu_server_stats": (I, [P, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -253,3 +260,87 @@ class GpuWorld:
         cnt = np.zeros(n, np.int64)
         self._ck(self.lib.pe_gpu_kernel_stats(self.h, ms, cnt))
         return {self.lib.pe_gpu_kernel_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(n)}
+
+
+class _SceneDesc(C.Structure):
+    _fields_ = [("n_shapes", C.c_int), ("shape_type", C.c_void_p), ("shape_param", C.c_void_p),
+                ("hull_vbeg", C.c_void_p), ("hull_vcnt", C.c_void_p), ("hull_fbeg", C.c_void_p), ("hull_fcnt", C.c_void_p),
+                ("n_hull_verts", C.c_int), ("hull_verts", C.c_void_p), ("n_hull_faces", C.c_int), ("hull_face_off", C.c_void_p),
+                ("hull_face_idx", C.c_void_p), ("n_bodies", C.c_int), ("body_shape", C.c_void_p), ("body_flags", C.c_void_p),
+                ("mass", C.c_void_p), ("friction", C.c_void_p), ("restitution", C.c_void_p), ("lin_damp", C.c_void_p),
+                ("ang_damp", C.c_void_p), ("origin", C.c_void_p), ("basis", C.c_void_p), ("lin_vel", C.c_void_p),
+                ("ang_vel", C.c_void_p)]
+
+
+QUEUED, RUNNING, DONE, REJECTED = 0, 1, 2, 3
+
+
+class Server:
+    """Request loop over one device-resident world (pe_gpu_server_*): submit scenes with a step
+    count, call step() to retire, admit by HBM footprint and advance all live scenes together."""
+
+    def __init__(self, real_bits=32, device=0, dt=1.0 / 60.0, gravity=(0.0, -9.8, 0.0), iterations=10, mode=COLORED,
+                 hbm_budget_bytes=64e9):
+        self.lib = load()
+        self.h = C.c_void_p()
+        cfg = _Config(real_bits, device)
+        rc = self.lib.pe_gpu_server_create(C.byref(cfg), float(dt), *map(float, gravity), int(iterations), int(mode),
+                                           float(hbm_budget_bytes), C.byref(self.h))
+        if rc != 0:
+            raise PeGpuError(f"pe_gpu_server_create failed ({rc})")
+        self.n_bodies = {}
+
+    def _ck(self, rc):
+        if rc != 0:
+            msg = self.lib.pe_gpu_server_last_error(self.h)
+            raise PeGpuError(f"pe_gpu_server call failed ({rc}): {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.pe_gpu_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, s, n_steps):
+        keep = [_i32(s.shape_type), _f64(s.shape_param).ravel(), _i32(s.hull_vbeg), _i32(s.hull_vcnt), _i32(s.hull_fbeg),
+                _i32(s.hull_fcnt), _f64(s.hull_verts).ravel() if len(s.hull_verts) else np.zeros(3),
+                _i32(s.hull_face_off), _i32(s.hull_face_idx) if len(s.hull_face_idx) else np.zeros(1, np.int32),
+                _i32(s.body_shape), _i32(s.body_flags), _f64(s.mass), _f64(s.friction), _f64(s.restitution),
+                _f64(s.lin_damp), _f64(s.ang_damp), _f64(s.origin).ravel(), _f64(s.basis).ravel(), _f64(s.lin_vel).ravel(),
+                _f64(s.ang_vel).ravel()]
+        ptr = [a.ctypes.data for a in keep]
+        d = _SceneDesc(s.n_shapes, ptr[0], ptr[1], ptr[2], ptr[3], ptr[4], ptr[5], len(s.hull_verts), ptr[6],
+                       len(s.hull_face_off) - 1, ptr[7], ptr[8], s.n_bodies, ptr[9], ptr[10], ptr[11], ptr[12], ptr[13],
+                       ptr[14], ptr[15], ptr[16], ptr[17], ptr[18], ptr[19])
+        rid = C.c_longlong()
+        self._ck(self.lib.pe_gpu_server_submit(self.h, C.byref(d), int(n_steps), C.byref(rid)))
+        self.n_bodies[rid.value] = s.n_bodies
+        return rid.value
+
+    def step(self):
+        live, queued = C.c_int(), C.c_int()
+        self._ck(self.lib.pe_gpu_server_step(self.h, C.byref(live), C.byref(queued)))
+        return live.value, queued.value
+
+    def result(self, rid):
+        """(state, final state dict or None); a finished request's state is returned once."""
+        n = self.n_bodies[rid]
+        o, b, v, w = np.zeros((n, 3)), np.zeros((n, 3, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+        st = C.c_int()
+        self._ck(self.lib.pe_gpu_server_result(self.h, C.c_longlong(rid), C.byref(st), o.ctypes.data, b.ctypes.data,
+                                                v.ctypes.data, w.ctypes.data))
+        if st.value in (DONE, REJECTED):
+            del self.n_bodies[rid]
+        return st.value, (dict(origin=o, basis=b, lin_vel=v, ang_vel=w) if st.value == DONE else None)
+
+    def stats(self):
+        out = np.zeros(10)
+        self._ck(self.lib.pe_gpu_server_stats(self.h, out))
+        keys = ("p50_step_ms", "p99_step_ms", "mean_step_ms", "steps", "body_steps", "admitted", "finished",
+                "peak_footprint_bytes", "live", "queued")
+        return dict(zip(keys, out.tolist()))

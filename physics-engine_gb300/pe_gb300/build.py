@@ -18,7 +18,7 @@ OUT = PKG / "lib"
 OBJ = PKG / "_build"
 LIB = OUT / "libpe_gpu.so"
 
-CU_SOURCES = ["pe_util.cu", "pe_world_f32.cu", "pe_world_f64.cu", "pe_capi.cu", "pe_noalloc.cu"]
+CU_SOURCES = ["pe_util.cu", "pe_world_f32.cu", "pe_world_f64.cu", "pe_capi.cu", "pe_noalloc.cu", "pe_server.cu"]
 CPP_SOURCES = ["pe_host_shapes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
@@ -68,7 +68,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int = 0) -> Path:
                 raise RuntimeError(f"compile failed: {' '.join(cmd)}")
     objs = [str(o) for _, o in jobs_list]
     if force or not LIB.exists() or LIB.stat().st_mtime < max(Path(o).stat().st_mtime for o in objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart", "-Xlinker", "--no-undefined"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
