@@ -352,6 +352,77 @@ def _cpu_scene_worker(job):
     return scene.n_bodies * steps, w.time_steps(steps)
 
 
+def run_serving(args, device):
+    """Serving: Poisson arrivals at 200 requests/s for --serve-seconds (60 s in the configuration);
+    each request is a pile of 16..2,048 bodies (log-uniform; drawn from a seeded pool of 256 scenes
+    generated like the batched piles) asking for K ~ U[60, 600] steps; admission by a 64 GB budget;
+    coloured, FP32.  Throughput = body-steps of all requests / wall time from the first arrival to
+    the last completion, through the public API (scenes submitted from host memory, final states
+    read back)."""
+    import pe_gb300 as pg
+    from pe_gb300 import scene as sc
+    rng = np.random.default_rng(200)
+    merged, offs = sc.batched_piles(n_scenes=256, seed=2048, size_range=(16, 2048), real_bits=32)
+    pool = [sc.extract(merged, offs, k) for k in range(256)]
+    rate, dur = 200.0, float(args.serve_seconds)
+    arr = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * dur * 2) + 16))
+    arr = arr[arr < dur]
+    ks = rng.integers(60, 601, size=len(arr))
+    picks = rng.integers(0, len(pool), size=len(arr))
+    srv = pg.Server(real_bits=32, device=device, dt=1.0 / 60.0, iterations=10, mode=pg.COLORED, hbm_budget_bytes=64e9)
+    rid = srv.submit(pool[0], 3)           # warm-up request (module loading, first allocations)
+    while srv.result(rid)[0] != pg.DONE:
+        srv.step()
+    base = srv.stats()
+    pending, due, lat, loop_ms = {}, {}, [], []
+    h2d = d2h = 0
+    nxt, steps = 0, 0
+    t0 = time.perf_counter()
+    with ClockSampler(device) as clk:
+        while nxt < len(arr) or pending:
+            now = time.perf_counter() - t0
+            while nxt < len(arr) and arr[nxt] <= now:
+                s = pool[picks[nxt]]
+                r = srv.submit(s, int(ks[nxt]))
+                pending[r] = arr[nxt]
+                due.setdefault(steps + int(ks[nxt]) + 1, []).append(r)
+                h2d += s.n_bodies * (18 * 8 + 7 * 8) + s.hull_verts.size * 8
+                nxt += 1
+            if not pending:
+                time.sleep(max(0.0, arr[nxt] - now))
+                continue
+            t1 = time.perf_counter()
+            srv.step()
+            loop_ms.append((time.perf_counter() - t1) * 1e3)
+            steps += 1
+            for r in due.pop(steps, []):
+                st, res = srv.result(r)
+                if st == pg.DONE:
+                    lat.append(time.perf_counter() - t0 - pending.pop(r))
+                    d2h += res["origin"].size * 8 * 6
+                else:                          # admission was delayed: look again next step
+                    due.setdefault(steps + 1, []).append(r)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    body_steps = st["body_steps"] - base["body_steps"]
+    lat.sort()
+    loop_ms.sort()
+    pct = lambda a, p: a[min(len(a) - 1, int(p * (len(a) - 1) + 0.5))] if a else None
+    value = body_steps / wall
+    cfg = dict(workload=f"serving: Poisson arrivals at 200 requests/s over {dur:g} s, piles of 16..2,048 bodies "
+                        "(log-uniform, box/sphere/cylinder/convex hull), K ~ U[60,600] steps, 64 GB admission budget, "
+                        "FP32, 10 SI iterations, coloured", requests=len(arr), scenes_in_pool=len(pool),
+               p50_step_ms=st["p50_step_ms"], p99_step_ms=st["p99_step_ms"], mean_step_ms=st["mean_step_ms"],
+               p50_loop_ms=pct(loop_ms, 0.5), p99_loop_ms=pct(loop_ms, 0.99),
+               p50_request_s=pct(lat, 0.5), p99_request_s=pct(lat, 0.99), finished=len(lat),
+               peak_footprint_gb=st["peak_footprint_bytes"] / 1e9, batched_steps=steps, wall_s=wall)
+    return dict(metric=METRIC, value=value, unit=UNIT, n_gpus=1, steps=steps, warmup=0,
+                ms_per_step=wall / max(steps, 1) * 1e3, higher_is_better=True, scaling="weak", vs_baseline=None,
+                dtype="f32", data="synthetic", config=cfg,
+                e2e=dict(value=value, unit=UNIT, h2d_bytes_per_step=h2d / max(steps, 1), d2h_bytes_per_step=d2h / max(steps, 1)),
+                gpu_launches=None, clocks=clk.summary())
+
+
 def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, steps=5):
     """The reference's CPU step (its algorithm restated in oracle/) on a bounded sample, all host
     threads.  One scene: the reference's thread pool inside one world.  Independent scenes: one
@@ -389,7 +460,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "stress", "tower", "large"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "stress", "tower", "large", "serving"])
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window of the serving workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scenes", type=int, default=4096, help="scene count of the batched workload")
     ap.add_argument("--no-per-scene", action="store_true", help="skip the one-scene-per-launch comparison")
@@ -400,6 +472,10 @@ def main():
 
     if args.impl == "reference":
         if rank != 0:
+            return 0
+        if args.workload == "serving":
+            print(json.dumps(dict(impl="reference", unavailable="the reference has no request loop; its CPU step is timed by "
+                                                                "the batched workload's reference arm")))
             return 0
         scene, bits, mode, offs, cfg = make_workload(args.workload, args.scenes)
         if offs is not None:   # independent scenes: the reference steps one World per scene
@@ -424,6 +500,11 @@ def main():
                               vs_baseline=None, dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg,
                               impl="reference", cpu_baseline=cb,
                               e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))))
+        return 0
+
+    if args.workload == "serving":
+        if rank == 0:
+            print(json.dumps(run_serving(args, local)))
         return 0
 
     dist = None

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 #include "pe_host.h"
 #include "pe_kernels.cuh"
@@ -188,8 +189,11 @@ private:
         return b;
     }
     ShapeTable<R> shapes() const;
+    // appends shapes; returns the first new index.  With `remap`, convex meshes identical to one
+    // appended this way before are not appended again: remap[s] is shape s's index in the tables.
     int append_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
-                      const int* fcnt, const double* hv, const int* foff, const int* fidx);   // returns the first new index
+                      const int* fcnt, const double* hv, const int* foff, const int* fidx, std::vector<int>* remap = nullptr);
+    std::unordered_map<std::string, int> hull_by_content_;
     void fill_body(R* f, size_t stride, int j, int shape, double mass, double fr, double re, double ld, double ad,
                    const double* o, const double* b, const double* v, const double* w) const;
     Results<R> results();

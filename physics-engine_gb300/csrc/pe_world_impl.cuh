@@ -104,20 +104,40 @@ void World<R>::set_shapes(int S, const int* type, const double* param, const int
     h_stype_.clear(); h_sparam_.clear(); h_sinertia_.clear(); h_shull_.clear();
     h_hvb_.clear(); h_hvc_.clear(); h_hfb_.clear(); h_hfc_.clear(); h_heb_.clear(); h_hec_.clear(); h_foff_.clear(); h_fidx_.clear();
     h_hv_.clear(); h_fn_.clear(); h_fmn_.clear(); h_fmx_.clear(); h_ea_.clear(); h_eb_.clear();
+    hull_by_content_.clear();
     append_shapes(S, type, param, vbeg, vcnt, fbeg, fcnt, hv, foff, fidx);
 }
 
 template <class R>
 int World<R>::append_shapes(int S, const int* type, const double* param, const int* vbeg, const int* vcnt, const int* fbeg,
-                            const int* fcnt, const double* hv, const int* foff, const int* fidx) {
+                            const int* fcnt, const double* hv, const int* foff, const int* fidx, std::vector<int>* remap) {
     const int s0 = S_;
     const size_t o_h = h_hvb_.size(), o_v = h_hv_.size(), o_f = h_fn_.size(), o_e = h_ea_.size(), o_fo = h_foff_.size(),
                  o_fi = h_fidx_.size();
+    if (remap) remap->assign(S, -1);
+    int added = 0;
     for (int s = 0; s < S; s++) {
         const int t = type[s];
+        std::string key;
+        if (remap && t == ST_HULL) {   // content key: vertices, then face index lists
+            key.reserve((size_t)vcnt[s] * 24 + (size_t)(foff[fbeg[s] + fcnt[s]] - foff[fbeg[s]] + fcnt[s] + 3) * 4);
+            const int head[3] = {vcnt[s], fcnt[s], foff[fbeg[s] + fcnt[s]] - foff[fbeg[s]]};
+            key.append(reinterpret_cast<const char*>(head), sizeof head);
+            key.append(reinterpret_cast<const char*>(hv + (size_t)vbeg[s] * 3), (size_t)vcnt[s] * 3 * sizeof(double));
+            for (int f = 0; f < fcnt[s]; f++) {
+                const int n = foff[fbeg[s] + f + 1] - foff[fbeg[s] + f];
+                key.append(reinterpret_cast<const char*>(&n), sizeof n);
+                key.append(reinterpret_cast<const char*>(fidx + foff[fbeg[s] + f]), (size_t)n * sizeof(int));
+            }
+            auto it = hull_by_content_.find(key);
+            if (it != hull_by_content_.end()) { (*remap)[s] = it->second; continue; }
+        }
+        const int gs = s0 + added++;
+        if (remap) (*remap)[s] = gs;
+        if (!key.empty()) hull_by_content_.emplace(std::move(key), gs);
         V3<R> p;
         for (int k = 0; k < 3; k++) h_sparam_.push_back(R(param[s * 3 + k]));
-        p = V3<R>(h_sparam_[(size_t)(s0 + s) * 3], h_sparam_[(size_t)(s0 + s) * 3 + 1], h_sparam_[(size_t)(s0 + s) * 3 + 2]);
+        p = V3<R>(h_sparam_[(size_t)gs * 3], h_sparam_[(size_t)gs * 3 + 1], h_sparam_[(size_t)gs * 3 + 2]);
         h_stype_.push_back(t);
         int hull = -1;
         M3<R> inertia;
@@ -153,7 +173,7 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
     }
     // hull face offsets are global per face: face f of hull h sits at hfb[h] + f, its offsets at
     // f_off[hfb[h] + f] .. f_off[hfb[h] + f + 1]
-    S_ = s0 + S;
+    S_ = s0 + added;
     PE_CK(cudaStreamSynchronize(st_));   // growth copies below run outside the stream
     upload_tail(stype_, h_stype_, s0, st_); upload_tail(sparam_, h_sparam_, (size_t)s0 * 3, st_); upload_tail(shull_, h_shull_, s0, st_);
     upload_tail(hvbeg_, h_hvb_, o_h, st_); upload_tail(hvcnt_, h_hvc_, o_h, st_); upload_tail(hfbeg_, h_hfb_, o_h, st_);
@@ -662,12 +682,23 @@ void World<R>::set_results(int n, const int* a, const int* b, const int* ps, con
 // ------------------------------------------------------------------ serving: scene repacking
 namespace {
 // kept bodies: field-major gather from the old layout (stride ocap) into the new one (stride ncap)
+// scene whose [off[s], off[s + 1]) holds r (the last such s when empty scenes share an offset)
+__device__ __forceinline__ int segment_of(const int* off, int ns, int r) {
+    int lo = 0, hi = ns;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= r) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 template <class R>
 __global__ void k_repack_bodies(const R* of, int ocap, const int* oshape, const int* oflags, R* nf, int ncap, int* nshape,
-                                int* nflags, const int* src, int n) {
+                                int* nflags, const int* koff, const int* first, int nk, int n) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const int i = src[j];
+    const int s = segment_of(koff, nk, j);
+    const int i = first[s] + j - koff[s];
     for (int k = 0; k < NBF; k++) nf[(size_t)k * ncap + j] = of[(size_t)k * ocap + i];
     nshape[j] = oshape[i];
     nflags[j] = oflags[i];
@@ -685,12 +716,7 @@ __global__ void k_repack_pool(const R* src, R* dst, const int* new_off, const in
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n_slots) return;
     const int r = t / kSlots, k = t - r * kSlots;
-    int lo = 0, hi = ns;   // scene s with new_off[s] <= r < new_off[s + 1]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (new_off[mid] <= r) lo = mid;
-        else hi = mid;
-    }
+    const int lo = segment_of(new_off, ns, r);
     dst[t] = src[(size_t)(old_start[lo] + r - new_off[lo]) * kSlots + k];
 }
 }  // namespace
@@ -705,23 +731,23 @@ void World<R>::repack(const int* keep, int n_keep, const SceneData* const* adds,
     for (int k = 0; k < n_keep; k++)
         if (keep[k] < 0 || keep[k] >= ons) throw std::runtime_error("repack: kept scene index out of range");
     // shapes of the added scenes go to the end of the shape tables
-    std::vector<int> sbase(n_add);
+    std::vector<std::vector<int>> smap(n_add);
     for (int a = 0; a < n_add; a++) {
         const SceneData& d = *adds[a];
         for (int sh : d.body_shape)
             if (sh < 0 || sh >= d.n_shapes()) throw std::runtime_error("repack: body shape index out of range");
-        sbase[a] = append_shapes(d.n_shapes(), d.shape_type.data(), d.shape_param.data(), d.hull_vbeg.data(), d.hull_vcnt.data(),
-                                 d.hull_fbeg.data(), d.hull_fcnt.data(), d.hull_verts.data(), d.hull_face_off.data(),
-                                 d.hull_face_idx.data());
+        append_shapes(d.n_shapes(), d.shape_type.data(), d.shape_param.data(), d.hull_vbeg.data(), d.hull_vcnt.data(),
+                      d.hull_fbeg.data(), d.hull_fcnt.data(), d.hull_verts.data(), d.hull_face_off.data(), d.hull_face_idx.data(),
+                      &smap[a]);
     }
-    // new body layout: kept scenes in order, then the added ones
-    std::vector<int> off(1, 0), src;
+    // new body layout: kept scenes in order (first old body of each), then the added ones
+    std::vector<int> off(1, 0), first;
     for (int k = 0; k < n_keep; k++) {
         const int s = keep[k];
-        for (int i = h_scene_off_[s]; i < h_scene_off_[s + 1]; i++) src.push_back(i);
-        off.push_back((int)src.size());
+        first.push_back(h_scene_off_[s]);
+        off.push_back(off.back() + h_scene_off_[s + 1] - h_scene_off_[s]);
     }
-    const int n_kept = (int)src.size();
+    const int n_kept = off.back();
     int n_new = 0;
     for (int a = 0; a < n_add; a++) { n_new += adds[a]->n_bodies(); off.push_back(n_kept + n_new); }
     const int N = n_kept + n_new, ncap = std::max(N, 1);
@@ -730,21 +756,22 @@ void World<R>::repack(const int* keep, int n_keep, const SceneData* const* adds,
     for (int a = 0, j = 0; a < n_add; a++) {
         const SceneData& d = *adds[a];
         for (int i = 0; i < d.n_bodies(); i++, j++) {
-            ashape[j] = sbase[a] + d.body_shape[i];
+            ashape[j] = smap[a][d.body_shape[i]];
             aflags[j] = d.body_flags[i];
             fill_body(blk.data(), n_new, j, ashape[j], d.mass[i], d.friction[i], d.restitution[i], d.lin_damp[i], d.ang_damp[i],
                       &d.origin[(size_t)i * 3], &d.basis[(size_t)i * 9], &d.lin_vel[(size_t)i * 3], &d.ang_vel[(size_t)i * 3]);
         }
     }
     DBuf<R> nf;
-    DBuf<int> nshape, nflags, dsrc;
+    DBuf<int> nshape, nflags, dkoff, dfirst;
     nf.ensure((size_t)NBF * ncap);
     nshape.ensure(ncap + 1);
     nflags.ensure(ncap + 1);
     if (n_kept) {
-        upload(dsrc, src, st_);
+        upload(dkoff, std::vector<int>(off.begin(), off.begin() + n_keep + 1), st_);
+        upload(dfirst, first, st_);
         launch(K_MISC, grid(n_kept), k_repack_bodies<R>, (const R*)bf_.p, bcap_, (const int*)bshape_.p, (const int*)bflags_.p, nf.p,
-               ncap, nshape.p, nflags.p, (const int*)dsrc.p, n_kept);
+               ncap, nshape.p, nflags.p, (const int*)dkoff.p, (const int*)dfirst.p, n_keep, n_kept);
     }
     DBuf<R> dblk;
     if (n_new) {
