@@ -186,17 +186,17 @@ __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* 
 }
 
 // next sweep axis of each scene: the axis of largest AABB-centre variance (sweep_and_prune.cpp:37-40).
-// Sums in double in a fixed order (deterministic run to run): per-tile partial sums of the sorted
-// centres, then one thread per scene adds its tiles in order.  A scene below two bodies keeps its
+// One block per scene sums the sorted centres in double, in an order fixed relative to the scene
+// (thread t takes positions t, t + blockDim, ... of the scene, then a fixed tree), so a scene gets
+// the same sums wherever it sits in a batch and run to run.  A scene below two bodies keeps its
 // axis, as the reference returns before updating it.
-constexpr int kAxisTile = 1024;
 template <class R>
-__global__ void k_bp_axis_partial(const R* smn, const R* smx, int n, const int* sscene, double* part) {
-    const int t = blockIdx.x;
-    const int lo = t * kAxisTile, hi = min(n, lo + kAxisTile);
+__global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, int* scene_axis) {
+    const int s = blockIdx.x;
+    const int lo = scene_off[s], hi = scene_off[s + 1];
+    const int cnt = hi - lo;
+    if (cnt < 2) return;   // whole block
     __shared__ double red[6][kBlock];
-    // tiles never mix scenes in the partial: positions are assigned to the scene of the tile's
-    // first element only when the whole tile is one scene; otherwise the combine step rescans
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
         for (int d = 0; d < 3; d++) {
@@ -211,37 +211,14 @@ __global__ void k_bp_axis_partial(const R* smn, const R* smx, int n, const int* 
         if ((int)threadIdx.x < w) for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x < 6) part[t * 6 + threadIdx.x] = red[threadIdx.x][0];
-}
-
-template <class R>
-__global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, const double* part, int* scene_axis, int n_scenes) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n_scenes) return;
-    const int lo = scene_off[s], hi = scene_off[s + 1];
-    const int cnt = hi - lo;
-    if (cnt < 2) return;
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    int k = lo;
-    while (k < hi) {
-        if (k % kAxisTile == 0 && k + kAxisTile <= hi) {   // a whole tile of this scene
-            for (int q = 0; q < 6; q++) acc[q] += part[(k / kAxisTile) * 6 + q];
-            k += kAxisTile;
-        } else {
-            for (int d = 0; d < 3; d++) {
-                const double c = (double)((smn[(size_t)d * n + k] + smx[(size_t)d * n + k]) * R(0.5));
-                acc[d] += c;
-                acc[3 + d] += c * c;
-            }
-            k++;
-        }
+    if (threadIdx.x == 0) {
+        double v[3];
+        for (int d = 0; d < 3; d++) v[d] = red[3 + d][0] - red[d][0] * red[d][0] / (double)cnt;
+        int ax = 0;
+        if (v[1] > v[0]) ax = 1;
+        if (v[2] > v[ax]) ax = 2;
+        scene_axis[s] = ax;
     }
-    double v[3];
-    for (int d = 0; d < 3; d++) v[d] = acc[3 + d] - acc[d] * acc[d] / (double)cnt;
-    int ax = 0;
-    if (v[1] > v[0]) ax = 1;
-    if (v[2] > v[ax]) ax = 2;
-    scene_axis[s] = ax;
 }
 
 // ===================================================================== narrowphase
@@ -264,7 +241,7 @@ template <class R> __device__ __forceinline__ int sat_class(const ShapeView<R>& 
     if (axes * (w(a) + w(b)) >= kSatHeavyCost) return PC_CONVEX_HEAVY;
     if (a.type == ST_HULL && b.type == ST_HULL) return PC_CONVEX_HULL_HULL;
     if (a.type == ST_CYLINDER) return PC_CONVEX_CYL_CYL;
-    return PC_CONVEX;   // box-hull either way round
+    return a.type == ST_BOX ? PC_CONVEX : PC_CONVEX_HULL_BOX;
 }
 
 template <class R>
@@ -595,9 +572,11 @@ template <class R> constexpr int sat_scratch_reals(int G) { return G == 1 ? 0 : 
 // Staged SAT of one pair by a group of G warps (tid in [0, 32 G)).  Each thread takes axes
 // f and f + 32 G of every 64 G-axis chunk, so a thread's axes ascend; the group stops at the
 // first chunk holding a separating axis.
-template <class R, int G>
+template <class R, int G, int TA, int TB>
 __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
     constexpr int T = 32 * G;
+    if (TA >= 0) c.sa.type = TA;   // shape types known at compile time: the other branches fold away
+    if (TB >= 0) c.sb.type = TB;
     const R margin = 0;
     SatStage<R> st;
     st.bind(smem);
@@ -888,12 +867,13 @@ __device__ bool sat_warp(Pair<R>& c, int lane) {
     return true;
 }
 
-// SAT pairs (PC_CONVEX, PC_CONVEX_HEAVY): G = 1 runs kSatWarps pairs per block, one warp each;
-// G = kSatGroup runs one pair per block.  Only thread 0 holds the pair's contact cache.
+// SAT pairs: G = 1 runs kSatWarps pairs per block, one warp each, instantiated per shape pairing
+// (TA, TB; one launch per pairing); G = kSatGroup runs one heavy pair per block, any pairing (-1).
+// Only thread 0 holds the pair's contact cache.
 // per-group stride, a multiple of 4 reals so that every group's vertex rows stay 16-byte aligned
 template <class R> constexpr int sat_group_reals(int G) { return (sat_stage_reals<R>() + sat_scratch_reals<R>(G) + 3) & ~3; }
 static_assert(sat_group_reals<float>(1) % 4 == 0 && (3 * (2 * kSatF + 2 * kSatE)) % 4 == 0, "SAT staging alignment");
-template <class R, int G>
+template <class R, int G, int TA, int TB>
 __global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 4 : 2)
 k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
          const int* pair_scene_off, const int* prev_off) {
@@ -906,7 +886,7 @@ k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, Shape
     Cache<R> cache;
     Pair<R> pr;
     np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr, tid == 0);
-    sat_staged<R, G>(pr, tid, reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G));
+    sat_staged<R, G, TA, TB>(pr, tid, reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G));
     if (tid == 0) np_finish(p, pairs, B, res, cache);
 }
 

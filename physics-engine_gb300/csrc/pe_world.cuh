@@ -241,7 +241,6 @@ private:
     DBuf<int> hist_, aux_, total_, count_, status_;
     DBuf<R> smn_, smx_;
     DBuf<int> sflag_, ssc_, bp_stage_;
-    DBuf<double> axis_part_;
     uint32_t* order_ = nullptr;   // sorted body order (points into val_)
     DBuf<int2> pairs_;
     int P_ = 0, pair_cap_ = 0;

@@ -343,10 +343,7 @@ template <class R> int World<R>::broadphase() {
     launch(K_BP_SWEEP, grid_warps(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
            pairs_.p, pair_cap_, status_.p);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
-    const int tiles = (n + kAxisTile - 1) / kAxisTile;
-    axis_part_.ensure((size_t)tiles * 6);
-    launch(K_BP_AXIS, tiles, k_bp_axis_partial<R>, smn_.p, smx_.p, n, ssc_.p, axis_part_.p);
-    launch(K_BP_AXIS, grid(NS_), k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, axis_part_.p, scene_axis_.p, NS_);
+    launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
     PE_CK(cudaGetLastError());
     P_ = P;
     return P;
@@ -373,9 +370,12 @@ template <class R> void World<R>::narrowphase() {
         const Bodies<R> bd = bodies();
         const ShapeTable<R> sh = shapes();
         if (!sat_attr_) {   // dynamic shared memory of the staged SAT kernels (above the 48 KB default for FP64)
-            PE_CK(cudaFuncSetAttribute(k_np_sat<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(kSatWarps * sat_group_reals<R>(1) * sizeof(R))));
-            PE_CK(cudaFuncSetAttribute(k_np_sat<R, kSatGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            const int light = (int)(kSatWarps * sat_group_reals<R>(1) * sizeof(R));
+            PE_CK(cudaFuncSetAttribute(k_np_sat<R, 1, ST_BOX, ST_HULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, light));
+            PE_CK(cudaFuncSetAttribute(k_np_sat<R, 1, ST_HULL, ST_BOX>, cudaFuncAttributeMaxDynamicSharedMemorySize, light));
+            PE_CK(cudaFuncSetAttribute(k_np_sat<R, 1, ST_HULL, ST_HULL>, cudaFuncAttributeMaxDynamicSharedMemorySize, light));
+            PE_CK(cudaFuncSetAttribute(k_np_sat<R, 1, ST_CYLINDER, ST_CYLINDER>, cudaFuncAttributeMaxDynamicSharedMemorySize, light));
+            PE_CK(cudaFuncSetAttribute(k_np_sat<R, kSatGroup, -1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)(sat_group_reals<R>(kSatGroup) * sizeof(R))));
             sat_attr_ = true;
         }
@@ -392,16 +392,22 @@ template <class R> void World<R>::narrowphase() {
                 case PC_SPHERE_HULL: launch(K_NP, g, k_np_class<R, PC_SPHERE_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_CYL_HULL: launch(K_NP, g, k_np_class<R, PC_CYL_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_CONVEX:
+                case PC_CONVEX_HULL_BOX:
                 case PC_CONVEX_HULL_HULL:
                 case PC_CONVEX_CYL_CYL: {
                     const size_t smem = (size_t)kSatWarps * sat_group_reals<R>(1) * sizeof(R);
-                    launch_smem(K_NP_SAT, (hi - lo + kSatWarps - 1) / kSatWarps, 32 * kSatWarps, smem, k_np_sat<R, 1>, lo, hi,
-                                order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
+                    const int gb = (hi - lo + kSatWarps - 1) / kSatWarps, bs = 32 * kSatWarps;
+                    auto kern = c == PC_CONVEX ? k_np_sat<R, 1, ST_BOX, ST_HULL>
+                              : c == PC_CONVEX_HULL_BOX ? k_np_sat<R, 1, ST_HULL, ST_BOX>
+                              : c == PC_CONVEX_HULL_HULL ? k_np_sat<R, 1, ST_HULL, ST_HULL>
+                              : k_np_sat<R, 1, ST_CYLINDER, ST_CYLINDER>;
+                    launch_smem(K_NP_SAT, gb, bs, smem, kern, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                                prev_res_off_.p);
                     break;
                 }
                 case PC_CONVEX_HEAVY: {
                     const size_t smem = (size_t)sat_group_reals<R>(kSatGroup) * sizeof(R);
-                    launch_smem(K_NP_SAT, hi - lo, 32 * kSatGroup, smem, k_np_sat<R, kSatGroup>, lo, hi, order_np_.p, pairs_.p, bd,
+                    launch_smem(K_NP_SAT, hi - lo, 32 * kSatGroup, smem, k_np_sat<R, kSatGroup, -1, -1>, lo, hi, order_np_.p, pairs_.p, bd,
                                 sh, rs, pair_scene_off_.p, prev_res_off_.p);
                     break;
                 }
