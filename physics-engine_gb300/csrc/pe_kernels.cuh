@@ -247,13 +247,17 @@ template <class R> __device__ __forceinline__ int sat_class(const ShapeView<R>& 
 template <class R>
 __global__ void k_np_classify(int P, const int2* pairs, Bodies<R> B, ShapeTable<R> S, int* cls, int* cls_count) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    const int2 q = pairs[p];
-    const ShapeView<R> sa = S.view(B.shape[q.x]), sb = S.view(B.shape[q.y]);
-    int c = pair_class(sa.type, sb.type);
-    if (c == PC_CONVEX) c = sat_class(sa, sb);
-    cls[p] = c;
-    atomicAdd(&cls_count[c], 1);
+    int c = -1 - (int)(threadIdx.x & 31);   // lanes past the end never match a class
+    if (p < P) {
+        const int2 q = pairs[p];
+        const ShapeView<R> sa = S.view(B.shape[q.x]), sb = S.view(B.shape[q.y]);
+        c = pair_class(sa.type, sb.type);
+        if (c == PC_CONVEX) c = sat_class(sa, sb);
+        cls[p] = c;
+    }
+    // one atomic per class present in the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cls_count[c], __popc(peers));
 }
 __global__ void k_np_bucket(int P, const int* cls, int* cursor, int* order);
 
@@ -1045,11 +1049,11 @@ __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* 
 // islands up to `max_len` results in coloured mode)
 template <class R>
 __global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Bodies<R> B, Rows<R> rows,
-                             const int* row_off, int iterations, int max_len) {
+                             const int* row_off, int iterations, int min_len, int max_len) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= *n_isl) return;
     const int lo = isl_off[s], hi = isl_off[s + 1];
-    if (hi - lo > max_len) return;
+    if (hi - lo < min_len || hi - lo > max_len) return;
     for (int it = 0; it < iterations; it++)
         for (int k = lo; k < hi; k++) {
             const int p = (int)order[k];
@@ -1057,12 +1061,15 @@ __global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_
         }
 }
 
+constexpr int kSmallResults = 8;   // islands up to this size run in the reference order, one thread each
+
 // coloured Gauss-Seidel of one island per block: greedy colouring in rounds (a result takes
 // colour c when it holds the smallest position among the uncoloured results on each of its
 // dynamic bodies), then every iteration runs the colours in turn, all results of a colour in
 // parallel.  Results still uncoloured after kMaxColors - 1 rounds form a last colour that one
 // thread runs in order.
 constexpr int kMaxColors = 64;
+constexpr int kColorBlock = 64;   // threads per island block: islands run tens of results per colour
 template <class R>
 __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Bodies<R> B, Rows<R> rows,
                               const int* row_off, int iterations, int min_len, int* claim, int* color, uint32_t* corder,

@@ -124,11 +124,18 @@ __global__ void k_radix_scatter(const uint64_t* key_in, const uint32_t* key2_in,
 }
 
 // ---------------------------------------------------------------- narrowphase bucketing
+// pairs grouped by class (order inside a class is free: every pair's result has its own slot);
+// one atomic per class present in a warp
 __global__ void k_np_bucket(int P, const int* cls, int* cursor, int* order) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    const int slot = atomicAdd(&cursor[cls[p]], 1);
-    order[slot] = p;
+    const int lane = threadIdx.x & 31;
+    const int c = p < P ? cls[p] : -1 - lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (c >= 0 && lane == leader) base = atomicAdd(&cursor[c], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (c >= 0) order[base + __popc(peers & ((1u << lane) - 1u))] = p;
 }
 
 } // namespace pe

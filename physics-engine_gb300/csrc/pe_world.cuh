@@ -256,7 +256,6 @@ private:
     DBuf<uint32_t> isl_corder_;
     DBuf<R> rows_;
     int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0, n_islands_ = 0;
-    int small_island_ = 8;    // islands with at most this many results run serially in one thread
     bool sat_attr_ = false;
 };
 

@@ -466,17 +466,15 @@ template <class R> void World<R>::solve(int mode) {
             n_islands_ = scan(isl_flag_.p, A + 1);
             launch(K_ISLAND, grid(A + 1), k_isl_offsets, A, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
             const int NI = n_islands_;
-            if (mode == 0) {
-                launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
-                       prm_.iterations, 0x7fffffff);
-            } else {
+            // islands of up to kSmallResults results (all of them in serial-order mode): one thread each
+            launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
+                   prm_.iterations, 0, mode == 0 ? 0x7fffffff : kSmallResults);
+            if (mode != 0) {
                 isl_corder_.ensure(A);
                 ncol_.ensure(1);
                 PE_CK(cudaMemsetAsync(ncol_.p, 0, sizeof(int), st_));
-                launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
-                       prm_.iterations, small_island_);
-                launch_block(K_SI_COLOR, NI, 256, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
-                             prm_.iterations, small_island_, claim_.p, color_.p, isl_corder_.p, ncol_.p);
+                launch_block(K_SI_COLOR, NI, kColorBlock, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(),
+                             row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p, ncol_.p);
                 PE_CK(cudaMemcpyAsync(&n_colors_, ncol_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
             }
         }
