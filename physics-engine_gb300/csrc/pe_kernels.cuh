@@ -576,9 +576,19 @@ template <class R> constexpr int sat_scratch_reals(int G) { return G == 1 ? 0 : 
 // Staged SAT of one pair by a group of G warps (tid in [0, 32 G)).  Each thread takes axes
 // f and f + 32 G of every 64 G-axis chunk, so a thread's axes ascend; the group stops at the
 // first chunk holding a separating axis.
+// What the staged SAT leaves for the contact step (one record of kSatOut reals per pair, written by
+// thread 0): the face-stage point, the edge-stage point, the final axis and the clipping faces,
+// in the order the reference adds them (convex_convex_collision_algorithm.cpp:300-308, :363-395,
+// :420-430).  flags: 1 face point, 2 edge point, 4 clip.
+enum SatOutField { SO_FLAGS = 0, SO_FN = 1, SO_FP = 4, SO_FD = 7, SO_EN = 8, SO_EP = 11, SO_ED = 14, SO_SEP = 15, SO_FB = 18,
+                   SO_FA = 19, kSatOut = 20 };
+template <class R> __device__ __forceinline__ void so_put3(R* o, int k, const V3<R>& v) { o[k] = v.x; o[k + 1] = v.y; o[k + 2] = v.z; }
+template <class R> __device__ __forceinline__ V3<R> so_get3(const R* o, int k) { return V3<R>(o[k], o[k + 1], o[k + 2]); }
+
 template <class R, int G, int TA, int TB>
-__device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
+__device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
     constexpr int T = 32 * G;
+    if (tid == 0) out[SO_FLAGS] = R(0);
     if (TA >= 0) c.sa.type = TA;   // shape types known at compile time: the other branches fold away
     if (TB >= 0) c.sb.type = TB;
     const R margin = 0;
@@ -616,7 +626,7 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
         pair_intervals2(c, n, ok, best, st.vA, st.vB, min0, max0, min1, max1, a0, a1, b0, b1);
         bool sep = false;
         for (int k = 0; k < 2; k++) sep |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
-        if (group_any<G>(sep)) return false;
+        if (group_any<G>(sep)) return;
         for (int k = 0; k < 2; k++) {
             if (!ok[k]) continue;
             const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
@@ -645,8 +655,12 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
         sep = group_bcast3<R, G>(sep, mine, bc);
         dpt = group_bcast3<R, G>(dpt, mine, bc);
         if (tid == 0 &&
-            ((on_a && shape_inside(c.sb, c.tb().inv_apply(dpt))) || (!on_a && shape_inside(c.sa, c.ta().inv_apply(dpt)))))
-            c.add(sep, dpt - sep * margin, -dmin + margin * 2);
+            ((on_a && shape_inside(c.sb, c.tb().inv_apply(dpt))) || (!on_a && shape_inside(c.sa, c.ta().inv_apply(dpt))))) {
+            out[SO_FLAGS] = R(1);
+            so_put3(out, SO_FN, sep);
+            so_put3(out, SO_FP, dpt - sep * margin);
+            out[SO_FD] = -dmin + margin * 2;
+        }
     }
     // ---- edge-pair axes (:323-361).  A box's 12 edges come in 3 classes of 4 whose direction
     // vectors are bit-identical (scaled unit-mesh differences), so they give identical axes,
@@ -684,7 +698,7 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
         pair_intervals2(c, cr, ok, best, st.vA, st.vB, min0, max0, min1, max1, a0, a1, b0, b1);
         bool sp = false;
         for (int k = 0; k < 2; k++) sp |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
-        if (group_any<G>(sp)) return false;
+        if (group_any<G>(sp)) return;
         for (int k = 0; k < 2; k++) {
             if (!ok[k]) continue;
             const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
@@ -740,7 +754,10 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
                 const R nl = rsqrt_(nl2);
                 pts = pts * (R(1.0) / nl);
                 if (dot(pts, dc) < 0) pts = pts * R(-1.0);
-                c.add(pts, wpb + ob - pts * margin, -nl + margin * 2);
+                out[SO_FLAGS] += R(2);
+                so_put3(out, SO_EN, pts);
+                so_put3(out, SO_EP, wpb + ob - pts * margin);
+                out[SO_ED] = -nl + margin * 2;
             }
         }
     }
@@ -760,8 +777,12 @@ __device__ bool sat_staged(Pair<R>& c, int tid, R* smem) {
         if (d < dmn) { dmn = d; fabest = f; }
     }
     group_argmin<R, G>(dmn, fabest, tid, rd, ri);
-    if (tid == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) clip_faces(c, sep, -c.ref_scale, R(0), fbest, fabest);
-    return true;
+    if (tid == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) {
+        out[SO_FLAGS] += R(4);
+        so_put3(out, SO_SEP, sep);
+        out[SO_FB] = R(fbest);
+        out[SO_FA] = R(fabest);
+    }
 }
 
 template <class R>
@@ -879,19 +900,41 @@ template <class R> constexpr int sat_group_reals(int G) { return (sat_stage_real
 static_assert(sat_group_reals<float>(1) % 4 == 0 && (3 * (2 * kSatF + 2 * kSatE)) % 4 == 0, "SAT staging alignment");
 template <class R, int G, int TA, int TB>
 __global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 4 : 2)
-k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
-         const int* pair_scene_off, const int* prev_off) {
+k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, R* sat_out) {
     extern __shared__ __align__(16) unsigned char sat_smem[];
     const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
     const int tid = G == 1 ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
     const int t = lo + blockIdx.x * (G == 1 ? kSatWarps : 1) + grp;
     if (t >= hi) return;   // whole groups leave together
+    const int2 q = pairs[order[t]];
+    Pair<R> pr;
+    pr.xa = B.xf(q.x);
+    pr.xb = B.xf(q.y);
+    pr.sa = S.view(B.shape[q.x]);
+    pr.sb = S.view(B.shape[q.y]);
+    pr.c = nullptr;
+    sat_staged<R, G, TA, TB>(pr, tid, reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G),
+                             sat_out + (size_t)t * kSatOut);
+}
+
+// contact step of the staged SAT pairs, one thread per pair: the pooled result is set up, the
+// recorded face-stage and edge-stage points are added and the faces clipped, in the reference's
+// order, and the result is sorted and written out
+template <class R>
+__global__ void k_np_sat_finish(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                                const int* pair_scene_off, const int* prev_off, const R* sat_out) {
+    const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= hi) return;
     const int p = order[t];
     Cache<R> cache;
     Pair<R> pr;
-    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr, tid == 0);
-    sat_staged<R, G, TA, TB>(pr, tid, reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G));
-    if (tid == 0) np_finish(p, pairs, B, res, cache);
+    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
+    const R* o = sat_out + (size_t)t * kSatOut;
+    const int fl = (int)o[SO_FLAGS];
+    if (fl & 1) pr.add(so_get3(o, SO_FN), so_get3(o, SO_FP), o[SO_FD]);
+    if (fl & 2) pr.add(so_get3(o, SO_EN), so_get3(o, SO_EP), o[SO_ED]);
+    if (fl & 4) clip_faces(pr, so_get3(o, SO_SEP), -pr.ref_scale, R(0), (int)o[SO_FB], (int)o[SO_FA]);
+    np_finish(p, pairs, B, res, cache);
 }
 
 // SAT pairs with a shape beyond the staging limits (PC_CONVEX_BIG): one warp each, unstaged

@@ -247,7 +247,7 @@ private:
     // narrowphase
     DBuf<int> cls_, cls_count_, order_np_;
     DBuf<int> res_a_, res_b_, res_np_;
-    DBuf<R> res_fr_, res_re_, res_pts_, res_dist_[2];
+    DBuf<R> res_fr_, res_re_, res_pts_, res_dist_[2], sat_out_;
     int cur_dist_ = 0;
     int R_ = 0;
     std::vector<int> h_pair_scene_off_;

@@ -313,6 +313,7 @@ template <class R> void World<R>::ensure_pair_capacity(int P) {
     res_dist_[0].ensure((size_t)cap * kSlots, true);
     res_dist_[1].ensure((size_t)cap * kSlots, true);
     row_off_.ensure(cap + 1); active_.ensure(cap + 1); color_.ensure(cap + 1);
+    sat_out_.ensure((size_t)cap * kSatOut);
     // point buffer: field-major over the capacity; its contents live for one step only
     pair_cap_ = cap;
 }
@@ -401,14 +402,17 @@ template <class R> void World<R>::narrowphase() {
                               : c == PC_CONVEX_HULL_BOX ? k_np_sat<R, 1, ST_HULL, ST_BOX>
                               : c == PC_CONVEX_HULL_HULL ? k_np_sat<R, 1, ST_HULL, ST_HULL>
                               : k_np_sat<R, 1, ST_CYLINDER, ST_CYLINDER>;
-                    launch_smem(K_NP_SAT, gb, bs, smem, kern, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
-                                prev_res_off_.p);
+                    launch_smem(K_NP_SAT, gb, bs, smem, kern, lo, hi, order_np_.p, pairs_.p, bd, sh, sat_out_.p);
+                    launch(K_NP_SAT, grid(hi - lo), k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                           prev_res_off_.p, (const R*)sat_out_.p);
                     break;
                 }
                 case PC_CONVEX_HEAVY: {
                     const size_t smem = (size_t)sat_group_reals<R>(kSatGroup) * sizeof(R);
                     launch_smem(K_NP_SAT, hi - lo, 32 * kSatGroup, smem, k_np_sat<R, kSatGroup, -1, -1>, lo, hi, order_np_.p, pairs_.p, bd,
-                                sh, rs, pair_scene_off_.p, prev_res_off_.p);
+                                sh, sat_out_.p);
+                    launch(K_NP_SAT, grid(hi - lo), k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                           prev_res_off_.p, (const R*)sat_out_.p);
                     break;
                 }
                 default:   // PC_CONVEX_BIG
