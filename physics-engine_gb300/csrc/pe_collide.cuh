@@ -434,8 +434,9 @@ template <class R> __device__ void add_on_box(Pair<R>& c, const V3<R>& pc, int f
     c.add(nw, pw - nw * margin, pen + 2 * margin);
 }
 
-template <class R> __device__ void add_on_cylinder(Pair<R>& c, const V3<R>& p, const V3<R>& pos, const V3<R>& axis, R radius, R h,
-                                                   const Xf<R>& t, R margin) {   // :116-139
+// the contact point addContactPointOnCylinder (:116-139) adds for a point p near the cylinder
+template <class R> __device__ void cyl_contact(const V3<R>& p, const V3<R>& pos, const V3<R>& axis, R radius, R h, const Xf<R>& t,
+                                               R margin, V3<R>& wn, V3<R>& wp, R& wd) {
     const V3<R> r = p - pos;
     const R dy = dot(r, axis);
     const R dxz = rsqrt_(sqnorm(r) - dy * dy);
@@ -446,7 +447,16 @@ template <class R> __device__ void add_on_cylinder(Pair<R>& c, const V3<R>& p, c
     else { dist = dtop; n = dy < 0 ? axis : -axis; }
     n = mv(t.b, n);
     const V3<R> pw = t.apply(p);
-    c.add(n, pw - n * margin, -dist + 2 * margin);
+    wn = n;
+    wp = pw - n * margin;
+    wd = -dist + 2 * margin;
+}
+template <class R> __device__ void add_on_cylinder(Pair<R>& c, const V3<R>& p, const V3<R>& pos, const V3<R>& axis, R radius, R h,
+                                                   const Xf<R>& t, R margin) {   // :116-139
+    V3<R> n, pw;
+    R d;
+    cyl_contact(p, pos, axis, radius, h, t, margin, n, pw, d);
+    c.add(n, pw, d);
 }
 
 template <class R> __device__ bool line_plane(const V3<R>& s, const V3<R>& d, const V3<R>& pp, const V3<R>& pn, R tol, R& t) {

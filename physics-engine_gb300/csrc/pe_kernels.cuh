@@ -937,6 +937,155 @@ __global__ void k_np_sat_finish(int lo, int hi, const int* order, const int2* pa
     np_finish(p, pairs, B, res, cache);
 }
 
+// CylinderConvexCollisionAlgorithm (cylinder_convex_collision_algorithm.cpp:109-203), one warp
+// per pair: in rounds of 32 faces (in the reference's descending face order, lane i taking the
+// i-th face of the round), each lane computes the contact points its face contributes, and lane 0
+// then adds them to the pair's cache in face order and, inside a face, in the reference's segment
+// order: the cache's merging depends on that order, the candidate points do not.
+constexpr int kCylHullCand = 12;   // points a face can give: 6 cylinder segments x 2 ends
+template <class R> constexpr int cyl_hull_warps() { return sizeof(R) == 4 ? 4 : 2; }
+template <class R>
+__global__ void __launch_bounds__(32 * cyl_hull_warps<R>())
+k_np_cyl_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+              const int* pair_scene_off, const int* prev_off) {
+    constexpr int W = cyl_hull_warps<R>(), K = kCylHullCand;
+    __shared__ R cand[W][32 * K][7];
+    __shared__ int ccnt[W][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = lo + blockIdx.x * W + warp;
+    if (t >= hi) return;   // whole warps
+    const int p = order[t];
+    Cache<R> cache;
+    Pair<R> c;
+    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, c, lane == 0);
+    const bool a_hull = c.sa.type == ST_HULL;
+    const ShapeView<R>& m = a_hull ? c.sa : c.sb;
+    const ShapeView<R>& cy = a_hull ? c.sb : c.sa;
+    const Xf<R>& to = a_hull ? c.ta() : c.tb();
+    const Xf<R>& tc = a_hull ? c.tb() : c.ta();
+    const R margin = 0;
+    if (lane == 0) cache.swap = a_hull;
+    const R cr = cy.radius, ch = cy.height / R(2.0);
+    const Xf<R> rel = to.inverse() * tc;
+    const V3<R> axis = rel.b.col(1), pos = rel.o;
+    V3<R> aa, bb;
+    shape_aabb(cy, rel, aa, bb);
+    const int dxs[4] = {1, -1, -1, 1}, dys[4] = {1, 1, -1, -1};
+    auto push = [&](int& k, const V3<R>& n, const V3<R>& pt, R d) {
+        R* e = cand[warp][lane * K + k];
+        e[0] = n.x; e[1] = n.y; e[2] = n.z; e[3] = pt.x; e[4] = pt.y; e[5] = pt.z; e[6] = d;
+        k++;
+    };
+    auto drain = [&]() {   // lane 0 adds the round's points in face order
+        __syncwarp();
+        if (lane == 0)
+            for (int l = 0; l < 32; l++)
+                for (int k = 0; k < ccnt[warp][l]; k++) {
+                    const R* e = cand[warp][l * K + k];
+                    c.add(V3<R>(e[0], e[1], e[2]), V3<R>(e[3], e[4], e[5]), e[6]);
+                }
+        __syncwarp();
+    };
+    // cylinder side segments against the faces the cylinder's box reaches
+    for (int base = 0; base < m.nf; base += 32) {
+        const int f = m.nf - 1 - base - lane;
+        int k = 0;
+        if (f >= 0 && face_hit(m, f, aa, bb)) {
+            const V3<R> fn = m.face_normal(f);
+            const R adc = dot(axis, fn);
+            V3<R> ddx, ddz;
+            const V3<R> ddy = axis;
+            bool vertical = false;
+            if (rabs(rabs(adc) - 1) < eps<R>()) {
+                ddz = normalized(cross(axis, V3<R>(1, 0, 0)));
+                ddx = normalized(cross(axis, ddz));
+                vertical = true;
+            } else {
+                ddx = normalized(cross(cross(fn, axis), axis));
+            }
+            auto seg = [&](const V3<R>& ps, const V3<R>& ds, R ls) {
+                R t1, t2, d1, d2;
+                if (segment_face(m, f, ps, ds, ls, margin, t1, t2, d1, d2)) {
+                    const V3<R> p1 = to.apply(ps + ds * t1 - fn * d1);
+                    const V3<R> p2 = to.apply(ps + ds * t2 - fn * d2);
+                    const V3<R> n = mv(to.b, fn);
+                    push(k, n, p1 - n * margin, d1 + margin * 2);
+                    push(k, n, p2 - n * margin, d2 + margin * 2);
+                }
+            };
+            for (int i = 0; i < 4; i++) {
+                const V3<R> ps = pos + ddx * R(dxs[i]) * cr + ddy * R(dys[i]) * ch;
+                const V3<R> ds = (dxs[i] == dys[i] ? ddy : ddx) * R(-dxs[i]);
+                const R ls = (dxs[i] == dys[i] ? ch : cr) * 2;
+                seg(ps, ds, ls);
+            }
+            if (vertical)
+                for (int i = 0; i < 3; i += 2) {
+                    const V3<R> ps = pos + ddz * R(dxs[i]) * cr + ddy * R(dys[i]) * ch;
+                    seg(ps, ddy * R(-dxs[i]), ch * 2);
+                }
+        }
+        ccnt[warp][lane] = k;
+        drain();
+    }
+    // hull edges of those faces against the cylinder (a face with more than K edges is left to
+    // lane 0, in its turn)
+    for (int base = 0; base < m.nf; base += 32) {
+        const int f = m.nf - 1 - base - lane;
+        int k = 0;
+        if (f >= 0 && face_hit(m, f, aa, bb)) {
+            const int n = m.face_size(f);
+            if (n > K) k = -1;
+            else
+                for (int i = 0; i < n; i++) {
+                    const V3<R> v1 = m.vert(m.face_vert(f, i));
+                    const V3<R> v2 = m.vert(m.face_vert(f, (i + 1) % n));
+                    R t1, t2;
+                    const V3<R> start = (v1 + v2) / R(2);
+                    const R ls = norm(v2 - v1) / 2;
+                    const V3<R> dir = (v2 - v1) / (ls * 2);
+                    if (segment_cylinder(start, dir, ls, pos, axis, ch, cr, margin, t1, t2)) {
+                        const V3<R> p1 = start + dir * t1, p2 = start + dir * t2;
+                        V3<R> wn, wp;
+                        R wd;
+                        cyl_contact((p1 + p2) / R(2), pos, axis, cr, ch, to, margin, wn, wp, wd);
+                        push(k, wn, wp, wd);
+                    }
+                }
+        }
+        ccnt[warp][lane] = k;
+        __syncwarp();
+        if (lane == 0)
+            for (int l = 0; l < 32; l++) {
+                if (ccnt[warp][l] >= 0) {
+                    for (int q = 0; q < ccnt[warp][l]; q++) {
+                        const R* e = cand[warp][l * K + q];
+                        c.add(V3<R>(e[0], e[1], e[2]), V3<R>(e[3], e[4], e[5]), e[6]);
+                    }
+                    continue;
+                }
+                const int g = m.nf - 1 - base - l, n = m.face_size(g);
+                for (int i = 0; i < n; i++) {
+                    const V3<R> v1 = m.vert(m.face_vert(g, i));
+                    const V3<R> v2 = m.vert(m.face_vert(g, (i + 1) % n));
+                    R t1, t2;
+                    const V3<R> start = (v1 + v2) / R(2);
+                    const R ls = norm(v2 - v1) / 2;
+                    const V3<R> dir = (v2 - v1) / (ls * 2);
+                    if (segment_cylinder(start, dir, ls, pos, axis, ch, cr, margin, t1, t2)) {
+                        const V3<R> p1 = start + dir * t1, p2 = start + dir * t2;
+                        add_on_cylinder(c, (p1 + p2) / R(2), pos, axis, cr, ch, to, margin);
+                    }
+                }
+            }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        cache.swap = false;
+        np_finish(p, pairs, B, res, cache);
+    }
+}
+
 // SAT pairs with a shape beyond the staging limits (PC_CONVEX_BIG): one warp each, unstaged
 template <class R>
 __global__ void k_np_sat_big(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,

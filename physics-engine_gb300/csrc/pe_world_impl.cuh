@@ -391,7 +391,12 @@ template <class R> void World<R>::narrowphase() {
                 case PC_SPHERE_CYL: launch(K_NP, g, k_np_class<R, PC_SPHERE_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_BOX_CYL: launch(K_NP, g, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_SPHERE_HULL: launch(K_NP, g, k_np_class<R, PC_SPHERE_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_CYL_HULL: launch(K_NP, g, k_np_class<R, PC_CYL_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_CYL_HULL: {
+                    const int w = cyl_hull_warps<R>();
+                    launch_block(K_NP, (hi - lo + w - 1) / w, 32 * w, k_np_cyl_hull<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,
+                                 pair_scene_off_.p, prev_res_off_.p);
+                    break;
+                }
                 case PC_CONVEX:
                 case PC_CONVEX_HULL_BOX:
                 case PC_CONVEX_HULL_HULL:
