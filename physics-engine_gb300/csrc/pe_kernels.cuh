@@ -1262,6 +1262,7 @@ constexpr int kSmallResults = 8;   // islands up to this size run in the referen
 // thread runs in order.
 constexpr int kMaxColors = 64;
 constexpr int kColorBlock = 64;   // threads per island block: islands run tens of results per colour
+constexpr int kBigIsland = 4096;  // larger islands are coloured and solved by the whole grid (k_gc_*)
 template <class R>
 __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Bodies<R> B, Rows<R> rows,
                               const int* row_off, int iterations, int min_len, int* claim, int* color, uint32_t* corder,
@@ -1269,7 +1270,7 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
     const int s = blockIdx.x;
     if (s >= *n_isl) return;
     const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
-    if (m <= min_len) return;
+    if (m <= min_len || m > kBigIsland) return;
     __shared__ int cnt[kMaxColors + 1];
     __shared__ int remaining;
     __shared__ int ncol;
@@ -1342,6 +1343,68 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
                 si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
             }
         __syncthreads();
+    }
+}
+
+// ---- islands above kBigIsland results: k_isl_colored's colouring rule in grid-wide kernels (round
+// c gives colour c to every uncoloured result that holds the smallest island position among the
+// uncoloured results on each of its dynamic bodies, so the colour classes follow the island order,
+// i.e. the reference's solve order, as closely as colouring allows), with up to kMaxColorsBig
+// colours, then one launch per colour and iteration.  Results of a colour touch disjoint dynamic
+// bodies, so their order inside the colour does not matter; results left after kMaxColorsBig - 1
+// rounds run in island order in one thread.
+constexpr int kMaxColorsBig = 1024;
+__global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big);
+template <class R>
+__global__ void k_gc_reset(int lo, int m, const uint32_t* order, Results<R> res, const int* color, int* claim) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m || color[lo + j] >= 0) return;
+    const int p = (int)order[lo + j];
+    claim[res.a[p]] = 0x7fffffff;
+    claim[res.b[p]] = 0x7fffffff;
+}
+template <class R>
+__global__ void k_gc_claim(int lo, int m, const uint32_t* order, Results<R> res, Bodies<R> B, const int* color, int* claim) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m || color[lo + j] >= 0) return;
+    const int p = (int)order[lo + j];
+    const int ia = res.a[p], ib = res.b[p];
+    if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
+    if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
+}
+// winners take colour c; *remaining += results still uncoloured after this round
+template <class R>
+__global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res, Bodies<R> B, const int* claim, int* color, int c,
+                            int* remaining) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    bool left = false;
+    if (j < m && color[lo + j] < 0) {
+        const int p = (int)order[lo + j];
+        const int ia = res.a[p], ib = res.b[p];
+        const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
+        if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) color[lo + j] = c;
+        else left = true;
+    }
+    const int n = __syncthreads_count(left);
+    if (threadIdx.x == 0 && n) atomicAdd(remaining, n);
+}
+// colour histogram (leftovers -> the last colour) and placement of every colour but the last
+__global__ void k_gc_count(int lo, int m, int* color, int* cnt);
+__global__ void k_gc_place(int lo, int m, const int* color, const uint32_t* order, int* cursor, uint32_t* corder);
+template <class R>
+__global__ void k_gc_pass(const uint32_t* list, int n, Results<R> res, Bodies<R> B, Rows<R> rows, const int* row_off) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int p = (int)list[j];
+    si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
+}
+template <class R>
+__global__ void k_gc_last(int lo, int m, const uint32_t* order, const int* color, Results<R> res, Bodies<R> B, Rows<R> rows,
+                          const int* row_off) {
+    for (int j = 0; j < m; j++) {
+        if (color[lo + j] != kMaxColorsBig - 1) continue;
+        const int p = (int)order[lo + j];
+        si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
     }
 }
 

@@ -177,4 +177,42 @@ __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* 
     if (k == A) { isl_off[scan[A]] = A; *n_isl_out = scan[A]; }
 }
 
+// islands with more than kBigIsland results
+__global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *n_isl) return;
+    if (isl_off[s + 1] - isl_off[s] > kBigIsland) big[atomicAdd(n_big, 1)] = s;
+}
+
+// colour histogram of an island (cnt[c + 1] counts colour c); uncoloured results join the last colour
+__global__ void k_gc_count(int lo, int m, int* color, int* cnt) {
+    __shared__ int h[kMaxColorsBig];
+    for (int k = threadIdx.x; k < kMaxColorsBig; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) {
+        int c = color[lo + j];
+        if (c < 0) { c = kMaxColorsBig - 1; color[lo + j] = c; }
+        atomicAdd(&h[c], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kMaxColorsBig; k += blockDim.x)
+        if (h[k]) atomicAdd(&cnt[k + 1], h[k]);
+}
+
+// results of every colour but the last, grouped by colour (any order inside a colour)
+__global__ void k_gc_place(int lo, int m, const int* color, const uint32_t* order, int* cursor, uint32_t* corder) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int c = j < m ? color[lo + j] : -1 - lane;
+    const bool live = c >= 0 && c < kMaxColorsBig - 1;
+    const int key = live ? c : -1 - lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (live && lane == leader) base = atomicAdd(&cursor[c], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (live) corder[base + __popc(peers & ((1u << lane) - 1u))] = order[lo + j];
+}
+
 } // namespace pe

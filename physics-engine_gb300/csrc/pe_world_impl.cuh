@@ -485,11 +485,76 @@ template <class R> void World<R>::solve(int mode) {
                 launch_block(K_SI_COLOR, NI, kColorBlock, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(),
                              row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p, ncol_.p);
                 PE_CK(cudaMemcpyAsync(&n_colors_, ncol_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+                solve_big_islands(NI, order);
             }
         }
     }
     launch(K_SI_MISC, grid(N_), k_si_sync<R>, bodies());
     PE_CK(cudaGetLastError());
+}
+
+// islands above kBigIsland results (coloured mode): grid-wide colouring rounds, then one launch per
+// colour and iteration (see k_gc_*)
+template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* order) {
+    gc_big_.ensure(NI + 1);
+    gc_n_.ensure(2);
+    PE_CK(cudaMemsetAsync(gc_n_.p, 0, sizeof(int), st_));
+    launch(K_SI_COLOR, grid(NI), k_isl_big, (const int*)isl_n_.p, (const int*)isl_off_.p, gc_big_.p, gc_n_.p);
+    int nb = 0;
+    PE_CK(cudaMemcpyAsync(&nb, gc_n_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+    if (nb == 0) return;
+    std::vector<int> big(nb);
+    PE_CK(cudaMemcpy(big.data(), gc_big_.p, nb * sizeof(int), cudaMemcpyDeviceToHost));
+    std::sort(big.begin(), big.end());
+    gc_cnt_.ensure(kMaxColorsBig + 1);
+    gc_cursor_.ensure(kMaxColorsBig);
+    const Results<R> rs = results();
+    const Bodies<R> bd = bodies();
+    const Rows<R> rw = rows();
+    std::vector<int> cnt(kMaxColorsBig + 1), start(kMaxColorsBig), cur(kMaxColorsBig);
+    for (int s : big) {
+        int lh[2];
+        PE_CK(cudaMemcpy(lh, isl_off_.p + s, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+        const int lo = lh[0], m = lh[1] - lh[0], g = grid(m);
+        PE_CK(cudaMemsetAsync(color_.p + lo, 0xff, (size_t)m * sizeof(int), st_));   // -1: uncoloured
+        // colouring rounds, the remaining count read back every 8 rounds (extra rounds find nothing to do)
+        int ncol = 0;
+        for (int c0 = 0; c0 < kMaxColorsBig - 1; c0 += 8) {
+            int c = c0;
+            for (; c < c0 + 8 && c < kMaxColorsBig - 1; c++) {
+                launch(K_SI_COLOR, g, k_gc_reset<R>, lo, m, order, rs, (const int*)color_.p, claim_.p);
+                launch(K_SI_COLOR, g, k_gc_claim<R>, lo, m, order, rs, bd, (const int*)color_.p, claim_.p);
+                PE_CK(cudaMemsetAsync(gc_n_.p + 1, 0, sizeof(int), st_));
+                launch(K_SI_COLOR, g, k_gc_assign<R>, lo, m, order, rs, bd, (const int*)claim_.p, color_.p, c, gc_n_.p + 1);
+            }
+            int rem = 0;
+            PE_CK(cudaMemcpyAsync(&rem, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
+            PE_CK(cudaStreamSynchronize(st_));
+            ncol = c;
+            if (rem == 0) break;
+        }
+        PE_CK(cudaMemsetAsync(gc_cnt_.p, 0, (kMaxColorsBig + 1) * sizeof(int), st_));
+        launch(K_SI_COLOR, g, k_gc_count, lo, m, color_.p, gc_cnt_.p);
+        PE_CK(cudaMemcpyAsync(cnt.data(), gc_cnt_.p, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaStreamSynchronize(st_));
+        int run = 0, used = 0;
+        for (int c = 0; c < kMaxColorsBig; c++) {
+            start[c] = run; cur[c] = lo + run; run += cnt[c + 1];
+            if (cnt[c + 1]) used = c + 1;
+        }
+        PE_CK(cudaMemcpyAsync(gc_cursor_.p, cur.data(), cur.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
+        launch(K_SI_COLOR, g, k_gc_place, lo, m, (const int*)color_.p, order, gc_cursor_.p, isl_corder_.p);
+        const bool last = cnt[kMaxColorsBig] > 0;
+        n_colors_ = std::max(n_colors_, std::min(used, ncol) + (last ? 1 : 0));
+        for (int it = 0; it < prm_.iterations; it++) {
+            for (int c = 0; c < used && c < kMaxColorsBig - 1; c++)
+                if (cnt[c + 1])
+                    launch(K_SI_COLOR, grid(cnt[c + 1]), k_gc_pass<R>, (const uint32_t*)isl_corder_.p + lo + start[c], cnt[c + 1], rs,
+                           bd, rw, (const int*)row_off_.p);
+            if (last) launch_block(K_SI_COLOR, 1, 1, k_gc_last<R>, lo, m, order, (const int*)color_.p, rs, bd, rw, (const int*)row_off_.p);
+        }
+    }
 }
 
 template <class R> void World<R>::step(int n, int mode) {
