@@ -156,14 +156,96 @@ __device__ __forceinline__ int sweep_warp(int i, int n, int lane, const int* sce
     return c;
 }
 
+// A position whose window along the axis holds more than kBigWindow candidates (a floor or a wall
+// spanning the scene) is swept by a whole block instead of a warp: 256 candidates per iteration,
+// warp ballots plus a block prefix of the warp counts keep the pairs in ascending j.
+constexpr int kBigWindow = 32768;
+template <class R>
+__device__ __forceinline__ bool big_window(int i, int n, const int* scene_axis, const R* smn, const R* smx, const int* sscene) {
+    const int j = i + kBigWindow;
+    if (j >= n) return false;
+    const int sc = sscene[i], ax = scene_axis[sc];
+    return sscene[j] == sc && !(smn[(size_t)ax * n + j] > smx[(size_t)ax * n + i]);
+}
+template <class R, bool WRITE>
+__device__ int sweep_block(int i, int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                           int2* out, const uint32_t* order, int* wcnt) {
+    const int sc = sscene[i];
+    const int ax = scene_axis[sc];
+    const R* amin = smn + (size_t)ax * n;
+    const R maxi_ax = smx[(size_t)ax * n + i];
+    const R mnx = smn[i], mny = smn[n + i], mnz = smn[2 * (size_t)n + i];
+    const R mxx = smx[i], mxy = smx[n + i], mxz = smx[2 * (size_t)n + i];
+    const int fi = sflag[i];
+    if (fi & BF_IGNORE) return 0;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+    const int a = WRITE ? (int)order[i] : 0;
+    const unsigned lt = (1u << lane) - 1u;
+    int c = 0;
+    for (int j0 = i + 1; j0 < n; j0 += blockDim.x) {
+        const int j = j0 + tid;
+        const bool in = j < n && !(amin[j] > maxi_ax) && sscene[j] == sc;
+        bool hit = false;
+        if (in) {
+            const int fj = sflag[j];
+            hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
+                  !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
+                  !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) wcnt[w] = __popc(m);
+        const int all_in = __syncthreads_and(in);
+        int before = 0, total = 0;
+        for (int k = 0; k < nw; k++) { if (k < w) before += wcnt[k]; total += wcnt[k]; }
+        if (WRITE && hit) out[c + before + __popc(m & lt)] = make_int2(a, (int)order[j]);
+        c += total;
+        __syncthreads();   // wcnt is rewritten next iteration
+        if (!all_in) break;
+    }
+    return c;
+}
+
 template <class R>
 __global__ void k_bp_count(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene, int* count,
-                           int* stage) {
+                           int* stage, int* big, int* n_big) {
     const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
+    if (big_window(i, n, scene_axis, smn, smx, sscene)) {   // left to k_bp_count_big
+        if (lane == 0) big[atomicAdd(n_big, 1)] = i;
+        return;
+    }
     const int c = sweep_warp<R, false>(i, n, lane, scene_axis, smn, smx, sflag, sscene, stage, nullptr, nullptr);
     if (lane == 0) count[i] = c;
+}
+// one block per listed position (blocks loop over the list)
+template <class R>
+__global__ void k_bp_count_big(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                               int* count, const int* big, const int* n_big) {
+    __shared__ int wcnt[32];
+    for (int b = blockIdx.x; b < *n_big; b += gridDim.x) {
+        const int i = big[b];
+        const int c = sweep_block<R, false>(i, n, scene_axis, smn, smx, sflag, sscene, nullptr, nullptr, wcnt);
+        if (threadIdx.x == 0) count[i] = c;
+        __syncthreads();
+    }
+}
+template <class R>
+__global__ void k_bp_write_big(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                               const uint32_t* order, const int* offset, int2* pairs, int pair_cap, int* status, const int* big,
+                               const int* n_big) {
+    __shared__ int wcnt[32];
+    for (int b = blockIdx.x; b < *n_big; b += gridDim.x) {
+        const int i = big[b];
+        const int base = offset[i], c = offset[i + 1] - base;
+        if (c == 0) continue;   // uniform in the block
+        if (base + c > pair_cap) {
+            if (threadIdx.x == 0) atomicOr(status, ST_PAIR_OVERFLOW);
+            continue;
+        }
+        sweep_block<R, true>(i, n, scene_axis, smn, smx, sflag, sscene, pairs + base, order, wcnt);
+        __syncthreads();
+    }
 }
 
 template <class R>
@@ -173,7 +255,7 @@ __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* 
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
     const int base = offset[i], c = offset[i + 1] - base;
-    if (c == 0) return;
+    if (c == 0 || big_window(i, n, scene_axis, smn, smx, sscene)) return;   // big windows: k_bp_write_big
     if (base + c > pair_cap) {
         if (lane == 0) atomicOr(status, ST_PAIR_OVERFLOW);
         return;

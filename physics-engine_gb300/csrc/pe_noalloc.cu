@@ -17,6 +17,7 @@ namespace pe {
 namespace {
 
 constexpr int kSapMaxBodies = 16384;
+constexpr int kSapBigBlocks = 64;   // blocks sharing the positions whose sweep window is crowded
 constexpr size_t kAlign = 256;
 constexpr size_t al(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
 constexpr int kSapTiles = (kSapMaxBodies + kRadixTile - 1) / kRadixTile;
@@ -24,7 +25,7 @@ constexpr int kSapAux = (256 * kSapTiles + 1023) / 1024 + (kSapMaxBodies + 1 + 1
 
 // byte layout of the scratch array
 struct SapLayout {
-    size_t key[2], key2[2], val[2], hist, aux, total, axis, status, smn, smx, sflag, sscene, count, stage, end;
+    size_t key[2], key2[2], val[2], hist, aux, total, axis, status, nbig, smn, smx, sflag, sscene, count, stage, big, end;
 };
 constexpr SapLayout sap_layout() {
     SapLayout L{};
@@ -38,12 +39,14 @@ constexpr SapLayout sap_layout() {
     L.total = o; o += al(4);
     L.axis = o; o += al(4);
     L.status = o; o += al(4);
+    L.nbig = o; o += al(4);
     L.smn = o; o += al(3 * n * 4);
     L.smx = o; o += al(3 * n * 4);
     L.sflag = o; o += al(n * 4);
     L.sscene = o; o += al(n * 4);
     L.count = o; o += al((n + 1) * 4);
     L.stage = o; o += al(n * kStage * 4);
+    L.big = o; o += al(n * 4);
     L.end = o;
     return L;
 }
@@ -64,11 +67,12 @@ __global__ void k_sap_keys(int n, const float* mn, int axis, uint64_t* key, uint
     val[i] = (uint32_t)i;
 }
 
-// sorted copies of the sweep inputs (as k_bp_gather); zeroes the scan's last count and the status
+// sorted copies of the sweep inputs (as k_bp_gather); zeroes the scan's last count, the status and
+// the count of crowded positions
 __global__ void k_sap_gather(int n, const float* mn, const float* mx, const int* flags, const uint32_t* order, float* smn,
-                             float* smx, int* sflag, int* sscene, int* count, int* status) {
+                             float* smx, int* sflag, int* sscene, int* count, int* status, int* n_big) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) { count[n] = 0; *status = 0; }
+    if (k == 0) { count[n] = 0; *status = 0; *n_big = 0; }
     if (k >= n) return;
     const int i = (int)order[k];
     for (int d = 0; d < 3; d++) {
@@ -149,6 +153,8 @@ extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min
     int* sscene = reinterpret_cast<int*>(base + kL.sscene);
     int* count = reinterpret_cast<int*>(base + kL.count);
     int* stage = reinterpret_cast<int*>(base + kL.stage);
+    int* big = reinterpret_cast<int*>(base + kL.big);
+    int* n_big = reinterpret_cast<int*>(base + kL.nbig);
 
     const int g = (n + kBlock - 1) / kBlock;
     k_sap_keys<<<g, kBlock, 0, st>>>(n, aabb_min, axis, key[0], key2[0], val[0], scene_axis);
@@ -166,15 +172,18 @@ extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min
         cur ^= 1;
     }
     const uint32_t* order = val[cur];
-    k_sap_gather<<<g, kBlock, 0, st>>>(n, aabb_min, aabb_max, flags, order, smn, smx, sflag, sscene, count, status);
+    k_sap_gather<<<g, kBlock, 0, st>>>(n, aabb_min, aabb_max, flags, order, smn, smx, sflag, sscene, count, status, n_big);
     const int gw = (int)(((size_t)n * 32 + kBlock - 1) / kBlock);
-    k_bp_count<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, stage);
+    k_bp_count<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, stage, big, n_big);
+    k_bp_count_big<float><<<kSapBigBlocks, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, big, n_big);
     const int ct = (n + 1 + 1023) / 1024;
     k_scan_tiles<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
     k_scan_aux<<<1, kBlock, 0, st>>>(aux, ct, total);
     k_scan_add<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
     k_bp_write<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, order, count, stage, reinterpret_cast<int2*>(pairs),
                                              pair_cap, status);
+    k_bp_write_big<float><<<kSapBigBlocks, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, order, count,
+                                                          reinterpret_cast<int2*>(pairs), pair_cap, status, big, n_big);
     k_sap_total<<<1, 1, 0, st>>>(total, n_pairs);
     if (cudaGetLastError() != cudaSuccess) return done(PE_GPU_ERR_CUDA, "kernel launch");
     return done(PE_GPU_OK, nullptr);

@@ -240,7 +240,8 @@ private:
     DBuf<uint32_t> key2_[2], val_[2];
     DBuf<int> hist_, aux_, total_, count_, status_;
     DBuf<R> smn_, smx_;
-    DBuf<int> sflag_, ssc_, bp_stage_;
+    DBuf<int> sflag_, ssc_, bp_stage_, bp_big_, bp_nbig_;
+    static constexpr int kBigSweepBlocks = 152;   // blocks that share the crowded positions
     uint32_t* order_ = nullptr;   // sorted body order (points into val_)
     DBuf<int2> pairs_;
     int P_ = 0, pair_cap_ = 0;

@@ -337,12 +337,21 @@ template <class R> int World<R>::broadphase() {
     radix_sort(n, scene_passes);
     launch(K_BP_GATHER, grid(n), k_bp_gather<R>, bodies(), order_, smn_.p, smx_.p, sflag_.p, ssc_.p);
     bp_stage_.ensure((size_t)n * kStage);
-    launch(K_BP_SWEEP, grid_warps(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p);
+    bp_big_.ensure(n + 1);
+    bp_nbig_.ensure(1);
+    PE_CK(cudaMemsetAsync(bp_nbig_.p, 0, sizeof(int), st_));
+    launch(K_BP_SWEEP, grid_warps(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p,
+           bp_big_.p, bp_nbig_.p);
+    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_count_big<R>, n, (const int*)scene_axis_.p, (const R*)smn_.p, (const R*)smx_.p,
+           (const int*)sflag_.p, (const int*)ssc_.p, count_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p);
     PE_CK(cudaMemsetAsync(count_.p + n, 0, sizeof(int), st_));
     const int P = scan(count_.p, n + 1);
     ensure_pair_capacity(P);
     launch(K_BP_SWEEP, grid_warps(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
            pairs_.p, pair_cap_, status_.p);
+    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_write_big<R>, n, (const int*)scene_axis_.p, (const R*)smn_.p, (const R*)smx_.p,
+           (const int*)sflag_.p, (const int*)ssc_.p, (const uint32_t*)order_, (const int*)count_.p, pairs_.p, pair_cap_, status_.p,
+           (const int*)bp_big_.p, (const int*)bp_nbig_.p);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
     launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
     PE_CK(cudaGetLastError());
