@@ -208,23 +208,6 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(workload):
-    """DRAM traffic per algorithmic byte of each kernel group, from the committed ncu summary
-    (`<workload> <group> <dram bytes> <algorithmic bytes>` lines, measured on a smaller case of
-    the same workload); scaled by this run's algorithmic bytes."""
-    p = ROOT / "profiles" / "ncu_traffic.txt"
-    out = {}
-    if p.exists():
-        for line in p.read_text().splitlines():
-            f = line.split()
-            if len(f) >= 4 and not line.startswith("#") and f[0] == workload:
-                try:
-                    out[f[1]] = float(f[2]) / float(f[3])
-                except (ValueError, ZeroDivisionError):
-                    pass
-    return out
-
-
 def algorithmic_bytes(counts, n_bodies, iters, real_bytes):
     """Algorithmic HBM bytes of one step (per kernel group), from the per-unit figures:
     body 268 B, pair 104 B (+12 B per hull vertex), manifold 8 B, contact point 184 B plus
@@ -287,8 +270,7 @@ def run_ours(args, rank, world, device):
     dom_bytes = alg[dom]   # bytes of the whole group in one step
     peak, peak_kind = measured_peak()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    ratio = ncu_traffic(args.workload).get(dom)
-    traffic = ratio * dom_bytes if ratio is not None else None
+    traffic = None   # ncu's per-kernel DRAM writes include write-backs of earlier kernels' dirty lines
     # end to end through the C ABI with host buffers
     st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
     g.set_state(st)                      # one untimed pass through the host path (pinned staging buffers)
