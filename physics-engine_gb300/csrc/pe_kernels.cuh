@@ -272,12 +272,13 @@ __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* 
 // (thread t takes positions t, t + blockDim, ... of the scene, then a fixed tree), so a scene gets
 // the same sums wherever it sits in a batch and run to run.  A scene below two bodies keeps its
 // axis, as the reference returns before updating it.
+constexpr int kAxisTile = 4096;   // scenes above this size sum scene-relative tiles in separate blocks
 template <class R>
 __global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, int* scene_axis) {
     const int s = blockIdx.x;
     const int lo = scene_off[s], hi = scene_off[s + 1];
     const int cnt = hi - lo;
-    if (cnt < 2) return;   // whole block
+    if (cnt < 2 || cnt > kAxisTile) return;   // whole block
     __shared__ double red[6][kBlock];
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
@@ -302,6 +303,32 @@ __global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_of
         scene_axis[s] = ax;
     }
 }
+
+// large scenes: block b sums tile item[b].y (positions lo + tile * kAxisTile, ...) of scene
+// item[b].x, in the same fixed order as k_bp_axis; then one thread per large scene adds its tiles
+// in tile order
+template <class R>
+__global__ void k_bp_axis_tiles(const R* smn, const R* smx, int n, const int* scene_off, const int2* item, double* part) {
+    const int s = item[blockIdx.x].x, t = item[blockIdx.x].y;
+    const int lo = scene_off[s] + t * kAxisTile, hi = min(scene_off[s + 1], lo + kAxisTile);
+    __shared__ double red[6][kBlock];
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+        for (int d = 0; d < 3; d++) {
+            const double c = (double)((smn[(size_t)d * n + k] + smx[(size_t)d * n + k]) * R(0.5));
+            acc[d] += c;
+            acc[3 + d] += c * c;
+        }
+    }
+    for (int q = 0; q < 6; q++) red[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) part[(size_t)blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
+}
+__global__ void k_bp_axis_combine(const int* scene_off, const int2* item, int n_item, const double* part, int* scene_axis);
 
 // ===================================================================== narrowphase
 // bucket pairs by algorithm class

@@ -241,6 +241,10 @@ private:
     DBuf<int> hist_, aux_, total_, count_, status_;
     DBuf<R> smn_, smx_;
     DBuf<int> sflag_, ssc_, bp_stage_, bp_big_, bp_nbig_;
+    DBuf<int2> axis_items_;
+    DBuf<double> axis_part_;
+    int axis_items_n_ = 0;
+    void build_axis_items();
     static constexpr int kBigSweepBlocks = 152;   // blocks that share the crowded positions
     uint32_t* order_ = nullptr;   // sorted body order (points into val_)
     DBuf<int2> pairs_;

@@ -244,6 +244,7 @@ template <class R> void World<R>::set_scenes(int ns, const int* off) {
     for (int s = 0; s < ns; s++) if (so[s + 1] < so[s]) throw std::runtime_error("scene offsets must not decrease");
     NS_ = ns;
     h_scene_off_ = so;
+    build_axis_items();
     std::vector<int> sc(std::max(N_, 1), 0);
     for (int s = 0; s < ns; s++) for (int i = so[s]; i < so[s + 1]; i++) sc[i] = s;
     upload(bscene_, sc, st_);
@@ -257,6 +258,18 @@ template <class R> void World<R>::set_scenes(int ns, const int* off) {
     P_ = 0;
     R_ = 0;
     PE_CK(cudaStreamSynchronize(st_));
+}
+
+// (scene, tile) work items of the scenes above kAxisTile bodies, consecutive per scene
+template <class R> void World<R>::build_axis_items() {
+    std::vector<int2> it;
+    for (size_t s = 0; s + 1 < h_scene_off_.size(); s++) {
+        const int cnt = h_scene_off_[s + 1] - h_scene_off_[s];
+        if (cnt <= kAxisTile) continue;
+        for (int t = 0; t * kAxisTile < cnt; t++) it.push_back(make_int2((int)s, t));
+    }
+    axis_items_n_ = (int)it.size();
+    if (axis_items_n_) upload(axis_items_, it, st_);
 }
 
 template <class R> void World<R>::set_params(double dt, double gx, double gy, double gz, int iters) {
@@ -354,6 +367,13 @@ template <class R> int World<R>::broadphase() {
            (const int*)bp_big_.p, (const int*)bp_nbig_.p);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
     launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
+    if (axis_items_n_ > 0) {   // scenes above kAxisTile bodies
+        axis_part_.ensure((size_t)axis_items_n_ * 6);
+        launch(K_BP_AXIS, axis_items_n_, k_bp_axis_tiles<R>, (const R*)smn_.p, (const R*)smx_.p, n, (const int*)scene_off_.p,
+               (const int2*)axis_items_.p, axis_part_.p);
+        launch(K_BP_AXIS, grid(axis_items_n_), k_bp_axis_combine, (const int*)scene_off_.p, (const int2*)axis_items_.p,
+               axis_items_n_, (const double*)axis_part_.p, scene_axis_.p);
+    }
     PE_CK(cudaGetLastError());
     P_ = P;
     return P;
@@ -899,6 +919,7 @@ void World<R>::repack(const int* keep, int n_keep, const SceneData* const* adds,
     NS_ = std::max(ns, 1);
     if (ns == 0) off = {0, 0};
     h_scene_off_ = off;
+    build_axis_items();
     std::vector<int> sc(std::max(N, 1), 0);
     for (int s = 0; s < ns; s++) for (int i = off[s]; i < off[s + 1]; i++) sc[i] = s;
     upload(bscene_, sc, st_);
