@@ -80,6 +80,7 @@ template <class R> void build(World<R>& W, const SceneFile& s) {
         Body<R>& b = W.bodies[i];
         b.shape = s.shape[i];
         b.kinematic = (s.flags[i] & 1) != 0;
+        b.ignore_collision = (s.flags[i] & 2) != 0;
         M3<R> basis;
         for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) basis.m[r][c] = R(s.bas[i * 9 + r * 3 + c]);
         W.init_body(b, R(s.mass[i]), basis, V3<R>(R(s.org[i * 3]), R(s.org[i * 3 + 1]), R(s.org[i * 3 + 2])));

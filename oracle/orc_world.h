@@ -81,6 +81,7 @@ private:
 template <class R> struct Body {
     int shape = 0;
     bool kinematic = false;
+    bool ignore_collision = false;
     R mass = 1, inv_mass = 1, friction = R(0.5), restitution = R(0.5), lin_damp = 0, ang_damp = 0;
     M3<R> local_inv_inertia = M3<R>::identity(), world_inv_inertia = M3<R>::identity();
     Transform<R> t;
@@ -165,6 +166,7 @@ public:
     bool validate(int i, int j) const {
         const Body<R>& a = bodies[i];
         const Body<R>& b = bodies[j];
+        if (a.ignore_collision || b.ignore_collision) return false;
         if (a.kinematic && b.kinematic) return false;
         if (i == j) return false;
         if (a.aabb_min.x > b.aabb_max.x || b.aabb_min.x > a.aabb_max.x) return false;

@@ -253,6 +253,7 @@ int main(int argc, char** argv) {
         rb->setLinearDamping(PE_R(s.lin_damp[i]));
         rb->setAngularDamping(PE_R(s.ang_damp[i]));
         rb->setKinematic((s.flags[i] & 1) != 0);
+        rb->setIgnoreCollision((s.flags[i] & 2) != 0);
         world->addRigidBody(rb);
         g_dump.index[rb] = i;
     }

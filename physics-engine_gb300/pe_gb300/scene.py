@@ -31,6 +31,7 @@ import numpy as np
 
 BOX, SPHERE, CYLINDER, HULL = 0, 1, 2, 3
 KINEMATIC = 1
+IGNORE_COLLISION = 2   # RigidBody::setIgnoreCollision: the body takes part in no pair
 
 MAGIC = b"PESCENE1"
 
@@ -159,9 +160,10 @@ class SceneBuilder:
         return self.shape_key[key]
 
     def body(self, shape, origin, basis=None, mass=1.0, v=(0, 0, 0), w=(0, 0, 0), friction=0.5,
-             restitution=0.5, kinematic=False, lin_damp=0.0, ang_damp=0.0):
+             restitution=0.5, kinematic=False, lin_damp=0.0, ang_damp=0.0, ignore_collision=False):
         basis = np.eye(3) if basis is None else np.asarray(basis, np.float64)
-        self.bodies.append((shape, KINEMATIC if kinematic else 0, float(mass), float(friction),
+        flags = (KINEMATIC if kinematic else 0) | (IGNORE_COLLISION if ignore_collision else 0)
+        self.bodies.append((shape, flags, float(mass), float(friction),
                             float(restitution), float(lin_damp), float(ang_damp),
                             np.asarray(origin, np.float64), basis, np.asarray(v, np.float64),
                             np.asarray(w, np.float64)))

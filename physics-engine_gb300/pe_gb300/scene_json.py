@@ -1,0 +1,176 @@
+"""Scene files in the reference's JSON layout (Simulator::loadScene, src/intf/simulator.cpp:250-594).
+
+``load_scene_json(path)`` reads the ``Configuration`` block (gravity) and the ``RigidBodies`` list
+into a ``Scene`` for the GPU world, following the reference loader's rules:
+
+* a value is used only when its key is present and not null; numbers may be integers or floats;
+  an array of the wrong length or a value of the wrong type is an error
+  (simulator.cpp:27-66, jsonNodeExists / jsonArrayExists);
+* ``kinematic`` bodies keep zero velocities: damping and velocities are read for dynamic bodies only
+  (:348-354);
+* ``rotation`` is a row-major 3x3 matrix (9 numbers) or a quaternion (w, x, y, z) (:362-375);
+* ``type``: ``box`` size = ``scale`` (3 numbers, default 1, 1, 1), ``sphere`` radius = ``scale[0]``
+  (1 number, default 1), ``cylinder`` radius, height = ``scale`` (2 numbers, default 0.5, 1)
+  (:379-395);
+* RigidBody defaults where a key is absent: mass 1, friction 0.5, restitution 0.5, no damping
+  (rigidbody.cpp:87-103).
+
+* a body without a ``type``, or with a type the loader does not know, is skipped (:535-545).
+
+What the rigid-body step here does not model is reported rather than silently dropped:
+``convex`` / ``concave`` / ``compound`` bodies raise ``UnsupportedScene`` (convex meshes come from
+OBJ files, concave and compound shapes are outside the step); fracturable bodies step as plain
+rigid bodies and ``DamageSources`` are not applied (no fracture solver), and sleep thresholds,
+finite lifetimes and tags are ignored (sleeping, lifetimes and the "wheel" tag are not on the
+path).  These, and the skipped bodies, are listed in ``ignored``.
+
+The time step is not part of the file: the reference simulator uses 1 / target frame rate (60 by
+default, simulator.cpp:1043), and the sequential-impulse solver 10 iterations
+(sequential_impulse_solver.cpp:8).
+"""
+from __future__ import annotations
+
+import json
+from numbers import Number
+from pathlib import Path
+
+import numpy as np
+
+from .scene import BOX, CYLINDER, SPHERE, SceneBuilder, quat_to_basis
+
+
+class UnsupportedScene(ValueError):
+    pass
+
+
+def _present(node, key):
+    return isinstance(node, dict) and key in node and node[key] is not None
+
+
+def _number(node, key):
+    if not _present(node, key):
+        return None
+    v = node[key]
+    if isinstance(v, bool) or not isinstance(v, Number):
+        raise ValueError(f"node {key} should be a number")
+    return float(v)
+
+
+def _boolean(node, key):
+    if not _present(node, key):
+        return None
+    v = node[key]
+    if not isinstance(v, bool):
+        raise ValueError(f"node {key} should be a boolean")
+    return v
+
+
+def _string(node, key):
+    if not _present(node, key):
+        return None
+    v = node[key]
+    if not isinstance(v, str):
+        raise ValueError(f"node {key} should be a string")
+    return v
+
+
+def _list(node, key):
+    if not _present(node, key):
+        return None
+    if not isinstance(node[key], list):
+        raise ValueError(f"node {key} should be an array")
+    return node[key]
+
+
+def _array(node, key, size):
+    if not _present(node, key):
+        return None
+    v = node[key]
+    if not isinstance(v, list):
+        raise ValueError(f"node {key} should be an array")
+    if size and len(v) != size:
+        raise ValueError(f"node {key} should have {size} elements")
+    for x in v:
+        if isinstance(x, bool) or not isinstance(x, Number):
+            raise ValueError(f"node {key} should have numeric elements")
+    return [float(x) for x in v]
+
+
+def load_scene_json(path, real_bits: int = 64, dt: float = 1.0 / 60.0, iterations: int = 10):
+    """Returns (Scene, ignored): the scene and the list of file features the step does not model."""
+    data = json.loads(Path(path).read_text())
+    gravity = (0.0, -9.8, 0.0)
+    ignored = []
+    if not isinstance(data, dict):
+        raise ValueError("a scene file holds one JSON object")
+    cfg = data.get("Configuration")
+    if _present(data, "Configuration"):
+        if not isinstance(cfg, dict):
+            raise ValueError("node Configuration should be an object")
+        g = _array(cfg, "gravity", 3)
+        if g is not None:
+            gravity = tuple(g)
+        for k in ("sleep_linear_velocity2_threshold", "sleep_angular_velocity2_threshold", "sleep_time_threshold"):
+            v = _number(cfg, k)
+            if v:
+                ignored.append(f"{k}={v:g} (no sleeping)")
+    sb = SceneBuilder(dt=dt, gravity=gravity, iterations=iterations)
+    bodies = _list(data, "RigidBodies") or []
+    if _list(data, "DamageSources"):
+        ignored.append("DamageSources (no fracture solver)")
+    for idx, rb in enumerate(bodies):
+        if not isinstance(rb, dict):
+            raise ValueError("node RigidBodies should have elements of type object")
+        kind = _string(rb, "type")
+        if kind in ("convex", "concave", "compound"):
+            raise UnsupportedScene(f"body {idx}: '{kind}' shapes are not handled by this loader")
+        if _boolean(rb, "fracturable"):
+            ignored.append(f"body {idx}: fracturable (stepped as a rigid body)")
+        _string(rb, "name")
+        tag = _string(rb, "tag")
+        if tag:
+            ignored.append(f"body {idx}: tag '{tag}'")
+        life = _number(rb, "lifetime")   # negative means forever (simulator.cpp:356-360)
+        if life is not None and 0 <= life < 1e100:
+            ignored.append(f"body {idx}: lifetime {life:g}")
+        kinematic = bool(_boolean(rb, "kinematic"))
+        ignore_collision = bool(_boolean(rb, "ignore_collision"))
+        ld = ad = 0.0
+        v = w = (0.0, 0.0, 0.0)
+        if not kinematic:
+            ld = _number(rb, "linear_damping") or 0.0
+            ad = _number(rb, "angular_damping") or 0.0
+            v = _array(rb, "linear_velocity", 3) or v
+            w = _array(rb, "angular_velocity", 3) or w
+        pos = _array(rb, "position", 0) or [0.0, 0.0, 0.0]
+        if len(pos) < 3:
+            raise ValueError(f"body {idx}: node position should have at least 3 elements")
+        basis = np.eye(3)
+        rot = _array(rb, "rotation", 0)
+        if rot is not None:
+            if len(rot) >= 9:
+                basis = np.array(rot[:9]).reshape(3, 3)
+            elif len(rot) >= 4:
+                basis = quat_to_basis(np.array(rot[:4]))
+            else:
+                raise ValueError(f"body {idx}: invalid rotation data")
+        mass = _number(rb, "mass")
+        fr = _number(rb, "friction")
+        re = _number(rb, "restitution")
+        if kind not in ("box", "sphere", "cylinder"):
+            # the reference logs the body and goes on without it (simulator.cpp:535-545)
+            ignored.append(f"body {idx}: type {kind!r} (body skipped)" if kind else f"body {idx}: no type (body skipped)")
+            continue
+        if kind == "box":
+            size = _array(rb, "scale", 3) or [1.0, 1.0, 1.0]
+            shape = sb.shape(BOX, size)
+        elif kind == "sphere":
+            r = _array(rb, "scale", 1)
+            shape = sb.shape(SPHERE, (r[0] if r else 1.0,))
+        else:
+            rh = _array(rb, "scale", 2) or [0.5, 1.0]
+            shape = sb.shape(CYLINDER, rh)
+        sb.body(shape, pos[:3], basis, mass=1.0 if mass is None else mass, v=v, w=w,
+                friction=0.5 if fr is None else fr, restitution=0.5 if re is None else re, kinematic=kinematic,
+                lin_damp=ld, ang_damp=ad, ignore_collision=ignore_collision)
+    return sb.build(real_bits), ignored

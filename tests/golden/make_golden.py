@@ -19,6 +19,7 @@ sys.path.insert(0, str(ROOT / "physics-engine_gb300"))
 sys.path.insert(0, str(ROOT / "oracle"))
 
 from pe_gb300 import scene as sc  # noqa: E402
+from pe_gb300.scene_json import load_scene_json  # noqa: E402
 import pedump  # noqa: E402
 import build_ref  # noqa: E402
 
@@ -37,6 +38,13 @@ CASES = {
     "pile_f32": (lambda: sc.pile(48, seed=6, real_bits=32, hull_range=(8, 24), drop=(0.0, 0.3)), 32, 40,
                  [0, 1, 24, 25, 38, 39]),
 }
+# the reference's own sample scene (a bomb sphere at 70 m/s into a 15-box tower on a kinematic
+# ground), read by the scene-file loader; the sphere reaches the tower near step 57
+SAMPLES = Path("/root/reference/SampleScenes")
+for bits in (64, 32):
+    CASES[f"json_bomb_tower_smaller_f{bits}"] = (
+        lambda bits=bits: load_scene_json(SAMPLES / "bomb_crash_tower_smaller.json", real_bits=bits)[0], bits, 120,
+        [0, 1, 30, 55, 56, 57, 58, 59, 60, 61, 62, 90, 119])
 for a in range(4):
     for b in range(a, 4):
         CASES[f"zoo_{a}{b}_f64"] = (lambda a=a, b=b: sc.pair_zoo(a, b, m=48, seed=100 + 4 * a + b, real_bits=64), 64, 2, [0, 1])
@@ -66,6 +74,7 @@ def make(name, ref_dir):
 
 if __name__ == "__main__":
     build_ref.build(Path("/root/reference"), 8)
-    for name in sorted(CASES):
+    names = sys.argv[1:] or sorted(CASES)
+    for name in names:
         p, c = make(name, build_ref.OUT)
         print(f"{name}: pairs {p} contact points {c}")

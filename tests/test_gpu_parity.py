@@ -76,6 +76,52 @@ def test_gpu_full_steps_serial_order_match_reference(name):
         compare_results(g.results(), results_of(d), what=f"{name} step {k}")
 
 
+@pytest.mark.parametrize("name", ["json_bomb_tower_smaller_f64", "json_bomb_tower_smaller_f32"])
+def test_gpu_scene_file_full_steps_match_reference(name):
+    """The reference's sample scene bomb_crash_tower_smaller.json (read by the scene-file loader)
+    stepped on the device in serial-order mode: 119 whole steps reproduce the reference's
+    trajectory through the impact (steps 58-62).  The steps start from the reference's state
+    after step 0, the one step whose sort keys tie (tied keys fix the pair set, not its order)."""
+    scene, bits, steps, rec = load_golden(name)
+    g = pg.GpuWorld(scene, bits)
+    d0 = rec[0]
+    s0 = dump_state(d0)
+    s0["lin_vel"], s0["ang_vel"] = d0["lin_vel_post"], d0["ang_vel_post"]
+    g.set_state(s0)
+    g.set_results(results_of(d0))
+    g.axis = int(d0["axis_after"])
+    done = 1
+    for k in sorted(rec)[1:]:
+        g.step(k + 1 - done, pg.SERIAL_ORDER)
+        done = k + 1
+        d = rec[k]
+        st = g.state()
+        compare_state(st, dump_state(d), keys=["origin", "basis", "aabb_min", "aabb_max", "world_inv_inertia"], what=f"{name} step {k}")
+        np.testing.assert_array_equal(st["lin_vel"], d["lin_vel_post"])
+        np.testing.assert_array_equal(st["ang_vel"], d["ang_vel_post"])
+        np.testing.assert_array_equal(g.pairs(), d["pairs"])
+        compare_results(g.results(), results_of(d), what=f"{name} step {k}")
+
+
+def test_gpu_ignore_collision_bodies_match_oracle():
+    """Bodies flagged ignore-collision (RigidBody::setIgnoreCollision) take part in no pair: a
+    mixed 4,096-body scene with every fifth body flagged gives the oracle's pairs and contacts."""
+    scene = sc.random_cube(n=4096, seed=23, extent=24.0, real_bits=32)
+    scene.body_flags[::5] |= sc.IGNORE_COLLISION
+    o = orc.OracleWorld(scene, 32)
+    g = pg.GpuWorld(scene, 32)
+    for w in (o, g):
+        w.integrate()
+        w.broadphase()
+    po, pgpu = o.pairs(), g.pairs()
+    assert len(po) > 1000
+    assert not np.isin(po, np.arange(0, 4096, 5)).any()
+    np.testing.assert_array_equal(pgpu, po)
+    o.narrowphase()
+    g.narrowphase()
+    compare_results(g.results(), o.results(), what="ignore-collision narrowphase")
+
+
 def test_gpu_stress_scene_broadphase_and_narrowphase_match_oracle():
     """65,536 mixed bodies in a 100 m cube (one-step stress): integration bit-exact, the
     pair set exact, and every contact result exact given the oracle's pair order."""
