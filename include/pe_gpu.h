@@ -32,6 +32,7 @@ extern "C" {
 #define PE_GPU_SHAPE_SPHERE 1
 #define PE_GPU_SHAPE_CYLINDER 2
 #define PE_GPU_SHAPE_CONVEX_MESH 3
+#define PE_GPU_SHAPE_COMPOUND 5       /* ShapeType::ST_Compound (shape.h:7-9); children via pe_gpu_set_compounds */
 
 /* body flags */
 #define PE_GPU_BODY_KINEMATIC 1        /* RigidBody::setKinematic (rigidbody.h:14) */
@@ -62,6 +63,24 @@ const char* pe_gpu_last_error(const pe_gpu_world* w);
 int pe_gpu_set_shapes(pe_gpu_world* w, int n_shapes, const int* type, const double* param, const int* hull_vbeg,
                       const int* hull_vcnt, const int* hull_fbeg, const int* hull_fcnt, int n_hull_verts,
                       const double* hull_verts, int n_hull_faces, const int* hull_face_off, const int* hull_face_idx);
+
+/* Compound shapes.  Replaces CompoundShape::addShape(local_transform, mass_ratio, child) for each
+ * child followed by CompoundShape::init() (compound_shape.cpp:7-47), for every shape that
+ * pe_gpu_set_shapes declared PE_GPU_SHAPE_COMPOUND.  Call after pe_gpu_set_shapes and before
+ * pe_gpu_set_bodies.  child_beg / child_cnt [n_shapes]: the children of shape s are
+ * [child_beg[s], child_beg[s] + child_cnt[s]) (ignored for other shapes); per child: child_shape
+ * (a non-compound shape of the same table), child_origin [3], child_basis [9, row-major] and
+ * child_ratio (mass ratio, >= 1e-5).  With local_inertia NULL the library runs init(): the
+ * children are relocated to their mass-ratio centroid, the compound's unit-mass inertia is
+ * computed from theirs, and centroid (optional, [3 n_shapes]) receives the relocation vector
+ * init() returns (zero for other shapes).  With local_inertia [9 n_shapes, row-major] the children
+ * are taken as already initialised (CompoundShape::getShapes() of a shape whose init() ran) and
+ * local_inertia[9 s..] is CompoundShape::getLocalInertia().  Collisions of a compound follow
+ * CompoundCompoundCollisionAlgorithm (compound_compound_collision_algorithm.cpp:8-46): a result
+ * whose second body is a compound names the compound as body A. */
+int pe_gpu_set_compounds(pe_gpu_world* w, const int* child_beg, const int* child_cnt, int n_children, const int* child_shape,
+                         const double* child_origin, const double* child_basis, const double* child_ratio,
+                         const double* local_inertia, double* centroid);
 
 /* Rigid bodies, all at once.  Replaces RigidBody::setMass / setCollisionShape / setTransform /
  * setLinearVelocity / setAngularVelocity / setFrictionCoeff / setRestitutionCoeff /

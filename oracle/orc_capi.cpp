@@ -16,13 +16,18 @@ struct SceneFile {
     double dt = 0.01, g[3] = {0, -9.8, 0};
     std::vector<int> type, vbeg, vcnt, fbeg, fcnt, foff, fidx, shape, flags;
     std::vector<double> param, hv, mass, fr, re, ld, ad, org, bas, v, w;
+    // compound children ("PESCENE2" files): per shape [cbeg, cbeg + ccnt), per child its shape,
+    // local origin, local basis (row-major) and mass ratio
+    std::vector<int> cbeg, ccnt, cshape;
+    std::vector<double> corg, cbas, cratio;
 };
 
 bool read_scene(const char* path, SceneFile& s) {
     FILE* f = fopen(path, "rb");
     if (!f) return false;
     char magic[8];
-    bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "PESCENE1", 8) == 0;
+    bool ok = fread(magic, 1, 8, f) == 8 && (memcmp(magic, "PESCENE1", 8) == 0 || memcmp(magic, "PESCENE2", 8) == 0);
+    const bool compound = ok && memcmp(magic, "PESCENE2", 8) == 0;
     int hdr[6];
     double w4[4];
     ok = ok && fread(hdr, sizeof(int), 6, f) == 6 && fread(w4, sizeof(double), 4, f) == 4;
@@ -35,6 +40,11 @@ bool read_scene(const char* path, SceneFile& s) {
          rdi(s.fcnt, s.S) && rdd(s.hv, s.HV * 3) && rdi(s.foff, s.HF + 1) && rdi(s.fidx, s.HI) && rdi(s.shape, s.N) &&
          rdi(s.flags, s.N) && rdd(s.mass, s.N) && rdd(s.fr, s.N) && rdd(s.re, s.N) && rdd(s.ld, s.N) && rdd(s.ad, s.N) &&
          rdd(s.org, s.N * 3) && rdd(s.bas, s.N * 9) && rdd(s.v, s.N * 3) && rdd(s.w, s.N * 3);
+    if (ok && compound) {
+        int C = 0;
+        ok = fread(&C, sizeof(int), 1, f) == 1 && C >= 0 && rdi(s.cbeg, s.S) && rdi(s.ccnt, s.S) && rdi(s.cshape, C) &&
+             rdd(s.corg, (size_t)C * 3) && rdd(s.cbas, (size_t)C * 9) && rdd(s.cratio, C);
+    }
     fclose(f);
     return ok;
 }
@@ -46,12 +56,18 @@ struct Handle {
     std::unique_ptr<Pool> pool;
 };
 
+template <class R> void put3(double* o, const V3<R>& v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
+template <class R> void put9(double* o, const M3<R>& m) { for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) o[r * 3 + c] = m.m[r][c]; }
+template <class R> V3<R> get3(const double* o) { return V3<R>(R(o[0]), R(o[1]), R(o[2])); }
+template <class R> M3<R> get9(const double* o) { M3<R> m; for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) m.m[r][c] = R(o[r * 3 + c]); return m; }
+
 template <class R> void build(World<R>& W, const SceneFile& s) {
     W.dt = R(s.dt);
     W.gravity = V3<R>(R(s.g[0]), R(s.g[1]), R(s.g[2]));
     W.iterations = s.iters;
     for (int i = 0; i < s.S; i++) {
         const double* p = &s.param[i * 3];
+        if (s.type[i] == ST_COMPOUND) { W.shapes.push_back(Shape<R>()); continue; }   // built below, once its children exist
         switch (s.type[i]) {
             case ST_BOX: W.shapes.push_back(make_box<R>(V3<R>(R(p[0]), R(p[1]), R(p[2])))); break;
             case ST_SPHERE: W.shapes.push_back(make_sphere<R>(R(p[0]))); break;
@@ -75,6 +91,21 @@ template <class R> void build(World<R>& W, const SceneFile& s) {
             }
         }
     }
+    for (int i = 0; i < s.S; i++) {
+        if (s.type[i] != ST_COMPOUND) continue;
+        if (s.cbeg.empty()) throw std::runtime_error("compound shape without a children table");
+        std::vector<Child<R>> kids;
+        for (int k = s.cbeg[i]; k < s.cbeg[i] + s.ccnt[i]; k++) {
+            Child<R> c;
+            c.shape = s.cshape[k];
+            c.local.origin = get3<R>(&s.corg[(size_t)k * 3]);
+            c.local.basis = get9<R>(&s.cbas[(size_t)k * 9]);
+            c.ratio = R(s.cratio[k]);
+            kids.push_back(c);
+        }
+        make_compound(W.shapes[i], kids, W.shapes);
+    }
+    link_children(W.shapes);
     W.bodies.resize(s.N);
     for (int i = 0; i < s.N; i++) {
         Body<R>& b = W.bodies[i];
@@ -93,10 +124,6 @@ template <class R> void build(World<R>& W, const SceneFile& s) {
     }
 }
 
-template <class R> void put3(double* o, const V3<R>& v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
-template <class R> void put9(double* o, const M3<R>& m) { for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) o[r * 3 + c] = m.m[r][c]; }
-template <class R> V3<R> get3(const double* o) { return V3<R>(R(o[0]), R(o[1]), R(o[2])); }
-template <class R> M3<R> get9(const double* o) { M3<R> m; for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) m.m[r][c] = R(o[r * 3 + c]); return m; }
 
 template <class F> auto with(void* h, F&& f) {
     Handle* H = static_cast<Handle*>(h);
@@ -114,8 +141,14 @@ void* orc_create(const char* scene_path, int real_bits, int threads) {
     auto* H = new Handle();
     H->bits = real_bits == 32 ? 32 : 64;
     if (threads > 1) H->pool.reset(new Pool(threads));
-    if (H->bits == 64) { H->w64.reset(new World<double>()); build(*H->w64, s); H->w64->pool = H->pool.get(); }
-    else { H->w32.reset(new World<float>()); build(*H->w32, s); H->w32->pool = H->pool.get(); }
+    try {
+        if (H->bits == 64) { H->w64.reset(new World<double>()); build(*H->w64, s); H->w64->pool = H->pool.get(); }
+        else { H->w32.reset(new World<float>()); build(*H->w32, s); H->w32->pool = H->pool.get(); }
+    } catch (const std::exception& e) {
+        fprintf(stderr, "orc_create: %s\n", e.what());
+        delete H;
+        return nullptr;
+    }
     return H;
 }
 

@@ -1070,8 +1070,44 @@ template <class R> bool cylinder_hull(PairCtx<R>& c) {
 }
 
 // narrow_phase_base.cpp:20-29 dispatch restricted to box/sphere/cylinder/convex-mesh
+template <class R> bool collide(PairCtx<R>& c);
+
+// CompoundCompoundCollisionAlgorithm::processCollision (compound_compound_collision_algorithm.cpp:8-37):
+// the compound goes first (a compound second swaps shapes, transforms and the result's objects,
+// so the result then names the compound as object A); every child (against every child of a
+// second compound) runs the algorithm of its shape pair into the same result, at the child's
+// world transform (body transform * local transform, :23-29), with the pair's reference scale.
+template <class R> bool compound_collide(PairCtx<R>& c) {
+    if (c.sb->type == ST_COMPOUND) {
+        std::swap(c.sa, c.sb);
+        std::swap(c.ta, c.tb);
+        std::swap(c.A, c.B);
+        std::swap(c.res->a, c.res->b);
+    }
+    if (c.sa->type != ST_COMPOUND) return false;
+    bool hit = false;
+    auto sub = [&](const Shape<R>* sa, const Shape<R>* sb, const Transform<R>* ta, const Transform<R>* tb) {   // :39-46
+        PairCtx<R> s = c;
+        s.sa = sa; s.sb = sb; s.ta = ta; s.tb = tb;
+        return collide(s);
+    };
+    for (auto& ch : c.sa->children) {
+        const Transform<R> taw = (*c.ta) * ch.local;
+        if (c.sb->type == ST_COMPOUND) {
+            for (auto& chb : c.sb->children) {
+                const Transform<R> tbw = (*c.tb) * chb.local;
+                hit |= sub(ch.s, chb.s, &taw, &tbw);
+            }
+        } else {
+            hit |= sub(ch.s, c.sb, &taw, c.tb);
+        }
+    }
+    return hit;
+}
+
 template <class R> bool collide(PairCtx<R>& c) {
     const int ta = c.sa->type, tb = c.sb->type;
+    if (ta == ST_COMPOUND || tb == ST_COMPOUND) return compound_collide(c);
     auto is = [&](int x, int y) { return (ta == x && tb == y) || (ta == y && tb == x); };
     if (ta == ST_BOX && tb == ST_BOX) return box_box(c);
     if (is(ST_BOX, ST_SPHERE)) return box_sphere(c);

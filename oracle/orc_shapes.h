@@ -1,14 +1,24 @@
-// Oracle shapes: box, sphere, cylinder and convex mesh, restating the reference's
-// src/rigid/shape/{box,sphere,cylinder,convex_mesh}_shape.cpp and the default meshes of
+// Oracle shapes: box, sphere, cylinder, convex mesh and compound, restating the reference's
+// src/rigid/shape/{box,sphere,cylinder,convex_mesh,compound}_shape.cpp and the default meshes of
 // src/rigid/shape/default_mesh.h.  Test infrastructure only.
 #pragma once
 #include <algorithm>
+#include <stdexcept>
 #include <vector>
 #include "orc_math.h"
 
 namespace orc {
 
-enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3 };
+enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3, ST_COMPOUND = 5 };
+
+template <class R> struct Shape;
+// one CompoundShape::ShapeEle (compound_shape.h:10-14); `s` points into the world's shape table
+template <class R> struct Child {
+    int shape = 0;
+    Transform<R> local;
+    R ratio = 0;
+    const Shape<R>* s = nullptr;
+};
 
 template <class R> struct Face {
     std::vector<int> idx;
@@ -27,6 +37,7 @@ template <class R> struct Shape {
     // hull bounding-volume tree (src/utils/bvh.cpp), flattened
     struct Node { int left = -1, right = -1, n = 0, index = 0; V3<R> aa, bb; };
     std::vector<Node> bvh;
+    std::vector<Child<R>> children;         // compound
 };
 
 // ---------------------------------------------------------------- default meshes
@@ -354,10 +365,62 @@ template <class R> Shape<R> make_hull(std::vector<V3<R>> verts, std::vector<Face
     return s;
 }
 
+// CompoundShape::addShape for each child (compound_shape.cpp:7-21) followed by init() (:25-47):
+// children relocated to their mass-ratio centroid, the compound's local inertia summed from the
+// children's rotated inertia plus the parallel-axis term, weighted by mass ratio.  `shapes` holds
+// the children's shapes.  Returns the centroid (init()'s relocation vector).
+template <class R> V3<R> make_compound(Shape<R>& s, std::vector<Child<R>> kids, const std::vector<Shape<R>>& shapes) {
+    s = Shape<R>();
+    s.type = ST_COMPOUND;
+    R total = 0;
+    for (auto& c : kids) {
+        if (shapes[c.shape].type == ST_COMPOUND) throw std::runtime_error("CompoundShape cannot contain another CompoundShape");
+        if (c.ratio < kEps<R>()) throw std::runtime_error("mass ratio must be greater than 0");
+        total += c.ratio;
+        s.volume += shapes[c.shape].volume;
+    }
+    V3<R> centroid(0, 0, 0);
+    for (auto& c : kids) centroid = centroid + c.local.origin * c.ratio;
+    centroid = centroid / total;
+    M3<R> L;
+    for (auto& c : kids) {
+        const M3<R>& si = shapes[c.shape].local_inertia;
+        const V3<R> p = c.local.origin - centroid;
+        c.local.origin = p;
+        const M3<R>& rot = c.local.basis;
+        M3<R> t;
+        const R pp = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+        for (int i = 0; i < 3; i++) t.m[i][i] = pp;
+        for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) t.m[i][j] -= p[i] * p[j];
+        const M3<R> a = mmt_r2l(mm(rot, si), rot);
+        const R k = c.ratio / total;
+        for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) L.m[i][j] = L.m[i][j] + (a.m[i][j] + t.m[i][j]) * k;
+    }
+    s.local_inertia = L;
+    s.children = kids;
+    return centroid;
+}
+
+// points every compound child at its shape (once the shape table no longer grows)
+template <class R> void link_children(std::vector<Shape<R>>& shapes) {
+    for (auto& s : shapes)
+        for (auto& c : s.children) c.s = &shapes[c.shape];
+}
+
 // ---------------------------------------------------------------- queries
 template <class R> void get_aabb(const Shape<R>& s, const Transform<R>& t, V3<R>& mn, V3<R>& mx) {
     const R MX = Limits<R>::max(), MN = Limits<R>::min();
     switch (s.type) {
+        case ST_COMPOUND: {   // compound_shape.cpp:49-58
+            mn = V3<R>(MX, MX, MX); mx = V3<R>(MN, MN, MN);
+            for (auto& c : s.children) {
+                V3<R> a, b;
+                get_aabb(*c.s, t * c.local, a, b);
+                mn = V3<R>(mn.x < a.x ? mn.x : a.x, mn.y < a.y ? mn.y : a.y, mn.z < a.z ? mn.z : a.z);   // PE_VEC_MIN2
+                mx = V3<R>(mx.x > b.x ? mx.x : b.x, mx.y > b.y ? mx.y : b.y, mx.z > b.z ? mx.z : b.z);
+            }
+            break;
+        }
         case ST_BOX: {   // box_shape.cpp:27-43
             mn = V3<R>(MX, MX, MX); mx = V3<R>(MN, MN, MN);
             for (int i = 0; i < 8; i++) {

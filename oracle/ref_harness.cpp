@@ -16,6 +16,7 @@
 #include "rigid/shape/sphere_shape.h"
 #include "rigid/shape/cylinder_shape.h"
 #include "rigid/shape/convex_mesh_shape.h"
+#include "rigid/shape/compound_shape.h"
 #include "rigid/collision/broad_phase/broad_phase_sweep_and_prune.h"
 #include "rigid/constraint/constraint_solver/sequential_impulse_solver.h"
 #include "utils/thread_pool.h"
@@ -36,6 +37,8 @@ struct Scene {
     double dt = 0.01, g[3] = {0, -9.8, 0};
     std::vector<int> type, hvbeg, hvcnt, hfbeg, hfcnt, face_off, face_idx, shape, flags;
     std::vector<double> param, hverts, mass, friction, restitution, lin_damp, ang_damp, origin, basis, v, w;
+    std::vector<int> cbeg, ccnt, cshape;   // compound children ("PESCENE2")
+    std::vector<double> corigin, cbasis, cratio;
 };
 
 template <class T> void rd(FILE* f, T* p, size_t n) {
@@ -48,7 +51,8 @@ Scene load(const char* path) {
     if (!f) { fprintf(stderr, "cannot open %s\n", path); _exit(2); }
     char magic[8];
     rd(f, magic, 8);
-    if (memcmp(magic, "PESCENE1", 8) != 0) { fprintf(stderr, "bad magic\n"); _exit(2); }
+    const bool compound = memcmp(magic, "PESCENE2", 8) == 0;
+    if (memcmp(magic, "PESCENE1", 8) != 0 && !compound) { fprintf(stderr, "bad magic\n"); _exit(2); }
     int hdr[6];
     rd(f, hdr, 6);
     s.n_shapes = hdr[0]; s.n_bodies = hdr[1]; s.n_hull_verts = hdr[2];
@@ -73,6 +77,16 @@ Scene load(const char* path) {
     s.basis.resize(N * 9); rd(f, s.basis.data(), N * 9);
     s.v.resize(N * 3); rd(f, s.v.data(), N * 3);
     s.w.resize(N * 3); rd(f, s.w.data(), N * 3);
+    if (compound) {
+        int C = 0;
+        rd(f, &C, 1);
+        s.cbeg.resize(S); rd(f, s.cbeg.data(), S);
+        s.ccnt.resize(S); rd(f, s.ccnt.data(), S);
+        s.cshape.resize(C); rd(f, s.cshape.data(), C);
+        s.corigin.resize(C * 3); rd(f, s.corigin.data(), C * 3);
+        s.cbasis.resize(C * 9); rd(f, s.cbasis.data(), C * 9);
+        s.cratio.resize(C); rd(f, s.cratio.data(), C);
+    }
     fclose(f);
     return s;
 }
@@ -238,7 +252,21 @@ int main(int argc, char** argv) {
     world->setConstraintSolver(solver);
 
     std::vector<pe_phys_shape::Shape*> shapes;
-    for (int i = 0; i < s.n_shapes; i++) shapes.push_back(make_shape(s, i));
+    for (int i = 0; i < s.n_shapes; i++) shapes.push_back(s.type[i] == 5 ? nullptr : make_shape(s, i));
+    // compound shapes: CompoundShape::addShape per child, then init() (children relocated to their
+    // centroid, local inertia), as examples/compound_demo/main.cpp builds them
+    for (int i = 0; i < s.n_shapes; i++) {
+        if (s.type[i] != 5) continue;
+        auto* cs = new pe_phys_shape::CompoundShape();
+        for (int k = s.cbeg[i]; k < s.cbeg[i] + s.ccnt[i]; k++) {
+            pe::Matrix3 b;
+            for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) b(r, c) = PE_R(s.cbasis[k * 9 + r * 3 + c]);
+            const double* o = &s.corigin[k * 3];
+            cs->addShape(pe::Transform(b, pe::Vector3(PE_R(o[0]), PE_R(o[1]), PE_R(o[2]))), PE_R(s.cratio[k]), shapes[s.cshape[k]]);
+        }
+        cs->init();
+        shapes[i] = cs;
+    }
     for (int i = 0; i < s.n_bodies; i++) {
         auto* rb = new pe_phys_object::RigidBody();
         rb->setMass(PE_R(s.mass[i]));

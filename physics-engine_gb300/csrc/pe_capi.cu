@@ -62,6 +62,18 @@ int pe_gpu_set_shapes(pe_gpu_world* h, int n, const int* type, const double* par
     return guard(h, [&](pe::WorldBase& w) { w.set_shapes(n, type, param, vbeg, vcnt, fbeg, fcnt, hv_n, hv, hf_n, foff, fidx); return PE_GPU_OK; });
 }
 
+int pe_gpu_set_compounds(pe_gpu_world* h, const int* child_beg, const int* child_cnt, int n_children, const int* child_shape,
+                         const double* child_origin, const double* child_basis, const double* child_ratio,
+                         const double* local_inertia, double* centroid) {
+    if (!child_beg || !child_cnt || n_children < 0 ||
+        (n_children > 0 && (!child_shape || !child_origin || !child_basis || !child_ratio)))
+        return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) {
+        w.set_compounds(child_beg, child_cnt, n_children, child_shape, child_origin, child_basis, child_ratio, local_inertia, centroid);
+        return PE_GPU_OK;
+    });
+}
+
 int pe_gpu_set_bodies(pe_gpu_world* h, int n, const int* shape, const int* flags, const double* mass, const double* fr,
                       const double* re, const double* ld, const double* ad, const double* o, const double* b, const double* v,
                       const double* w) {

@@ -953,10 +953,11 @@ template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_con
 // the shared-memory staging limits) the unstaged warp path.
 enum PairClass { PC_BOX_BOX = 0, PC_BOX_SPHERE, PC_SPHERE_SPHERE, PC_SPHERE_CYL, PC_BOX_CYL, PC_CONVEX, PC_SPHERE_HULL,
                  PC_CYL_HULL, PC_CONVEX_HEAVY, PC_CONVEX_BIG, PC_CONVEX_HULL_HULL, PC_CONVEX_CYL_CYL, PC_CONVEX_HULL_BOX,
-                 PC_COUNT };
+                 PC_COMPOUND, PC_COUNT };
 
 __host__ __device__ inline int pair_class(int ta, int tb) {
     const int lo = ta < tb ? ta : tb, hi = ta < tb ? tb : ta;
+    if (hi == ST_COMPOUND) return PC_COMPOUND;   // CompoundCompoundCollisionAlgorithm, either side
     if (lo == ST_BOX && hi == ST_BOX) return PC_BOX_BOX;
     if (lo == ST_BOX && hi == ST_SPHERE) return PC_BOX_SPHERE;
     if (lo == ST_SPHERE && hi == ST_SPHERE) return PC_SPHERE_SPHERE;

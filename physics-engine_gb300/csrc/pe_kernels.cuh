@@ -49,7 +49,8 @@ __global__ void k_integrate(Bodies<R> B, ShapeTable<R> S, StepParams P, int do_m
         B.set_vec(WX, i, nw);
     }
     V3<R> mn, mx;
-    shape_aabb(sh, t, mn, mx);
+    if (sh.type == ST_COMPOUND) compound_aabb(S, B.shape[i], t, mn, mx);
+    else shape_aabb(sh, t, mn, mx);
     B.set_vec(MNX, i, mn);
     B.set_vec(MXX, i, mx);
     // RigidBody::getAABBScale (rigidbody.cpp:119-123)
@@ -406,8 +407,10 @@ __device__ __forceinline__ void np_setup(int p, const int2* pairs, const Bodies<
 // ContactResult::sortContactPoints (stable order by distance over all 8 slots, size = first
 // invalid slot) and write-out of result p
 template <class R>
-__device__ __forceinline__ void np_finish(int p, const int2* pairs, const Bodies<R>& B, const Results<R>& res, const Cache<R>& cache) {
-    const int2 q = pairs[p];
+__device__ __forceinline__ void np_finish(int p, const int2* pairs, const Bodies<R>& B, const Results<R>& res, const Cache<R>& cache,
+                                          bool swapped = false) {
+    int2 q = pairs[p];
+    if (swapped) q = make_int2(q.y, q.x);   // the result names its objects in swapped order
     int perm[kSlots];
     for (int k = 0; k < kSlots; k++) {
         int j = k;
@@ -445,6 +448,51 @@ __global__ void k_np_class(int lo, int hi, const int* order, const int2* pairs, 
     np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
     collide(pr, CLS);
     np_finish(p, pairs, B, res, cache);
+}
+
+// CompoundCompoundCollisionAlgorithm::processCollision (compound_compound_collision_algorithm.cpp:8-46),
+// one thread per pair with a compound on either side.  A compound second swaps the pair (shapes,
+// transforms and the result's objects: ContactResult::setObjects(B, A), so the result names the
+// compound as object A); then every child of the compound, against every child of a second
+// compound or against the other shape, runs its shape pair's algorithm into the same contact
+// cache at the child's world transform (body transform * local transform).  Local contact
+// positions stay relative to the bodies.
+template <class R>
+__global__ void k_np_compound(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                              const int* pair_scene_off, const int* prev_off) {
+    const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= hi) return;
+    const int p = order[t];
+    Cache<R> cache;
+    Pair<R> pr;
+    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
+    int sa = B.shape[pairs[p].x], sb = B.shape[pairs[p].y];
+    bool swapped = false;
+    if (pr.sb.type == ST_COMPOUND) {
+        const ShapeView<R> v = pr.sa; pr.sa = pr.sb; pr.sb = v;
+        const Xf<R> x = pr.xa; pr.xa = pr.xb; pr.xb = x;
+        const Xf<R> y = cache.ta; cache.ta = cache.tb; cache.tb = y;
+        const R z = cache.scale_a; cache.scale_a = cache.scale_b; cache.scale_b = z;
+        const int w = sa; sa = sb; sb = w;
+        swapped = true;
+    }
+    const Xf<R> ta = pr.xa, tb = pr.xb;
+    const bool b_comp = pr.sb.type == ST_COMPOUND;
+    for (int i = S.c_beg[sa], ie = S.c_beg[sa] + S.c_cnt[sa]; i < ie; i++) {
+        Pair<R> c = pr;
+        c.sa = S.view(S.c_shape[i]);
+        c.xa = ta * S.child_xf(i);
+        if (b_comp) {
+            for (int j = S.c_beg[sb], je = S.c_beg[sb] + S.c_cnt[sb]; j < je; j++) {
+                c.sb = S.view(S.c_shape[j]);
+                c.xb = tb * S.child_xf(j);
+                collide(c, pair_class(c.sa.type, c.sb.type));
+            }
+        } else {
+            collide(c, pair_class(c.sa.type, c.sb.type));
+        }
+    }
+    np_finish(p, pairs, B, res, cache, swapped);
 }
 
 // ---------------------------------------------------------------- warp-cooperative SAT

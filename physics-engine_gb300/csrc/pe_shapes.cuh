@@ -11,7 +11,7 @@
 
 namespace pe {
 
-enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3 };
+enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3, ST_COMPOUND = 5 };
 
 // unit meshes (host builds them; device reads them from constant memory)
 constexpr int kBoxV = 24, kBoxF = 6, kBoxE = 12;
@@ -98,8 +98,19 @@ template <class R> struct ShapeTable {
     const int* h_vbeg; const int* h_vcnt; const int* h_fbeg; const int* h_fcnt; const int* h_ebeg; const int* h_ecnt;
     const R* hv; const int* f_off; const int* f_idx; const R* f_n; const R* f_min; const R* f_max;
     const R* e_a; const R* e_b;
+    // compound shapes: children [c_beg[s], c_beg[s] + c_cnt[s]) of shape s, each a non-compound
+    // shape c_shape[k] at local transform c_xf[12k..] (basis row-major, then origin), relocated by
+    // CompoundShape::init()
+    const int* c_beg; const int* c_cnt; const int* c_shape; const R* c_xf;
 
 #ifdef __CUDACC__
+    __device__ Xf<R> child_xf(int k) const {
+        const R* x = c_xf + (size_t)k * 12;
+        Xf<R> t;
+        for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) t.b.m[r][c] = x[r * 3 + c];
+        t.o = V3<R>(x[9], x[10], x[11]);
+        return t;
+    }
     __device__ ShapeView<R> view(int s) const {
         ShapeView<R> v;
         v.type = type[s];
@@ -156,6 +167,20 @@ template <class R> __device__ void shape_aabb(const ShapeView<R>& s, const Xf<R>
     }
     mn = mn + t.o;
     mx = mx + t.o;
+}
+
+// CompoundShape::getAABB (compound_shape.cpp:49-58): the union (PE_VEC_MIN2 / PE_VEC_MAX2) of the
+// children's boxes at body transform * local transform
+template <class R> __device__ void compound_aabb(const ShapeTable<R>& S, int s, const Xf<R>& t, V3<R>& mn, V3<R>& mx) {
+    const R MX = Lim<R>::max(), MN = Lim<R>::min();
+    mn = V3<R>(MX, MX, MX);
+    mx = V3<R>(MN, MN, MN);
+    for (int k = S.c_beg[s], e = S.c_beg[s] + S.c_cnt[s]; k < e; k++) {
+        V3<R> a, b;
+        shape_aabb(S.view(S.c_shape[k]), t * S.child_xf(k), a, b);
+        mn = V3<R>(mn.x < a.x ? mn.x : a.x, mn.y < a.y ? mn.y : a.y, mn.z < a.z ? mn.z : a.z);
+        mx = V3<R>(mx.x > b.x ? mx.x : b.x, mx.y > b.y ? mx.y : b.y, mx.z > b.z ? mx.z : b.z);
+    }
 }
 
 // Shape::localIsInside

@@ -61,6 +61,8 @@ public:
     virtual void set_bodies(int n, const int* shape, const int* flags, const double* mass, const double* fr,
                             const double* re, const double* ld, const double* ad, const double* o, const double* b,
                             const double* v, const double* w) = 0;
+    virtual void set_compounds(const int* cbeg, const int* ccnt, int C, const int* cshape, const double* corg,
+                               const double* cbas, const double* cratio, const double* local_inertia, double* centroid) = 0;
     virtual void set_scenes(int n, const int* off) = 0;
     virtual void set_params(double dt, double gx, double gy, double gz, int iters) = 0;
     virtual void step(int n, int mode) = 0;
@@ -103,6 +105,8 @@ public:
     void set_bodies(int n, const int* shape, const int* flags, const double* mass, const double* fr, const double* re,
                     const double* ld, const double* ad, const double* o, const double* b, const double* v,
                     const double* w) override;
+    void set_compounds(const int* cbeg, const int* ccnt, int C, const int* cshape, const double* corg, const double* cbas,
+                       const double* cratio, const double* local_inertia, double* centroid) override;
     void set_scenes(int n, const int* off) override;
     void set_params(double dt, double gx, double gy, double gz, int iters) override;
     void step(int n, int mode) override;
@@ -227,6 +231,12 @@ private:
     // host copies of the shape tables (shapes are only ever appended after set_shapes)
     std::vector<int> h_shull_, h_hvb_, h_hvc_, h_hfb_, h_hfc_, h_heb_, h_hec_, h_foff_, h_fidx_;
     std::vector<R> h_hv_, h_fn_, h_fmn_, h_fmx_, h_ea_, h_eb_;
+    // compound children (per shape: first child and count; per child: shape and 12-real transform)
+    DBuf<int> cbeg_, ccnt_, cshape_;
+    DBuf<R> cxf_;
+    std::vector<int> h_cbeg_, h_ccnt_, h_cshape_;
+    std::vector<char> h_cready_;
+    std::vector<R> h_cxf_;
     // bodies
     int N_ = 0, bcap_ = 0;
     DBuf<R> bf_;

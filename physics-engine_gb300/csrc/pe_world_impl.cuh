@@ -64,6 +64,7 @@ template <class R> ShapeTable<R> World<R>::shapes() const {
     t.h_vbeg = hvbeg_.p; t.h_vcnt = hvcnt_.p; t.h_fbeg = hfbeg_.p; t.h_fcnt = hfcnt_.p; t.h_ebeg = hebeg_.p; t.h_ecnt = hecnt_.p;
     t.hv = hv_.p; t.f_off = hfoff_.p; t.f_idx = hfidx_.p; t.f_n = hfn_.p; t.f_min = hfmin_.p; t.f_max = hfmax_.p;
     t.e_a = hea_.p; t.e_b = heb_.p;
+    t.c_beg = cbeg_.p; t.c_cnt = ccnt_.p; t.c_shape = cshape_.p; t.c_xf = cxf_.p;
     return t;
 }
 
@@ -105,6 +106,7 @@ void World<R>::set_shapes(int S, const int* type, const double* param, const int
     h_hvb_.clear(); h_hvc_.clear(); h_hfb_.clear(); h_hfc_.clear(); h_heb_.clear(); h_hec_.clear(); h_foff_.clear(); h_fidx_.clear();
     h_hv_.clear(); h_fn_.clear(); h_fmn_.clear(); h_fmx_.clear(); h_ea_.clear(); h_eb_.clear();
     hull_by_content_.clear();
+    h_cbeg_.clear(); h_ccnt_.clear(); h_cshape_.clear(); h_cready_.clear(); h_cxf_.clear();
     append_shapes(S, type, param, vbeg, vcnt, fbeg, fcnt, hv, foff, fidx);
 }
 
@@ -165,9 +167,15 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
             h_fmx_.insert(h_fmx_.end(), h.f_max.begin(), h.f_max.end());
             h_ea_.insert(h_ea_.end(), h.e_a.begin(), h.e_a.end());
             h_eb_.insert(h_eb_.end(), h.e_b.begin(), h.e_b.end());
+        } else if (t == ST_COMPOUND && !remap) {
+            inertia = M3<R>();   // set by set_compounds (CompoundShape::init)
         } else {
-            throw std::runtime_error("unsupported shape type " + std::to_string(t));
+            throw std::runtime_error(t == ST_COMPOUND ? "compound shapes are not supported in batched requests"
+                                                      : "unsupported shape type " + std::to_string(t));
         }
+        h_cbeg_.push_back(0);
+        h_ccnt_.push_back(0);
+        h_cready_.push_back(t != ST_COMPOUND);
         h_shull_.push_back(hull);
         h_sinertia_.push_back(inertia);
     }
@@ -181,8 +189,78 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
     upload_tail(hv_, h_hv_, o_v, st_); upload_tail(hfoff_, h_foff_, o_fo, st_); upload_tail(hfidx_, h_fidx_, o_fi, st_);
     upload_tail(hfn_, h_fn_, o_f, st_); upload_tail(hfmin_, h_fmn_, o_f, st_); upload_tail(hfmax_, h_fmx_, o_f, st_);
     upload_tail(hea_, h_ea_, o_e, st_); upload_tail(heb_, h_eb_, o_e, st_);
+    upload_tail(cbeg_, h_cbeg_, s0, st_); upload_tail(ccnt_, h_ccnt_, s0, st_);
     PE_CK(cudaStreamSynchronize(st_));
     return s0;
+}
+
+// CompoundShape::addShape for each child (compound_shape.cpp:7-21) and init() (:25-47) for every
+// compound shape of the table: the children are relocated to their mass-ratio centroid and the
+// compound's unit-mass local inertia is the sum over children of (rot * I_child * rot^T + the
+// parallel-axis term |p|^2 E - p p^T) * ratio / total ratio, in the reference's operation order.
+// With `local_inertia` the children are taken as already initialised and the given inertia is used.
+template <class R>
+void World<R>::set_compounds(const int* cbeg, const int* ccnt, int C, const int* cshape, const double* corg, const double* cbas,
+                             const double* cratio, const double* local_inertia, double* centroid) {
+    if (N_ > 0) throw std::runtime_error("compound shapes must be set before the bodies");
+    h_cshape_.clear();
+    h_cxf_.clear();
+    for (int s = 0; s < S_; s++) {
+        h_cbeg_[s] = 0;
+        h_ccnt_[s] = 0;
+        if (centroid) centroid[s * 3] = centroid[s * 3 + 1] = centroid[s * 3 + 2] = 0;
+        if (h_stype_[s] != ST_COMPOUND) continue;
+        const int b = cbeg[s], n = ccnt[s];
+        if (n < 1 || b < 0 || b + n > C) throw std::runtime_error("compound shape " + std::to_string(s) + ": bad children range");
+        struct Kid { int shape; M3<R> basis; V3<R> origin; R ratio; };
+        std::vector<Kid> kids(n);
+        R total = 0;
+        for (int k = 0; k < n; k++) {
+            Kid& c = kids[k];
+            c.shape = cshape[b + k];
+            if (c.shape < 0 || c.shape >= S_ || h_stype_[c.shape] == ST_COMPOUND)
+                throw std::runtime_error("compound shape " + std::to_string(s) + ": a child must name a non-compound shape");
+            c.ratio = R(cratio[b + k]);
+            if (c.ratio < eps<R>()) throw std::runtime_error("mass ratio must be greater than 0");
+            for (int r = 0; r < 3; r++) for (int q = 0; q < 3; q++) c.basis.m[r][q] = R(cbas[(size_t)(b + k) * 9 + r * 3 + q]);
+            c.origin = V3<R>(R(corg[(size_t)(b + k) * 3]), R(corg[(size_t)(b + k) * 3 + 1]), R(corg[(size_t)(b + k) * 3 + 2]));
+            total += c.ratio;
+        }
+        M3<R> L;
+        if (local_inertia) {
+            for (int r = 0; r < 3; r++) for (int q = 0; q < 3; q++) L.m[r][q] = R(local_inertia[(size_t)s * 9 + r * 3 + q]);
+        } else {
+            V3<R> cen(0, 0, 0);
+            for (auto& c : kids) cen = cen + c.origin * c.ratio;
+            cen = cen / total;
+            for (auto& c : kids) {
+                const V3<R> p = c.origin - cen;
+                c.origin = p;
+                M3<R> t;
+                const R pp = p.x * p.x + p.y * p.y + p.z * p.z;
+                for (int i = 0; i < 3; i++) t.m[i][i] = pp;
+                for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) t.m[i][j] -= p[i] * p[j];
+                const M3<R> a = world_inertia(c.basis, h_sinertia_[c.shape]);
+                const R k = c.ratio / total;
+                for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) L.m[i][j] = L.m[i][j] + (a.m[i][j] + t.m[i][j]) * k;
+            }
+            if (centroid) { centroid[s * 3] = cen.x; centroid[s * 3 + 1] = cen.y; centroid[s * 3 + 2] = cen.z; }
+        }
+        h_sinertia_[s] = L;
+        h_cbeg_[s] = (int)h_cshape_.size();
+        h_ccnt_[s] = n;
+        h_cready_[s] = 1;
+        for (auto& c : kids) {
+            h_cshape_.push_back(c.shape);
+            for (int r = 0; r < 3; r++) for (int q = 0; q < 3; q++) h_cxf_.push_back(c.basis.m[r][q]);
+            h_cxf_.push_back(c.origin.x); h_cxf_.push_back(c.origin.y); h_cxf_.push_back(c.origin.z);
+        }
+    }
+    upload(cbeg_, h_cbeg_, st_);
+    upload(ccnt_, h_ccnt_, st_);
+    upload(cshape_, h_cshape_, st_);
+    upload(cxf_, h_cxf_, st_);
+    PE_CK(cudaStreamSynchronize(st_));
 }
 
 // RigidBody::setMass + setCollisionShape (rigidbody.cpp:11-41) and the initial pose: body j of a
@@ -227,6 +305,7 @@ void World<R>::set_bodies(int n, const int* shape, const int* flags, const doubl
     std::vector<R> f((size_t)NBF * bcap_, R(0));
     for (int i = 0; i < n; i++) {
         if (shape[i] < 0 || shape[i] >= S_) throw std::runtime_error("body " + std::to_string(i) + ": bad shape index");
+        if (!h_cready_[shape[i]]) throw std::runtime_error("body " + std::to_string(i) + ": compound shape without children");
         fill_body(f.data(), bcap_, i, shape[i], mass[i], fr[i], re[i], ld[i], ad[i], o + i * 3, b + i * 9, v + i * 3, w + i * 3);
     }
     upload(bf_, f, st_);
@@ -449,6 +528,9 @@ template <class R> void World<R>::narrowphase() {
                            prev_res_off_.p, (const R*)sat_out_.p);
                     break;
                 }
+                case PC_COMPOUND:
+                    launch(K_NP, g, k_np_compound<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
+                    break;
                 default:   // PC_CONVEX_BIG
                     launch(K_NP_SAT, grid_warps(hi - lo), k_np_sat_big<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,
                            pair_scene_off_.p, prev_res_off_.p);

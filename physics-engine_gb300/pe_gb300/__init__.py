@@ -44,6 +44,7 @@ def load(build_if_missing: bool = True):
         "pe_gpu_last_error": (C.c_char_p, [P]),
         "pe_gpu_set_shapes": (I, [P, I, ip, dp, ip, ip, ip, ip, I, dp, I, ip, ip]),
         "pe_gpu_set_bodies": (I, [P, I, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, dp]),
+        "pe_gpu_set_compounds": (I, [P, ip, ip, I, ip, dp, dp, dp, P, dp]),
         "pe_gpu_set_scenes": (I, [P, I, ip]),
         "pe_gpu_set_params": (I, [P, D, D, D, D, I]),
         "pe_gpu_step": (I, [P, I, I]),
@@ -111,6 +112,14 @@ class GpuWorld:
             self.h, s.n_shapes, _i32(s.shape_type), _f64(s.shape_param).ravel(), _i32(s.hull_vbeg), _i32(s.hull_vcnt),
             _i32(s.hull_fbeg), _i32(s.hull_fcnt), len(s.hull_verts), _f64(s.hull_verts).ravel() if len(s.hull_verts) else np.zeros(1),
             len(s.hull_face_off) - 1, _i32(s.hull_face_off), _i32(s.hull_face_idx) if len(s.hull_face_idx) else np.zeros(1, np.int32)))
+        self.centroids = np.zeros((s.n_shapes, 3))
+        if (np.asarray(s.shape_type) == 5).any():   # compound shapes: addShape + init()
+            cb, cc = s.compound_tables()
+            C_ = s.n_children
+            self._ck(self.lib.pe_gpu_set_compounds(
+                self.h, _i32(cb), _i32(cc), C_, _i32(s.child_shape) if C_ else np.zeros(1, np.int32),
+                _f64(s.child_origin).ravel() if C_ else np.zeros(3), _f64(s.child_basis).ravel() if C_ else np.zeros(9),
+                _f64(s.child_ratio) if C_ else np.zeros(1), None, self.centroids.reshape(-1)))
         self._ck(self.lib.pe_gpu_set_bodies(
             self.h, s.n_bodies, _i32(s.body_shape), _i32(s.body_flags), _f64(s.mass), _f64(s.friction), _f64(s.restitution),
             _f64(s.lin_damp), _f64(s.ang_damp), _f64(s.origin).ravel(), _f64(s.basis).ravel(), _f64(s.lin_vel).ravel(),

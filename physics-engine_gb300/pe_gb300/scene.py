@@ -30,10 +30,12 @@ from pathlib import Path
 import numpy as np
 
 BOX, SPHERE, CYLINDER, HULL = 0, 1, 2, 3
+COMPOUND = 5   # ShapeType::ST_Compound (ST_ConcaveMesh = 4 is not on the path)
 KINEMATIC = 1
 IGNORE_COLLISION = 2   # RigidBody::setIgnoreCollision: the body takes part in no pair
 
 MAGIC = b"PESCENE1"
+MAGIC_COMPOUND = b"PESCENE2"   # the same layout followed by the compound-children tables
 
 
 @dataclasses.dataclass
@@ -64,6 +66,33 @@ class Scene:
     basis: np.ndarray = None           # float64 [N,3,3]
     lin_vel: np.ndarray = None         # float64 [N,3]
     ang_vel: np.ndarray = None         # float64 [N,3]
+    # compound shapes (CompoundShape::addShape arguments, before init() relocates them): shape s of
+    # type COMPOUND owns children [cmp_beg[s], cmp_beg[s] + cmp_cnt[s]); a child names a
+    # non-compound shape of the same table and its local transform and mass ratio
+    cmp_beg: np.ndarray = None         # int32 [S]
+    cmp_cnt: np.ndarray = None         # int32 [S]
+    child_shape: np.ndarray = None     # int32 [C]
+    child_origin: np.ndarray = None    # float64 [C,3]
+    child_basis: np.ndarray = None     # float64 [C,3,3]
+    child_ratio: np.ndarray = None     # float64 [C]
+
+    def __post_init__(self):
+        if self.child_shape is None:
+            self.child_shape = np.zeros(0, np.int32)
+            self.child_origin = np.zeros((0, 3))
+            self.child_basis = np.zeros((0, 3, 3))
+            self.child_ratio = np.zeros(0)
+
+    @property
+    def n_children(self) -> int:
+        return int(self.child_shape.shape[0])
+
+    def compound_tables(self):
+        """(cmp_beg, cmp_cnt) per shape, zeros where the scene has no compound shapes."""
+        S = self.n_shapes
+        if self.cmp_beg is None:
+            return np.zeros(S, np.int32), np.zeros(S, np.int32)
+        return self.cmp_beg, self.cmp_cnt
 
     @property
     def n_bodies(self) -> int:
@@ -82,7 +111,7 @@ class Scene:
             s.dt = float(np.float32(self.dt))
             s.gravity = tuple(float(np.float32(g)) for g in self.gravity)
             for f in ("shape_param", "hull_verts", "mass", "friction", "restitution", "lin_damp",
-                      "ang_damp", "origin", "basis", "lin_vel", "ang_vel"):
+                      "ang_damp", "origin", "basis", "lin_vel", "ang_vel", "child_origin", "child_basis", "child_ratio"):
                 setattr(s, f, r(getattr(self, f)))
         return s
 
@@ -90,8 +119,9 @@ class Scene:
     def write(self, path) -> None:
         """Write the little-endian ``.pescene`` layout read by every consumer of a scene."""
         S, N = self.n_shapes, self.n_bodies
+        compound = self.n_children > 0 or bool((self.shape_type == COMPOUND).any())
         with open(path, "wb") as f:
-            f.write(MAGIC)
+            f.write(MAGIC_COMPOUND if compound else MAGIC)
             f.write(struct.pack("<6i", S, N, len(self.hull_verts), len(self.hull_face_off) - 1,
                                 len(self.hull_face_idx), int(self.iterations)))
             f.write(struct.pack("<4d", float(self.dt), *map(float, self.gravity)))
@@ -103,11 +133,17 @@ class Scene:
                          (self.ang_damp, "<f8"), (self.origin, "<f8"), (self.basis, "<f8"),
                          (self.lin_vel, "<f8"), (self.ang_vel, "<f8")):
                 f.write(np.ascontiguousarray(a, dtype=t).tobytes())
+            if compound:
+                cb, cc = self.compound_tables()
+                f.write(struct.pack("<i", self.n_children))
+                for a, t in ((cb, "<i4"), (cc, "<i4"), (self.child_shape, "<i4"), (self.child_origin, "<f8"),
+                             (self.child_basis, "<f8"), (self.child_ratio, "<f8")):
+                    f.write(np.ascontiguousarray(a, dtype=t).tobytes())
 
     @staticmethod
     def read(path, real_bits: int = 64) -> "Scene":
         b = Path(path).read_bytes()
-        if b[:8] != MAGIC:
+        if b[:8] not in (MAGIC, MAGIC_COMPOUND):
             raise ValueError("not a .pescene file")
         S, N, HV, HF, HI, iters = struct.unpack_from("<6i", b, 8)
         dt, gx, gy, gz = struct.unpack_from("<4d", b, 32)
@@ -133,6 +169,13 @@ class Scene:
         s.basis = take(N * 9, "<f8", (N, 3, 3))
         s.lin_vel = take(N * 3, "<f8", (N, 3))
         s.ang_vel = take(N * 3, "<f8", (N, 3))
+        if b[:8] == MAGIC_COMPOUND:
+            C = int(take(1, "<i4")[0])
+            s.cmp_beg, s.cmp_cnt = take(S, "<i4"), take(S, "<i4")
+            s.child_shape = take(C, "<i4")
+            s.child_origin = take(C * 3, "<f8", (C, 3))
+            s.child_basis = take(C * 9, "<f8", (C, 3, 3))
+            s.child_ratio = take(C, "<f8")
         return s
 
 
@@ -159,6 +202,34 @@ class SceneBuilder:
             self.shape_key[key] = len(self.shapes) - 1
         return self.shape_key[key]
 
+    def compound(self, children):
+        """A compound shape (CompoundShape::addShape for each child): children are
+        (shape, origin, basis or None, mass ratio) with shape a non-compound shape of this builder.
+        Every consumer runs CompoundShape::init() on it (children relocated to their mass-ratio
+        centroid, local inertia from theirs); compound_centroid gives the relocation vector."""
+        if not children:
+            raise ValueError("a compound shape needs at least one child")
+        kids = []
+        for sh, o, b, r in children:
+            if self.shapes[sh][0] == COMPOUND:
+                raise ValueError("CompoundShape cannot contain another CompoundShape")
+            if not r >= 1e-5:   # compound_shape.cpp:14-16 (PE_EPS)
+                raise ValueError("mass ratio must be greater than 0")
+            kids.append((int(sh), np.asarray(o, np.float64), np.eye(3) if b is None else np.asarray(b, np.float64),
+                         float(r)))
+        self.shapes.append((COMPOUND, (0.0, 0.0, 0.0), kids))
+        return len(self.shapes) - 1
+
+    def compound_centroid(self, shape):
+        """The vector CompoundShape::init() returns (compound_shape.cpp:27-33): the mass-ratio
+        weighted mean of the children's origins, summed in child order."""
+        kids = self.shapes[shape][2]
+        c, total = np.zeros(3), 0.0
+        for _, o, _, r in kids:
+            c = c + o * r
+            total += r
+        return c / total
+
     def body(self, shape, origin, basis=None, mass=1.0, v=(0, 0, 0), w=(0, 0, 0), friction=0.5,
              restitution=0.5, kinematic=False, lin_damp=0.0, ang_damp=0.0, ignore_collision=False):
         basis = np.eye(3) if basis is None else np.asarray(basis, np.float64)
@@ -177,7 +248,12 @@ class SceneBuilder:
         vbeg, vcnt, fbeg, fcnt = (np.zeros(S, np.int32) for _ in range(4))
         verts, face_off, face_idx = [], [0], []
         nv = nf = 0
+        cmp_beg, cmp_cnt = np.zeros(S, np.int32), np.zeros(S, np.int32)
+        kids = []
         for i, (t, _, h) in enumerate(self.shapes):
+            if t == COMPOUND:
+                cmp_beg[i], cmp_cnt[i] = len(kids), len(h)
+                kids.extend(h)
             if t != HULL:
                 continue
             hv, hf = self.hulls[h]
@@ -192,6 +268,12 @@ class SceneBuilder:
         s.hull_verts = np.concatenate(verts) if verts else np.zeros((0, 3))
         s.hull_face_off = np.array(face_off, np.int32)
         s.hull_face_idx = np.array(face_idx, np.int32)
+        if kids:
+            s.cmp_beg, s.cmp_cnt = cmp_beg, cmp_cnt
+            s.child_shape = np.array([k[0] for k in kids], np.int32)
+            s.child_origin = np.array([k[1] for k in kids], np.float64).reshape(-1, 3)
+            s.child_basis = np.array([k[2] for k in kids], np.float64).reshape(-1, 3, 3)
+            s.child_ratio = np.array([k[3] for k in kids], np.float64)
         B = self.bodies
         s.body_shape = np.array([b[0] for b in B], np.int32)
         s.body_flags = np.array([b[1] for b in B], np.int32)
@@ -373,6 +455,62 @@ def pair_zoo(kind_a, kind_b, m=64, seed=0, spacing=20.0, real_bits=64, hull_rang
     return sb.build(real_bits)
 
 
+def _rot(axis, angle):
+    c, s_ = np.cos(angle), np.sin(angle)
+    x, y, z = axis
+    return np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s_, x * z * (1 - c) + y * s_],
+                     [y * x * (1 - c) + z * s_, c + y * y * (1 - c), y * z * (1 - c) - x * s_],
+                     [z * x * (1 - c) - y * s_, z * y * (1 - c) + x * s_, c + z * z * (1 - c)]])
+
+
+def compound_pile(n=24, seed=0, real_bits=64, dt=1.0 / 60.0, iterations=10, spacing=2.6, drop=(0.5, 3.0),
+                  n_primitives=12, friction=0.5, restitution=0.3, hull_children=True) -> Scene:
+    """Compound bodies dropped on a static ground box among primitive bodies.  Three compound
+    kinds rotate through the ``n`` compounds: the reference's compound demo "jack" (a unit box
+    hub, a long cylinder up, short cylinders down and along +-x, +-z, mass ratios 0.3 / 0.2 /
+    0.1, examples/compound_demo/main.cpp:48-80), a dumbbell (two spheres on a cylinder bar), and
+    a box with a convex-hull cap.  Bodies are placed like the demo: the body origin minus the
+    centroid init() returns.  The primitives (box, sphere, cylinder, hull) fall among them so
+    that pairs meet compounds on both sides of the pair order."""
+    rng = np.random.default_rng(seed)
+    sb = SceneBuilder(dt=dt, iterations=iterations)
+    g = sb.shape(BOX, (60.0, 1.0, 60.0))
+    sb.body(g, (0.0, -0.5, 0.0), mass=0.0, friction=friction, restitution=restitution, kinematic=True)
+    hub = sb.shape(BOX, (1.0, 1.0, 1.0))
+    long_arm = sb.shape(CYLINDER, (0.2, 2.0))
+    arm = sb.shape(CYLINDER, (0.2, 1.0))
+    rz, rx = _rot((0, 0, 1), np.pi / 2), _rot((1, 0, 0), np.pi / 2)
+    jack = sb.compound([(hub, (0, 0, 0), None, 0.3), (long_arm, (0, 1.5, 0), None, 0.2), (arm, (0, -1, 0), None, 0.1),
+                        (arm, (1, 0, 0), rz, 0.1), (arm, (-1, 0, 0), rz, 0.1), (arm, (0, 0, 1), rx, 0.1),
+                        (arm, (0, 0, -1), rx, 0.1)])
+    ball = sb.shape(SPHERE, (0.45,))
+    bar = sb.shape(CYLINDER, (0.12, 1.6))
+    dumbbell = sb.compound([(ball, (-0.9, 0, 0), None, 0.4), (ball, (0.9, 0, 0), None, 0.4), (bar, (0, 0, 0), rz, 0.2)])
+    kinds = [jack, dumbbell]
+    if hull_children:
+        hv, hf = random_hull(rng, 12, 0.6)
+        cap = sb.shape(HULL, hull=(hv, hf))
+        base = sb.shape(BOX, (1.2, 0.6, 1.2))
+        kinds.append(sb.compound([(base, (0, 0, 0), None, 0.6), (cap, (0.1, 0.55, -0.05), _rot((0, 1, 0), 0.3), 0.4)]))
+    side = int(np.ceil(np.sqrt(n + n_primitives)))
+    slots = rng.permutation(side * side)[:n + n_primitives]
+    rots = random_rotations(rng, n + n_primitives)
+    for i, slot in enumerate(slots):
+        cx, cz = divmod(int(slot), side)
+        o = np.array([(cx - (side - 1) / 2) * spacing, 2.5 + rng.uniform(*drop) + 1.5 * (i % 3),
+                      (cz - (side - 1) / 2) * spacing])
+        v = (0.0, rng.uniform(-1.0, 0.0), 0.0)
+        w = rng.normal(size=3) * 0.5
+        if i < n:
+            c = kinds[i % len(kinds)]
+            sb.body(c, o - sb.compound_centroid(c), rots[i], mass=float(rng.uniform(1.0, 4.0)), v=v, w=w,
+                    friction=friction, restitution=restitution)
+        else:
+            _random_body(sb, rng, (BOX, SPHERE, CYLINDER, HULL)[i % 4], o, 300.0, rots[i], v, w, friction=friction,
+                         restitution=restitution, hull_range=(8, 16))
+    return sb.build(real_bits)
+
+
 def concat(scenes):
     """Scenes side by side in one Scene (bodies of scene i at [off[i], off[i+1])); shapes are
     concatenated and re-indexed.  Used for batched stepping of independent scenes."""
@@ -384,7 +522,16 @@ def concat(scenes):
                             "ang_damp", "origin", "basis", "lin_vel", "ang_vel")}
     face_off = [0]
     offs = [0]
+    kid_cols = {k: [] for k in ("cmp_beg", "cmp_cnt", "child_shape", "child_origin", "child_basis", "child_ratio")}
+    kb = 0
     for s in scenes:
+        cb, cc = s.compound_tables()
+        kid_cols["cmp_beg"].append(cb + kb)
+        kid_cols["cmp_cnt"].append(cc)
+        kid_cols["child_shape"].append(s.child_shape + sh_base)
+        for k in ("child_origin", "child_basis", "child_ratio"):
+            kid_cols[k].append(getattr(s, k))
+        kb += s.n_children
         if (s.dt, tuple(s.gravity), s.iterations) != (first.dt, tuple(first.gravity), first.iterations):
             raise ValueError("batched scenes must share dt, gravity and iterations")
         cols["shape_type"].append(s.shape_type)
@@ -409,6 +556,12 @@ def concat(scenes):
         setattr(out, k, np.concatenate(v))
     out.hull_verts = out.hull_verts.reshape(-1, 3)
     out.hull_face_off = np.array(face_off, np.int32)
+    if kb:
+        for k, v in kid_cols.items():
+            setattr(out, k, np.concatenate(v))
+        out.child_shape = out.child_shape.astype(np.int32)
+        out.child_origin = out.child_origin.reshape(-1, 3)
+        out.child_basis = out.child_basis.reshape(-1, 3, 3)
     return out, np.array(offs, np.int32)
 
 

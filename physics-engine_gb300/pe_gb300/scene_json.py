@@ -17,9 +17,15 @@ into a ``Scene`` for the GPU world, following the reference loader's rules:
 
 * a body without a ``type``, or with a type the loader does not know, is skipped (:535-545).
 
+* ``compound`` bodies take their children from ``shapes`` (:438-531).  The reference loader never
+  calls ``CompoundShape::init()``, which leaves the compound's inertia uninitialised; here every
+  consumer runs ``init()`` (children relocated to their mass-ratio centroid, inertia from the
+  children) and the loader moves the body origin by the rotated centroid, so each child stays
+  where the file places it.
+
 What the rigid-body step here does not model is reported rather than silently dropped:
-``convex`` / ``concave`` / ``compound`` bodies raise ``UnsupportedScene`` (convex meshes come from
-OBJ files, concave and compound shapes are outside the step); fracturable bodies step as plain
+``convex`` / ``concave`` bodies and convex sub-shapes raise ``UnsupportedScene`` (convex meshes
+come from OBJ files, concave meshes are outside the step); fracturable bodies step as plain
 rigid bodies and ``DamageSources`` are not applied (no fracture solver), and sleep thresholds,
 finite lifetimes and tags are ignored (sleeping, lifetimes and the "wheel" tag are not on the
 path).  These, and the skipped bodies, are listed in ``ignored``.
@@ -96,6 +102,56 @@ def _array(node, key, size):
     return [float(x) for x in v]
 
 
+def _rotation(node, where):
+    rot = _array(node, "rotation", 0)
+    if rot is None:
+        return np.eye(3)
+    if len(rot) >= 9:
+        return np.array(rot[:9]).reshape(3, 3)
+    if len(rot) >= 4:
+        return quat_to_basis(np.array(rot[:4]))
+    raise ValueError(f"{where}: invalid rotation data")
+
+
+def _primitive(sb, node, kind):
+    """box / sphere / cylinder shape of a body or compound sub-shape (simulator.cpp:379-395, :472-490)."""
+    if kind == "box":
+        return sb.shape(BOX, _array(node, "scale", 3) or [1.0, 1.0, 1.0])
+    if kind == "sphere":
+        r = _array(node, "scale", 1)
+        return sb.shape(SPHERE, (r[0] if r else 1.0,))
+    return sb.shape(CYLINDER, _array(node, "scale", 2) or [0.5, 1.0])
+
+
+def _compound(sb, rb, idx):
+    """CompoundShape from the "shapes" list (simulator.cpp:438-531): per sub-shape a mass ratio
+    (default 1), a position (3 numbers), a rotation and a box / sphere / cylinder type with the
+    body rules for "scale".  The reference deletes the body and goes on iterating its sub-shapes
+    when a sub-shape is invalid (a use after free); here such a file is an error."""
+    kids = _list(rb, "shapes")
+    if kids is None:
+        return None
+    children = []
+    for k, node in enumerate(kids):
+        where = f"body {idx} sub-shape {k}"
+        if not isinstance(node, dict):
+            raise ValueError("node shapes should have elements of type object")
+        ratio = _number(node, "mass_ratio")
+        pos = _array(node, "position", 3) or [0.0, 0.0, 0.0]
+        rot = _rotation(node, where)
+        sub = _string(node, "type")
+        if sub == "convex":
+            raise UnsupportedScene(f"{where}: 'convex' sub-shapes are not handled by this loader")
+        if sub in ("compound", "concave"):
+            raise ValueError(f"{where}: compound sub-shapes cannot be compound or concave")
+        if sub not in ("box", "sphere", "cylinder"):
+            raise ValueError(f"{where}: invalid compound sub-shape type {sub!r}")
+        children.append((_primitive(sb, node, sub), pos, rot, 1.0 if ratio is None else ratio))
+    if not children:
+        raise ValueError(f"body {idx}: a compound needs at least one sub-shape")
+    return sb.compound(children)
+
+
 def load_scene_json(path, real_bits: int = 64, dt: float = 1.0 / 60.0, iterations: int = 10):
     """Returns (Scene, ignored): the scene and the list of file features the step does not model."""
     data = json.loads(Path(path).read_text())
@@ -122,7 +178,7 @@ def load_scene_json(path, real_bits: int = 64, dt: float = 1.0 / 60.0, iteration
         if not isinstance(rb, dict):
             raise ValueError("node RigidBodies should have elements of type object")
         kind = _string(rb, "type")
-        if kind in ("convex", "concave", "compound"):
+        if kind in ("convex", "concave"):
             raise UnsupportedScene(f"body {idx}: '{kind}' shapes are not handled by this loader")
         if _boolean(rb, "fracturable"):
             ignored.append(f"body {idx}: fracturable (stepped as a rigid body)")
@@ -145,32 +201,26 @@ def load_scene_json(path, real_bits: int = 64, dt: float = 1.0 / 60.0, iteration
         pos = _array(rb, "position", 0) or [0.0, 0.0, 0.0]
         if len(pos) < 3:
             raise ValueError(f"body {idx}: node position should have at least 3 elements")
-        basis = np.eye(3)
-        rot = _array(rb, "rotation", 0)
-        if rot is not None:
-            if len(rot) >= 9:
-                basis = np.array(rot[:9]).reshape(3, 3)
-            elif len(rot) >= 4:
-                basis = quat_to_basis(np.array(rot[:4]))
-            else:
-                raise ValueError(f"body {idx}: invalid rotation data")
+        basis = _rotation(rb, f"body {idx}")
         mass = _number(rb, "mass")
         fr = _number(rb, "friction")
         re = _number(rb, "restitution")
-        if kind not in ("box", "sphere", "cylinder"):
+        if kind not in ("box", "sphere", "cylinder", "compound"):
             # the reference logs the body and goes on without it (simulator.cpp:535-545)
             ignored.append(f"body {idx}: type {kind!r} (body skipped)" if kind else f"body {idx}: no type (body skipped)")
             continue
-        if kind == "box":
-            size = _array(rb, "scale", 3) or [1.0, 1.0, 1.0]
-            shape = sb.shape(BOX, size)
-        elif kind == "sphere":
-            r = _array(rb, "scale", 1)
-            shape = sb.shape(SPHERE, (r[0] if r else 1.0,))
+        origin = np.array(pos[:3])
+        if kind == "compound":
+            shape = _compound(sb, rb, idx)
+            if shape is None:
+                ignored.append(f"body {idx}: compound without sub-shapes (body skipped)")
+                continue
+            # init() relocates the children to their centroid; the body origin moves with them so
+            # that every child stays where the file puts it
+            origin = origin + basis @ sb.compound_centroid(shape)
         else:
-            rh = _array(rb, "scale", 2) or [0.5, 1.0]
-            shape = sb.shape(CYLINDER, rh)
-        sb.body(shape, pos[:3], basis, mass=1.0 if mass is None else mass, v=v, w=w,
+            shape = _primitive(sb, rb, kind)
+        sb.body(shape, origin, basis, mass=1.0 if mass is None else mass, v=v, w=w,
                 friction=0.5 if fr is None else fr, restitution=0.5 if re is None else re, kinematic=kinematic,
                 lin_damp=ld, ang_damp=ad, ignore_collision=ignore_collision)
     return sb.build(real_bits), ignored

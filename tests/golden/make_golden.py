@@ -38,6 +38,10 @@ CASES = {
     "pile_f32": (lambda: sc.pile(48, seed=6, real_bits=32, hull_range=(8, 24), drop=(0.0, 0.3)), 32, 40,
                  [0, 1, 24, 25, 38, 39]),
 }
+# compound bodies (jacks, dumbbells, box + hull caps) among primitives on a ground box
+for bits in (64, 32):
+    CASES[f"compound_f{bits}"] = (lambda bits=bits: sc.compound_pile(n=24, seed=3 + bits, drop=(0.0, 0.5), real_bits=bits),
+                                  bits, 120, [0, 1, 2, 30, 31, 45, 60, 61, 90, 91, 118, 119])
 # the reference's own sample scene (a bomb sphere at 70 m/s into a 15-box tower on a kinematic
 # ground), read by the scene-file loader; the sphere reaches the tower near step 57
 SAMPLES = Path("/root/reference/SampleScenes")
@@ -45,6 +49,12 @@ for bits in (64, 32):
     CASES[f"json_bomb_tower_smaller_f{bits}"] = (
         lambda bits=bits: load_scene_json(SAMPLES / "bomb_crash_tower_smaller.json", real_bits=bits)[0], bits, 120,
         [0, 1, 30, 55, 56, 57, 58, 59, 60, 61, 62, 90, 119])
+# the reference's sample scene compound.json: ten compound bodies (box hubs with cylinder arms)
+# and four primitives dropped onto a kinematic ground box
+for bits in (64, 32):
+    CASES[f"json_compound_f{bits}"] = (
+        lambda bits=bits: load_scene_json(SAMPLES / "compound.json", real_bits=bits)[0], bits, 150,
+        [0, 1, 40, 60, 61, 90, 91, 120, 148, 149])
 for a in range(4):
     for b in range(a, 4):
         CASES[f"zoo_{a}{b}_f64"] = (lambda a=a, b=b: sc.pair_zoo(a, b, m=48, seed=100 + 4 * a + b, real_bits=64), 64, 2, [0, 1])

@@ -58,7 +58,8 @@ def test_gpu_phases_match_reference(name):
             compare_state(g.state(), dump_state(d), what=f"{name} integrate step {k}")
 
 
-@pytest.mark.parametrize("name", ["cube_f32", "cube_f64", "zoo_22_f64", "zoo_23_f32", "zoo_33_f64", "pile_f64"])
+@pytest.mark.parametrize("name", ["cube_f32", "cube_f64", "zoo_22_f64", "zoo_23_f32", "zoo_33_f64", "pile_f64", "compound_f64",
+                                  "compound_f32"])
 def test_gpu_full_steps_serial_order_match_reference(name):
     """Whole steps on the device in serial-order mode reproduce the reference trajectory
     (scenes whose sort keys never tie, so the broadphase order is the reference's)."""
@@ -76,12 +77,14 @@ def test_gpu_full_steps_serial_order_match_reference(name):
         compare_results(g.results(), results_of(d), what=f"{name} step {k}")
 
 
-@pytest.mark.parametrize("name", ["json_bomb_tower_smaller_f64", "json_bomb_tower_smaller_f32"])
+@pytest.mark.parametrize("name", ["json_bomb_tower_smaller_f64", "json_bomb_tower_smaller_f32", "json_compound_f64",
+                                  "json_compound_f32"])
 def test_gpu_scene_file_full_steps_match_reference(name):
-    """The reference's sample scene bomb_crash_tower_smaller.json (read by the scene-file loader)
-    stepped on the device in serial-order mode: 119 whole steps reproduce the reference's
-    trajectory through the impact (steps 58-62).  The steps start from the reference's state
-    after step 0, the one step whose sort keys tie (tied keys fix the pair set, not its order)."""
+    """The reference's sample scenes bomb_crash_tower_smaller.json and compound.json (read by the
+    scene-file loader) stepped on the device in serial-order mode: every whole step after the
+    first reproduces the reference's trajectory (through the bomb's impact at steps 58-62; the
+    compounds landing from step 40 on).  The steps start from the reference's state after step 0,
+    the one step whose sort keys tie (tied keys fix the pair set, not its order)."""
     scene, bits, steps, rec = load_golden(name)
     g = pg.GpuWorld(scene, bits)
     d0 = rec[0]
@@ -101,6 +104,27 @@ def test_gpu_scene_file_full_steps_match_reference(name):
         np.testing.assert_array_equal(st["ang_vel"], d["ang_vel_post"])
         np.testing.assert_array_equal(g.pairs(), d["pairs"])
         compare_results(g.results(), results_of(d), what=f"{name} step {k}")
+
+
+def test_gpu_compound_pile_matches_oracle():
+    """300 compound bodies (jacks, dumbbells, box + hull caps) among 200 primitives, FP32: 60
+    whole serial-order steps equal the oracle's, checked every 10 steps (state, pairs, every
+    contact result), so compound-primitive pairs in both orders and compound-compound pairs all
+    run through the compound kernel."""
+    scene = sc.compound_pile(n=300, n_primitives=200, seed=9, spacing=2.4, drop=(0.0, 0.5), real_bits=32)
+    o = orc.OracleWorld(scene, 32, threads=8)
+    g = pg.GpuWorld(scene, 32)
+    comp = np.nonzero(scene.shape_type[scene.body_shape] == sc.COMPOUND)[0]
+    seen = 0
+    for k in range(6):
+        o.step(10)
+        g.step(10, pg.SERIAL_ORDER)
+        compare_state(g.state(), o.state(), what=f"compound pile step {10 * k + 9}")
+        np.testing.assert_array_equal(g.pairs(), o.pairs())
+        ro = o.results()
+        compare_results(g.results(), ro, what=f"compound pile step {10 * k + 9}")
+        seen += int(ro["point_size"][np.isin(ro["res_a"], comp)].sum())
+    assert seen > 200
 
 
 def test_gpu_ignore_collision_bodies_match_oracle():

@@ -102,10 +102,52 @@ def test_unknown_or_missing_types_are_skipped(tmp_path):
     assert any("capsule" in x for x in ignored) and any("no type" in x for x in ignored)
 
 
-@pytest.mark.parametrize("kind", ["convex", "concave", "compound"])
-def test_mesh_and_compound_bodies_are_refused(tmp_path, kind):
+@pytest.mark.parametrize("kind", ["convex", "concave"])
+def test_mesh_bodies_are_refused(tmp_path, kind):
     with pytest.raises(UnsupportedScene):
         load_scene_json(write(tmp_path, {"RigidBodies": [{"type": "box"}, {"type": kind}]}))
+
+
+def test_compound_bodies(tmp_path):
+    """Sub-shapes in file order with their mass ratios (default 1), positions and rotations; the
+    body origin moves by the rotated centroid so that init()'s relocation keeps every child in
+    place."""
+    rz = [0, -1, 0, 1, 0, 0, 0, 0, 1]
+    doc = {"RigidBodies": [{"type": "compound", "position": [1, 2, 3], "rotation": rz, "mass": 2.0, "shapes": [
+        {"type": "box", "scale": [1, 2, 3], "mass_ratio": 0.5},
+        {"type": "sphere", "scale": [0.5], "position": [2, 0, 0]},
+        {"type": "cylinder", "scale": [0.2, 1], "position": [0, 1, 0], "rotation": [1, 0, 0, 0], "mass_ratio": 0.5}]}]}
+    s, ignored = load_scene_json(write(tmp_path, doc))
+    assert ignored == [] and s.n_bodies == 1
+    c = s.body_shape[0]
+    assert s.shape_type[c] == sc.COMPOUND and s.cmp_cnt[c] == 3
+    kids = s.child_shape[s.cmp_beg[c]:s.cmp_beg[c] + 3]
+    assert list(s.shape_type[kids]) == [sc.BOX, sc.SPHERE, sc.CYLINDER]
+    np.testing.assert_array_equal(s.child_ratio, [0.5, 1.0, 0.5])
+    np.testing.assert_array_equal(s.child_origin, [[0, 0, 0], [2, 0, 0], [0, 1, 0]])
+    centroid = np.array([2.0, 0.5, 0.0]) / 2.0
+    np.testing.assert_allclose(s.origin[0], np.array([1, 2, 3]) + np.array(rz, float).reshape(3, 3) @ centroid)
+    # a body written back and read again keeps its children
+    p = tmp_path / "s.pescene"
+    s.write(p)
+    t = sc.Scene.read(p)
+    np.testing.assert_array_equal(t.child_shape, s.child_shape)
+    np.testing.assert_array_equal(t.child_basis, s.child_basis)
+
+
+@pytest.mark.parametrize("sub, err", [({"type": "convex", "mesh": "a.obj"}, UnsupportedScene),
+                                      ({"type": "compound"}, ValueError), ({"type": "concave"}, ValueError),
+                                      ({"type": "capsule"}, ValueError), ({"scale": [1, 1, 1]}, ValueError),
+                                      ({"type": "box", "mass_ratio": 0.0}, ValueError),
+                                      ({"type": "box", "position": [0, 0]}, ValueError)])
+def test_invalid_compound_sub_shapes(tmp_path, sub, err):
+    with pytest.raises(err):
+        load_scene_json(write(tmp_path, {"RigidBodies": [{"type": "compound", "shapes": [{"type": "box"}, sub]}]}))
+
+
+def test_compound_without_sub_shapes_is_skipped(tmp_path):
+    s, ignored = load_scene_json(write(tmp_path, {"RigidBodies": [{"type": "compound"}, {"type": "box"}]}))
+    assert s.n_bodies == 1 and any("compound without sub-shapes" in x for x in ignored)
 
 
 def test_unmodelled_features_are_reported(tmp_path):
@@ -154,6 +196,9 @@ def test_reference_sample_scenes():
     assert s.n_bodies == 2022 and (s.shape_type[s.body_shape] == sc.BOX).sum() == 2021
     s, ignored = load_scene_json(SAMPLES / "urban_combat_layout.json")
     assert s.n_bodies == 401 and any("fracturable" in x for x in ignored)
-    for name in ("compound_smaller.json", "standford_bunny_smaller.json"):
-        with pytest.raises(UnsupportedScene):
-            load_scene_json(SAMPLES / name)
+    s, _ = load_scene_json(SAMPLES / "compound_smaller.json")
+    assert s.n_bodies == 3 and s.n_children == 7
+    s, _ = load_scene_json(SAMPLES / "compound.json")
+    assert s.n_bodies == 14 and (s.shape_type[s.body_shape] == sc.COMPOUND).sum() == 10
+    with pytest.raises(UnsupportedScene):
+        load_scene_json(SAMPLES / "standford_bunny_smaller.json")
