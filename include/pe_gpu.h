@@ -90,6 +90,28 @@ int pe_gpu_set_bodies(pe_gpu_world* w, int n, const int* shape, const int* flags
                       const double* friction, const double* restitution, const double* lin_damp, const double* ang_damp,
                       const double* origin, const double* basis, const double* lin_vel, const double* ang_vel);
 
+/* Joint constraints, all at once, in World::addConstraint order (world.h:90); call after
+ * pe_gpu_set_bodies, which clears them.  Replaces BallJointConstraint / HingeJointConstraint /
+ * SliderJointConstraint with setObjectA/B, setAnchorA/B, setAxisA/B, setUseLimits, setMinAngle,
+ * setMaxAngle, setUseMotor, setTargetSpeed (ball_joint_constraint.h, hinge_joint_constraint.h,
+ * slider_joint_constraint.h).  type[j]: PE_GPU_JOINT_*; bodies[2j..]: bodies A and B; flags[j]:
+ * PE_GPU_JOINT_USE_LIMITS | PE_GPU_JOINT_USE_MOTOR (hinge); params[15j..]: anchor_a, anchor_b,
+ * axis_a, axis_b (3 each, in the bodies' frames), min_angle, max_angle, target_speed.  The solver
+ * runs every contact and then every joint in each iteration, as SequentialImpulseSolver::solve
+ * (sequential_impulse_solver.cpp:60-68); in coloured mode joints take part in the colouring. */
+#define PE_GPU_JOINT_BALL 0
+#define PE_GPU_JOINT_HINGE 1
+#define PE_GPU_JOINT_SLIDER 2
+#define PE_GPU_JOINT_USE_LIMITS 1
+#define PE_GPU_JOINT_USE_MOTOR 2
+int pe_gpu_set_joints(pe_gpu_world* w, int n, const int* type, const int* bodies, const int* flags, const double* params);
+
+/* Body pairs that never collide: RigidBody::addIgnoreCollisionId (rigidbody.h:126) as checked by
+ * BroadPhaseBase::validateCollisionPair (broad_phase_base.cpp:11-12), which excludes a pair when
+ * either body lists the other.  pairs[2k..]: body indices.  Call after pe_gpu_set_bodies, which
+ * clears them; a call replaces the previous pairs. */
+int pe_gpu_set_ignore_pairs(pe_gpu_world* w, int n, const int* pairs);
+
 /* Independent scenes in one world: bodies [body_off[s], body_off[s+1]) form scene s.  Each scene
  * behaves as its own pe_intf::World (own sweep axis, own contact-result pool).  Default: one scene. */
 int pe_gpu_set_scenes(pe_gpu_world* w, int n_scenes, const int* body_off);

@@ -20,6 +20,9 @@ struct SceneFile {
     // local origin, local basis (row-major) and mass ratio
     std::vector<int> cbeg, ccnt, cshape;
     std::vector<double> corg, cbas, cratio;
+    // tagged sections: joints (type, bodies a b, flags, 15 reals) and ignored body pairs
+    std::vector<int> jtype, jbody, jflag, ign;
+    std::vector<double> jreal;
 };
 
 bool read_scene(const char* path, SceneFile& s) {
@@ -44,6 +47,14 @@ bool read_scene(const char* path, SceneFile& s) {
         int C = 0;
         ok = fread(&C, sizeof(int), 1, f) == 1 && C >= 0 && rdi(s.cbeg, s.S) && rdi(s.ccnt, s.S) && rdi(s.cshape, C) &&
              rdd(s.corg, (size_t)C * 3) && rdd(s.cbas, (size_t)C * 9) && rdd(s.cratio, C);
+        int th[2];
+        while (ok && fread(th, sizeof(int), 2, f) == 2) {
+            const int n = th[1];
+            if (n < 0) { ok = false; break; }
+            if (th[0] == 1) ok = rdi(s.jtype, n) && rdi(s.jbody, (size_t)2 * n) && rdi(s.jflag, n) && rdd(s.jreal, (size_t)15 * n);
+            else if (th[0] == 2) ok = rdi(s.ign, (size_t)2 * n);
+            else ok = false;
+        }
     }
     fclose(f);
     return ok;
@@ -121,6 +132,21 @@ template <class R> void build(World<R>& W, const SceneFile& s) {
         b.restitution = R(s.re[i]);
         b.lin_damp = R(s.ld[i]);
         b.ang_damp = R(s.ad[i]);
+    }
+    for (size_t k = 0; k + 1 < s.ign.size(); k += 2) {   // RigidBody::addIgnoreCollisionId
+        W.bodies[s.ign[k]].ignore_ids.push_back(s.ign[k + 1]);
+    }
+    for (size_t k = 0; k < s.jtype.size(); k++) {   // World::addConstraint
+        Joint<R> j;
+        const double* r = &s.jreal[k * 15];
+        j.type = s.jtype[k];
+        j.a = s.jbody[2 * k];
+        j.b = s.jbody[2 * k + 1];
+        j.use_limits = (s.jflag[k] & 1) != 0;
+        j.use_motor = (s.jflag[k] & 2) != 0;
+        j.anchor_a = get3<R>(r); j.anchor_b = get3<R>(r + 3); j.axis_a = get3<R>(r + 6); j.axis_b = get3<R>(r + 9);
+        j.min_angle = R(r[12]); j.max_angle = R(r[13]); j.target_speed = R(r[14]);
+        W.joints.push_back(j);
     }
 }
 

@@ -99,17 +99,17 @@ template <class R> inline M3<R> mscale(const M3<R>& a, R s) {
     return o;
 }
 
-// Eigen's closed-form 3x3 inverse (cofactors / determinant of the first column)
+// Eigen's closed-form 3x3 inverse (Eigen/src/LU/InverseImpl.h, compute_inverse<..., 3>): the
+// determinant expands the cofactors of column 0; entry (r, c) of the inverse is cofactor (c, r) / det
 template <class R> inline M3<R> inverse3(const M3<R>& a) {
-    auto cof = [&](int i, int j) {
+    auto cof = [&](int i, int j) {   // cofactor_3x3<i, j>
         const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-        return a.m[j1][i1] * a.m[j2][i2] - a.m[j1][i2] * a.m[j2][i1];
+        return a.m[i1][j1] * a.m[i2][j2] - a.m[i1][j2] * a.m[i2][j1];
     };
-    const R c0 = cof(0, 0), c1 = cof(1, 0), c2 = cof(2, 0);
-    const R det = sum3(c0 * a.m[0][0], c1 * a.m[1][0], c2 * a.m[2][0], is_double<R>());
+    const R det = sum3(cof(0, 0) * a.m[0][0], cof(1, 0) * a.m[1][0], cof(2, 0) * a.m[2][0], is_double<R>());
     const R inv = R(1) / det;
     M3<R> o;
-    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.m[i][j] = cof(i, j) * inv;
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) o.m[r][c] = cof(c, r) * inv;
     return o;
 }
 

@@ -11,6 +11,7 @@
 #include <thread>
 #include <vector>
 #include "orc_collide.h"
+#include "orc_joints.h"
 
 namespace orc {
 
@@ -82,6 +83,7 @@ template <class R> struct Body {
     int shape = 0;
     bool kinematic = false;
     bool ignore_collision = false;
+    std::vector<int> ignore_ids;   // RigidBody::_ignore_collision_ids, as body indices
     R mass = 1, inv_mass = 1, friction = R(0.5), restitution = R(0.5), lin_damp = 0, ang_damp = 0;
     M3<R> local_inv_inertia = M3<R>::identity(), world_inv_inertia = M3<R>::identity();
     Transform<R> t;
@@ -106,6 +108,7 @@ public:
     std::vector<std::pair<int, int>> pairs;
     std::vector<CResult<R>> results;        // pooled: slots survive between steps (stale distances)
     std::vector<std::vector<Row<R>>> rows;
+    std::vector<Joint<R>> joints;           // World::_constraints (joint constraints, in order)
     Pool* pool = nullptr;
 
     void for_loop(int n, const std::function<void(int)>& f) { if (pool) pool->for_loop(n, f); else for (int i = 0; i < n; i++) f(i); }
@@ -169,6 +172,8 @@ public:
         if (a.ignore_collision || b.ignore_collision) return false;
         if (a.kinematic && b.kinematic) return false;
         if (i == j) return false;
+        for (int k : a.ignore_ids) if (k == j) return false;
+        for (int k : b.ignore_ids) if (k == i) return false;
         if (a.aabb_min.x > b.aabb_max.x || b.aabb_min.x > a.aabb_max.x) return false;
         if (a.aabb_min.y > b.aabb_max.y || b.aabb_min.y > a.aabb_max.y) return false;
         if (a.aabb_min.z > b.aabb_max.z || b.aabb_min.z > a.aabb_max.z) return false;
@@ -268,8 +273,11 @@ public:
                 ci.mu = cr.friction;
             }
         });
-        for (int it = 0; it < iterations; it++)
+        for (auto& j : joints) joint_init(j, bodies[j.a], bodies[j.b], dt, kerp);   // sequential_impulse_solver.cpp:46-48
+        for (int it = 0; it < iterations; it++) {   // :60-68: contacts, then the other constraints
             for (size_t i = 0; i < results.size(); i++) iterate(i);
+            for (auto& j : joints) joint_iterate(j, bodies[j.a], bodies[j.b]);
+        }
         for_loop((int)bodies.size(), [&](int i) {   // syncTempVelocity
             Body<R>& b = bodies[i];
             if (b.kinematic) return;

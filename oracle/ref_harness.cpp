@@ -17,6 +17,9 @@
 #include "rigid/shape/cylinder_shape.h"
 #include "rigid/shape/convex_mesh_shape.h"
 #include "rigid/shape/compound_shape.h"
+#include "rigid/constraint/constraint/ball_joint_constraint.h"
+#include "rigid/constraint/constraint/hinge_joint_constraint.h"
+#include "rigid/constraint/constraint/slider_joint_constraint.h"
 #include "rigid/collision/broad_phase/broad_phase_sweep_and_prune.h"
 #include "rigid/constraint/constraint_solver/sequential_impulse_solver.h"
 #include "utils/thread_pool.h"
@@ -39,6 +42,8 @@ struct Scene {
     std::vector<double> param, hverts, mass, friction, restitution, lin_damp, ang_damp, origin, basis, v, w;
     std::vector<int> cbeg, ccnt, cshape;   // compound children ("PESCENE2")
     std::vector<double> corigin, cbasis, cratio;
+    std::vector<int> jtype, jbody, jflag, ign;   // tagged sections: joints, ignored body pairs
+    std::vector<double> jreal;
 };
 
 template <class T> void rd(FILE* f, T* p, size_t n) {
@@ -86,6 +91,20 @@ Scene load(const char* path) {
         s.corigin.resize(C * 3); rd(f, s.corigin.data(), C * 3);
         s.cbasis.resize(C * 9); rd(f, s.cbasis.data(), C * 9);
         s.cratio.resize(C); rd(f, s.cratio.data(), C);
+        int th[2];
+        while (fread(th, sizeof(int), 2, f) == 2) {
+            const int n = th[1];
+            if (th[0] == 1) {
+                s.jtype.resize(n); rd(f, s.jtype.data(), n);
+                s.jbody.resize(2 * n); rd(f, s.jbody.data(), 2 * n);
+                s.jflag.resize(n); rd(f, s.jflag.data(), n);
+                s.jreal.resize(15 * n); rd(f, s.jreal.data(), 15 * n);
+            } else if (th[0] == 2) {
+                s.ign.resize(2 * n); rd(f, s.ign.data(), 2 * n);
+            } else {
+                fprintf(stderr, "unknown scene section %d\n", th[0]); _exit(2);
+            }
+        }
     }
     fclose(f);
     return s;
@@ -267,8 +286,10 @@ int main(int argc, char** argv) {
         cs->init();
         shapes[i] = cs;
     }
+    std::vector<pe_phys_object::RigidBody*> rbs;
     for (int i = 0; i < s.n_bodies; i++) {
         auto* rb = new pe_phys_object::RigidBody();
+        rbs.push_back(rb);
         rb->setMass(PE_R(s.mass[i]));
         rb->setCollisionShape(shapes[s.shape[i]]);
         pe::Matrix3 b;
@@ -284,6 +305,31 @@ int main(int argc, char** argv) {
         rb->setIgnoreCollision((s.flags[i] & 2) != 0);
         world->addRigidBody(rb);
         g_dump.index[rb] = i;
+    }
+
+    for (size_t k = 0; k + 1 < s.ign.size(); k += 2) rbs[s.ign[k]]->addIgnoreCollisionId(rbs[s.ign[k + 1]]->getGlobalId());
+    for (size_t k = 0; k < s.jtype.size(); k++) {
+        const double* r = &s.jreal[k * 15];
+        auto v3 = [&](int o) { return pe::Vector3(PE_R(r[o]), PE_R(r[o + 1]), PE_R(r[o + 2])); };
+        pe_phys_constraint::Constraint* c = nullptr;
+        if (s.jtype[k] == 0) {
+            auto* j = new pe_phys_constraint::BallJointConstraint();
+            j->setAnchorA(v3(0)); j->setAnchorB(v3(3));
+            c = j;
+        } else if (s.jtype[k] == 1) {
+            auto* j = new pe_phys_constraint::HingeJointConstraint();
+            j->setAnchorA(v3(0)); j->setAnchorB(v3(3)); j->setAxisA(v3(6)); j->setAxisB(v3(9));
+            j->setUseLimits((s.jflag[k] & 1) != 0); j->setMinAngle(PE_R(r[12])); j->setMaxAngle(PE_R(r[13]));
+            j->setUseMotor((s.jflag[k] & 2) != 0); j->setTargetSpeed(PE_R(r[14]));
+            c = j;
+        } else {
+            auto* j = new pe_phys_constraint::SliderJointConstraint();
+            j->setAnchorA(v3(0)); j->setAnchorB(v3(3)); j->setAxisA(v3(6)); j->setAxisB(v3(9));
+            c = j;
+        }
+        c->setObjectA(rbs[s.jbody[2 * k]]);
+        c->setObjectB(rbs[s.jbody[2 * k + 1]]);
+        world->addConstraint(c);
     }
 
     g_dump.f = dump_none ? nullptr : fopen(argv[2], "wb");

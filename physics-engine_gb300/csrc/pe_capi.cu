@@ -81,6 +81,16 @@ int pe_gpu_set_bodies(pe_gpu_world* h, int n, const int* shape, const int* flags
     return guard(h, [&](pe::WorldBase& W) { W.set_bodies(n, shape, flags, mass, fr, re, ld, ad, o, b, v, w); return PE_GPU_OK; });
 }
 
+int pe_gpu_set_joints(pe_gpu_world* h, int n, const int* type, const int* bodies, const int* flags, const double* params) {
+    if (n < 0 || (n > 0 && (!type || !bodies || !flags || !params))) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_joints(n, type, bodies, flags, params); return PE_GPU_OK; });
+}
+
+int pe_gpu_set_ignore_pairs(pe_gpu_world* h, int n, const int* pairs) {
+    if (n < 0 || (n > 0 && !pairs)) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_ignore_pairs(n, pairs); return PE_GPU_OK; });
+}
+
 int pe_gpu_set_scenes(pe_gpu_world* h, int n, const int* off) {
     if (n < 1 || !off) return PE_GPU_ERR_ARG;
     return guard(h, [&](pe::WorldBase& w) { w.set_scenes(n, off); return PE_GPU_OK; });

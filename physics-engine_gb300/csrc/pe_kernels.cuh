@@ -122,7 +122,8 @@ __global__ void k_bp_gather(Bodies<R> B, const uint32_t* order, R* smn, R* smx, 
 constexpr int kStage = 4;
 template <class R, bool WRITE>
 __device__ __forceinline__ int sweep_warp(int i, int n, int lane, const int* scene_axis, const R* smn, const R* smx,
-                                          const int* sflag, const int* sscene, int* stage, int2* out, const uint32_t* order) {
+                                          const int* sflag, const int* sscene, int* stage, int2* out, const uint32_t* order,
+                                          const IgnoreLists& ign) {
     const int sc = sscene[i];
     const int ax = scene_axis[sc];
     const R* amin = smn + (size_t)ax * n;
@@ -144,6 +145,7 @@ __device__ __forceinline__ int sweep_warp(int i, int n, int lane, const int* sce
             hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
                   !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
                   !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
+            if (hit && ign.off && ((fi | fj) & BF_IGN_LIST)) hit = !ign.ignored(i, j);
         }
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (hit) {
@@ -170,7 +172,7 @@ __device__ __forceinline__ bool big_window(int i, int n, const int* scene_axis, 
 }
 template <class R, bool WRITE>
 __device__ int sweep_block(int i, int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
-                           int2* out, const uint32_t* order, int* wcnt) {
+                           int2* out, const uint32_t* order, int* wcnt, const IgnoreLists& ign) {
     const int sc = sscene[i];
     const int ax = scene_axis[sc];
     const R* amin = smn + (size_t)ax * n;
@@ -192,6 +194,7 @@ __device__ int sweep_block(int i, int n, const int* scene_axis, const R* smn, co
             hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
                   !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
                   !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
+            if (hit && ign.off && ((fi | fj) & BF_IGN_LIST)) hit = !ign.ignored(i, j);
         }
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (lane == 0) wcnt[w] = __popc(m);
@@ -208,7 +211,7 @@ __device__ int sweep_block(int i, int n, const int* scene_axis, const R* smn, co
 
 template <class R>
 __global__ void k_bp_count(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene, int* count,
-                           int* stage, int* big, int* n_big) {
+                           int* stage, int* big, int* n_big, IgnoreLists ign) {
     const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
@@ -216,17 +219,17 @@ __global__ void k_bp_count(int n, const int* scene_axis, const R* smn, const R* 
         if (lane == 0) big[atomicAdd(n_big, 1)] = i;
         return;
     }
-    const int c = sweep_warp<R, false>(i, n, lane, scene_axis, smn, smx, sflag, sscene, stage, nullptr, nullptr);
+    const int c = sweep_warp<R, false>(i, n, lane, scene_axis, smn, smx, sflag, sscene, stage, nullptr, nullptr, ign);
     if (lane == 0) count[i] = c;
 }
 // one block per listed position (blocks loop over the list)
 template <class R>
 __global__ void k_bp_count_big(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
-                               int* count, const int* big, const int* n_big) {
+                               int* count, const int* big, const int* n_big, IgnoreLists ign) {
     __shared__ int wcnt[32];
     for (int b = blockIdx.x; b < *n_big; b += gridDim.x) {
         const int i = big[b];
-        const int c = sweep_block<R, false>(i, n, scene_axis, smn, smx, sflag, sscene, nullptr, nullptr, wcnt);
+        const int c = sweep_block<R, false>(i, n, scene_axis, smn, smx, sflag, sscene, nullptr, nullptr, wcnt, ign);
         if (threadIdx.x == 0) count[i] = c;
         __syncthreads();
     }
@@ -234,7 +237,7 @@ __global__ void k_bp_count_big(int n, const int* scene_axis, const R* smn, const
 template <class R>
 __global__ void k_bp_write_big(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
                                const uint32_t* order, const int* offset, int2* pairs, int pair_cap, int* status, const int* big,
-                               const int* n_big) {
+                               const int* n_big, IgnoreLists ign) {
     __shared__ int wcnt[32];
     for (int b = blockIdx.x; b < *n_big; b += gridDim.x) {
         const int i = big[b];
@@ -244,14 +247,15 @@ __global__ void k_bp_write_big(int n, const int* scene_axis, const R* smn, const
             if (threadIdx.x == 0) atomicOr(status, ST_PAIR_OVERFLOW);
             continue;
         }
-        sweep_block<R, true>(i, n, scene_axis, smn, smx, sflag, sscene, pairs + base, order, wcnt);
+        sweep_block<R, true>(i, n, scene_axis, smn, smx, sflag, sscene, pairs + base, order, wcnt, ign);
         __syncthreads();
     }
 }
 
 template <class R>
 __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
-                           const uint32_t* order, const int* offset, const int* stage, int2* pairs, int pair_cap, int* status) {
+                           const uint32_t* order, const int* offset, const int* stage, int2* pairs, int pair_cap, int* status,
+                           IgnoreLists ign) {
     const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
@@ -264,7 +268,7 @@ __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* 
     if (c <= kStage) {
         if (lane < c) pairs[base + lane] = make_int2((int)order[i], (int)order[stage[(size_t)i * kStage + lane]]);
     } else {
-        sweep_warp<R, true>(i, n, lane, scene_axis, smn, smx, sflag, sscene, nullptr, pairs + base, order);
+        sweep_warp<R, true>(i, n, lane, scene_axis, smn, smx, sflag, sscene, nullptr, pairs + base, order, ign);
     }
 }
 
@@ -1346,6 +1350,186 @@ __device__ __forceinline__ void si_iterate_result(const Bodies<R>& B, const Rows
     if (!kb) { B.set_vec(TVX, ib, tvb); B.set_vec(TWX, ib, twb); }
 }
 
+// ---------------------------------------------------------------- joints
+// Ball/Hinge/SliderJointConstraint::initSequentialImpulse and iterateSequentialImpulse
+// (ball_joint_constraint.cpp:6-27, hinge_joint_constraint.cpp:6-97, slider_joint_constraint.cpp:7-65)
+// in the reference's operation order.  A kinematic body contributes no inverse mass or inertia
+// (RigidBody::getKinematicInvMass / getKinematicWorldInvInertia) and takes no impulse.
+template <class R> __device__ __forceinline__ M3<R> skew3(const V3<R>& v) {   // Constraint::getSkewSymmetricMatrix
+    M3<R> m;
+    m.m[0][0] = 0; m.m[0][1] = -v.z; m.m[0][2] = v.y;
+    m.m[1][0] = v.z; m.m[1][1] = 0; m.m[1][2] = -v.x;
+    m.m[2][0] = -v.y; m.m[2][1] = v.x; m.m[2][2] = 0;
+    return m;
+}
+template <class R> __device__ __forceinline__ M3<R> madd3(const M3<R>& a, const M3<R>& b) {
+    M3<R> o;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.m[i][j] = a.m[i][j] + b.m[i][j];
+    return o;
+}
+template <class R> __device__ __forceinline__ V3<R> jp3(const R* p, int k) { return V3<R>(p[k], p[k + 1], p[k + 2]); }
+template <class R> __device__ __forceinline__ void jw3(R* p, int k, const V3<R>& v) { p[k] = v.x; p[k + 1] = v.y; p[k + 2] = v.z; }
+template <class R> __device__ __forceinline__ M3<R> jp9(const R* p, int k) {
+    M3<R> m;
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) m.m[i][j] = p[k + i * 3 + j];
+    return m;
+}
+template <class R> __device__ __forceinline__ void jw9(R* p, int k, const M3<R>& m) {
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) p[k + i * 3 + j] = m.m[i][j];
+}
+
+template <class R>
+__global__ void k_joint_init(Joints<R> J, Bodies<R> B, StepParams P) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J.n) return;
+    const int ia = J.body[j].x, ib = J.body[j].y, type = J.type[j], fl = J.flag[j];
+    const bool ka = (B.flags[ia] & BF_KINEMATIC) != 0, kb = (B.flags[ib] & BF_KINEMATIC) != 0;
+    const R* q = J.param + (size_t)j * NJP;
+    R* w = J.row + (size_t)j * NJR;
+    const R dt = R(P.dt), kerp = R(0.2);
+    const Xf<R> ta = B.xf(ia), tb = B.xf(ib);
+    const V3<R> anc_a = jp3(q, JP_ANCHOR_A), anc_b = jp3(q, JP_ANCHOR_B);
+    const V3<R> ra = mv(ta.b, anc_a), rb = mv(tb.b, anc_b);
+    jw3(w, JR_RA, ra);
+    jw3(w, JR_RB, rb);
+    const R ims = (ka ? R(0) : B.at(INVM, ia)) + (kb ? R(0) : B.at(INVM, ib));
+    const M3<R> Ia = ka ? M3<R>() : B.mat(I00, ia), Ib = kb ? M3<R>() : B.mat(I00, ib);
+    const V3<R> rel = ta.apply(anc_a) - tb.apply(anc_b);
+    auto ball = [&]() {
+        M3<R> d;
+        for (int k = 0; k < 3; k++) d.m[k][k] = ims;
+        const M3<R> jmj = inverse3(madd3(madd3(d, world_inertia(skew3(ra), Ia)), world_inertia(skew3(rb), Ib)));
+        jw9(w, JR_JMJ_BALL, jmj);
+        jw3(w, JR_RHS_BALL, mv(jmj, rel) * (-kerp / dt));
+    };
+    if (type == JT_BALL) { ball(); return; }
+    const V3<R> wax = mv(ta.b, jp3(q, JP_AXIS_A)), wbx = mv(tb.b, jp3(q, JP_AXIS_B));
+    V3<R> t0, t1, u0, u1;
+    ortho_units(jp3(q, JP_AXIS_A), t0, t1);
+    t0 = mv(ta.b, t0);
+    t1 = mv(ta.b, t1);
+    jw3(w, JR_WAX, wax);
+    jw3(w, JR_T0, t0);
+    jw3(w, JR_T1, t1);
+    if (type == JT_HINGE) {
+        const bool lim = (fl & 1) != 0, mot = (fl & 2) != 0;
+        if (lim) {
+            ortho_units(jp3(q, JP_AXIS_B), u0, u1);
+            u0 = mv(tb.b, u0);
+        }
+        ball();
+        const M3<R> Is = madd3(Ia, Ib);
+        const R j0 = R(1.0) / dot(t0, mv(Is, t0)), j1 = R(1.0) / dot(t1, mv(Is, t1));
+        const V3<R> u = cross(wax, wbx);
+        w[JR_JMJ2] = j0;
+        w[JR_JMJ2 + 1] = j1;
+        w[JR_RHS2] = j0 * (dot(u, t0) * kerp / dt);
+        w[JR_RHS2 + 1] = j1 * (dot(u, t1) * kerp / dt);
+        R jml = 0;
+        if (mot || lim) jml = R(1.0) / dot(wax, mv(Is, wax));
+        w[JR_JMJ_ML] = jml;
+        if (mot) w[JR_RHS_MOTOR] = jml * -q[JP_SPEED];
+        w[JR_LIMIT] = 0;
+        if (lim) {
+            const R c = dot(t0, u0), sn = dot(cross(t0, u0), wax);
+            const R angle = atan2(sn, c);
+            if (angle < q[JP_MIN]) {
+                w[JR_LIMIT] = 1;
+                w[JR_RHS_LIMIT] = -jml * (q[JP_MIN] - angle) * kerp / dt;
+            } else if (angle > q[JP_MAX]) {
+                w[JR_LIMIT] = 1;
+                w[JR_RHS_LIMIT] = -jml * (q[JP_MAX] - angle) * kerp / dt;
+            }
+        }
+        return;
+    }
+    // slider
+    ortho_units(jp3(q, JP_AXIS_B), u0, u1);
+    const V3<R> ts[2] = {t0, t1};
+    R jp[2];
+    for (int k = 0; k < 2; k++) {
+        const V3<R> xa = cross(ra, ts[k]), xb = cross(rb, ts[k]);
+        jp[k] = R(1.0) / (ims + dot(mv(Ia, xa), xa) + dot(mv(Ib, xb), xb));
+    }
+    w[JR_JMJ2] = jp[0];
+    w[JR_JMJ2 + 1] = jp[1];
+    w[JR_RHS2] = jp[0] * (dot(rel, t0) * (-kerp / dt));
+    w[JR_RHS2 + 1] = jp[0] * (dot(rel, t1) * (-kerp / dt));   // the first row's jmj, as slider_joint_constraint.cpp:40
+    jw9(w, JR_JMJ_ROT, inverse3(madd3(Ia, Ib)));
+}
+
+// RigidBody::applyTempImpulse / applyTempAngularImpulse (rigidbody.cpp:166-181)
+template <class R> __device__ __forceinline__ void jt_impulse(const Bodies<R>& B, int i, const V3<R>& r, const V3<R>& imp) {
+    if (B.flags[i] & BF_KINEMATIC) return;
+    B.set_vec(TVX, i, B.vec(TVX, i) + imp * B.at(INVM, i));
+    B.set_vec(TWX, i, B.vec(TWX, i) + mv(B.mat(I00, i), cross(r, imp)));
+}
+template <class R> __device__ __forceinline__ void jt_ang_impulse(const Bodies<R>& B, int i, const V3<R>& imp) {
+    if (B.flags[i] & BF_KINEMATIC) return;
+    B.set_vec(TWX, i, B.vec(TWX, i) + mv(B.mat(I00, i), imp));
+}
+
+template <class R> __device__ void joint_iterate(const Joints<R>& J, const Bodies<R>& B, int j) {
+    const int ia = J.body[j].x, ib = J.body[j].y, type = J.type[j], fl = J.flag[j];
+    const R* w = J.row + (size_t)j * NJR;
+    const V3<R> ra = jp3(w, JR_RA), rb = jp3(w, JR_RB);
+    const V3<R> va = B.vec(TVX, ia) + cross(B.vec(TWX, ia), ra), vb = B.vec(TVX, ib) + cross(B.vec(TWX, ib), rb);
+    if (type == JT_SLIDER) {
+        const V3<R> t0 = jp3(w, JR_T0), t1 = jp3(w, JR_T1);
+        const R p0 = w[JR_RHS2] - w[JR_JMJ2] * dot(t0, va - vb);
+        const R p1 = w[JR_RHS2 + 1] - w[JR_JMJ2 + 1] * dot(t1, va - vb);
+        const V3<R> pv = t0 * p0 + t1 * p1;
+        jt_impulse(B, ia, ra, pv);
+        jt_impulse(B, ib, rb, -pv);
+        const V3<R> rot = mv(jp9(w, JR_JMJ_ROT), B.vec(TWX, ia) - B.vec(TWX, ib));
+        const V3<R> ri = -rot;
+        jt_ang_impulse(B, ia, ri);
+        jt_ang_impulse(B, ib, -ri);
+        return;
+    }
+    const V3<R> bi = jp3(w, JR_RHS_BALL) - mv(jp9(w, JR_JMJ_BALL), va - vb);
+    jt_impulse(B, ia, ra, bi);
+    jt_impulse(B, ib, rb, -bi);
+    if (type == JT_BALL) return;
+    // hinge rows; motor and limit read the angular velocities left by the impulses before them
+    const V3<R> t0 = jp3(w, JR_T0), t1 = jp3(w, JR_T1), wax = jp3(w, JR_WAX);
+    const V3<R> dw = B.vec(TWX, ia) - B.vec(TWX, ib);
+    const R h0 = w[JR_RHS2] - w[JR_JMJ2] * dot(t0, dw);
+    const R h1 = w[JR_RHS2 + 1] - w[JR_JMJ2 + 1] * dot(t1, dw);
+    const V3<R> iv = t0 * h0 + t1 * h1;
+    jt_ang_impulse(B, ia, iv);
+    jt_ang_impulse(B, ib, -iv);
+    if (fl & 2) {
+        const R mi = w[JR_RHS_MOTOR] - w[JR_JMJ_ML] * dot(wax, B.vec(TWX, ia) - B.vec(TWX, ib));
+        jt_ang_impulse(B, ia, wax * mi);
+        jt_ang_impulse(B, ib, -wax * mi);
+    }
+    if ((fl & 1) && w[JR_LIMIT] != 0) {
+        const R delta = dot(wax, B.vec(TWX, ia) - B.vec(TWX, ib));
+        const R nd = delta * w[JR_RHS_LIMIT] > 0 ? R(0) : delta;
+        const R li = w[JR_RHS_LIMIT] - w[JR_JMJ_ML] * nd;
+        jt_ang_impulse(B, ia, wax * li);
+        jt_ang_impulse(B, ib, -wax * li);
+    }
+}
+
+// Island items: a contact result index, or a joint index with kJointItem set.  Within an island
+// the contacts come first in result order, then the joints in order, so one pass over an island's
+// items is the reference's iteration (every contact, then every other constraint) restricted to
+// the island.
+constexpr uint32_t kJointItem = 0x80000000u;
+template <class R> __device__ __forceinline__ int2 item_bodies(uint32_t item, const Results<R>& res, const Joints<R>& J) {
+    if (item & kJointItem) return J.body[item & ~kJointItem];
+    return make_int2(res.a[item], res.b[item]);
+}
+template <class R>
+__device__ __forceinline__ void iterate_item(uint32_t item, const Results<R>& res, const Joints<R>& J, const Bodies<R>& B,
+                                             const Rows<R>& rows, const int* row_off) {
+    if (item & kJointItem) { joint_iterate(J, B, (int)(item & ~kJointItem)); return; }
+    const int p = (int)item;
+    si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
+}
+
 // ---------------------------------------------------------------- contact islands
 // Islands: connected components of dynamic bodies linked by contact results (a kinematic body
 // links nothing: its temporary velocity never changes).  Results of different islands touch
@@ -1378,6 +1562,27 @@ __global__ void k_isl_union(int A, const int* active, Results<R> res, Bodies<R> 
     if ((B.flags[ia] & BF_KINEMATIC) || (B.flags[ib] & BF_KINEMATIC)) return;
     uf_union(parent, ia, ib);
 }
+// joints link their bodies like contact results do
+template <class R>
+__global__ void k_isl_union_joints(Joints<R> J, Bodies<R> B, int* parent) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J.n) return;
+    const int ia = J.body[j].x, ib = J.body[j].y;
+    if ((B.flags[ia] & BF_KINEMATIC) || (B.flags[ib] & BF_KINEMATIC)) return;
+    uf_union(parent, ia, ib);
+}
+// sort keys of the joints, after the A active results: the island label of a dynamic body; a joint
+// between two kinematic bodies (which moves nothing) gets the label n_bodies, an island of its own
+template <class R>
+__global__ void k_isl_keys_joints(Joints<R> J, Bodies<R> B, const int* parent, int A, uint64_t* key, uint32_t* key2, uint32_t* val) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J.n) return;
+    const int ia = J.body[j].x, ib = J.body[j].y;
+    const bool ka = (B.flags[ia] & BF_KINEMATIC) != 0, kb = (B.flags[ib] & BF_KINEMATIC) != 0;
+    key[A + j] = ka && kb ? (uint64_t)B.n : (uint64_t)uf_find(parent, ka ? ib : ia);
+    key2[A + j] = 0;
+    val[A + j] = kJointItem | (uint32_t)j;
+}
 // sort keys: island label (smallest body index of the island) of each active result
 template <class R>
 __global__ void k_isl_keys(int A, const int* active, Results<R> res, Bodies<R> B, const int* parent, uint64_t* key, uint32_t* key2,
@@ -1397,17 +1602,14 @@ __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* 
 // serial order inside each island: one thread per island (all islands in serial-order mode,
 // islands up to `max_len` results in coloured mode)
 template <class R>
-__global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Bodies<R> B, Rows<R> rows,
-                             const int* row_off, int iterations, int min_len, int max_len) {
+__global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
+                             Rows<R> rows, const int* row_off, int iterations, int min_len, int max_len) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= *n_isl) return;
     const int lo = isl_off[s], hi = isl_off[s + 1];
     if (hi - lo < min_len || hi - lo > max_len) return;
     for (int it = 0; it < iterations; it++)
-        for (int k = lo; k < hi; k++) {
-            const int p = (int)order[k];
-            si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
-        }
+        for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
 }
 
 constexpr int kSmallResults = 8;   // islands up to this size run in the reference order, one thread each
@@ -1421,8 +1623,8 @@ constexpr int kMaxColors = 64;
 constexpr int kColorBlock = 64;   // threads per island block: islands run tens of results per colour
 constexpr int kBigIsland = 4096;  // larger islands are coloured and solved by the whole grid (k_gc_*)
 template <class R>
-__global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Bodies<R> B, Rows<R> rows,
-                              const int* row_off, int iterations, int min_len, int* claim, int* color, uint32_t* corder,
+__global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
+                              Rows<R> rows, const int* row_off, int iterations, int min_len, int* claim, int* color, uint32_t* corder,
                               int* n_colors_out) {
     const int s = blockIdx.x;
     if (s >= *n_isl) return;
@@ -1437,24 +1639,24 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
     for (int c = 0; c < kMaxColors - 1; c++) {
         for (int j = threadIdx.x; j < m; j += blockDim.x) {
             if (color[lo + j] >= 0) continue;
-            const int p = (int)order[lo + j];
-            claim[res.a[p]] = 0x7fffffff;
-            claim[res.b[p]] = 0x7fffffff;
+            const int2 q = item_bodies(order[lo + j], res, J);
+            claim[q.x] = 0x7fffffff;
+            claim[q.y] = 0x7fffffff;
         }
         if (threadIdx.x == 0) remaining = 0;
         __syncthreads();
         for (int j = threadIdx.x; j < m; j += blockDim.x) {
             if (color[lo + j] >= 0) continue;
-            const int p = (int)order[lo + j];
-            const int ia = res.a[p], ib = res.b[p];
+            const int2 q = item_bodies(order[lo + j], res, J);
+            const int ia = q.x, ib = q.y;
             if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
             if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
         }
         __syncthreads();
         for (int j = threadIdx.x; j < m; j += blockDim.x) {
             if (color[lo + j] >= 0) continue;
-            const int p = (int)order[lo + j];
-            const int ia = res.a[p], ib = res.b[p];
+            const int2 q = item_bodies(order[lo + j], res, J);
+            const int ia = q.x, ib = q.y;
             const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
             if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) color[lo + j] = c;
             else atomicAdd(&remaining, 1);
@@ -1488,17 +1690,11 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
         for (int c = 0; c < kMaxColors - 1; c++) {
             const int a = cnt[c], b = cnt[c + 1];
             if (a == b) continue;
-            for (int j = a + threadIdx.x; j < b; j += blockDim.x) {
-                const int p = (int)corder[lo + j];
-                si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
-            }
+            for (int j = a + threadIdx.x; j < b; j += blockDim.x) iterate_item(corder[lo + j], res, J, B, rows, row_off);
             __syncthreads();
         }
         if (threadIdx.x == 0)
-            for (int j = cnt[kMaxColors - 1]; j < cnt[kMaxColors]; j++) {
-                const int p = (int)corder[lo + j];
-                si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
-            }
+            for (int j = cnt[kMaxColors - 1]; j < cnt[kMaxColors]; j++) iterate_item(corder[lo + j], res, J, B, rows, row_off);
         __syncthreads();
     }
 }
@@ -1513,31 +1709,31 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
 constexpr int kMaxColorsBig = 1024;
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big);
 template <class R>
-__global__ void k_gc_reset(int lo, int m, const uint32_t* order, Results<R> res, const int* color, int* claim) {
+__global__ void k_gc_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, const int* color, int* claim) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m || color[lo + j] >= 0) return;
-    const int p = (int)order[lo + j];
-    claim[res.a[p]] = 0x7fffffff;
-    claim[res.b[p]] = 0x7fffffff;
+    const int2 q = item_bodies(order[lo + j], res, J);
+    claim[q.x] = 0x7fffffff;
+    claim[q.y] = 0x7fffffff;
 }
 template <class R>
-__global__ void k_gc_claim(int lo, int m, const uint32_t* order, Results<R> res, Bodies<R> B, const int* color, int* claim) {
+__global__ void k_gc_claim(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B, const int* color, int* claim) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m || color[lo + j] >= 0) return;
-    const int p = (int)order[lo + j];
-    const int ia = res.a[p], ib = res.b[p];
+    const int2 q = item_bodies(order[lo + j], res, J);
+    const int ia = q.x, ib = q.y;
     if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
     if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
 }
 // winners take colour c; *remaining += results still uncoloured after this round
 template <class R>
-__global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res, Bodies<R> B, const int* claim, int* color, int c,
-                            int* remaining) {
+__global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B, const int* claim, int* color,
+                            int c, int* remaining) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool left = false;
     if (j < m && color[lo + j] < 0) {
-        const int p = (int)order[lo + j];
-        const int ia = res.a[p], ib = res.b[p];
+        const int2 q = item_bodies(order[lo + j], res, J);
+        const int ia = q.x, ib = q.y;
         const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
         if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) color[lo + j] = c;
         else left = true;
@@ -1549,19 +1745,17 @@ __global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res
 __global__ void k_gc_count(int lo, int m, int* color, int* cnt);
 __global__ void k_gc_place(int lo, int m, const int* color, const uint32_t* order, int* cursor, uint32_t* corder);
 template <class R>
-__global__ void k_gc_pass(const uint32_t* list, int n, Results<R> res, Bodies<R> B, Rows<R> rows, const int* row_off) {
+__global__ void k_gc_pass(const uint32_t* list, int n, Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const int p = (int)list[j];
-    si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
+    iterate_item(list[j], res, J, B, rows, row_off);
 }
 template <class R>
-__global__ void k_gc_last(int lo, int m, const uint32_t* order, const int* color, Results<R> res, Bodies<R> B, Rows<R> rows,
+__global__ void k_gc_last(int lo, int m, const uint32_t* order, const int* color, Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows,
                           const int* row_off) {
     for (int j = 0; j < m; j++) {
         if (color[lo + j] != kMaxColorsBig - 1) continue;
-        const int p = (int)order[lo + j];
-        si_iterate_result(B, rows, res.a[p], res.b[p], row_off[p], res.npts[p]);
+        iterate_item(order[lo + j], res, J, B, rows, row_off);
     }
 }
 

@@ -114,15 +114,17 @@ template <class R> PE_HD M3<R> world_inertia(const M3<R>& rot, const M3<R>& loca
     return o;
 }
 // Eigen's closed-form 3x3 inverse
+// (compute_inverse<..., 3>: the determinant expands the cofactors of column 0, and entry (r, c)
+// of the inverse is cofactor (c, r) / det; exact for matrices that are not bitwise symmetric)
 template <class R> PE_HD M3<R> inverse3(const M3<R>& a) {
-    auto cof = [&](int i, int j) {
+    auto cof = [&](int i, int j) {   // cofactor_3x3<i, j>
         const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-        return a.m[j1][i1] * a.m[j2][i2] - a.m[j1][i2] * a.m[j2][i1];
+        return a.m[i1][j1] * a.m[i2][j2] - a.m[i1][j2] * a.m[i2][j1];
     };
     const R det = sum3(cof(0, 0) * a.m[0][0], cof(1, 0) * a.m[1][0], cof(2, 0) * a.m[2][0], dbl<R>());
     const R inv = R(1) / det;
     M3<R> o;
-    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) o.m[i][j] = cof(i, j) * inv;
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) o.m[r][c] = cof(c, r) * inv;
     return o;
 }
 

@@ -174,16 +174,17 @@ extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min
     const uint32_t* order = val[cur];
     k_sap_gather<<<g, kBlock, 0, st>>>(n, aabb_min, aabb_max, flags, order, smn, smx, sflag, sscene, count, status, n_big);
     const int gw = (int)(((size_t)n * 32 + kBlock - 1) / kBlock);
-    k_bp_count<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, stage, big, n_big);
-    k_bp_count_big<float><<<kSapBigBlocks, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, big, n_big);
+    const IgnoreLists no_lists;   // this entry point takes no ignored-pair lists
+    k_bp_count<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, stage, big, n_big, no_lists);
+    k_bp_count_big<float><<<kSapBigBlocks, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, big, n_big, no_lists);
     const int ct = (n + 1 + 1023) / 1024;
     k_scan_tiles<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
     k_scan_aux<<<1, kBlock, 0, st>>>(aux, ct, total);
     k_scan_add<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
     k_bp_write<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, order, count, stage, reinterpret_cast<int2*>(pairs),
-                                             pair_cap, status);
+                                             pair_cap, status, no_lists);
     k_bp_write_big<float><<<kSapBigBlocks, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, order, count,
-                                                          reinterpret_cast<int2*>(pairs), pair_cap, status, big, n_big);
+                                                          reinterpret_cast<int2*>(pairs), pair_cap, status, big, n_big, no_lists);
     k_sap_total<<<1, 1, 0, st>>>(total, n_pairs);
     if (cudaGetLastError() != cudaSuccess) return done(PE_GPU_ERR_CUDA, "kernel launch");
     return done(PE_GPU_OK, nullptr);

@@ -17,7 +17,23 @@ enum BodyField {
     INVM, MASS, FRIC, REST, LDAMP, ADAMP, SCALE,   // SCALE: RigidBody::getAABBScale of the current AABB
     NBF
 };
-enum BodyFlag { BF_KINEMATIC = 1, BF_IGNORE = 2 };
+enum BodyFlag { BF_KINEMATIC = 1, BF_IGNORE = 2, BF_IGN_LIST = 4 };   // BF_IGN_LIST: the body has ignored partners
+
+// RigidBody::_ignore_collision_ids as symmetric partner lists: body i never pairs with
+// ids[off[i] .. off[i+1]); `order` maps sorted positions to bodies.  off == nullptr: no lists.
+struct IgnoreLists {
+    const int* off = nullptr;
+    const int* ids = nullptr;
+    const uint32_t* order = nullptr;
+#ifdef __CUDACC__
+    __device__ bool ignored(int pi, int pj) const {   // sorted positions pi, pj
+        const int a = (int)order[pi], b = (int)order[pj];
+        for (int k = off[a], e = off[a + 1]; k < e; k++)
+            if (ids[k] == b) return true;
+        return false;
+    }
+#endif
+};
 
 template <class R> struct Bodies {
     R* f;
@@ -71,6 +87,21 @@ template <class R> struct Rows {
     int cap;
     R* f;
     __host__ __device__ R& at(int k, int i) const { return f[(size_t)k * cap + i]; }
+};
+
+// joint constraints (World::addConstraint, in order): Ball/Hinge/SliderJointConstraint
+enum JointType { JT_BALL = 0, JT_HINGE = 1, JT_SLIDER = 2 };
+enum JointParam { JP_ANCHOR_A = 0, JP_ANCHOR_B = 3, JP_AXIS_A = 6, JP_AXIS_B = 9, JP_MIN = 12, JP_MAX = 13, JP_SPEED = 14, NJP = 15 };
+// per-step solver data of one joint (initSequentialImpulse), joint-major
+enum JointRow { JR_RA = 0, JR_RB = 3, JR_WAX = 6, JR_T0 = 9, JR_T1 = 12, JR_RHS_BALL = 15, JR_JMJ_BALL = 18, JR_JMJ_ROT = 27,
+                JR_RHS2 = 36, JR_JMJ2 = 38, JR_JMJ_ML = 40, JR_RHS_MOTOR = 41, JR_RHS_LIMIT = 42, JR_LIMIT = 43, NJR = 44 };
+template <class R> struct Joints {
+    int n = 0;
+    const int* type = nullptr;
+    const int2* body = nullptr;    // (a, b)
+    const int* flag = nullptr;     // bit 0 use_limits, bit 1 use_motor
+    const R* param = nullptr;      // [NJP * n]
+    R* row = nullptr;              // [NJR * n]
 };
 
 struct StepParams {

@@ -63,6 +63,8 @@ public:
                             const double* v, const double* w) = 0;
     virtual void set_compounds(const int* cbeg, const int* ccnt, int C, const int* cshape, const double* corg,
                                const double* cbas, const double* cratio, const double* local_inertia, double* centroid) = 0;
+    virtual void set_joints(int n, const int* type, const int* body, const int* flag, const double* param) = 0;
+    virtual void set_ignore_pairs(int n, const int* pairs) = 0;
     virtual void set_scenes(int n, const int* off) = 0;
     virtual void set_params(double dt, double gx, double gy, double gz, int iters) = 0;
     virtual void step(int n, int mode) = 0;
@@ -107,6 +109,8 @@ public:
                     const double* w) override;
     void set_compounds(const int* cbeg, const int* ccnt, int C, const int* cshape, const double* corg, const double* cbas,
                        const double* cratio, const double* local_inertia, double* centroid) override;
+    void set_joints(int n, const int* type, const int* body, const int* flag, const double* param) override;
+    void set_ignore_pairs(int n, const int* pairs) override;
     void set_scenes(int n, const int* off) override;
     void set_params(double dt, double gx, double gy, double gz, int iters) override;
     void step(int n, int mode) override;
@@ -237,6 +241,16 @@ private:
     std::vector<int> h_cbeg_, h_ccnt_, h_cshape_;
     std::vector<char> h_cready_;
     std::vector<R> h_cxf_;
+    // joints (World::_constraints) and ignored collision pairs
+    int n_joints_ = 0, n_ign_ = 0;
+    DBuf<int> jtype_, jflag_, ign_off_, ign_ids_;
+    DBuf<int2> jbody_;
+    DBuf<R> jparam_, jrow_;
+    Joints<R> joints() {
+        Joints<R> j;
+        j.n = n_joints_; j.type = jtype_.p; j.body = jbody_.p; j.flag = jflag_.p; j.param = jparam_.p; j.row = jrow_.p;
+        return j;
+    }
     // bodies
     int N_ = 0, bcap_ = 0;
     DBuf<R> bf_;

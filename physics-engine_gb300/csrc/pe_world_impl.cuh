@@ -263,6 +263,54 @@ void World<R>::set_compounds(const int* cbeg, const int* ccnt, int C, const int*
     PE_CK(cudaStreamSynchronize(st_));
 }
 
+// World::addConstraint for each joint, in order (sequential_impulse_solver.cpp:46-48, 60-68 run
+// them after the contacts of every iteration)
+template <class R>
+void World<R>::set_joints(int n, const int* type, const int* body, const int* flag, const double* param) {
+    std::vector<int> t(type, type + n), f(flag, flag + n);
+    std::vector<int2> b(n);
+    std::vector<R> q((size_t)n * NJP);
+    for (int j = 0; j < n; j++) {
+        if (t[j] < JT_BALL || t[j] > JT_SLIDER) throw std::runtime_error("joint " + std::to_string(j) + ": unknown type");
+        b[j] = make_int2(body[2 * j], body[2 * j + 1]);
+        if (b[j].x < 0 || b[j].x >= N_ || b[j].y < 0 || b[j].y >= N_ || b[j].x == b[j].y)
+            throw std::runtime_error("joint " + std::to_string(j) + ": bad bodies");
+        for (int k = 0; k < NJP; k++) q[(size_t)j * NJP + k] = R(param[(size_t)j * NJP + k]);
+    }
+    n_joints_ = n;
+    upload(jtype_, t, st_);
+    upload(jflag_, f, st_);
+    upload(jbody_, b, st_);
+    upload(jparam_, q, st_);
+    jrow_.ensure((size_t)std::max(n, 1) * NJR);
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
+// RigidBody::addIgnoreCollisionId: symmetric partner lists, and BF_IGN_LIST on the bodies that have one
+template <class R> void World<R>::set_ignore_pairs(int n, const int* pairs) {
+    std::vector<std::vector<int>> part(N_);
+    for (int k = 0; k < n; k++) {
+        const int a = pairs[2 * k], b = pairs[2 * k + 1];
+        if (a < 0 || a >= N_ || b < 0 || b >= N_) throw std::runtime_error("ignored pair " + std::to_string(k) + ": bad body");
+        part[a].push_back(b);
+        part[b].push_back(a);
+    }
+    std::vector<int> off(N_ + 1, 0), ids;
+    for (int i = 0; i < N_; i++) {
+        ids.insert(ids.end(), part[i].begin(), part[i].end());
+        off[i + 1] = (int)ids.size();
+    }
+    std::vector<int> fl(N_);
+    PE_CK(cudaMemcpyAsync(fl.data(), bflags_.p, N_ * sizeof(int), cudaMemcpyDeviceToHost, st_));
+    PE_CK(cudaStreamSynchronize(st_));
+    for (int i = 0; i < N_; i++) fl[i] = (fl[i] & ~BF_IGN_LIST) | (off[i + 1] > off[i] ? BF_IGN_LIST : 0);
+    upload(bflags_, fl, st_);
+    upload(ign_off_, off, st_);
+    upload(ign_ids_, ids, st_);
+    n_ign_ = n;
+    PE_CK(cudaStreamSynchronize(st_));
+}
+
 // RigidBody::setMass + setCollisionShape (rigidbody.cpp:11-41) and the initial pose: body j of a
 // field-major array with the given stride
 template <class R>
@@ -310,7 +358,11 @@ void World<R>::set_bodies(int n, const int* shape, const int* flags, const doubl
     }
     upload(bf_, f, st_);
     upload(bshape_, std::vector<int>(shape, shape + n), st_);
-    upload(bflags_, std::vector<int>(flags, flags + n), st_);
+    std::vector<int> fl(flags, flags + n);
+    for (auto& x : fl) x &= BF_KINEMATIC | BF_IGNORE;   // BF_IGN_LIST belongs to set_ignore_pairs
+    upload(bflags_, fl, st_);
+    n_joints_ = 0;   // joints and ignored pairs name bodies: set them again after the bodies
+    n_ign_ = 0;
     claim_.ensure(n + 1);
     set_scenes(1, nullptr);
 }
@@ -432,18 +484,20 @@ template <class R> int World<R>::broadphase() {
     bp_big_.ensure(n + 1);
     bp_nbig_.ensure(1);
     PE_CK(cudaMemsetAsync(bp_nbig_.p, 0, sizeof(int), st_));
+    IgnoreLists ign;
+    if (n_ign_ > 0) { ign.off = ign_off_.p; ign.ids = ign_ids_.p; ign.order = order_; }
     launch(K_BP_SWEEP, grid_warps(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p,
-           bp_big_.p, bp_nbig_.p);
+           bp_big_.p, bp_nbig_.p, ign);
     launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_count_big<R>, n, (const int*)scene_axis_.p, (const R*)smn_.p, (const R*)smx_.p,
-           (const int*)sflag_.p, (const int*)ssc_.p, count_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p);
+           (const int*)sflag_.p, (const int*)ssc_.p, count_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p, ign);
     PE_CK(cudaMemsetAsync(count_.p + n, 0, sizeof(int), st_));
     const int P = scan(count_.p, n + 1);
     ensure_pair_capacity(P);
     launch(K_BP_SWEEP, grid_warps(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
-           pairs_.p, pair_cap_, status_.p);
+           pairs_.p, pair_cap_, status_.p, ign);
     launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_write_big<R>, n, (const int*)scene_axis_.p, (const R*)smn_.p, (const R*)smx_.p,
            (const int*)sflag_.p, (const int*)ssc_.p, (const uint32_t*)order_, (const int*)count_.p, pairs_.p, pair_cap_, status_.p,
-           (const int*)bp_big_.p, (const int*)bp_nbig_.p);
+           (const int*)bp_big_.p, (const int*)bp_nbig_.p, ign);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
     launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
     if (axis_items_n_ > 0) {   // scenes above kAxisTile bodies
@@ -566,38 +620,46 @@ template <class R> void World<R>::solve(int mode) {
         PE_CK(cudaMemcpyAsync(color_.p, active_.p, (P + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
         n_active_ = scan(color_.p, P + 1);
         launch(K_SI_MISC, grid(P), k_active_compact, P, res_np_.p, color_.p, active_.p);
-        const int A = n_active_;
-        if (A > 0) {
-            // contact islands: union-find over dynamic bodies, results grouped by island keeping order
-            parent_.ensure(N_ + 1);
-            launch(K_ISLAND, grid(N_), k_isl_init, N_, parent_.p);
-            launch(K_ISLAND, grid(A), k_isl_union<R>, A, active_.p, results(), bodies(), parent_.p);
-            for (int k = 0; k < 2; k++) { key_[k].ensure(A); key2_[k].ensure(A); val_[k].ensure(A); }
+    }
+    const int A = n_active_, NJ = n_joints_;
+    const Joints<R> jt = joints();
+    if (NJ > 0) launch(K_SI_SETUP, grid(NJ), k_joint_init<R>, jt, bodies(), prm_);
+    const int M = A + NJ;   // island items: active contact results, then joints
+    if (M > 0) {
+        // islands: union-find over dynamic bodies linked by contacts and joints; items grouped by
+        // island keeping their order (contacts in result order, then joints in order)
+        parent_.ensure(N_ + 1);
+        launch(K_ISLAND, grid(N_), k_isl_init, N_, parent_.p);
+        if (A > 0) launch(K_ISLAND, grid(A), k_isl_union<R>, A, active_.p, results(), bodies(), parent_.p);
+        if (NJ > 0) launch(K_ISLAND, grid(NJ), k_isl_union_joints<R>, jt, bodies(), parent_.p);
+        for (int k = 0; k < 2; k++) { key_[k].ensure(M); key2_[k].ensure(M); val_[k].ensure(M); }
+        if (A > 0)
             launch(K_ISLAND, grid(A), k_isl_keys<R>, A, active_.p, results(), bodies(), parent_.p, key_[0].p, key2_[0].p, val_[0].p);
-            int label_passes = 0;
-            for (int m = N_ - 1; m > 0; m >>= 8) label_passes++;
-            const int cur = radix_sort_keys(A, label_passes, 0);
-            const uint64_t* skey = key_[cur].p;
-            const uint32_t* order = val_[cur].p;
-            isl_flag_.ensure(A + 1);
-            isl_off_.ensure(A + 1);
-            isl_n_.ensure(1);
-            launch(K_ISLAND, grid(A + 1), k_isl_flags, A, skey, isl_flag_.p);
-            n_islands_ = scan(isl_flag_.p, A + 1);
-            launch(K_ISLAND, grid(A + 1), k_isl_offsets, A, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
-            const int NI = n_islands_;
-            // islands of up to kSmallResults results (all of them in serial-order mode): one thread each
-            launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(), row_off_.p,
-                   prm_.iterations, 0, mode == 0 ? 0x7fffffff : kSmallResults);
-            if (mode != 0) {
-                isl_corder_.ensure(A);
-                ncol_.ensure(1);
-                PE_CK(cudaMemsetAsync(ncol_.p, 0, sizeof(int), st_));
-                launch_block(K_SI_COLOR, NI, kColorBlock, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), bodies(), rows(),
-                             row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p, ncol_.p);
-                PE_CK(cudaMemcpyAsync(&n_colors_, ncol_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-                solve_big_islands(NI, order);
-            }
+        if (NJ > 0) launch(K_ISLAND, grid(NJ), k_isl_keys_joints<R>, jt, bodies(), parent_.p, A, key_[0].p, key2_[0].p, val_[0].p);
+        int label_passes = 0;
+        for (int m = NJ > 0 ? N_ : N_ - 1; m > 0; m >>= 8) label_passes++;   // joint labels reach n_bodies
+        const int cur = radix_sort_keys(M, label_passes, 0);
+        const uint64_t* skey = key_[cur].p;
+        const uint32_t* order = val_[cur].p;
+        isl_flag_.ensure(M + 1);
+        isl_off_.ensure(M + 1);
+        isl_n_.ensure(1);
+        launch(K_ISLAND, grid(M + 1), k_isl_flags, M, skey, isl_flag_.p);
+        n_islands_ = scan(isl_flag_.p, M + 1);
+        launch(K_ISLAND, grid(M + 1), k_isl_offsets, M, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
+        const int NI = n_islands_;
+        // islands of up to kSmallResults items (all of them in serial-order mode): one thread each
+        launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(), row_off_.p,
+               prm_.iterations, 0, mode == 0 ? 0x7fffffff : kSmallResults);
+        if (mode != 0) {
+            isl_corder_.ensure(M);
+            color_.ensure(M + 1);
+            ncol_.ensure(1);
+            PE_CK(cudaMemsetAsync(ncol_.p, 0, sizeof(int), st_));
+            launch_block(K_SI_COLOR, NI, kColorBlock, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
+                         row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p, ncol_.p);
+            PE_CK(cudaMemcpyAsync(&n_colors_, ncol_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+            solve_big_islands(NI, order);
         }
     }
     launch(K_SI_MISC, grid(N_), k_si_sync<R>, bodies());
@@ -621,6 +683,7 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
     gc_cnt_.ensure(kMaxColorsBig + 1);
     gc_cursor_.ensure(kMaxColorsBig);
     const Results<R> rs = results();
+    const Joints<R> jt = joints();
     const Bodies<R> bd = bodies();
     const Rows<R> rw = rows();
     std::vector<int> cnt(kMaxColorsBig + 1), start(kMaxColorsBig), cur(kMaxColorsBig);
@@ -634,10 +697,10 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         for (int c0 = 0; c0 < kMaxColorsBig - 1; c0 += 8) {
             int c = c0;
             for (; c < c0 + 8 && c < kMaxColorsBig - 1; c++) {
-                launch(K_SI_COLOR, g, k_gc_reset<R>, lo, m, order, rs, (const int*)color_.p, claim_.p);
-                launch(K_SI_COLOR, g, k_gc_claim<R>, lo, m, order, rs, bd, (const int*)color_.p, claim_.p);
+                launch(K_SI_COLOR, g, k_gc_reset<R>, lo, m, order, rs, jt, (const int*)color_.p, claim_.p);
+                launch(K_SI_COLOR, g, k_gc_claim<R>, lo, m, order, rs, jt, bd, (const int*)color_.p, claim_.p);
                 PE_CK(cudaMemsetAsync(gc_n_.p + 1, 0, sizeof(int), st_));
-                launch(K_SI_COLOR, g, k_gc_assign<R>, lo, m, order, rs, bd, (const int*)claim_.p, color_.p, c, gc_n_.p + 1);
+                launch(K_SI_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, c, gc_n_.p + 1);
             }
             int rem = 0;
             PE_CK(cudaMemcpyAsync(&rem, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -662,8 +725,9 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
             for (int c = 0; c < used && c < kMaxColorsBig - 1; c++)
                 if (cnt[c + 1])
                     launch(K_SI_COLOR, grid(cnt[c + 1]), k_gc_pass<R>, (const uint32_t*)isl_corder_.p + lo + start[c], cnt[c + 1], rs,
-                           bd, rw, (const int*)row_off_.p);
-            if (last) launch_block(K_SI_COLOR, 1, 1, k_gc_last<R>, lo, m, order, (const int*)color_.p, rs, bd, rw, (const int*)row_off_.p);
+                           jt, bd, rw, (const int*)row_off_.p);
+            if (last)
+                launch_block(K_SI_COLOR, 1, 1, k_gc_last<R>, lo, m, order, (const int*)color_.p, rs, jt, bd, rw, (const int*)row_off_.p);
         }
     }
 }

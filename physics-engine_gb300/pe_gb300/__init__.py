@@ -45,6 +45,8 @@ def load(build_if_missing: bool = True):
         "pe_gpu_set_shapes": (I, [P, I, ip, dp, ip, ip, ip, ip, I, dp, I, ip, ip]),
         "pe_gpu_set_bodies": (I, [P, I, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp, dp]),
         "pe_gpu_set_compounds": (I, [P, ip, ip, I, ip, dp, dp, dp, P, dp]),
+        "pe_gpu_set_joints": (I, [P, I, ip, ip, ip, dp]),
+        "pe_gpu_set_ignore_pairs": (I, [P, I, ip]),
         "pe_gpu_set_scenes": (I, [P, I, ip]),
         "pe_gpu_set_params": (I, [P, D, D, D, D, I]),
         "pe_gpu_step": (I, [P, I, I]),
@@ -124,6 +126,11 @@ class GpuWorld:
             self.h, s.n_bodies, _i32(s.body_shape), _i32(s.body_flags), _f64(s.mass), _f64(s.friction), _f64(s.restitution),
             _f64(s.lin_damp), _f64(s.ang_damp), _f64(s.origin).ravel(), _f64(s.basis).ravel(), _f64(s.lin_vel).ravel(),
             _f64(s.ang_vel).ravel()))
+        if s.n_joints:
+            self._ck(self.lib.pe_gpu_set_joints(self.h, s.n_joints, _i32(s.joint_type), _i32(s.joint_body).ravel(),
+                                                _i32(s.joint_flag), _f64(s.joint_real).ravel()))
+        if len(s.ignore_pairs):
+            self._ck(self.lib.pe_gpu_set_ignore_pairs(self.h, len(s.ignore_pairs), _i32(s.ignore_pairs).ravel()))
         self._ck(self.lib.pe_gpu_set_params(self.h, float(s.dt), *map(float, s.gravity), int(s.iterations)))
         if scenes is not None:
             self.set_scenes(scenes)

@@ -31,6 +31,7 @@ import numpy as np
 
 BOX, SPHERE, CYLINDER, HULL = 0, 1, 2, 3
 COMPOUND = 5   # ShapeType::ST_Compound (ST_ConcaveMesh = 4 is not on the path)
+JOINT_BALL, JOINT_HINGE, JOINT_SLIDER = 0, 1, 2   # ConstraintType::CT_{BALL,HINGE,SLIDER}_JOINT
 KINEMATIC = 1
 IGNORE_COLLISION = 2   # RigidBody::setIgnoreCollision: the body takes part in no pair
 
@@ -76,12 +77,33 @@ class Scene:
     child_basis: np.ndarray = None     # float64 [C,3,3]
     child_ratio: np.ndarray = None     # float64 [C]
 
+    # joints (World::addConstraint of Ball/Hinge/SliderJointConstraint, in order): type JOINT_*,
+    # bodies (a, b), flags (bit 0 use_limits, bit 1 use_motor) and 15 reals: anchor_a, anchor_b,
+    # axis_a, axis_b (3 each), min_angle, max_angle, target_speed
+    joint_type: np.ndarray = None      # int32 [J]
+    joint_body: np.ndarray = None      # int32 [J,2]
+    joint_flag: np.ndarray = None      # int32 [J]
+    joint_real: np.ndarray = None      # float64 [J,15]
+    # RigidBody::addIgnoreCollisionId: body pairs that never collide
+    ignore_pairs: np.ndarray = None    # int32 [K,2]
+
     def __post_init__(self):
         if self.child_shape is None:
             self.child_shape = np.zeros(0, np.int32)
             self.child_origin = np.zeros((0, 3))
             self.child_basis = np.zeros((0, 3, 3))
             self.child_ratio = np.zeros(0)
+        if self.joint_type is None:
+            self.joint_type = np.zeros(0, np.int32)
+            self.joint_body = np.zeros((0, 2), np.int32)
+            self.joint_flag = np.zeros(0, np.int32)
+            self.joint_real = np.zeros((0, 15))
+        if self.ignore_pairs is None:
+            self.ignore_pairs = np.zeros((0, 2), np.int32)
+
+    @property
+    def n_joints(self) -> int:
+        return int(self.joint_type.shape[0])
 
     @property
     def n_children(self) -> int:
@@ -111,7 +133,8 @@ class Scene:
             s.dt = float(np.float32(self.dt))
             s.gravity = tuple(float(np.float32(g)) for g in self.gravity)
             for f in ("shape_param", "hull_verts", "mass", "friction", "restitution", "lin_damp",
-                      "ang_damp", "origin", "basis", "lin_vel", "ang_vel", "child_origin", "child_basis", "child_ratio"):
+                      "ang_damp", "origin", "basis", "lin_vel", "ang_vel", "child_origin", "child_basis", "child_ratio",
+                      "joint_real"):
                 setattr(s, f, r(getattr(self, f)))
         return s
 
@@ -119,7 +142,8 @@ class Scene:
     def write(self, path) -> None:
         """Write the little-endian ``.pescene`` layout read by every consumer of a scene."""
         S, N = self.n_shapes, self.n_bodies
-        compound = self.n_children > 0 or bool((self.shape_type == COMPOUND).any())
+        compound = (self.n_children > 0 or bool((self.shape_type == COMPOUND).any()) or self.n_joints > 0
+                    or len(self.ignore_pairs) > 0)
         with open(path, "wb") as f:
             f.write(MAGIC_COMPOUND if compound else MAGIC)
             f.write(struct.pack("<6i", S, N, len(self.hull_verts), len(self.hull_face_off) - 1,
@@ -139,6 +163,15 @@ class Scene:
                 for a, t in ((cb, "<i4"), (cc, "<i4"), (self.child_shape, "<i4"), (self.child_origin, "<f8"),
                              (self.child_basis, "<f8"), (self.child_ratio, "<f8")):
                     f.write(np.ascontiguousarray(a, dtype=t).tobytes())
+                # tagged sections: 1 joints, 2 ignored body pairs
+                if self.n_joints:
+                    f.write(struct.pack("<2i", 1, self.n_joints))
+                    for a, t in ((self.joint_type, "<i4"), (self.joint_body, "<i4"), (self.joint_flag, "<i4"),
+                                 (self.joint_real, "<f8")):
+                        f.write(np.ascontiguousarray(a, dtype=t).tobytes())
+                if len(self.ignore_pairs):
+                    f.write(struct.pack("<2i", 2, len(self.ignore_pairs)))
+                    f.write(np.ascontiguousarray(self.ignore_pairs, dtype="<i4").tobytes())
 
     @staticmethod
     def read(path, real_bits: int = 64) -> "Scene":
@@ -176,6 +209,17 @@ class Scene:
             s.child_origin = take(C * 3, "<f8", (C, 3))
             s.child_basis = take(C * 9, "<f8", (C, 3, 3))
             s.child_ratio = take(C, "<f8")
+            while off < len(b):
+                tag, n = (int(x) for x in take(2, "<i4"))
+                if tag == 1:
+                    s.joint_type = take(n, "<i4")
+                    s.joint_body = take(2 * n, "<i4", (n, 2))
+                    s.joint_flag = take(n, "<i4")
+                    s.joint_real = take(15 * n, "<f8", (n, 15))
+                elif tag == 2:
+                    s.ignore_pairs = take(2 * n, "<i4", (n, 2))
+                else:
+                    raise ValueError(f"unknown .pescene section {tag}")
         return s
 
 
@@ -189,6 +233,8 @@ class SceneBuilder:
         self.shape_key = {}
         self.hulls = []           # (verts [V,3], faces list[list[int]])
         self.bodies = []
+        self.joints = []
+        self.ignores = []
 
     def shape(self, kind, params=(0.0, 0.0, 0.0), hull=None):
         params = tuple(float(p) for p in params) + (0.0,) * (3 - len(params))
@@ -219,6 +265,20 @@ class SceneBuilder:
                          float(r)))
         self.shapes.append((COMPOUND, (0.0, 0.0, 0.0), kids))
         return len(self.shapes) - 1
+
+    def joint(self, kind, a, b, anchor_a=(0, 0, 0), anchor_b=(0, 0, 0), axis_a=(1, 0, 0), axis_b=(1, 0, 0),
+              limits=None, motor_speed=None):
+        """World::addConstraint of a ball, hinge or slider joint between bodies a and b (anchors and
+        axes in the bodies' frames; hinge limits (min_angle, max_angle) and motor target speed)."""
+        flag = (1 if limits is not None else 0) | (2 if motor_speed is not None else 0)
+        lo, hi = limits if limits is not None else (0.0, 0.0)
+        real = [*anchor_a, *anchor_b, *axis_a, *axis_b, lo, hi, motor_speed or 0.0]
+        self.joints.append((int(kind), int(a), int(b), flag, [float(x) for x in real]))
+        return len(self.joints) - 1
+
+    def ignore_pair(self, a, b):
+        """RigidBody::addIgnoreCollisionId: bodies a and b never form a collision pair."""
+        self.ignores.append((int(a), int(b)))
 
     def compound_centroid(self, shape):
         """The vector CompoundShape::init() returns (compound_shape.cpp:27-33): the mass-ratio
@@ -274,6 +334,13 @@ class SceneBuilder:
             s.child_origin = np.array([k[1] for k in kids], np.float64).reshape(-1, 3)
             s.child_basis = np.array([k[2] for k in kids], np.float64).reshape(-1, 3, 3)
             s.child_ratio = np.array([k[3] for k in kids], np.float64)
+        if self.joints:
+            s.joint_type = np.array([j[0] for j in self.joints], np.int32)
+            s.joint_body = np.array([[j[1], j[2]] for j in self.joints], np.int32)
+            s.joint_flag = np.array([j[3] for j in self.joints], np.int32)
+            s.joint_real = np.array([j[4] for j in self.joints], np.float64)
+        if self.ignores:
+            s.ignore_pairs = np.array(self.ignores, np.int32)
         B = self.bodies
         s.body_shape = np.array([b[0] for b in B], np.int32)
         s.body_flags = np.array([b[1] for b in B], np.int32)
@@ -511,6 +578,113 @@ def compound_pile(n=24, seed=0, real_bits=64, dt=1.0 / 60.0, iterations=10, spac
     return sb.build(real_bits)
 
 
+def joint_demo(real_bits=64, chain=6, motor_speed=2.0, hinge_limits=True, dt=1.0 / 60.0, iterations=10) -> Scene:
+    """The reference's constraints demo (examples/constraints_demo/main.cpp:23-164): a ball-joint
+    double pendulum on a kinematic sphere, a hinge with angle limits carrying a second hinged
+    stick, and a box slider on a kinematic rail between two kinematic stops, with the demo's
+    ignored collision pairs between jointed bodies; plus a motor-driven hinge paddle and a chain
+    of ``chain`` boxes hanging by ball joints from a kinematic anchor, released horizontally."""
+    sb = SceneBuilder(dt=dt, iterations=iterations)
+    pi = np.pi
+    I3 = np.eye(3)
+
+    def xf(b, o):
+        return (np.asarray(b, np.float64), np.asarray(o, np.float64))
+
+    def mul(t1, t2):
+        return (t1[0] @ t2[0], t1[0] @ t2[1] + t1[1])
+
+    def add(kind, params, t, mass=1.0, kinematic=False, restitution=0.5):
+        sh = sb.shape(kind, params)
+        return sb.body(sh, t[1], t[0], mass=mass, friction=0.5, restitution=restitution, kinematic=kinematic,
+                       ang_damp=0.0 if kinematic else 0.8)
+
+    add(BOX, (30, 10, 30), xf(I3, (0, -5, 0)), mass=10000.0, kinematic=True)
+    # ball joints
+    rb2 = add(SPHERE, (0.5,), xf(I3, (0, 0.5, 0)), kinematic=True)
+    rb3 = add(CYLINDER, (0.2, 6), xf(_rot((0, 0, 1), pi / 6), (-3.3 * np.sin(pi / 6), 3.3 * np.cos(pi / 6) + 0.5, 0)))
+    sb.ignore_pair(rb2, rb3)
+    sb.joint(JOINT_BALL, rb2, rb3, (0, 0, 0), (0, -3.3, 0))
+    rb4 = add(SPHERE, (0.4,), xf(I3, (-6.6 * np.sin(pi / 6), 6.6 * np.cos(pi / 6) + 0.5, 0)))
+    sb.ignore_pair(rb4, rb3)
+    rb5 = add(CYLINDER, (0.2, 6), xf(_rot((0, 0, 1), pi / 2), (-3.3 - 6.6 * np.sin(pi / 6), 6.6 * np.cos(pi / 6) + 0.5, 0)))
+    sb.ignore_pair(rb4, rb5)
+    sb.joint(JOINT_BALL, rb4, rb5, (0, 0, 0), (0, -3.3, 0))
+    sb.joint(JOINT_BALL, rb3, rb4, (0, 3.3, 0), (0, 0, 0))
+    # hinge joints
+    t = xf(_rot((1, 0, 0), pi / 6), (4, 8, 0))
+    rb6 = add(CYLINDER, (0.2, 1), t, kinematic=True)
+    rb7 = add(CYLINDER, (0.2, 4), mul(t, xf(_rot((0, 0, -1), pi / 2), (2, 0, 0))))
+    sb.ignore_pair(rb6, rb7)
+    sb.joint(JOINT_HINGE, rb6, rb7, (0, 0, 0), (0, -2, 0), (0, 1, 0), (-1, 0, 0),
+             limits=(-pi / 3, pi / 3) if hinge_limits else None)
+    rb8 = add(CYLINDER, (0.2, 2), mul(t, xf(_rot((1, 0, 0), pi / 2), (4, 0, 0.75))))
+    sb.ignore_pair(rb7, rb8)
+    sb.joint(JOINT_HINGE, rb7, rb8, (0, 2, 0), (0, -0.75, 0), (0, 1, 0), (0, 0, -1))
+    # slider
+    t0 = xf(_rot((0, 1, 0), -pi / 4), (-1, 6, 0))
+    tt = mul(t0, xf(_rot((0, 0, 1), pi / 3), (0, 0, 0)))
+    rail = add(BOX, (0.3, 10, 0.3), tt, kinematic=True)
+    add(BOX, (1, 0.4, 1), mul(tt, xf(I3, (0, 5.2, 0))), kinematic=True)
+    add(BOX, (1, 0.4, 1), mul(tt, xf(I3, (0, -5.2, 0))), kinematic=True)
+    slider = add(BOX, (1, 1.2, 1), mul(tt, xf(I3, (0, 4.4, 0))))
+    sb.ignore_pair(rail, slider)
+    sb.joint(JOINT_SLIDER, rail, slider, (0, 0, 0), (0, 0, 0), (0, 1, 0), (0, 1, 0))
+    # motor hinge: a paddle spun about a kinematic post
+    post = add(BOX, (0.2, 2, 0.2), xf(I3, (8, 1, -4)), kinematic=True)
+    paddle = add(BOX, (2, 0.2, 0.5), xf(I3, (8, 2.3, -4)))
+    sb.ignore_pair(post, paddle)
+    sb.joint(JOINT_HINGE, post, paddle, (0, 1.3, 0), (0, 0, 0), (0, 1, 0), (0, 1, 0), motor_speed=motor_speed)
+    # a chain of boxes hanging from a kinematic anchor by ball joints, released horizontally
+    prev = add(SPHERE, (0.2,), xf(I3, (-8, 10, 5)), kinematic=True)
+    link = _rot((0, 0, 1), pi / 2)
+    for k in range(chain):
+        cur = add(BOX, (0.3, 1.0, 0.3), xf(link, (-8 + 0.5 + k * 1.0, 10, 5)))
+        sb.ignore_pair(prev, cur)
+        sb.joint(JOINT_BALL, prev, cur, (0, 0, 0) if k == 0 else (0, -0.5, 0), (0, 0.5, 0))
+        prev = cur
+    return sb.build(real_bits)
+
+
+def chain_field(n_chains=64, links=8, seed=0, spacing=3.0, height=6.0, hinge_limits=True, real_bits=64, dt=1.0 / 60.0,
+                iterations=10) -> Scene:
+    """``n_chains`` chains of ``links`` boxes, each hanging from a kinematic anchor sphere and
+    released horizontally above a static ground box.  Consecutive links are joined by a ball joint,
+    a hinge (every third joint, limited to +-60 degrees on odd chains, motor-driven on chains
+    divisible by 4) or a slider (every fifth joint); jointed neighbours ignore each other's
+    collisions, so the links meet the ground and the other chains only."""
+    rng = np.random.default_rng(seed)
+    sb = SceneBuilder(dt=dt, iterations=iterations)
+    g = sb.shape(BOX, (n_chains ** 0.5 * spacing * 2 + 20, 1.0, n_chains ** 0.5 * spacing * 2 + 20))
+    sb.body(g, (0, -0.5, 0), mass=0.0, kinematic=True)
+    ball = sb.shape(SPHERE, (0.15,))
+    link = sb.shape(BOX, (0.8, 0.25, 0.25))
+    side = int(np.ceil(np.sqrt(n_chains)))
+    for c in range(n_chains):
+        cx, cz = divmod(c, side)
+        x0 = (cx - (side - 1) / 2) * spacing + rng.uniform(-0.2, 0.2)
+        z0 = (cz - (side - 1) / 2) * spacing + rng.uniform(-0.2, 0.2)
+        yaw = _rot((0, 1, 0), rng.uniform(0, 2 * np.pi))
+        d = yaw @ np.array([1.0, 0, 0])
+        a0 = np.array([x0, height + rng.uniform(0, 1), z0])
+        prev = sb.body(ball, a0, kinematic=True, mass=0.0)
+        for k in range(links):
+            cur = sb.body(link, a0 + d * (0.4 + 0.8 * k), yaw, mass=float(rng.uniform(0.5, 2.0)), ang_damp=0.1,
+                          friction=0.5, restitution=0.2)
+            sb.ignore_pair(prev, cur)
+            anc_a = (0, 0, 0) if k == 0 else (0.4, 0, 0)
+            if k > 0 and k % 5 == 0:
+                sb.joint(JOINT_SLIDER, prev, cur, anc_a, (-0.4, 0, 0), (1, 0, 0), (1, 0, 0))
+            elif k > 0 and k % 3 == 0:
+                sb.joint(JOINT_HINGE, prev, cur, anc_a, (-0.4, 0, 0), (0, 0, 1), (0, 0, 1),
+                         limits=(-np.pi / 3, np.pi / 3) if c % 2 and hinge_limits else None,
+                         motor_speed=1.5 if c % 4 == 0 else None)
+            else:
+                sb.joint(JOINT_BALL, prev, cur, anc_a, (-0.4, 0, 0))
+            prev = cur
+    return sb.build(real_bits)
+
+
 def concat(scenes):
     """Scenes side by side in one Scene (bodies of scene i at [off[i], off[i+1])); shapes are
     concatenated and re-indexed.  Used for batched stepping of independent scenes."""
@@ -524,7 +698,13 @@ def concat(scenes):
     offs = [0]
     kid_cols = {k: [] for k in ("cmp_beg", "cmp_cnt", "child_shape", "child_origin", "child_basis", "child_ratio")}
     kb = 0
+    extra = {k: [] for k in ("joint_type", "joint_body", "joint_flag", "joint_real", "ignore_pairs")}
     for s in scenes:
+        extra["joint_type"].append(s.joint_type)
+        extra["joint_body"].append(s.joint_body + offs[-1])
+        extra["joint_flag"].append(s.joint_flag)
+        extra["joint_real"].append(s.joint_real)
+        extra["ignore_pairs"].append(s.ignore_pairs + offs[-1])
         cb, cc = s.compound_tables()
         kid_cols["cmp_beg"].append(cb + kb)
         kid_cols["cmp_cnt"].append(cc)
@@ -556,6 +736,11 @@ def concat(scenes):
         setattr(out, k, np.concatenate(v))
     out.hull_verts = out.hull_verts.reshape(-1, 3)
     out.hull_face_off = np.array(face_off, np.int32)
+    out.joint_type = np.concatenate(extra["joint_type"]).astype(np.int32)
+    out.joint_body = np.concatenate(extra["joint_body"]).astype(np.int32).reshape(-1, 2)
+    out.joint_flag = np.concatenate(extra["joint_flag"]).astype(np.int32)
+    out.joint_real = np.concatenate(extra["joint_real"]).reshape(-1, 15)
+    out.ignore_pairs = np.concatenate(extra["ignore_pairs"]).astype(np.int32).reshape(-1, 2)
     if kb:
         for k, v in kid_cols.items():
             setattr(out, k, np.concatenate(v))

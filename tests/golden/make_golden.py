@@ -38,6 +38,14 @@ CASES = {
     "pile_f32": (lambda: sc.pile(48, seed=6, real_bits=32, hull_range=(8, 24), drop=(0.0, 0.3)), 32, 40,
                  [0, 1, 24, 25, 38, 39]),
 }
+# joints: the reference's constraints demo (ball-joint pendulum, limited hinges, slider) plus a
+# motor hinge and a hanging ball-joint chain, with ignored collision pairs
+# (the "_nolimit" variants leave out the hinge angle limit, whose angle comes from atan2)
+for bits in (64, 32):
+    CASES[f"joints_f{bits}"] = (lambda bits=bits: sc.joint_demo(real_bits=bits), bits, 180,
+                                [0, 1, 2, 30, 60, 61, 90, 120, 150, 178, 179])
+    CASES[f"joints_nolimit_f{bits}"] = (lambda bits=bits: sc.joint_demo(hinge_limits=False, real_bits=bits), bits, 180,
+                                        [0, 1, 2, 30, 60, 61, 90, 120, 150, 178, 179])
 # compound bodies (jacks, dumbbells, box + hull caps) among primitives on a ground box
 for bits in (64, 32):
     CASES[f"compound_f{bits}"] = (lambda bits=bits: sc.compound_pile(n=24, seed=3 + bits, drop=(0.0, 0.5), real_bits=bits),

@@ -15,6 +15,15 @@ from pe_testlib import compare_results, compare_state, dump_state, golden_names,
 pytestmark = pytest.mark.gpu
 
 
+# fixtures whose hinge angle limits are active: the limit angle comes from atan2, where CUDA's
+# and the C library's results may differ in the last place, and (min_angle - angle) cancels, so
+# their solved velocities are held to a per-step bound instead of bit equality: 1e-6 in FP64,
+# 5e-6 in FP32 (a last-place change of a float angle near the limit moves the limit impulse's
+# velocities by up to ~3e-6)
+ATAN2_FIXTURES = {"joints_f64", "joints_f32"}
+PER_STEP_ATOL = {64: 1e-6, 32: 5e-6}
+
+
 def keys_tie_free(d, axis):
     k = d["aabb_min"][:, axis]
     return len(np.unique(k)) == len(k)
@@ -46,8 +55,13 @@ def test_gpu_phases_match_reference(name):
         g.set_results(results_of(d))
         g.solve(pg.SERIAL_ORDER)
         st = g.state()
-        np.testing.assert_array_equal(st["lin_vel"], d["lin_vel_post"], err_msg=f"{name} solve step {k}")
-        np.testing.assert_array_equal(st["ang_vel"], d["ang_vel_post"], err_msg=f"{name} solve step {k}")
+        if name in ATAN2_FIXTURES:
+            for f in ("lin_vel", "ang_vel"):
+                np.testing.assert_allclose(st[f], d[f + "_post"], rtol=0, atol=PER_STEP_ATOL[bits],
+                                           err_msg=f"{name} solve step {k}")
+        else:
+            np.testing.assert_array_equal(st["lin_vel"], d["lin_vel_post"], err_msg=f"{name} solve step {k}")
+            np.testing.assert_array_equal(st["ang_vel"], d["ang_vel_post"], err_msg=f"{name} solve step {k}")
         # integration from the previous step's end state
         if k - 1 in rec:
             p = rec[k - 1]
@@ -59,7 +73,7 @@ def test_gpu_phases_match_reference(name):
 
 
 @pytest.mark.parametrize("name", ["cube_f32", "cube_f64", "zoo_22_f64", "zoo_23_f32", "zoo_33_f64", "pile_f64", "compound_f64",
-                                  "compound_f32"])
+                                  "compound_f32", "joints_nolimit_f64", "joints_nolimit_f32"])
 def test_gpu_full_steps_serial_order_match_reference(name):
     """Whole steps on the device in serial-order mode reproduce the reference trajectory
     (scenes whose sort keys never tie, so the broadphase order is the reference's)."""
