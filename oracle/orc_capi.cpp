@@ -98,7 +98,7 @@ template <class R> void build(World<R>& W, const SceneFile& s) {
                     face.normal = normalized(cross(vs[face.idx[1]] - p1, vs[face.idx[2]] - p1));
                     fs.push_back(face);
                 }
-                W.shapes.push_back(make_hull<R>(vs, fs));
+                W.shapes.push_back(s.type[i] == ST_CONCAVE ? make_concave<R>(vs, fs) : make_hull<R>(vs, fs));
             }
         }
     }

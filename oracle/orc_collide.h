@@ -920,8 +920,8 @@ template <class R> bool sphere_triangle(const V3<R>& ctr, R radius, const V3<R>*
 }
 
 // sphere_convex_collision_algorithm.cpp:11-34, 165-211
-template <class R> bool sphere_hull(PairCtx<R>& c) {
-    const bool a_is_hull = c.sa->type == ST_HULL;
+template <class R> bool sphere_hull(PairCtx<R>& c) {   // also the concave mesh (concave_sphere_collision_algorithm.cpp:8-31)
+    const bool a_is_hull = c.sa->type == ST_HULL || c.sa->type == ST_CONCAVE;
     const Shape<R>& mesh = a_is_hull ? *c.sa : *c.sb;
     const Shape<R>& sph = a_is_hull ? *c.sb : *c.sa;
     const Transform<R>& tm = a_is_hull ? *c.ta : *c.tb;
@@ -990,8 +990,8 @@ template <class R> bool segment_face(const Face<R>& f, const Shape<R>& mesh, con
 }
 
 // cylinder_convex_collision_algorithm.cpp:11-51, 109-203
-template <class R> bool cylinder_hull(PairCtx<R>& c) {
-    const bool a_is_hull = c.sa->type == ST_HULL;
+template <class R> bool cylinder_hull(PairCtx<R>& c) {   // also the concave mesh (concave_cylinder_collision_algorithm.cpp:37-47)
+    const bool a_is_hull = c.sa->type == ST_HULL || c.sa->type == ST_CONCAVE;
     const Shape<R>& mesh = a_is_hull ? *c.sa : *c.sb;
     const Shape<R>& cyl = a_is_hull ? *c.sb : *c.sa;
     const Transform<R>& to = a_is_hull ? *c.ta : *c.tb;
@@ -1072,6 +1072,42 @@ template <class R> bool cylinder_hull(PairCtx<R>& c) {
 // narrow_phase_base.cpp:20-29 dispatch restricted to box/sphere/cylinder/convex-mesh
 template <class R> bool collide(PairCtx<R>& c);
 
+// ConcaveConvexCollisionAlgorithm (concave_convex_collision_algorithm.cpp:8-67), for a box or a
+// convex mesh against a concave mesh (ConcaveBoxCollisionAlgorithm routes boxes here too): the
+// convex shape's box in the concave mesh's frame selects faces through the face tree; each face
+// becomes a one-face convex shape (its vertices in face order, its normal, no unique edges and no
+// face tree: setMesh is never called on it) run through the convex-convex algorithm with the
+// convex shape first, at the concave body's transform.
+template <class R> bool concave_convex(PairCtx<R>& c) {
+    const bool a_concave = c.sa->type == ST_CONCAVE;
+    const Shape<R>& cc = a_concave ? *c.sa : *c.sb;
+    const Shape<R>* cv = a_concave ? c.sb : c.sa;
+    const Transform<R>* tcc = a_concave ? c.ta : c.tb;
+    const Transform<R>* tcv = a_concave ? c.tb : c.ta;
+    c.res->swap = a_concave;
+    V3<R> AA, BB;
+    get_aabb(*cv, tcc->inverse() * *tcv, AA, BB);
+    std::vector<int> hit;
+    bvh_search(cc, AA, BB, hit);
+    for (int fi : hit) {
+        const Face<R>& f = cc.faces[fi];
+        Shape<R> face;
+        face.type = ST_HULL;
+        Face<R> ff;
+        for (size_t k = 0; k < f.idx.size(); k++) {
+            face.verts.push_back(cc.verts[f.idx[k]]);
+            ff.idx.push_back((int)k);
+        }
+        ff.normal = f.normal;
+        face.faces.push_back(ff);
+        PairCtx<R> s = c;
+        s.sa = cv; s.sb = &face; s.ta = tcv; s.tb = tcc;
+        convex_convex(s);
+    }
+    c.res->swap = false;
+    return true;
+}
+
 // CompoundCompoundCollisionAlgorithm::processCollision (compound_compound_collision_algorithm.cpp:8-37):
 // the compound goes first (a compound second swaps shapes, transforms and the result's objects,
 // so the result then names the compound as object A); every child (against every child of a
@@ -1108,6 +1144,13 @@ template <class R> bool compound_collide(PairCtx<R>& c) {
 template <class R> bool collide(PairCtx<R>& c) {
     const int ta = c.sa->type, tb = c.sb->type;
     if (ta == ST_COMPOUND || tb == ST_COMPOUND) return compound_collide(c);
+    if (ta == ST_CONCAVE || tb == ST_CONCAVE) {   // narrow_phase_base.cpp:20-29, row and column 4
+        const int o = ta == ST_CONCAVE ? tb : ta;
+        if (o == ST_SPHERE) return sphere_hull(c);
+        if (o == ST_CYLINDER) return cylinder_hull(c);
+        if (o == ST_BOX || o == ST_HULL) return concave_convex(c);
+        return false;   // concave-concave: no algorithm
+    }
     auto is = [&](int x, int y) { return (ta == x && tb == y) || (ta == y && tb == x); };
     if (ta == ST_BOX && tb == ST_BOX) return box_box(c);
     if (is(ST_BOX, ST_SPHERE)) return box_sphere(c);

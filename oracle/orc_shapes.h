@@ -9,7 +9,7 @@
 
 namespace orc {
 
-enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3, ST_COMPOUND = 5 };
+enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3, ST_CONCAVE = 4, ST_COMPOUND = 5 };
 
 template <class R> struct Shape;
 // one CompoundShape::ShapeEle (compound_shape.h:10-14); `s` points into the world's shape table
@@ -362,6 +362,20 @@ template <class R> Shape<R> make_hull(std::vector<V3<R>> verts, std::vector<Face
             }
         }
     }
+    return s;
+}
+
+// ConcaveMeshShape::setMesh (concave_mesh_shape.cpp:6-17): the mesh as given (no recentring, no
+// unique edges), unit local inertia, zero volume, and the face tree with leaves of
+// max(faces / 2047, 1) faces (the tree sorts the faces in place).
+template <class R> Shape<R> make_concave(std::vector<V3<R>> verts, std::vector<Face<R>> faces) {
+    Shape<R> s;
+    s.type = ST_CONCAVE;
+    s.verts = std::move(verts);
+    s.faces = std::move(faces);
+    s.local_inertia = M3<R>::identity();
+    s.volume = 0;
+    build_bvh(s, 0, (int)s.faces.size() - 1, std::max((int)s.faces.size() / 2047, 1));
     return s;
 }
 

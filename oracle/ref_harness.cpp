@@ -17,6 +17,7 @@
 #include "rigid/shape/cylinder_shape.h"
 #include "rigid/shape/convex_mesh_shape.h"
 #include "rigid/shape/compound_shape.h"
+#include "rigid/shape/concave_mesh_shape.h"
 #include "rigid/constraint/constraint/ball_joint_constraint.h"
 #include "rigid/constraint/constraint/hinge_joint_constraint.h"
 #include "rigid/constraint/constraint/slider_joint_constraint.h"
@@ -116,7 +117,8 @@ pe_phys_shape::Shape* make_shape(const Scene& s, int i) {
         case 0: return new pe_phys_shape::BoxShape(pe::Vector3(PE_R(p[0]), PE_R(p[1]), PE_R(p[2])));
         case 1: return new pe_phys_shape::SphereShape(PE_R(p[0]));
         case 2: return new pe_phys_shape::CylinderShape(PE_R(p[0]), PE_R(p[1]));
-        case 3: {
+        case 3:
+        case 4: {
             pe::Mesh mesh;
             for (int k = 0; k < s.hvcnt[i]; k++) {
                 const double* q = &s.hverts[(s.hvbeg[i] + k) * 3];
@@ -128,6 +130,11 @@ pe_phys_shape::Shape* make_shape(const Scene& s, int i) {
                 mesh.faces.push_back(face);
             }
             pe::Mesh::perFaceNormal(mesh);
+            if (s.type[i] == 4) {
+                auto* cc = new pe_phys_shape::ConcaveMeshShape();
+                cc->setMesh(mesh);
+                return cc;
+            }
             auto* cm = new pe_phys_shape::ConvexMeshShape();
             cm->setMesh(mesh);
             return cm;

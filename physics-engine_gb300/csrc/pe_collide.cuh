@@ -809,8 +809,28 @@ template <class R> __device__ bool face_hit(const ShapeView<R>& m, int f, const 
     return true;
 }
 
+// BVH::search (bvh.cpp:105-125) of a mesh's face tree for the box [aa, bb]: the right-first stack
+// walk of a tree built on index ranges meets the leaves in descending order and reports every face
+// of a leaf whose box overlaps, ascending.  Convex meshes (one face per leaf) test the face boxes.
+template <class R, class Visit>
+__device__ void mesh_query(const ShapeView<R>& m, const V3<R>& aa, const V3<R>& bb, Visit&& visit) {
+    if (m.nl == 0) {
+        for (int f = m.nf - 1; f >= 0; f--)
+            if (face_hit(m, f, aa, bb)) visit(f);
+        return;
+    }
+    for (int l = m.nl - 1; l >= 0; l--) {
+        const R* mn = m.l_min + l * 3;
+        const R* mx = m.l_max + l * 3;
+        if (mn[0] > bb.x || mn[1] > bb.y || mn[2] > bb.z) continue;
+        if (mx[0] < aa.x || mx[1] < aa.y || mx[2] < aa.z) continue;
+        for (int f = m.l_beg[l], e = m.l_beg[l] + m.l_cnt[l]; f < e; f++) visit(f);
+    }
+}
+__host__ __device__ inline bool is_mesh(int t) { return t == ST_HULL || t == ST_CONCAVE; }
+
 template <class R> __device__ bool sphere_hull(Pair<R>& c) {   // sphere_convex_collision_algorithm.cpp:11-34, 165-211
-    const bool a_hull = c.sa.type == ST_HULL;
+    const bool a_hull = is_mesh(c.sa.type);
     const ShapeView<R>& m = a_hull ? c.sa : c.sb;
     const ShapeView<R>& sp = a_hull ? c.sb : c.sa;
     const Xf<R>& tm = a_hull ? c.ta() : c.tb();
@@ -821,8 +841,7 @@ template <class R> __device__ bool sphere_hull(Pair<R>& c) {   // sphere_convex_
     const R r = sp.radius;
     const V3<R> aa = rel - V3<R>(r, r, r), bb = rel + V3<R>(r, r, r);
     bool ret = false;
-    for (int f = m.nf - 1; f >= 0; f--) {
-        if (!face_hit(m, f, aa, bb)) continue;
+    mesh_query(m, aa, bb, [&](int f) {
         const int n = m.face_size(f);
         for (int i = 0; i < n - 2; i++) {
             const V3<R> vs[3] = {m.vert(m.face_vert(f, 0)), m.vert(m.face_vert(f, i + 1)), m.vert(m.face_vert(f, i + 2))};
@@ -835,7 +854,7 @@ template <class R> __device__ bool sphere_hull(Pair<R>& c) {   // sphere_convex_
                 ret = true;
             }
         }
-    }
+    });
     c.c->swap = false;
     return ret;
 }
@@ -875,7 +894,7 @@ template <class R> __device__ bool segment_face(const ShapeView<R>& m, int f, co
 }
 
 template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_convex_collision_algorithm.cpp:11-51, 109-203
-    const bool a_hull = c.sa.type == ST_HULL;
+    const bool a_hull = is_mesh(c.sa.type);
     const ShapeView<R>& m = a_hull ? c.sa : c.sb;
     const ShapeView<R>& cy = a_hull ? c.sb : c.sa;
     const Xf<R>& to = a_hull ? c.ta() : c.tb();
@@ -899,8 +918,7 @@ template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_con
             c.add(n, p2 - n * margin, d2 + margin * 2);
         }
     };
-    for (int f = m.nf - 1; f >= 0; f--) {
-        if (!face_hit(m, f, aa, bb)) continue;
+    mesh_query(m, aa, bb, [&](int f) {
         const V3<R> fn = m.face_normal(f);
         const R adc = dot(axis, fn);
         V3<R> ddx, ddz;
@@ -925,9 +943,8 @@ template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_con
                 seg_on_mesh(f, ps, ddy * R(-dxs[i]), ch * 2);
             }
         }
-    }
-    for (int f = m.nf - 1; f >= 0; f--) {
-        if (!face_hit(m, f, aa, bb)) continue;
+    });
+    mesh_query(m, aa, bb, [&](int f) {
         const int n = m.face_size(f);
         for (int i = 0; i < n; i++) {
             const V3<R> v1 = m.vert(m.face_vert(f, i));
@@ -941,7 +958,54 @@ template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_con
                 add_on_cylinder(c, (p1 + p2) / R(2), pos, axis, cr, ch, to, margin);
             }
         }
-    }
+    });
+    c.c->swap = false;
+    return true;
+}
+
+// ======================================================================= concave meshes
+// ConcaveConvexCollisionAlgorithm (concave_convex_collision_algorithm.cpp:8-67; boxes go the same
+// way through ConcaveBoxCollisionAlgorithm): the convex shape's box in the concave mesh's frame
+// selects faces through the face tree; each face becomes a one-face convex shape (its vertices in
+// face order, its normal, no unique edges: setMesh is never called on it) that the convex-convex
+// algorithm meets with the convex shape first, at the concave body's transform.
+constexpr int kFaceVerts = 32;   // longest face polygon a concave mesh may hold (checked at upload)
+template <class R> __device__ bool concave_convex(Pair<R>& c) {
+    const bool a_cc = c.sa.type == ST_CONCAVE;
+    const ShapeView<R>& cc = a_cc ? c.sa : c.sb;
+    const ShapeView<R> cv = a_cc ? c.sb : c.sa;
+    const Xf<R> tcc = a_cc ? c.xa : c.xb;
+    const Xf<R> tcv = a_cc ? c.xb : c.xa;
+    c.c->swap = a_cc;
+    V3<R> aa, bb;
+    shape_aabb(cv, tcc.inverse() * tcv, aa, bb);
+    R fv[kFaceVerts * 3];
+    int fidx[kFaceVerts];
+    int foff[2];
+    R fn[3], fmn[3], fmx[3];
+    mesh_query(cc, aa, bb, [&](int f) {
+        const int n = cc.face_size(f);
+        foff[0] = 0;
+        foff[1] = n;
+        for (int k = 0; k < 3; k++) { fmn[k] = Lim<R>::max(); fmx[k] = Lim<R>::min(); }
+        for (int i = 0; i < n; i++) {
+            const V3<R> p = cc.vert(cc.face_vert(f, i));
+            fv[i * 3] = p.x; fv[i * 3 + 1] = p.y; fv[i * 3 + 2] = p.z;
+            fidx[i] = i;
+            for (int k = 0; k < 3; k++) { fmn[k] = fmn[k] < p[k] ? fmn[k] : p[k]; fmx[k] = fmx[k] > p[k] ? fmx[k] : p[k]; }
+        }
+        const V3<R> nrm = cc.face_normal(f);
+        fn[0] = nrm.x; fn[1] = nrm.y; fn[2] = nrm.z;
+        ShapeView<R> face = cc;
+        face.type = ST_HULL;
+        face.hv = fv; face.nv = n;
+        face.f_off = foff; face.f_idx = fidx; face.f_n = fn; face.f_min = fmn; face.f_max = fmx; face.nf = 1;
+        face.e_a = nullptr; face.e_b = nullptr; face.ne = 0;
+        face.nl = 0;
+        Pair<R> s = c;
+        s.sa = cv; s.sb = face; s.xa = tcv; s.xb = tcc;
+        convex_convex(s);
+    });
     c.c->swap = false;
     return true;
 }
@@ -953,11 +1017,12 @@ template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_con
 // the shared-memory staging limits) the unstaged warp path.
 enum PairClass { PC_BOX_BOX = 0, PC_BOX_SPHERE, PC_SPHERE_SPHERE, PC_SPHERE_CYL, PC_BOX_CYL, PC_CONVEX, PC_SPHERE_HULL,
                  PC_CYL_HULL, PC_CONVEX_HEAVY, PC_CONVEX_BIG, PC_CONVEX_HULL_HULL, PC_CONVEX_CYL_CYL, PC_CONVEX_HULL_BOX,
-                 PC_COMPOUND, PC_COUNT };
+                 PC_COMPOUND, PC_CONCAVE, PC_COUNT };
 
 __host__ __device__ inline int pair_class(int ta, int tb) {
     const int lo = ta < tb ? ta : tb, hi = ta < tb ? tb : ta;
     if (hi == ST_COMPOUND) return PC_COMPOUND;   // CompoundCompoundCollisionAlgorithm, either side
+    if (lo == ST_CONCAVE || hi == ST_CONCAVE) return PC_CONCAVE;   // the Concave*CollisionAlgorithm family
     if (lo == ST_BOX && hi == ST_BOX) return PC_BOX_BOX;
     if (lo == ST_BOX && hi == ST_SPHERE) return PC_BOX_SPHERE;
     if (lo == ST_SPHERE && hi == ST_SPHERE) return PC_SPHERE_SPHERE;
@@ -968,8 +1033,18 @@ __host__ __device__ inline int pair_class(int ta, int tb) {
     return PC_CONVEX;   // cylinder-cylinder, box-hull, hull-hull
 }
 
+// a concave mesh against any convex shape (narrow_phase_base.cpp:20-29, row and column 4);
+// concave-concave has no algorithm
+template <class R> __device__ void concave_pair(Pair<R>& c) {
+    const int o = c.sa.type == ST_CONCAVE ? c.sb.type : c.sa.type;
+    if (o == ST_SPHERE) sphere_hull(c);
+    else if (o == ST_CYLINDER) cylinder_hull(c);
+    else if (o == ST_BOX || o == ST_HULL) concave_convex(c);
+}
+
 template <class R> __device__ void collide(Pair<R>& c, int cls) {
     switch (cls) {
+        case PC_CONCAVE: concave_pair(c); break;
         case PC_BOX_BOX: box_box(c); break;
         case PC_BOX_SPHERE: box_sphere(c); break;
         case PC_SPHERE_SPHERE: sphere_sphere(c); break;

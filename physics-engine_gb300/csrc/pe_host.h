@@ -21,8 +21,12 @@ template <class R> struct HullPrep {
     std::vector<R> e_a, e_b;          // [ne*3]
     M3<R> inertia;                    // per unit mass (divided by the volume)
     R volume = 0;
+    std::vector<int> l_beg, l_cnt;    // concave meshes: face-tree leaves in tree order (face ranges)
+    std::vector<R> l_min, l_max;      // [nl*3] leaf boxes
 };
-template <class R> HullPrep<R> prepare_hull(const double* verts, int nv, const int* face_off, const int* face_idx, int nf);
+// ConvexMeshShape::setMesh, or ConcaveMeshShape::setMesh with `concave`
+template <class R> HullPrep<R> prepare_hull(const double* verts, int nv, const int* face_off, const int* face_idx, int nf,
+                                            bool concave = false);
 
 // A scene as a caller describes it (the arrays of pe_gpu_set_shapes and pe_gpu_set_bodies), owned
 // on the host; shape indices of the bodies and hull indices are local to the scene.

@@ -136,7 +136,17 @@ template <class R> void face_tree(std::vector<HFace<R>>& faces, const std::vecto
 }
 } // namespace
 
-template <class R> HullPrep<R> prepare_hull(const double* verts, int nv, const int* face_off, const int* face_idx, int nf) {
+// leaves of the face tree over [l, r] (the splits of face_tree), in tree order
+static void tree_leaves(int l, int r, int leaf, std::vector<std::pair<int, int>>& out) {
+    if (l > r) return;
+    if (r - l + 1 <= leaf) { out.emplace_back(l, r); return; }
+    const int mid = (l + r) / 2;
+    tree_leaves(l, mid, leaf, out);
+    tree_leaves(mid + 1, r, leaf, out);
+}
+
+template <class R>
+HullPrep<R> prepare_hull(const double* verts, int nv, const int* face_off, const int* face_idx, int nf, bool concave) {
     std::vector<V3<R>> v(nv);
     for (int i = 0; i < nv; i++) v[i] = V3<R>(R(verts[i * 3]), R(verts[i * 3 + 1]), R(verts[i * 3 + 2]));
     std::vector<HFace<R>> faces(nf);
@@ -144,6 +154,46 @@ template <class R> HullPrep<R> prepare_hull(const double* verts, int nv, const i
         for (int k = face_off[f]; k < face_off[f + 1]; k++) faces[f].idx.push_back(face_idx[k]);
         const V3<R>& p1 = v[faces[f].idx[0]];
         faces[f].n = normalized(cross(v[faces[f].idx[1]] - p1, v[faces[f].idx[2]] - p1));   // Mesh::perFaceNormal
+    }
+    if (concave) {
+        // ConcaveMeshShape::setMesh (concave_mesh_shape.cpp:6-17): the mesh as given, unit inertia,
+        // no volume, the face tree with leaves of max(faces / 2047, 1) faces, no unique edges
+        HullPrep<R> h;
+        h.inertia = M3<R>();
+        for (int i = 0; i < 3; i++) h.inertia.m[i][i] = R(1);
+        const int leaf = std::max(nf / 2047, 1);
+        face_tree(faces, v, 0, nf - 1, leaf);
+        for (auto& p : v) { h.v.push_back(p.x); h.v.push_back(p.y); h.v.push_back(p.z); }
+        h.f_off.push_back(0);
+        std::vector<V3<R>> fmn, fmx;
+        for (const auto& f : faces) {
+            V3<R> mn(Lim<R>::max(), Lim<R>::max(), Lim<R>::max()), mx(Lim<R>::min(), Lim<R>::min(), Lim<R>::min());
+            for (int k : f.idx) {
+                h.f_idx.push_back(k);
+                for (int d = 0; d < 3; d++) {
+                    if (v[k][d] < mn[d]) mn[d] = v[k][d];
+                    if (v[k][d] > mx[d]) mx[d] = v[k][d];
+                }
+            }
+            h.f_off.push_back((int)h.f_idx.size());
+            for (int d = 0; d < 3; d++) { h.f_n.push_back(f.n[d]); h.f_min.push_back(mn[d]); h.f_max.push_back(mx[d]); }
+            fmn.push_back(mn);
+            fmx.push_back(mx);
+        }
+        std::vector<std::pair<int, int>> lv;
+        tree_leaves(0, nf - 1, leaf, lv);
+        for (auto& q : lv) {
+            V3<R> mn(Lim<R>::max(), Lim<R>::max(), Lim<R>::max()), mx(Lim<R>::min(), Lim<R>::min(), Lim<R>::min());
+            for (int f = q.first; f <= q.second; f++)
+                for (int d = 0; d < 3; d++) {
+                    if (fmn[f][d] < mn[d]) mn[d] = fmn[f][d];
+                    if (fmx[f][d] > mx[d]) mx[d] = fmx[f][d];
+                }
+            h.l_beg.push_back(q.first);
+            h.l_cnt.push_back(q.second - q.first + 1);
+            for (int d = 0; d < 3; d++) { h.l_min.push_back(mn[d]); h.l_max.push_back(mx[d]); }
+        }
+        return h;
     }
     // polyhedral mass properties (convex_mesh_shape.cpp:29-100), integrals over fan triangles
     const R mult[10] = {R(1.0) / 6, R(1.0) / 24, R(1.0) / 24, R(1.0) / 24, R(1.0) / 60,
@@ -248,7 +298,7 @@ template M3<float> sphere_inertia<float>(float);
 template M3<double> sphere_inertia<double>(double);
 template M3<float> cylinder_inertia<float>(float, float);
 template M3<double> cylinder_inertia<double>(double, double);
-template HullPrep<float> prepare_hull<float>(const double*, int, const int*, const int*, int);
-template HullPrep<double> prepare_hull<double>(const double*, int, const int*, const int*, int);
+template HullPrep<float> prepare_hull<float>(const double*, int, const int*, const int*, int, bool);
+template HullPrep<double> prepare_hull<double>(const double*, int, const int*, const int*, int, bool);
 
 } // namespace pe

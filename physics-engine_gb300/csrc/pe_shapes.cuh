@@ -11,7 +11,7 @@
 
 namespace pe {
 
-enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3, ST_COMPOUND = 5 };
+enum ShapeType { ST_BOX = 0, ST_SPHERE = 1, ST_CYLINDER = 2, ST_HULL = 3, ST_CONCAVE = 4, ST_COMPOUND = 5 };
 
 // unit meshes (host builds them; device reads them from constant memory)
 constexpr int kBoxV = 24, kBoxF = 6, kBoxE = 12;
@@ -49,6 +49,13 @@ template <class R> struct ShapeView {
     const R* e_a;              // unique edge endpoints [ne*3]
     const R* e_b;
     int ne;
+    // concave meshes: the face tree's leaves in tree order, each a face range and its box
+    // (nl == 0 for convex meshes, whose leaves hold one face each)
+    int nl;
+    const int* l_beg;
+    const int* l_cnt;
+    const R* l_min;            // [nl*3]
+    const R* l_max;
 
 #ifdef __CUDACC__
     __device__ int face_count() const { return type == ST_BOX ? kBoxF : (type == ST_CYLINDER ? kCylF : nf); }
@@ -98,6 +105,8 @@ template <class R> struct ShapeTable {
     const int* h_vbeg; const int* h_vcnt; const int* h_fbeg; const int* h_fcnt; const int* h_ebeg; const int* h_ecnt;
     const R* hv; const int* f_off; const int* f_idx; const R* f_n; const R* f_min; const R* f_max;
     const R* e_a; const R* e_b;
+    // concave meshes (hull tables plus the face-tree leaves): leaves [h_lbeg[h], h_lbeg[h] + h_lcnt[h])
+    const int* h_lbeg; const int* h_lcnt; const int* lf_beg; const int* lf_cnt; const R* lf_min; const R* lf_max;
     // compound shapes: children [c_beg[s], c_beg[s] + c_cnt[s]) of shape s, each a non-compound
     // shape c_shape[k] at local transform c_xf[12k..] (basis row-major, then origin), relocated by
     // CompoundShape::init()
@@ -122,13 +131,19 @@ template <class R> struct ShapeTable {
         v.r2 = p0 * 2;
         v.hv = nullptr; v.nv = 0; v.f_off = nullptr; v.f_idx = nullptr; v.f_n = nullptr; v.f_min = nullptr; v.f_max = nullptr;
         v.nf = 0; v.e_a = nullptr; v.e_b = nullptr; v.ne = 0;
-        if (v.type == ST_HULL) {
+        v.nl = 0; v.l_beg = nullptr; v.l_cnt = nullptr; v.l_min = nullptr; v.l_max = nullptr;
+        if (v.type == ST_HULL || v.type == ST_CONCAVE) {
             const int h = hull[s];
             const int vb = h_vbeg[h], fb = h_fbeg[h], eb = h_ebeg[h];
             v.hv = hv + vb * 3; v.nv = h_vcnt[h];
             v.f_off = f_off + fb; v.f_idx = f_idx; v.f_n = f_n + fb * 3; v.f_min = f_min + fb * 3; v.f_max = f_max + fb * 3;
             v.nf = h_fcnt[h];
             v.e_a = e_a + eb * 3; v.e_b = e_b + eb * 3; v.ne = h_ecnt[h];
+            if (v.type == ST_CONCAVE) {
+                const int lb = h_lbeg[h];
+                v.nl = h_lcnt[h];
+                v.l_beg = lf_beg + lb; v.l_cnt = lf_cnt + lb; v.l_min = lf_min + lb * 3; v.l_max = lf_max + lb * 3;
+            }
         }
         return v;
     }

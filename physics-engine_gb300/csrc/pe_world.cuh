@@ -235,6 +235,11 @@ private:
     // host copies of the shape tables (shapes are only ever appended after set_shapes)
     std::vector<int> h_shull_, h_hvb_, h_hvc_, h_hfb_, h_hfc_, h_heb_, h_hec_, h_foff_, h_fidx_;
     std::vector<R> h_hv_, h_fn_, h_fmn_, h_fmx_, h_ea_, h_eb_;
+    // concave meshes' face-tree leaves (per hull: first leaf and count; per leaf: face range and box)
+    DBuf<int> hlbeg_, hlcnt_, lfbeg_, lfcnt_;
+    DBuf<R> lfmin_, lfmax_;
+    std::vector<int> h_hlb_, h_hlc_, h_lfb_, h_lfc_;
+    std::vector<R> h_lfmn_, h_lfmx_;
     // compound children (per shape: first child and count; per child: shape and 12-real transform)
     DBuf<int> cbeg_, ccnt_, cshape_;
     DBuf<R> cxf_;

@@ -65,6 +65,7 @@ template <class R> ShapeTable<R> World<R>::shapes() const {
     t.hv = hv_.p; t.f_off = hfoff_.p; t.f_idx = hfidx_.p; t.f_n = hfn_.p; t.f_min = hfmin_.p; t.f_max = hfmax_.p;
     t.e_a = hea_.p; t.e_b = heb_.p;
     t.c_beg = cbeg_.p; t.c_cnt = ccnt_.p; t.c_shape = cshape_.p; t.c_xf = cxf_.p;
+    t.h_lbeg = hlbeg_.p; t.h_lcnt = hlcnt_.p; t.lf_beg = lfbeg_.p; t.lf_cnt = lfcnt_.p; t.lf_min = lfmin_.p; t.lf_max = lfmax_.p;
     return t;
 }
 
@@ -107,6 +108,7 @@ void World<R>::set_shapes(int S, const int* type, const double* param, const int
     h_hv_.clear(); h_fn_.clear(); h_fmn_.clear(); h_fmx_.clear(); h_ea_.clear(); h_eb_.clear();
     hull_by_content_.clear();
     h_cbeg_.clear(); h_ccnt_.clear(); h_cshape_.clear(); h_cready_.clear(); h_cxf_.clear();
+    h_hlb_.clear(); h_hlc_.clear(); h_lfb_.clear(); h_lfc_.clear(); h_lfmn_.clear(); h_lfmx_.clear();
     append_shapes(S, type, param, vbeg, vcnt, fbeg, fcnt, hv, foff, fidx);
 }
 
@@ -115,15 +117,15 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
                             const int* fcnt, const double* hv, const int* foff, const int* fidx, std::vector<int>* remap) {
     const int s0 = S_;
     const size_t o_h = h_hvb_.size(), o_v = h_hv_.size(), o_f = h_fn_.size(), o_e = h_ea_.size(), o_fo = h_foff_.size(),
-                 o_fi = h_fidx_.size();
+                 o_fi = h_fidx_.size(), o_l = h_lfb_.size();
     if (remap) remap->assign(S, -1);
     int added = 0;
     for (int s = 0; s < S; s++) {
         const int t = type[s];
         std::string key;
-        if (remap && t == ST_HULL) {   // content key: vertices, then face index lists
+        if (remap && (t == ST_HULL || t == ST_CONCAVE)) {   // content key: kind, vertices, then face index lists
             key.reserve((size_t)vcnt[s] * 24 + (size_t)(foff[fbeg[s] + fcnt[s]] - foff[fbeg[s]] + fcnt[s] + 3) * 4);
-            const int head[3] = {vcnt[s], fcnt[s], foff[fbeg[s] + fcnt[s]] - foff[fbeg[s]]};
+            const int head[4] = {t, vcnt[s], fcnt[s], foff[fbeg[s] + fcnt[s]] - foff[fbeg[s]]};
             key.append(reinterpret_cast<const char*>(head), sizeof head);
             key.append(reinterpret_cast<const char*>(hv + (size_t)vbeg[s] * 3), (size_t)vcnt[s] * 3 * sizeof(double));
             for (int f = 0; f < fcnt[s]; f++) {
@@ -146,13 +148,24 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
         if (t == ST_BOX) inertia = box_inertia(p);
         else if (t == ST_SPHERE) inertia = sphere_inertia(p.x);
         else if (t == ST_CYLINDER) inertia = cylinder_inertia(p.x, p.y);
-        else if (t == ST_HULL) {
+        else if (t == ST_HULL || t == ST_CONCAVE) {
             // local face offsets of this shape
             std::vector<int> lo(fcnt[s] + 1);
             for (int f = 0; f <= fcnt[s]; f++) lo[f] = foff[fbeg[s] + f] - foff[fbeg[s]];
-            if (fcnt[s] >= 16382) throw std::runtime_error("convex mesh with more than 16381 faces is not supported");
-            HullPrep<R> h = prepare_hull<R>(hv + (size_t)vbeg[s] * 3, vcnt[s], lo.data(), fidx + foff[fbeg[s]], fcnt[s]);
+            if (t == ST_HULL && fcnt[s] >= 16382) throw std::runtime_error("convex mesh with more than 16381 faces is not supported");
+            if (t == ST_CONCAVE)
+                for (int f = 0; f < fcnt[s]; f++)
+                    if (lo[f + 1] - lo[f] > kFaceVerts)
+                        throw std::runtime_error("concave mesh face with more than " + std::to_string(kFaceVerts) + " vertices");
+            HullPrep<R> h = prepare_hull<R>(hv + (size_t)vbeg[s] * 3, vcnt[s], lo.data(), fidx + foff[fbeg[s]], fcnt[s],
+                                            t == ST_CONCAVE);
             inertia = h.inertia;
+            h_hlb_.push_back((int)h_lfb_.size());
+            h_hlc_.push_back((int)h.l_beg.size());
+            h_lfb_.insert(h_lfb_.end(), h.l_beg.begin(), h.l_beg.end());
+            h_lfc_.insert(h_lfc_.end(), h.l_cnt.begin(), h.l_cnt.end());
+            h_lfmn_.insert(h_lfmn_.end(), h.l_min.begin(), h.l_min.end());
+            h_lfmx_.insert(h_lfmx_.end(), h.l_max.begin(), h.l_max.end());
             hull = (int)h_hvb_.size();
             h_hvb_.push_back((int)h_hv_.size() / 3); h_hvc_.push_back(vcnt[s]);
             h_hfb_.push_back((int)h_fn_.size() / 3); h_hfc_.push_back(fcnt[s]);
@@ -190,6 +203,9 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
     upload_tail(hfn_, h_fn_, o_f, st_); upload_tail(hfmin_, h_fmn_, o_f, st_); upload_tail(hfmax_, h_fmx_, o_f, st_);
     upload_tail(hea_, h_ea_, o_e, st_); upload_tail(heb_, h_eb_, o_e, st_);
     upload_tail(cbeg_, h_cbeg_, s0, st_); upload_tail(ccnt_, h_ccnt_, s0, st_);
+    upload_tail(hlbeg_, h_hlb_, o_h, st_); upload_tail(hlcnt_, h_hlc_, o_h, st_);
+    upload_tail(lfbeg_, h_lfb_, o_l, st_); upload_tail(lfcnt_, h_lfc_, o_l, st_);
+    upload_tail(lfmin_, h_lfmn_, o_l * 3, st_); upload_tail(lfmax_, h_lfmx_, o_l * 3, st_);
     PE_CK(cudaStreamSynchronize(st_));
     return s0;
 }
@@ -218,8 +234,9 @@ void World<R>::set_compounds(const int* cbeg, const int* ccnt, int C, const int*
         for (int k = 0; k < n; k++) {
             Kid& c = kids[k];
             c.shape = cshape[b + k];
-            if (c.shape < 0 || c.shape >= S_ || h_stype_[c.shape] == ST_COMPOUND)
-                throw std::runtime_error("compound shape " + std::to_string(s) + ": a child must name a non-compound shape");
+            if (c.shape < 0 || c.shape >= S_ || h_stype_[c.shape] == ST_COMPOUND || h_stype_[c.shape] == ST_CONCAVE)
+                throw std::runtime_error("compound shape " + std::to_string(s) +
+                                         ": a child must name a shape that is neither compound nor concave");
             c.ratio = R(cratio[b + k]);
             if (c.ratio < eps<R>()) throw std::runtime_error("mass ratio must be greater than 0");
             for (int r = 0; r < 3; r++) for (int q = 0; q < 3; q++) c.basis.m[r][q] = R(cbas[(size_t)(b + k) * 9 + r * 3 + q]);
@@ -584,6 +601,10 @@ template <class R> void World<R>::narrowphase() {
                 }
                 case PC_COMPOUND:
                     launch(K_NP, g, k_np_compound<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
+                    break;
+                case PC_CONCAVE:
+                    launch(K_NP, g, k_np_class<R, PC_CONCAVE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                           prev_res_off_.p);
                     break;
                 default:   // PC_CONVEX_BIG
                     launch(K_NP_SAT, grid_warps(hi - lo), k_np_sat_big<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,

@@ -30,7 +30,8 @@ from pathlib import Path
 import numpy as np
 
 BOX, SPHERE, CYLINDER, HULL = 0, 1, 2, 3
-COMPOUND = 5   # ShapeType::ST_Compound (ST_ConcaveMesh = 4 is not on the path)
+CONCAVE = 4    # ShapeType::ST_ConcaveMesh: a triangle mesh (static terrain), shares the hull tables
+COMPOUND = 5   # ShapeType::ST_Compound
 JOINT_BALL, JOINT_HINGE, JOINT_SLIDER = 0, 1, 2   # ConstraintType::CT_{BALL,HINGE,SLIDER}_JOINT
 KINEMATIC = 1
 IGNORE_COLLISION = 2   # RigidBody::setIgnoreCollision: the body takes part in no pair
@@ -238,9 +239,9 @@ class SceneBuilder:
 
     def shape(self, kind, params=(0.0, 0.0, 0.0), hull=None):
         params = tuple(float(p) for p in params) + (0.0,) * (3 - len(params))
-        if kind == HULL:
+        if kind in (HULL, CONCAVE):
             self.hulls.append(hull)
-            self.shapes.append((HULL, (0.0, 0.0, 0.0), len(self.hulls) - 1))
+            self.shapes.append((kind, (0.0, 0.0, 0.0), len(self.hulls) - 1))
             return len(self.shapes) - 1
         key = (kind, params)
         if key not in self.shape_key:
@@ -259,6 +260,8 @@ class SceneBuilder:
         for sh, o, b, r in children:
             if self.shapes[sh][0] == COMPOUND:
                 raise ValueError("CompoundShape cannot contain another CompoundShape")
+            if self.shapes[sh][0] == CONCAVE:
+                raise ValueError("CompoundShape cannot contain ConcaveMeshShape")
             if not r >= 1e-5:   # compound_shape.cpp:14-16 (PE_EPS)
                 raise ValueError("mass ratio must be greater than 0")
             kids.append((int(sh), np.asarray(o, np.float64), np.eye(3) if b is None else np.asarray(b, np.float64),
@@ -314,7 +317,7 @@ class SceneBuilder:
             if t == COMPOUND:
                 cmp_beg[i], cmp_cnt[i] = len(kids), len(h)
                 kids.extend(h)
-            if t != HULL:
+            if t not in (HULL, CONCAVE):
                 continue
             hv, hf = self.hulls[h]
             vbeg[i], vcnt[i], fbeg[i], fcnt[i] = nv, len(hv), nf, len(hf)
@@ -682,6 +685,56 @@ def chain_field(n_chains=64, links=8, seed=0, spacing=3.0, height=6.0, hinge_lim
             else:
                 sb.joint(JOINT_BALL, prev, cur, anc_a, (-0.4, 0, 0))
             prev = cur
+    return sb.build(real_bits)
+
+
+def heightfield(nx, nz, cell=1.0, amp=0.6, seed=0):
+    """A terrain triangle mesh over [0, nx*cell] x [0, nz*cell] centred on the origin: heights from
+    a few seeded sines, two triangles per cell wound counter-clockwise seen from above (normals up)."""
+    rng = np.random.default_rng(seed)
+    xs = (np.arange(nx + 1) - nx / 2) * cell
+    zs = (np.arange(nz + 1) - nz / 2) * cell
+    X, Z = np.meshgrid(xs, zs, indexing="ij")
+    H = np.zeros_like(X)
+    for _ in range(4):
+        kx, kz, ph = rng.uniform(0.1, 0.5), rng.uniform(0.1, 0.5), rng.uniform(0, 2 * np.pi)
+        H += amp / 4 * np.sin(kx * X + ph) * np.cos(kz * Z - ph)
+    verts = np.stack([X.ravel(), H.ravel(), Z.ravel()], axis=1)
+    idx = lambda i, j: i * (nz + 1) + j
+    faces = []
+    for i in range(nx):
+        for j in range(nz):
+            faces.append([idx(i, j), idx(i, j + 1), idx(i + 1, j + 1)])
+            faces.append([idx(i, j), idx(i + 1, j + 1), idx(i + 1, j)])
+    return verts, faces
+
+
+def terrain_drop(n=40, nx=16, nz=16, seed=0, real_bits=64, dt=1.0 / 60.0, iterations=10, drop=(0.8, 2.5),
+                 compounds=True) -> Scene:
+    """Bodies of every kind (box, sphere, cylinder, convex hull and, optionally, compound) dropped
+    onto a static concave heightfield of nx x nz cells (2 triangles each; 16 x 16 gives 512
+    faces, above 4,094 faces the face tree gets leaves of several faces)."""
+    rng = np.random.default_rng(seed)
+    sb = SceneBuilder(dt=dt, iterations=iterations)
+    hv, hf = heightfield(nx, nz, seed=seed)
+    t = sb.shape(CONCAVE, hull=(hv, hf))
+    sb.body(t, (0.0, 0.0, 0.0), mass=0.0, friction=0.6, restitution=0.2, kinematic=True)
+    kinds = [BOX, SPHERE, CYLINDER, HULL]
+    if compounds:
+        hub = sb.shape(BOX, (0.5, 0.5, 0.5))
+        arm = sb.shape(CYLINDER, (0.1, 0.8))
+        jack = sb.compound([(hub, (0, 0, 0), None, 0.5), (arm, (0.55, 0, 0), _rot((0, 0, 1), np.pi / 2), 0.25),
+                            (arm, (-0.55, 0, 0), _rot((0, 0, 1), np.pi / 2), 0.25)])
+    span = min(nx, nz) * 0.8 / 2
+    rots = random_rotations(rng, n)
+    for i in range(n):
+        o = np.array([rng.uniform(-span, span), rng.uniform(*drop) + 0.6, rng.uniform(-span, span)])
+        if compounds and i % 5 == 4:
+            sb.body(jack, o - sb.compound_centroid(jack), rots[i], mass=float(rng.uniform(0.5, 2.0)), friction=0.6,
+                    restitution=0.2)
+        else:
+            _random_body(sb, rng, kinds[i % 4], o, 300.0, rots[i], (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), friction=0.6,
+                         restitution=0.2, hull_range=(8, 16))
     return sb.build(real_bits)
 
 

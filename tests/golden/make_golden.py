@@ -46,6 +46,13 @@ for bits in (64, 32):
                                 [0, 1, 2, 30, 60, 61, 90, 120, 150, 178, 179])
     CASES[f"joints_nolimit_f{bits}"] = (lambda bits=bits: sc.joint_demo(hinge_limits=False, real_bits=bits), bits, 180,
                                         [0, 1, 2, 30, 60, 61, 90, 120, 150, 178, 179])
+# static concave terrain: every body kind dropped on a 16 x 16 heightfield (512 faces, one face per
+# tree leaf), and on a 64 x 64 one (8,192 faces, four faces per leaf)
+for bits in (64, 32):
+    CASES[f"terrain_f{bits}"] = (lambda bits=bits: sc.terrain_drop(n=40, seed=11, real_bits=bits), bits, 150,
+                                 [0, 1, 30, 45, 60, 61, 90, 120, 148, 149])
+CASES["terrain_big_f32"] = (lambda: sc.terrain_drop(n=120, nx=64, nz=64, seed=12, real_bits=32), 32, 90,
+                            [0, 1, 40, 60, 61, 88, 89])
 # compound bodies (jacks, dumbbells, box + hull caps) among primitives on a ground box
 for bits in (64, 32):
     CASES[f"compound_f{bits}"] = (lambda bits=bits: sc.compound_pile(n=24, seed=3 + bits, drop=(0.0, 0.5), real_bits=bits),

@@ -73,7 +73,8 @@ def test_gpu_phases_match_reference(name):
 
 
 @pytest.mark.parametrize("name", ["cube_f32", "cube_f64", "zoo_22_f64", "zoo_23_f32", "zoo_33_f64", "pile_f64", "compound_f64",
-                                  "compound_f32", "joints_nolimit_f64", "joints_nolimit_f32"])
+                                  "compound_f32", "joints_nolimit_f64", "joints_nolimit_f32", "terrain_f64", "terrain_f32",
+                                  "terrain_big_f32"])
 def test_gpu_full_steps_serial_order_match_reference(name):
     """Whole steps on the device in serial-order mode reproduce the reference trajectory
     (scenes whose sort keys never tie, so the broadphase order is the reference's)."""
@@ -139,6 +140,25 @@ def test_gpu_compound_pile_matches_oracle():
         compare_results(g.results(), ro, what=f"compound pile step {10 * k + 9}")
         seen += int(ro["point_size"][np.isin(ro["res_a"], comp)].sum())
     assert seen > 200
+
+
+def test_gpu_terrain_matches_oracle():
+    """600 bodies of every kind (compounds included) dropped on a 96 x 96 concave heightfield
+    (18,432 triangles: face-tree leaves of nine faces), FP32: 60 whole serial-order steps equal the
+    oracle's, checked every 10 steps (state, pairs, every contact result)."""
+    scene = sc.terrain_drop(n=600, nx=96, nz=96, seed=23, real_bits=32)
+    o = orc.OracleWorld(scene, 32, threads=8)
+    g = pg.GpuWorld(scene, 32)
+    touching = 0
+    for k in range(6):
+        o.step(10)
+        g.step(10, pg.SERIAL_ORDER)
+        compare_state(g.state(), o.state(), what=f"terrain step {10 * k + 9}")
+        np.testing.assert_array_equal(g.pairs(), o.pairs())
+        ro = o.results()
+        compare_results(g.results(), ro, what=f"terrain step {10 * k + 9}")
+        touching = int(((ro["res_a"] == 0) | (ro["res_b"] == 0)).sum())
+    assert touching > 300
 
 
 def test_gpu_ignore_collision_bodies_match_oracle():
