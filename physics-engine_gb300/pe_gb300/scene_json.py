@@ -23,9 +23,13 @@ into a ``Scene`` for the GPU world, following the reference loader's rules:
   children) and the loader moves the body origin by the rotated centroid, so each child stays
   where the file places it.
 
+* ``convex`` / ``concave`` bodies (and convex compound sub-shapes) read the OBJ file named by
+  ``mesh`` (Mesh::loadFromObj, every coordinate scaled by ``scale[0]`` as the reference does); a
+  path that does not exist relative to the working directory is tried relative to the scene
+  file, and a body whose file is missing is skipped, as the reference skips it (:412-416).
+
 What the rigid-body step here does not model is reported rather than silently dropped:
-``convex`` / ``concave`` bodies and convex sub-shapes raise ``UnsupportedScene`` (convex meshes
-come from OBJ files, concave meshes are outside the step); fracturable bodies step as plain
+fracturable bodies step as plain
 rigid bodies and ``DamageSources`` are not applied (no fracture solver), and sleep thresholds,
 finite lifetimes and tags are ignored (sleeping, lifetimes and the "wheel" tag are not on the
 path).  These, and the skipped bodies, are listed in ``ignored``.
@@ -42,7 +46,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .scene import BOX, CYLINDER, SPHERE, SceneBuilder, quat_to_basis
+from .scene import BOX, CONCAVE, CYLINDER, HULL, SPHERE, SceneBuilder, quat_to_basis
 
 
 class UnsupportedScene(ValueError):
@@ -102,6 +106,52 @@ def _array(node, key, size):
     return [float(x) for x in v]
 
 
+def _atoi(tok):
+    """C atoi: optional sign and leading digits, 0 when there are none."""
+    tok = tok.lstrip()
+    k = 1 if tok[:1] in ("+", "-") else 0
+    while k < len(tok) and tok[k].isdigit():
+        k += 1
+    digits = tok[:k]
+    return int(digits) if digits not in ("", "+", "-") else 0
+
+
+def load_obj(path, scale_x=1.0, real_bits=64):
+    """Mesh::loadFromObj (common/mesh.cpp:36-67): "v" lines give vertices, every coordinate
+    multiplied by the first scale component (the reference scales y and z by size.x() too), in the
+    world's precision; "f" lines give faces from the index before the first '/' of each corner,
+    1-based.  Returns (vertices [n,3], faces)."""
+    verts, faces = [], []
+    f32 = real_bits == 32
+    sx = np.float32(scale_x) if f32 else float(scale_x)
+    for line in Path(path).read_text().splitlines():
+        parts = line[:1023].split()
+        if not parts:
+            continue
+        if parts[0] == "v":
+            xyz = parts[1:4]
+            if f32:
+                verts.append([float(np.float32(np.float32(v) * sx)) for v in xyz])
+            else:
+                verts.append([float(v) * sx for v in xyz])
+        elif parts[0] == "f":
+            faces.append([_atoi(t.split("/")[0]) - 1 for t in parts[1:]])
+    for f in faces:
+        if len(f) < 3:
+            raise ValueError(f"{path}: invalid mesh face: less than 3 vertices")
+    return np.array(verts, np.float64).reshape(-1, 3), faces
+
+
+def _mesh_path(node, base):
+    p = _string(node, "mesh")
+    if p is None:
+        return None
+    q = Path(p)
+    if not q.exists() and not q.is_absolute() and base is not None and (base / q).exists():
+        q = base / q   # relative to the scene file when not found relative to the working directory
+    return q
+
+
 def _rotation(node, where):
     rot = _array(node, "rotation", 0)
     if rot is None:
@@ -123,7 +173,7 @@ def _primitive(sb, node, kind):
     return sb.shape(CYLINDER, _array(node, "scale", 2) or [0.5, 1.0])
 
 
-def _compound(sb, rb, idx):
+def _compound(sb, rb, idx, base=None, real_bits=64):
     """CompoundShape from the "shapes" list (simulator.cpp:438-531): per sub-shape a mass ratio
     (default 1), a position (3 numbers), a rotation and a box / sphere / cylinder type with the
     body rules for "scale".  The reference deletes the body and goes on iterating its sub-shapes
@@ -140,13 +190,23 @@ def _compound(sb, rb, idx):
         pos = _array(node, "position", 3) or [0.0, 0.0, 0.0]
         rot = _rotation(node, where)
         sub = _string(node, "type")
-        if sub == "convex":
-            raise UnsupportedScene(f"{where}: 'convex' sub-shapes are not handled by this loader")
-        if sub in ("compound", "concave"):
+        if sub == "convex":   # simulator.cpp:492-503: the scale is read unchecked
+            mp = _mesh_path(node, base)
+            if mp is None:
+                raise ValueError(f"{where}: convex sub-shape mesh path not specified")
+            sc = _array(node, "scale", 3)
+            if sc is None:
+                raise ValueError(f"{where}: convex sub-shape needs a scale")
+            if not mp.exists():
+                raise UnsupportedScene(f"{where}: mesh file not found: {mp}")
+            shape = sb.shape(HULL, hull=load_obj(mp, sc[0], real_bits))
+        elif sub in ("compound", "concave"):
             raise ValueError(f"{where}: compound sub-shapes cannot be compound or concave")
-        if sub not in ("box", "sphere", "cylinder"):
+        elif sub not in ("box", "sphere", "cylinder"):
             raise ValueError(f"{where}: invalid compound sub-shape type {sub!r}")
-        children.append((_primitive(sb, node, sub), pos, rot, 1.0 if ratio is None else ratio))
+        else:
+            shape = _primitive(sb, node, sub)
+        children.append((shape, pos, rot, 1.0 if ratio is None else ratio))
     if not children:
         raise ValueError(f"body {idx}: a compound needs at least one sub-shape")
     return sb.compound(children)
@@ -155,6 +215,7 @@ def _compound(sb, rb, idx):
 def load_scene_json(path, real_bits: int = 64, dt: float = 1.0 / 60.0, iterations: int = 10):
     """Returns (Scene, ignored): the scene and the list of file features the step does not model."""
     data = json.loads(Path(path).read_text())
+    base = Path(path).resolve().parent
     gravity = (0.0, -9.8, 0.0)
     ignored = []
     if not isinstance(data, dict):
@@ -178,8 +239,6 @@ def load_scene_json(path, real_bits: int = 64, dt: float = 1.0 / 60.0, iteration
         if not isinstance(rb, dict):
             raise ValueError("node RigidBodies should have elements of type object")
         kind = _string(rb, "type")
-        if kind in ("convex", "concave"):
-            raise UnsupportedScene(f"body {idx}: '{kind}' shapes are not handled by this loader")
         if _boolean(rb, "fracturable"):
             ignored.append(f"body {idx}: fracturable (stepped as a rigid body)")
         _string(rb, "name")
@@ -205,13 +264,23 @@ def load_scene_json(path, real_bits: int = 64, dt: float = 1.0 / 60.0, iteration
         mass = _number(rb, "mass")
         fr = _number(rb, "friction")
         re = _number(rb, "restitution")
-        if kind not in ("box", "sphere", "cylinder", "compound"):
+        if kind not in ("box", "sphere", "cylinder", "compound", "convex", "concave"):
             # the reference logs the body and goes on without it (simulator.cpp:535-545)
             ignored.append(f"body {idx}: type {kind!r} (body skipped)" if kind else f"body {idx}: no type (body skipped)")
             continue
         origin = np.array(pos[:3])
-        if kind == "compound":
-            shape = _compound(sb, rb, idx)
+        if kind in ("convex", "concave"):   # simulator.cpp:407-437: an OBJ mesh scaled by scale[0]
+            mp = _mesh_path(rb, base)
+            if mp is None:
+                ignored.append(f"body {idx}: mesh path not specified (body skipped)")
+                continue
+            if not mp.exists():
+                ignored.append(f"body {idx}: mesh file not found: {mp} (body skipped)")
+                continue
+            sc = _array(rb, "scale", 3) or [1.0, 1.0, 1.0]
+            shape = sb.shape(HULL if kind == "convex" else CONCAVE, hull=load_obj(mp, sc[0], real_bits))
+        elif kind == "compound":
+            shape = _compound(sb, rb, idx, base, real_bits)
             if shape is None:
                 ignored.append(f"body {idx}: compound without sub-shapes (body skipped)")
                 continue

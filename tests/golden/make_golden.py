@@ -64,6 +64,34 @@ for bits in (64, 32):
     CASES[f"json_bomb_tower_smaller_f{bits}"] = (
         lambda bits=bits: load_scene_json(SAMPLES / "bomb_crash_tower_smaller.json", real_bits=bits)[0], bits, 120,
         [0, 1, 30, 55, 56, 57, 58, 59, 60, 61, 62, 90, 119])
+# a scene file naming the reference's own OBJ test meshes: its vase (589 faces) scaled 8x as a static
+# concave body on a ground box, and its convex test mesh (42 faces) as falling bodies among boxes
+# and spheres; written to a temporary file and read by the scene-file loader
+def obj_scene(bits):
+    import json
+    import tempfile
+    ref = Path("/root/reference/test")
+    bodies = [{"type": "box", "kinematic": True, "position": [0, -0.5, 0], "scale": [40, 1, 40]},
+              {"type": "concave", "kinematic": True, "mesh": str(ref / "utils/bvh/vase.obj"), "scale": [8, 8, 8],
+               "position": [0, 4.2, 0]}]
+    rng = np.random.default_rng(7)
+    for i in range(24):
+        p = [float(rng.uniform(-3, 3)), float(8.5 + 0.9 * i), float(rng.uniform(-3, 3))]
+        if i % 3 == 0:
+            bodies.append({"type": "convex", "mesh": str(ref / "rigid/shape/convex_mesh_shape/mesh.obj"),
+                           "scale": [0.8, 0.8, 0.8], "position": p, "mass": 2})
+        elif i % 3 == 1:
+            bodies.append({"type": "sphere", "scale": [0.35], "position": p})
+        else:
+            bodies.append({"type": "box", "scale": [0.6, 0.4, 0.5], "position": p, "rotation": [0.9, 0.1, 0.3, 0.2]})
+    with tempfile.TemporaryDirectory() as td:
+        f = Path(td) / "scene.json"
+        f.write_text(json.dumps({"RigidBodies": bodies}))
+        return load_scene_json(f, real_bits=bits)[0]
+
+
+for bits in (64, 32):
+    CASES[f"json_obj_f{bits}"] = (lambda bits=bits: obj_scene(bits), bits, 150, [0, 1, 40, 60, 61, 90, 120, 148, 149])
 # the reference's sample scene compound.json: ten compound bodies (box hubs with cylinder arms)
 # and four primitives dropped onto a kinematic ground box
 for bits in (64, 32):

@@ -74,7 +74,7 @@ def test_gpu_phases_match_reference(name):
 
 @pytest.mark.parametrize("name", ["cube_f32", "cube_f64", "zoo_22_f64", "zoo_23_f32", "zoo_33_f64", "pile_f64", "compound_f64",
                                   "compound_f32", "joints_nolimit_f64", "joints_nolimit_f32", "terrain_f64", "terrain_f32",
-                                  "terrain_big_f32"])
+                                  "terrain_big_f32", "json_obj_f64", "json_obj_f32"])
 def test_gpu_full_steps_serial_order_match_reference(name):
     """Whole steps on the device in serial-order mode reproduce the reference trajectory
     (scenes whose sort keys never tie, so the broadphase order is the reference's)."""

@@ -102,10 +102,48 @@ def test_unknown_or_missing_types_are_skipped(tmp_path):
     assert any("capsule" in x for x in ignored) and any("no type" in x for x in ignored)
 
 
+TETRA = """# a tetrahedron
+v 0 0 0
+v 1 0 0
+vt 0.5 0.5
+v 0 1 0
+v 0 0 1
+vn 0 0 1
+f 1/1/1 3/1/1 2/1/1
+f 1//1 2//1 4//1
+f 1 4 3
+f 2 3 4
+"""
+
+
 @pytest.mark.parametrize("kind", ["convex", "concave"])
-def test_mesh_bodies_are_refused(tmp_path, kind):
-    with pytest.raises(UnsupportedScene):
-        load_scene_json(write(tmp_path, {"RigidBodies": [{"type": "box"}, {"type": kind}]}))
+def test_mesh_bodies_read_obj_files(tmp_path, kind):
+    """Mesh::loadFromObj: "v" lines (every coordinate times scale[0]), "f" corners before the first
+    '/', 1-based; a path is tried relative to the scene file as well."""
+    (tmp_path / "tet.obj").write_text(TETRA)
+    doc = {"RigidBodies": [{"type": kind, "mesh": "tet.obj", "scale": [2, 5, 7], "position": [0, 3, 0]}]}
+    s, ignored = load_scene_json(write(tmp_path, doc))
+    assert ignored == [] and s.n_bodies == 1
+    assert s.shape_type[s.body_shape[0]] == (sc.HULL if kind == "convex" else sc.CONCAVE)
+    np.testing.assert_array_equal(s.hull_verts, [[0, 0, 0], [2, 0, 0], [0, 2, 0], [0, 0, 2]])
+    assert s.hull_vcnt[s.body_shape[0]] == 4 and s.hull_fcnt[s.body_shape[0]] == 4
+    np.testing.assert_array_equal(s.hull_face_idx[:6], [0, 2, 1, 0, 1, 3])
+
+
+def test_obj_coordinates_in_float_precision(tmp_path):
+    """For a 32-bit world the product is formed in float, as the reference's float build does."""
+    (tmp_path / "m.obj").write_text("v 0.1 0.2 0.3\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    s, _ = load_scene_json(write(tmp_path, {"RigidBodies": [{"type": "convex", "mesh": "m.obj", "scale": [0.7, 1, 1]}]}),
+                           real_bits=32)
+    assert s.hull_verts[0, 0] == float(np.float32(np.float32("0.1") * np.float32(0.7)))
+
+
+@pytest.mark.parametrize("kind", ["convex", "concave"])
+def test_mesh_bodies_without_file_are_skipped(tmp_path, kind):
+    doc = {"RigidBodies": [{"type": "box"}, {"type": kind, "mesh": "missing.obj"}, {"type": kind}]}
+    s, ignored = load_scene_json(write(tmp_path, doc))
+    assert s.n_bodies == 1
+    assert any("mesh file not found" in x for x in ignored) and any("mesh path not specified" in x for x in ignored)
 
 
 def test_compound_bodies(tmp_path):
@@ -135,7 +173,8 @@ def test_compound_bodies(tmp_path):
     np.testing.assert_array_equal(t.child_basis, s.child_basis)
 
 
-@pytest.mark.parametrize("sub, err", [({"type": "convex", "mesh": "a.obj"}, UnsupportedScene),
+@pytest.mark.parametrize("sub, err", [({"type": "convex", "mesh": "a.obj", "scale": [1, 1, 1]}, UnsupportedScene),
+                                      ({"type": "convex", "mesh": "a.obj"}, ValueError), ({"type": "convex"}, ValueError),
                                       ({"type": "compound"}, ValueError), ({"type": "concave"}, ValueError),
                                       ({"type": "capsule"}, ValueError), ({"scale": [1, 1, 1]}, ValueError),
                                       ({"type": "box", "mass_ratio": 0.0}, ValueError),
@@ -200,5 +239,5 @@ def test_reference_sample_scenes():
     assert s.n_bodies == 3 and s.n_children == 7
     s, _ = load_scene_json(SAMPLES / "compound.json")
     assert s.n_bodies == 14 and (s.shape_type[s.body_shape] == sc.COMPOUND).sum() == 10
-    with pytest.raises(UnsupportedScene):
-        load_scene_json(SAMPLES / "standford_bunny_smaller.json")
+    s, ignored = load_scene_json(SAMPLES / "standford_bunny_smaller.json")   # its OBJ file is not shipped
+    assert s.n_bodies == 5 and any("mesh file not found" in x for x in ignored)
