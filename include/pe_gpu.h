@@ -32,6 +32,7 @@ extern "C" {
 #define PE_GPU_SHAPE_SPHERE 1
 #define PE_GPU_SHAPE_CYLINDER 2
 #define PE_GPU_SHAPE_CONVEX_MESH 3
+#define PE_GPU_SHAPE_CONCAVE_MESH 4   /* ConcaveMeshShape::setMesh (concave_mesh_shape.cpp:6-17): the hull tables' layout */
 #define PE_GPU_SHAPE_COMPOUND 5       /* ShapeType::ST_Compound (shape.h:7-9); children via pe_gpu_set_compounds */
 
 /* body flags */
