@@ -4,6 +4,7 @@
 // (serial replay of the reference order per scene, or graph-coloured Gauss-Seidel).
 #pragma once
 #include <cstdint>
+#include <cooperative_groups.h>
 #include "pe_state.cuh"
 
 namespace pe {
@@ -1750,6 +1751,34 @@ __global__ void k_gc_pass(const uint32_t* list, int n, Results<R> res, Joints<R>
     if (j >= n) return;
     iterate_item(list[j], res, J, B, rows, row_off);
 }
+// All iterations of a big island in one cooperative launch: colour after colour (the items of a
+// colour spread over the whole grid), a grid-wide barrier between colours, the leftover colour in
+// island order on one thread at the end of each iteration.  The same updates in the same order as
+// one launch per colour and iteration, without the launch gaps that dominate when an island has
+// hundreds of colours of a few hundred items.
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_gc_solve(const uint32_t* corder, const int* cstart, const int* ccount, int ncol,
+                                                     int iterations, int lo, int m, const uint32_t* order, const int* color, int last,
+                                                     Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
+    for (int it = 0; it < iterations; it++) {
+        for (int c = 0; c < ncol; c++) {
+            const int n = ccount[c];
+            if (n == 0) continue;   // the same for every thread
+            const uint32_t* list = corder + cstart[c];
+            for (int j = t; j < n; j += T) iterate_item(list[j], res, J, B, rows, row_off);
+            grid.sync();
+        }
+        if (last) {
+            if (t == 0)
+                for (int j = 0; j < m; j++)
+                    if (color[lo + j] == kMaxColorsBig - 1) iterate_item(order[lo + j], res, J, B, rows, row_off);
+            grid.sync();
+        }
+    }
+}
+
 template <class R>
 __global__ void k_gc_last(int lo, int m, const uint32_t* order, const int* color, Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows,
                           const int* row_off) {

@@ -6,6 +6,8 @@
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
+#include <tuple>
+#include <utility>
 #include <vector>
 #include "pe_host.h"
 #include "pe_kernels.cuh"
@@ -42,11 +44,11 @@ template <class T> struct DBuf {   // device array that grows on demand
 
 // kernel groups for per-kernel device time (profiling mode)
 enum KernelId { K_INTEGRATE = 0, K_BP_KEYS, K_RADIX, K_SCAN, K_BP_GATHER, K_BP_SWEEP, K_BP_AXIS, K_NP_BUCKET, K_NP, K_NP_SAT,
-                K_SI_SETUP, K_ISLAND, K_SI_SERIAL, K_SI_COLOR, K_SI_MISC, K_MISC, K_COUNT };
+                K_SI_SETUP, K_ISLAND, K_SI_SERIAL, K_SI_COLOR, K_GC_COLOR, K_GC_SOLVE, K_SI_MISC, K_MISC, K_COUNT };
 inline const char* kernel_name(int k) {
     static const char* n[K_COUNT] = {"integrate", "bp_keys", "radix_sort", "scan", "bp_gather", "bp_sweep", "bp_axis",
                                      "np_bucket", "narrowphase", "np_sat", "si_setup", "islands", "si_serial", "si_colored",
-                                     "si_misc", "misc"};
+                                     "big_island_color", "big_island_solve", "si_misc", "misc"};
     return k >= 0 && k < K_COUNT ? n[k] : "";
 }
 
@@ -171,6 +173,30 @@ private:
             pending_.push_back({id, e0, e1});
         }
     }
+    // cooperative launch (all blocks resident; grid-wide barriers inside the kernel)
+    template <class... P, class... A> void launch_coop(int id, int g, int block, void (*kern)(P...), A... args) {
+        klaunch_[id]++;
+        step_launches_++;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (prof_) {
+            if (ev_pool_.size() < 2) { cudaEvent_t a, b; PE_CK(cudaEventCreate(&a)); PE_CK(cudaEventCreate(&b)); ev_pool_.push_back(a); ev_pool_.push_back(b); }
+            e0 = ev_pool_.back(); ev_pool_.pop_back();
+            e1 = ev_pool_.back(); ev_pool_.pop_back();
+            PE_CK(cudaEventRecord(e0, st_));
+        }
+        std::tuple<P...> held(args...);   // the kernel's exact parameter types
+        void* ptrs[sizeof...(P)];
+        fill_ptrs(held, ptrs, std::index_sequence_for<P...>{});
+        PE_CK(cudaLaunchCooperativeKernel((const void*)kern, dim3(g), dim3(block), ptrs, 0, st_));
+        if (prof_) {
+            PE_CK(cudaEventRecord(e1, st_));
+            pending_.push_back({id, e0, e1});
+        }
+    }
+    template <class Tup, size_t... I> static void fill_ptrs(Tup& t, void** p, std::index_sequence<I...>) {
+        ((p[I] = (void*)&std::get<I>(t)), ...);
+    }
+    int coop_blocks_ = 0;   // co-resident blocks of k_gc_solve
     struct Pending { int id; cudaEvent_t e0, e1; };
     void resolve_prof() {
         if (pending_.empty()) return;
@@ -288,7 +314,7 @@ private:
     // solver
     DBuf<int> row_off_, active_, color_, claim_, parent_, isl_flag_, isl_off_, isl_n_, ncol_;
     DBuf<uint32_t> isl_corder_;
-    DBuf<int> gc_big_, gc_n_, gc_cnt_, gc_cursor_;
+    DBuf<int> gc_big_, gc_n_, gc_cnt_, gc_cursor_, gc_cstart_, gc_ccount_;
     void solve_big_islands(int NI, const uint32_t* order);
     DBuf<R> rows_;
     int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0, n_islands_ = 0;

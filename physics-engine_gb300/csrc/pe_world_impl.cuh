@@ -718,10 +718,10 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         for (int c0 = 0; c0 < kMaxColorsBig - 1; c0 += 8) {
             int c = c0;
             for (; c < c0 + 8 && c < kMaxColorsBig - 1; c++) {
-                launch(K_SI_COLOR, g, k_gc_reset<R>, lo, m, order, rs, jt, (const int*)color_.p, claim_.p);
-                launch(K_SI_COLOR, g, k_gc_claim<R>, lo, m, order, rs, jt, bd, (const int*)color_.p, claim_.p);
+                launch(K_GC_COLOR, g, k_gc_reset<R>, lo, m, order, rs, jt, (const int*)color_.p, claim_.p);
+                launch(K_GC_COLOR, g, k_gc_claim<R>, lo, m, order, rs, jt, bd, (const int*)color_.p, claim_.p);
                 PE_CK(cudaMemsetAsync(gc_n_.p + 1, 0, sizeof(int), st_));
-                launch(K_SI_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, c, gc_n_.p + 1);
+                launch(K_GC_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, c, gc_n_.p + 1);
             }
             int rem = 0;
             PE_CK(cudaMemcpyAsync(&rem, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -730,7 +730,7 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
             if (rem == 0) break;
         }
         PE_CK(cudaMemsetAsync(gc_cnt_.p, 0, (kMaxColorsBig + 1) * sizeof(int), st_));
-        launch(K_SI_COLOR, g, k_gc_count, lo, m, color_.p, gc_cnt_.p);
+        launch(K_GC_COLOR, g, k_gc_count, lo, m, color_.p, gc_cnt_.p);
         PE_CK(cudaMemcpyAsync(cnt.data(), gc_cnt_.p, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, st_));
         PE_CK(cudaStreamSynchronize(st_));
         int run = 0, used = 0;
@@ -739,17 +739,24 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
             if (cnt[c + 1]) used = c + 1;
         }
         PE_CK(cudaMemcpyAsync(gc_cursor_.p, cur.data(), cur.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
-        launch(K_SI_COLOR, g, k_gc_place, lo, m, (const int*)color_.p, order, gc_cursor_.p, isl_corder_.p);
+        launch(K_GC_COLOR, g, k_gc_place, lo, m, (const int*)color_.p, order, gc_cursor_.p, isl_corder_.p);
         const bool last = cnt[kMaxColorsBig] > 0;
         n_colors_ = std::max(n_colors_, std::min(used, ncol) + (last ? 1 : 0));
-        for (int it = 0; it < prm_.iterations; it++) {
-            for (int c = 0; c < used && c < kMaxColorsBig - 1; c++)
-                if (cnt[c + 1])
-                    launch(K_SI_COLOR, grid(cnt[c + 1]), k_gc_pass<R>, (const uint32_t*)isl_corder_.p + lo + start[c], cnt[c + 1], rs,
-                           jt, bd, rw, (const int*)row_off_.p);
-            if (last)
-                launch_block(K_SI_COLOR, 1, 1, k_gc_last<R>, lo, m, order, (const int*)color_.p, rs, jt, bd, rw, (const int*)row_off_.p);
+        // every iteration in one cooperative launch: colour lists, then the grid-wide passes
+        const int top = std::min(used, kMaxColorsBig - 1);
+        std::vector<int> cs(std::max(top, 1)), cc(std::max(top, 1));
+        for (int c = 0; c < top; c++) { cs[c] = lo + start[c]; cc[c] = cnt[c + 1]; }
+        upload(gc_cstart_, cs, st_);
+        upload(gc_ccount_, cc, st_);
+        if (coop_blocks_ == 0) {
+            int per_sm = 0, sms = 0;
+            PE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_solve<R>, kBlock, 0));
+            PE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_));
+            coop_blocks_ = std::max(per_sm, 1) * sms;
         }
+        launch_coop(K_GC_SOLVE, coop_blocks_, kBlock, k_gc_solve<R>, (const uint32_t*)isl_corder_.p, (const int*)gc_cstart_.p,
+                    (const int*)gc_ccount_.p, top, prm_.iterations, lo, m, order, (const int*)color_.p, last ? 1 : 0, rs, jt, bd, rw,
+                    (const int*)row_off_.p);
     }
 }
 
