@@ -1710,6 +1710,14 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
 constexpr int kMaxColorsBig = 1024;
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big);
 template <class R>
+__global__ void k_gc_mask_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, unsigned long long* mask) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const int2 q = item_bodies(order[lo + j], res, J);
+    mask[q.x] = 0ull;
+    mask[q.y] = 0ull;
+}
+template <class R>
 __global__ void k_gc_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, const int* color, int* claim) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m || color[lo + j] >= 0) return;
@@ -1726,18 +1734,30 @@ __global__ void k_gc_claim(int lo, int m, const uint32_t* order, Results<R> res,
     if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
     if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
 }
-// winners take colour c; *remaining += results still uncoloured after this round
+// winners of the round take the smallest colour that no earlier winner on either of their dynamic
+// bodies holds (first fit over a 64-bit mask per body; all 64 taken: the leftover colour), so an
+// island needs about as many colours as its bodies have contacts, not as many as it has rounds;
+// *remaining += results still uncoloured after this round
 template <class R>
 __global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B, const int* claim, int* color,
-                            int c, int* remaining) {
+                            unsigned long long* mask, int* remaining) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool left = false;
     if (j < m && color[lo + j] < 0) {
         const int2 q = item_bodies(order[lo + j], res, J);
         const int ia = q.x, ib = q.y;
         const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
-        if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) color[lo + j] = c;
-        else left = true;
+        if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) {
+            const unsigned long long used = (da ? mask[ia] : 0ull) | (db ? mask[ib] : 0ull);
+            const int c = used == ~0ull ? kMaxColorsBig - 1 : __ffsll((long long)~used) - 1;
+            color[lo + j] = c;
+            if (c < 64) {   // winners of a round hold disjoint dynamic bodies
+                if (da) mask[ia] |= 1ull << c;
+                if (db) mask[ib] |= 1ull << c;
+            }
+        } else {
+            left = true;
+        }
     }
     const int n = __syncthreads_count(left);
     if (threadIdx.x == 0 && n) atomicAdd(remaining, n);

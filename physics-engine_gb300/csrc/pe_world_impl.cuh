@@ -713,6 +713,8 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         PE_CK(cudaMemcpy(lh, isl_off_.p + s, 2 * sizeof(int), cudaMemcpyDeviceToHost));
         const int lo = lh[0], m = lh[1] - lh[0], g = grid(m);
         PE_CK(cudaMemsetAsync(color_.p + lo, 0xff, (size_t)m * sizeof(int), st_));   // -1: uncoloured
+        gc_mask_.ensure(N_ + 1);
+        launch(K_GC_COLOR, g, k_gc_mask_reset<R>, lo, m, order, rs, jt, gc_mask_.p);
         // colouring rounds, the remaining count read back every 8 rounds (extra rounds find nothing to do)
         int ncol = 0;
         for (int c0 = 0; c0 < kMaxColorsBig - 1; c0 += 8) {
@@ -721,7 +723,7 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
                 launch(K_GC_COLOR, g, k_gc_reset<R>, lo, m, order, rs, jt, (const int*)color_.p, claim_.p);
                 launch(K_GC_COLOR, g, k_gc_claim<R>, lo, m, order, rs, jt, bd, (const int*)color_.p, claim_.p);
                 PE_CK(cudaMemsetAsync(gc_n_.p + 1, 0, sizeof(int), st_));
-                launch(K_GC_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, c, gc_n_.p + 1);
+                launch(K_GC_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, gc_mask_.p, gc_n_.p + 1);
             }
             int rem = 0;
             PE_CK(cudaMemcpyAsync(&rem, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
