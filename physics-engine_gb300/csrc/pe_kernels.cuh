@@ -1700,6 +1700,81 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
     }
 }
 
+// Serial-order mode for an island of up to kBigIsland items, in parallel and exact: levels in rounds
+// (an item takes level r in the round where it holds the smallest position among the unleveled
+// items on each of its dynamic bodies), so every item runs after all lower-position items that
+// share a dynamic body with it and before all higher-position ones: each body receives its updates
+// in island order, i.e. the reference's order, and items of one level touch disjoint bodies.  Every
+// iteration runs the levels in turn with a block barrier between them.  An island that needs more
+// than kMaxLevels levels runs in order on one thread instead.
+constexpr int kMaxLevels = 256;
+constexpr int kLevelBlock = 256;
+template <class R>
+__global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res,
+                                                            Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off, int iterations,
+                                                            int min_len, int* claim, int* level, uint32_t* lorder) {
+    const int s = blockIdx.x;
+    if (s >= *n_isl) return;
+    const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
+    if (m <= min_len || m > kBigIsland) return;
+    __shared__ int cnt[kMaxLevels + 1];
+    __shared__ int remaining;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) level[lo + j] = -1;
+    __syncthreads();
+    int rem = m;
+    for (int r = 0; r < kMaxLevels && rem > 0; r++) {
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            if (level[lo + j] >= 0) continue;
+            const int2 q = item_bodies(order[lo + j], res, J);
+            claim[q.x] = 0x7fffffff;
+            claim[q.y] = 0x7fffffff;
+        }
+        if (threadIdx.x == 0) remaining = 0;
+        __syncthreads();
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            if (level[lo + j] >= 0) continue;
+            const int2 q = item_bodies(order[lo + j], res, J);
+            if (!(B.flags[q.x] & BF_KINEMATIC)) atomicMin(&claim[q.x], j);
+            if (!(B.flags[q.y] & BF_KINEMATIC)) atomicMin(&claim[q.y], j);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            if (level[lo + j] >= 0) continue;
+            const int2 q = item_bodies(order[lo + j], res, J);
+            const bool da = !(B.flags[q.x] & BF_KINEMATIC), db = !(B.flags[q.y] & BF_KINEMATIC);
+            if ((!da || claim[q.x] == j) && (!db || claim[q.y] == j)) level[lo + j] = r;
+            else atomicAdd(&remaining, 1);
+        }
+        __syncthreads();
+        rem = remaining;
+        __syncthreads();
+    }
+    if (rem > 0) {   // too many levels: the island in order on one thread
+        if (threadIdx.x == 0)
+            for (int it = 0; it < iterations; it++)
+                for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
+        return;
+    }
+    for (int k = threadIdx.x; k <= kMaxLevels; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    int nl = 0;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) atomicAdd(&cnt[level[lo + j] + 1], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kMaxLevels; k++) cnt[k + 1] += cnt[k];   // cnt[l] = first slot of level l
+        int fill[kMaxLevels];
+        for (int k = 0; k < kMaxLevels; k++) fill[k] = cnt[k];
+        for (int j = 0; j < m; j++) lorder[lo + fill[level[lo + j]]++] = order[lo + j];
+    }
+    __syncthreads();
+    for (int k = 0; k < kMaxLevels; k++) if (cnt[k + 1] > cnt[k]) nl = k + 1;
+    for (int it = 0; it < iterations; it++)
+        for (int l = 0; l < nl; l++) {
+            for (int j = cnt[l] + threadIdx.x; j < cnt[l + 1]; j += blockDim.x) iterate_item(lorder[lo + j], res, J, B, rows, row_off);
+            __syncthreads();
+        }
+}
+
 // ---- islands above kBigIsland results: k_isl_colored's colouring rule in grid-wide kernels (round
 // c gives colour c to every uncoloured result that holds the smallest island position among the
 // uncoloured results on each of its dynamic bodies, so the colour classes follow the island order,
@@ -1734,13 +1809,14 @@ __global__ void k_gc_claim(int lo, int m, const uint32_t* order, Results<R> res,
     if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
     if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
 }
-// winners of the round take the smallest colour that no earlier winner on either of their dynamic
-// bodies holds (first fit over a 64-bit mask per body; all 64 taken: the leftover colour), so an
-// island needs about as many colours as its bodies have contacts, not as many as it has rounds;
-// *remaining += results still uncoloured after this round
+// coloured mode (mask given): winners of the round take the smallest colour that no earlier winner
+// on either of their dynamic bodies holds (first fit over a 64-bit mask per body; all 64 taken: the
+// leftover colour), so an island needs about as many colours as its bodies have contacts, not as
+// many as it has rounds.  Serial-order mode (no mask): winners take the round number, the exact
+// level schedule of k_isl_levels.  *remaining += results still uncoloured after this round
 template <class R>
 __global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B, const int* claim, int* color,
-                            unsigned long long* mask, int* remaining) {
+                            unsigned long long* mask, int round, int* remaining) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool left = false;
     if (j < m && color[lo + j] < 0) {
@@ -1748,12 +1824,16 @@ __global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res
         const int ia = q.x, ib = q.y;
         const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
         if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) {
-            const unsigned long long used = (da ? mask[ia] : 0ull) | (db ? mask[ib] : 0ull);
-            const int c = used == ~0ull ? kMaxColorsBig - 1 : __ffsll((long long)~used) - 1;
-            color[lo + j] = c;
-            if (c < 64) {   // winners of a round hold disjoint dynamic bodies
-                if (da) mask[ia] |= 1ull << c;
-                if (db) mask[ib] |= 1ull << c;
+            if (!mask) {   // levels of the exact serial-order schedule: the round number
+                color[lo + j] = round;
+            } else {
+                const unsigned long long used = (da ? mask[ia] : 0ull) | (db ? mask[ib] : 0ull);
+                const int c = used == ~0ull ? kMaxColorsBig - 1 : __ffsll((long long)~used) - 1;
+                color[lo + j] = c;
+                if (c < 64) {   // winners of a round hold disjoint dynamic bodies
+                    if (da) mask[ia] |= 1ull << c;
+                    if (db) mask[ib] |= 1ull << c;
+                }
             }
         } else {
             left = true;
@@ -1806,6 +1886,14 @@ __global__ void k_gc_last(int lo, int m, const uint32_t* order, const int* color
         if (color[lo + j] != kMaxColorsBig - 1) continue;
         iterate_item(order[lo + j], res, J, B, rows, row_off);
     }
+}
+
+// one island [lo, lo + m) in order on one thread (a big island whose level schedule ran out of levels)
+template <class R>
+__global__ void k_isl_one(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off,
+                          int iterations) {
+    for (int it = 0; it < iterations; it++)
+        for (int k = lo; k < lo + m; k++) iterate_item(order[k], res, J, B, rows, row_off);
 }
 
 // RigidBody::clearTempVelocity (rigidbody.cpp:160-164) at SequentialImpulseSolver::setupSolver

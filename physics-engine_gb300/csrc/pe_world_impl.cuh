@@ -669,10 +669,18 @@ template <class R> void World<R>::solve(int mode) {
         n_islands_ = scan(isl_flag_.p, M + 1);
         launch(K_ISLAND, grid(M + 1), k_isl_offsets, M, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
         const int NI = n_islands_;
-        // islands of up to kSmallResults items (all of them in serial-order mode): one thread each
+        // islands of up to kSmallResults items: one thread each
         launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(), row_off_.p,
-               prm_.iterations, 0, mode == 0 ? 0x7fffffff : kSmallResults);
-        if (mode != 0) {
+               prm_.iterations, 0, kSmallResults);
+        if (mode == 0) {
+            // serial order, larger islands: the exact level schedule, a block per island up to
+            // kBigIsland items, grid-wide above
+            isl_corder_.ensure(M);
+            color_.ensure(M + 1);
+            launch_block(K_SI_SERIAL, NI, kLevelBlock, k_isl_levels<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
+                         row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p);
+            solve_big_islands(NI, order, true);
+        } else {
             isl_corder_.ensure(M);
             color_.ensure(M + 1);
             ncol_.ensure(1);
@@ -680,7 +688,7 @@ template <class R> void World<R>::solve(int mode) {
             launch_block(K_SI_COLOR, NI, kColorBlock, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
                          row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p, ncol_.p);
             PE_CK(cudaMemcpyAsync(&n_colors_, ncol_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-            solve_big_islands(NI, order);
+            solve_big_islands(NI, order, false);
         }
     }
     launch(K_SI_MISC, grid(N_), k_si_sync<R>, bodies());
@@ -689,7 +697,7 @@ template <class R> void World<R>::solve(int mode) {
 
 // islands above kBigIsland results (coloured mode): grid-wide colouring rounds, then one launch per
 // colour and iteration (see k_gc_*)
-template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* order) {
+template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* order, bool exact) {
     gc_big_.ensure(NI + 1);
     gc_n_.ensure(2);
     PE_CK(cudaMemsetAsync(gc_n_.p, 0, sizeof(int), st_));
@@ -713,8 +721,12 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         PE_CK(cudaMemcpy(lh, isl_off_.p + s, 2 * sizeof(int), cudaMemcpyDeviceToHost));
         const int lo = lh[0], m = lh[1] - lh[0], g = grid(m);
         PE_CK(cudaMemsetAsync(color_.p + lo, 0xff, (size_t)m * sizeof(int), st_));   // -1: uncoloured
-        gc_mask_.ensure(N_ + 1);
-        launch(K_GC_COLOR, g, k_gc_mask_reset<R>, lo, m, order, rs, jt, gc_mask_.p);
+        unsigned long long* mask = nullptr;   // exact level schedule: colour = round
+        if (!exact) {
+            gc_mask_.ensure(N_ + 1);
+            mask = gc_mask_.p;
+            launch(K_GC_COLOR, g, k_gc_mask_reset<R>, lo, m, order, rs, jt, mask);
+        }
         // colouring rounds, the remaining count read back every 8 rounds (extra rounds find nothing to do)
         int ncol = 0;
         for (int c0 = 0; c0 < kMaxColorsBig - 1; c0 += 8) {
@@ -723,7 +735,7 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
                 launch(K_GC_COLOR, g, k_gc_reset<R>, lo, m, order, rs, jt, (const int*)color_.p, claim_.p);
                 launch(K_GC_COLOR, g, k_gc_claim<R>, lo, m, order, rs, jt, bd, (const int*)color_.p, claim_.p);
                 PE_CK(cudaMemsetAsync(gc_n_.p + 1, 0, sizeof(int), st_));
-                launch(K_GC_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, gc_mask_.p, gc_n_.p + 1);
+                launch(K_GC_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, mask, c, gc_n_.p + 1);
             }
             int rem = 0;
             PE_CK(cudaMemcpyAsync(&rem, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -735,6 +747,10 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         launch(K_GC_COLOR, g, k_gc_count, lo, m, color_.p, gc_cnt_.p);
         PE_CK(cudaMemcpyAsync(cnt.data(), gc_cnt_.p, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, st_));
         PE_CK(cudaStreamSynchronize(st_));
+        if (exact && cnt[kMaxColorsBig] > 0) {   // out of levels: the island in order on one thread
+            launch_block(K_GC_SOLVE, 1, 1, k_isl_one<R>, lo, m, order, rs, jt, bd, rw, (const int*)row_off_.p, prm_.iterations);
+            continue;
+        }
         int run = 0, used = 0;
         for (int c = 0; c < kMaxColorsBig; c++) {
             start[c] = run; cur[c] = lo + run; run += cnt[c + 1];
