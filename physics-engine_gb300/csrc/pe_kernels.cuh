@@ -1842,6 +1842,68 @@ __global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res
     const int n = __syncthreads_count(left);
     if (threadIdx.x == 0 && n) atomicAdd(remaining, n);
 }
+// All colouring rounds of a big island in one cooperative launch: per round the phases of
+// k_gc_reset, k_gc_claim and k_gc_assign over the grid with a grid-wide barrier between them, and
+// the round's count of items left (read by every thread after the barrier) decides whether another
+// round runs.  The same colours as one launch per phase; *n_rounds receives the rounds run.
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_gc_rounds(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
+                                                      int* claim, int* color, unsigned long long* mask, int* left, int max_rounds,
+                                                      int* n_rounds) {
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    __shared__ int bleft;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
+    for (int r = 0; r < max_rounds; r++) {
+        for (int j = t; j < m; j += T) {
+            if (color[lo + j] >= 0) continue;
+            const int2 q = item_bodies(order[lo + j], res, J);
+            claim[q.x] = 0x7fffffff;
+            claim[q.y] = 0x7fffffff;
+        }
+        grid.sync();
+        for (int j = t; j < m; j += T) {
+            if (color[lo + j] >= 0) continue;
+            const int2 q = item_bodies(order[lo + j], res, J);
+            if (!(B.flags[q.x] & BF_KINEMATIC)) atomicMin(&claim[q.x], j);
+            if (!(B.flags[q.y] & BF_KINEMATIC)) atomicMin(&claim[q.y], j);
+        }
+        grid.sync();
+        if (threadIdx.x == 0) bleft = 0;
+        __syncthreads();
+        int mine = 0;
+        for (int j = t; j < m; j += T) {
+            if (color[lo + j] >= 0) continue;
+            const int2 q = item_bodies(order[lo + j], res, J);
+            const int ia = q.x, ib = q.y;
+            const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
+            if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) {
+                if (!mask) {
+                    color[lo + j] = r;
+                } else {
+                    const unsigned long long used = (da ? mask[ia] : 0ull) | (db ? mask[ib] : 0ull);
+                    const int c = used == ~0ull ? kMaxColorsBig - 1 : __ffsll((long long)~used) - 1;
+                    color[lo + j] = c;
+                    if (c < 64) {
+                        if (da) mask[ia] |= 1ull << c;
+                        if (db) mask[ib] |= 1ull << c;
+                    }
+                }
+            } else {
+                mine++;
+            }
+        }
+        if (mine) atomicAdd(&bleft, mine);
+        __syncthreads();
+        if (threadIdx.x == 0 && bleft) atomicAdd(&left[r], bleft);
+        grid.sync();
+        if (*(volatile int*)&left[r] == 0) {   // the same value for every thread after the barrier
+            if (t == 0) *n_rounds = r + 1;
+            return;
+        }
+    }
+    if (t == 0) *n_rounds = max_rounds;
+}
+
 // colour histogram (leftovers -> the last colour) and placement of every colour but the last
 __global__ void k_gc_count(int lo, int m, int* color, int* cnt);
 __global__ void k_gc_place(int lo, int m, const int* color, const uint32_t* order, int* cursor, uint32_t* corder);

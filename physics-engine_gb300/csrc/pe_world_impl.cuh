@@ -728,21 +728,21 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
             launch(K_GC_COLOR, g, k_gc_mask_reset<R>, lo, m, order, rs, jt, mask);
         }
         // colouring rounds, the remaining count read back every 8 rounds (extra rounds find nothing to do)
-        int ncol = 0;
-        for (int c0 = 0; c0 < kMaxColorsBig - 1; c0 += 8) {
-            int c = c0;
-            for (; c < c0 + 8 && c < kMaxColorsBig - 1; c++) {
-                launch(K_GC_COLOR, g, k_gc_reset<R>, lo, m, order, rs, jt, (const int*)color_.p, claim_.p);
-                launch(K_GC_COLOR, g, k_gc_claim<R>, lo, m, order, rs, jt, bd, (const int*)color_.p, claim_.p);
-                PE_CK(cudaMemsetAsync(gc_n_.p + 1, 0, sizeof(int), st_));
-                launch(K_GC_COLOR, g, k_gc_assign<R>, lo, m, order, rs, jt, bd, (const int*)claim_.p, color_.p, mask, c, gc_n_.p + 1);
-            }
-            int rem = 0;
-            PE_CK(cudaMemcpyAsync(&rem, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
-            PE_CK(cudaStreamSynchronize(st_));
-            ncol = c;
-            if (rem == 0) break;
+        // all rounds in one cooperative launch (up to kMaxColorsBig - 1; items left over take the last colour)
+        if (coop_blocks_ == 0) {
+            int per_sm = 0, sms = 0;
+            PE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_solve<R>, kBlock, 0));
+            int per_sm2 = 0;
+            PE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_gc_rounds<R>, kBlock, 0));
+            PE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_));
+            coop_blocks_ = std::max(std::min(per_sm, per_sm2), 1) * sms;
         }
+        gc_left_.ensure(kMaxColorsBig);
+        PE_CK(cudaMemsetAsync(gc_left_.p, 0, kMaxColorsBig * sizeof(int), st_));
+        launch_coop(K_GC_COLOR, coop_blocks_, kBlock, k_gc_rounds<R>, lo, m, order, rs, jt, bd, claim_.p, color_.p, mask, gc_left_.p,
+                    kMaxColorsBig - 1, gc_n_.p + 1);
+        int ncol = 0;
+        PE_CK(cudaMemcpyAsync(&ncol, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
         PE_CK(cudaMemsetAsync(gc_cnt_.p, 0, (kMaxColorsBig + 1) * sizeof(int), st_));
         launch(K_GC_COLOR, g, k_gc_count, lo, m, color_.p, gc_cnt_.p);
         PE_CK(cudaMemcpyAsync(cnt.data(), gc_cnt_.p, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -766,12 +766,6 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         for (int c = 0; c < top; c++) { cs[c] = lo + start[c]; cc[c] = cnt[c + 1]; }
         upload(gc_cstart_, cs, st_);
         upload(gc_ccount_, cc, st_);
-        if (coop_blocks_ == 0) {
-            int per_sm = 0, sms = 0;
-            PE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_solve<R>, kBlock, 0));
-            PE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_));
-            coop_blocks_ = std::max(per_sm, 1) * sms;
-        }
         launch_coop(K_GC_SOLVE, coop_blocks_, kBlock, k_gc_solve<R>, (const uint32_t*)isl_corder_.p, (const int*)gc_cstart_.p,
                     (const int*)gc_ccount_.p, top, prm_.iterations, lo, m, order, (const int*)color_.p, last ? 1 : 0, rs, jt, bd, rw,
                     (const int*)row_off_.p);

@@ -142,6 +142,59 @@ def test_gpu_compound_pile_matches_oracle():
     assert seen > 200
 
 
+def largest_island(res, kinematic):
+    """Results with points in the largest island of dynamic bodies (union-find on the host)."""
+    a, b = res["res_a"][res["point_size"] > 0], res["res_b"][res["point_size"] > 0]
+    parent = {}
+
+    def find(x):
+        while parent.setdefault(x, x) != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+    for x, y in zip(a, b):
+        if not kinematic[x] and not kinematic[y]:
+            parent[find(x)] = find(y)
+    sizes = {}
+    for x, y in zip(a, b):
+        r = find(y if kinematic[x] else x)
+        sizes[r] = sizes.get(r, 0) + 1
+    return max(sizes.values())
+
+
+def test_gpu_big_island_serial_order_matches_oracle():
+    """A settled pour of 4,096 bodies in a 10 x 10 m container forms one island of more than 4,096
+    contact results, which serial-order mode runs as the grid-wide level schedule (cooperative
+    colouring rounds and passes).  From the oracle's state, five steps with the oracle's pair order
+    give the oracle's contacts and velocities bit for bit."""
+    scene = sc.container_pour(n=4096, seed=3, floor=(10.0, 10.0), spawn_height=(1.0, 21.0), wall_height=25.0, hull_pool=32,
+                              real_bits=32)
+    o = orc.OracleWorld(scene, 32, threads=16)
+    o.step(400)
+    assert largest_island(o.results(), (scene.body_flags & sc.KINEMATIC) != 0) > 4096
+    g = pg.GpuWorld(scene, 32)
+    g.set_state(o.state())
+    g.set_results(o.results())
+    g.axis = o.axis
+    for k in range(5):
+        o.integrate()
+        g.integrate()
+        compare_state(g.state(), o.state(), what=f"integrate {k}")
+        o.broadphase()
+        g.broadphase()
+        po = o.pairs()
+        assert sorted(map(tuple, np.sort(po, axis=1))) == sorted(map(tuple, np.sort(g.pairs(), axis=1)))
+        g.set_pairs(po)
+        o.narrowphase()
+        g.narrowphase()
+        compare_results(g.results(), o.results(), what=f"narrowphase {k}")
+        o.solve()
+        g.solve(pg.SERIAL_ORDER)
+        so, sg = o.state(), g.state()
+        np.testing.assert_array_equal(sg["lin_vel"], so["lin_vel"], err_msg=f"solve {k}")
+        np.testing.assert_array_equal(sg["ang_vel"], so["ang_vel"], err_msg=f"solve {k}")
+
+
 def test_gpu_terrain_matches_oracle():
     """600 bodies of every kind (compounds included) dropped on a 96 x 96 concave heightfield
     (18,432 triangles: face-tree leaves of nine faces), FP32: 60 whole serial-order steps equal the
