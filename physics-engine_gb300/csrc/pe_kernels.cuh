@@ -210,6 +210,107 @@ __device__ int sweep_block(int i, int n, const int* scene_axis, const R* smn, co
     return c;
 }
 
+// A crowded position's window (the candidates j > i of its scene whose minimum along the axis does
+// not exceed i's maximum: a prefix of the scene's sorted positions, found by binary search) swept in
+// up to kMaxChunks chunks of at least kChunk candidates, one block per chunk: chunk counts are summed
+// per position, and each chunk writes its pairs after those of the chunks before it, so the pairs
+// keep ascending j.
+constexpr int kChunk = 4096;
+constexpr int kMaxChunks = 32;
+template <class R, bool WRITE>
+__device__ int sweep_range_block(int i, int jb, int je, int n, const R* smn, const R* smx, const int* sflag, int2* out,
+                                 const uint32_t* order, int* wcnt, const IgnoreLists& ign) {
+    const R mnx = smn[i], mny = smn[n + i], mnz = smn[2 * (size_t)n + i];
+    const R mxx = smx[i], mxy = smx[n + i], mxz = smx[2 * (size_t)n + i];
+    const int fi = sflag[i];
+    if (fi & BF_IGNORE) return 0;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+    const int a = WRITE ? (int)order[i] : 0;
+    const unsigned lt = (1u << lane) - 1u;
+    int c = 0;
+    for (int j0 = jb; j0 < je; j0 += blockDim.x) {
+        const int j = j0 + tid;
+        bool hit = false;
+        if (j < je) {
+            const int fj = sflag[j];
+            hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
+                  !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
+                  !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
+            if (hit && ign.off && ((fi | fj) & BF_IGN_LIST)) hit = !ign.ignored(i, j);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) wcnt[w] = __popc(m);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int k = 0; k < nw; k++) { if (k < w) before += wcnt[k]; total += wcnt[k]; }
+        if (WRITE && hit) out[c + before + __popc(m & lt)] = make_int2(a, (int)order[j]);
+        c += total;
+        __syncthreads();   // wcnt is rewritten next iteration
+    }
+    return c;
+}
+// per crowded position: window end, chunk size and chunk count
+template <class R>
+__global__ void k_bp_big_windows(int n, const int* scene_axis, const int* scene_off, const R* smn, const R* smx, const int* sscene,
+                                 const int* big, const int* n_big, int* wend, int* csize, int* nchunk) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < *n_big; b += gridDim.x * blockDim.x) {
+        const int i = big[b], sc = sscene[i];
+        const R* amin = smn + (size_t)scene_axis[sc] * n;
+        const R mx = smx[(size_t)scene_axis[sc] * n + i];
+        int lo = i + 1, hi = scene_off[sc + 1];   // first j with amin[j] > mx, else the scene's end
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (amin[mid] > mx) hi = mid;
+            else lo = mid + 1;
+        }
+        const int len = lo - (i + 1);
+        int cs = (len + kMaxChunks - 1) / kMaxChunks;
+        cs = cs < kChunk ? kChunk : cs;
+        wend[b] = lo;
+        csize[b] = cs;
+        nchunk[b] = (len + cs - 1) / cs;
+    }
+}
+__global__ void k_bp_chunk_offsets(const int* n_big, const int* nchunk, int* choff, int* total);
+__device__ __forceinline__ int chunk_owner(int c, const int* choff, int nb) {   // last b with choff[b] <= c
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (choff[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+template <class R>
+__global__ void k_bp_count_chunks(int n, const R* smn, const R* smx, const int* sflag, const int* big, const int* n_big, const int* wend,
+                                  const int* csize, const int* choff, const int* total, int* ccount, IgnoreLists ign) {
+    __shared__ int wcnt[32];
+    for (int c = blockIdx.x; c < *total; c += gridDim.x) {
+        const int b = chunk_owner(c, choff, *n_big), i = big[b];
+        const int jb = i + 1 + (c - choff[b]) * csize[b], je = jb + csize[b] < wend[b] ? jb + csize[b] : wend[b];
+        const int k = sweep_range_block<R, false>(i, jb, je, n, smn, smx, sflag, nullptr, nullptr, wcnt, ign);
+        if (threadIdx.x == 0) ccount[c] = k;
+    }
+}
+// per crowded position: its pair count and the offsets of its chunks' pairs
+__global__ void k_bp_chunk_sums(const int* big, const int* n_big, const int* choff, const int* nchunk, const int* ccount, int* cpref,
+                                int* count);
+template <class R>
+__global__ void k_bp_write_chunks(int n, const R* smn, const R* smx, const int* sflag, const uint32_t* order, const int* offset,
+                                  const int* big, const int* n_big, const int* wend, const int* csize, const int* choff, const int* total,
+                                  const int* cpref, int2* pairs, int pair_cap, int* status, IgnoreLists ign) {
+    __shared__ int wcnt[32];
+    for (int c = blockIdx.x; c < *total; c += gridDim.x) {
+        const int b = chunk_owner(c, choff, *n_big), i = big[b];
+        if (offset[i + 1] > pair_cap) {
+            if (threadIdx.x == 0) atomicOr(status, ST_PAIR_OVERFLOW);
+            continue;
+        }
+        const int jb = i + 1 + (c - choff[b]) * csize[b], je = jb + csize[b] < wend[b] ? jb + csize[b] : wend[b];
+        sweep_range_block<R, true>(i, jb, je, n, smn, smx, sflag, pairs + offset[i] + cpref[c], order, wcnt, ign);
+    }
+}
+
 template <class R>
 __global__ void k_bp_count(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene, int* count,
                            int* stage, int* big, int* n_big, IgnoreLists ign) {

@@ -215,6 +215,22 @@ __global__ void k_gc_place(int lo, int m, const int* color, const uint32_t* orde
     if (live) corder[base + __popc(peers & ((1u << lane) - 1u))] = order[lo + j];
 }
 
+// exclusive offsets of the crowded positions' chunks (few positions: one thread)
+__global__ void k_bp_chunk_offsets(const int* n_big, const int* nchunk, int* choff, int* total) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int run = 0;
+    for (int b = 0; b < *n_big; b++) { choff[b] = run; run += nchunk[b]; }
+    *total = run;
+}
+__global__ void k_bp_chunk_sums(const int* big, const int* n_big, const int* choff, const int* nchunk, const int* ccount, int* cpref,
+                                int* count) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < *n_big; b += gridDim.x * blockDim.x) {
+        int run = 0;
+        for (int k = choff[b]; k < choff[b] + nchunk[b]; k++) { cpref[k] = run; run += ccount[k]; }
+        count[big[b]] = run;
+    }
+}
+
 // axis of each large scene from its tile sums (items of a scene are consecutive, tile 0 first)
 __global__ void k_bp_axis_combine(const int* scene_off, const int2* item, int n_item, const double* part, int* scene_axis) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;

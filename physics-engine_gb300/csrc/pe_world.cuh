@@ -296,6 +296,7 @@ private:
     DBuf<int> hist_, aux_, total_, count_, status_;
     DBuf<R> smn_, smx_;
     DBuf<int> sflag_, ssc_, bp_stage_, bp_big_, bp_nbig_;
+    DBuf<int> bp_wend_, bp_csize_, bp_nch_, bp_choff_, bp_ctot_, bp_ccount_, bp_cpref_;   // crowded windows in chunks
     DBuf<int2> axis_items_;
     DBuf<double> axis_part_;
     int axis_items_n_ = 0;

@@ -505,16 +505,26 @@ template <class R> int World<R>::broadphase() {
     if (n_ign_ > 0) { ign.off = ign_off_.p; ign.ids = ign_ids_.p; ign.order = order_; }
     launch(K_BP_SWEEP, grid_warps(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p,
            bp_big_.p, bp_nbig_.p, ign);
-    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_count_big<R>, n, (const int*)scene_axis_.p, (const R*)smn_.p, (const R*)smx_.p,
-           (const int*)sflag_.p, (const int*)ssc_.p, count_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p, ign);
+    // crowded positions: windows in chunks of one block each (at most kMaxChunks per position)
+    bp_wend_.ensure(n + 1); bp_csize_.ensure(n + 1); bp_nch_.ensure(n + 1); bp_choff_.ensure(n + 1); bp_ctot_.ensure(1);
+    bp_ccount_.ensure((size_t)kMaxChunks * n + 1); bp_cpref_.ensure((size_t)kMaxChunks * n + 1);
+    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_big_windows<R>, n, (const int*)scene_axis_.p, (const int*)scene_off_.p, (const R*)smn_.p,
+           (const R*)smx_.p, (const int*)ssc_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p, bp_wend_.p, bp_csize_.p, bp_nch_.p);
+    launch_block(K_BP_SWEEP, 1, 32, k_bp_chunk_offsets, (const int*)bp_nbig_.p, (const int*)bp_nch_.p, bp_choff_.p, bp_ctot_.p);
+    launch(K_BP_SWEEP, 2 * kBigSweepBlocks, k_bp_count_chunks<R>, n, (const R*)smn_.p, (const R*)smx_.p, (const int*)sflag_.p,
+           (const int*)bp_big_.p, (const int*)bp_nbig_.p, (const int*)bp_wend_.p, (const int*)bp_csize_.p, (const int*)bp_choff_.p,
+           (const int*)bp_ctot_.p, bp_ccount_.p, ign);
+    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_chunk_sums, (const int*)bp_big_.p, (const int*)bp_nbig_.p, (const int*)bp_choff_.p,
+           (const int*)bp_nch_.p, (const int*)bp_ccount_.p, bp_cpref_.p, count_.p);
     PE_CK(cudaMemsetAsync(count_.p + n, 0, sizeof(int), st_));
     const int P = scan(count_.p, n + 1);
     ensure_pair_capacity(P);
     launch(K_BP_SWEEP, grid_warps(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
            pairs_.p, pair_cap_, status_.p, ign);
-    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_write_big<R>, n, (const int*)scene_axis_.p, (const R*)smn_.p, (const R*)smx_.p,
-           (const int*)sflag_.p, (const int*)ssc_.p, (const uint32_t*)order_, (const int*)count_.p, pairs_.p, pair_cap_, status_.p,
-           (const int*)bp_big_.p, (const int*)bp_nbig_.p, ign);
+    launch(K_BP_SWEEP, 2 * kBigSweepBlocks, k_bp_write_chunks<R>, n, (const R*)smn_.p, (const R*)smx_.p, (const int*)sflag_.p,
+           (const uint32_t*)order_, (const int*)count_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p, (const int*)bp_wend_.p,
+           (const int*)bp_csize_.p, (const int*)bp_choff_.p, (const int*)bp_ctot_.p, (const int*)bp_cpref_.p, pairs_.p, pair_cap_,
+           status_.p, ign);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
     launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
     if (axis_items_n_ > 0) {   // scenes above kAxisTile bodies
