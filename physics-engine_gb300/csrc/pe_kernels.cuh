@@ -1943,30 +1943,32 @@ __global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res
     const int n = __syncthreads_count(left);
     if (threadIdx.x == 0 && n) atomicAdd(remaining, n);
 }
-// All colouring rounds of a big island in one cooperative launch: per round the phases of
-// k_gc_reset, k_gc_claim and k_gc_assign over the grid with a grid-wide barrier between them, and
-// the round's count of items left (read by every thread after the barrier) decides whether another
-// round runs.  The same colours as one launch per phase; *n_rounds receives the rounds run.
+// All colouring rounds of a big island in one cooperative launch.  A round's claim on a body is
+// ((kMaxColorsBig - round) << 32 | island position): claims of earlier rounds carry larger tags, so
+// the round's smallest position wins without resetting the claims, and a round is two phases (claim,
+// then assign) with a grid-wide barrier after each; the round's count of items left (read by every
+// thread after the barrier) decides whether another round runs.  The winners are those of
+// k_gc_claim / k_gc_assign; *n_rounds receives the rounds run.
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_gc_rounds(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
-                                                      int* claim, int* color, unsigned long long* mask, int* left, int max_rounds,
-                                                      int* n_rounds) {
+                                                      unsigned long long* claim, int* color, unsigned long long* mask, int* left,
+                                                      int max_rounds, int* n_rounds) {
     cooperative_groups::grid_group grid = cooperative_groups::this_grid();
     __shared__ int bleft;
     const int t = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
+    for (int j = t; j < m; j += T) {
+        const int2 q = item_bodies(order[lo + j], res, J);
+        claim[q.x] = ~0ull;
+        claim[q.y] = ~0ull;
+    }
+    grid.sync();
     for (int r = 0; r < max_rounds; r++) {
+        const unsigned long long tag = (unsigned long long)(kMaxColorsBig - r) << 32;
         for (int j = t; j < m; j += T) {
             if (color[lo + j] >= 0) continue;
             const int2 q = item_bodies(order[lo + j], res, J);
-            claim[q.x] = 0x7fffffff;
-            claim[q.y] = 0x7fffffff;
-        }
-        grid.sync();
-        for (int j = t; j < m; j += T) {
-            if (color[lo + j] >= 0) continue;
-            const int2 q = item_bodies(order[lo + j], res, J);
-            if (!(B.flags[q.x] & BF_KINEMATIC)) atomicMin(&claim[q.x], j);
-            if (!(B.flags[q.y] & BF_KINEMATIC)) atomicMin(&claim[q.y], j);
+            if (!(B.flags[q.x] & BF_KINEMATIC)) atomicMin(&claim[q.x], tag | (unsigned)j);
+            if (!(B.flags[q.y] & BF_KINEMATIC)) atomicMin(&claim[q.y], tag | (unsigned)j);
         }
         grid.sync();
         if (threadIdx.x == 0) bleft = 0;
@@ -1977,7 +1979,8 @@ __global__ void __launch_bounds__(kBlock) k_gc_rounds(int lo, int m, const uint3
             const int2 q = item_bodies(order[lo + j], res, J);
             const int ia = q.x, ib = q.y;
             const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
-            if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) {
+            const unsigned long long key = tag | (unsigned)j;
+            if ((!da || claim[ia] == key) && (!db || claim[ib] == key)) {
                 if (!mask) {
                     color[lo + j] = r;
                 } else {

@@ -749,7 +749,8 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         }
         gc_left_.ensure(kMaxColorsBig);
         PE_CK(cudaMemsetAsync(gc_left_.p, 0, kMaxColorsBig * sizeof(int), st_));
-        launch_coop(K_GC_COLOR, coop_blocks_, kBlock, k_gc_rounds<R>, lo, m, order, rs, jt, bd, claim_.p, color_.p, mask, gc_left_.p,
+        gc_claim_.ensure(N_ + 1);
+        launch_coop(K_GC_COLOR, coop_blocks_, kBlock, k_gc_rounds<R>, lo, m, order, rs, jt, bd, gc_claim_.p, color_.p, mask, gc_left_.p,
                     kMaxColorsBig - 1, gc_n_.p + 1);
         int ncol = 0;
         PE_CK(cudaMemcpyAsync(&ncol, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
