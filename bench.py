@@ -271,17 +271,21 @@ def run_ours(args, rank, world, device):
     peak, peak_kind = measured_peak()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = None   # ncu's per-kernel DRAM writes include write-backs of earlier kernels' dirty lines
-    # end to end through the C ABI with host buffers
-    st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
-    g.set_state(st)                      # one untimed pass through the host path (pinned staging buffers)
+    # end to end through the C ABI with host buffers: each step copies the poses and velocities in
+    # from page-locked host arrays and reads the stepped ones back into them
+    import torch   # page-locked host memory
+    io = ("origin", "basis", "lin_vel", "ang_vel")
+    st = {f: torch.empty((N, 3, 3) if f == "basis" else (N, 3), dtype=torch.float64, pin_memory=True).numpy() for f in io}
+    g.state(fields=io, out=st)
+    g.set_state(st)                      # one untimed pass through the host path
     g.step(1, mode)
-    st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
+    g.state(fields=io, out=st)
     e2e_times = []
     for _ in range(max(3, args.steps // 2)):
         t0 = time.perf_counter()
         g.set_state(st)
         g.step(1, mode)
-        st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
+        g.state(fields=io, out=st)
         e2e_times.append(time.perf_counter() - t0)
     io_bytes = N * 18 * 8   # float64 poses and velocities through the C ABI, each way
     per_scene = per_scene_gpu(pg, scene, offs, g.state(fields=("origin", "basis", "lin_vel", "ang_vel")), bits, mode,

@@ -317,6 +317,7 @@ private:
     DBuf<uint32_t> isl_corder_;
     DBuf<int> gc_big_, gc_n_, gc_cnt_, gc_cursor_, gc_cstart_, gc_ccount_;
     DBuf<unsigned long long> gc_mask_, gc_claim_;
+    DBuf<double> xfer_;   // state transfers in the C ABI's layout
     DBuf<int> gc_left_;   // items left after each colouring round
     void solve_big_islands(int NI, const uint32_t* order, bool exact);
     DBuf<R> rows_;

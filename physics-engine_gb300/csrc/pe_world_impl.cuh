@@ -813,61 +813,49 @@ template <class R> R* World<R>::staging(size_t n) {
 
 template <class R>
 void World<R>::get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) {
-    struct G { double* dst; int k0; int nk; };
-    const G groups[7] = {{o, OX, 3}, {b, B00, 9}, {v, VX, 3}, {w, WX, 3}, {mn, MNX, 3}, {mx, MXX, 3}, {iw, I00, 9}};
-    int cols = 0;
-    for (const G& g : groups) if (g.dst) cols += g.nk;
-    if (!N_ || !cols) return;
-    R* h = staging((size_t)cols * N_);
-    int c = 0;
-    for (const G& g : groups) {
-        if (!g.dst) continue;
-        PE_CK(cudaMemcpyAsync(h + (size_t)c * N_, bf_.p + (size_t)g.k0 * bcap_, (size_t)g.nk * N_ * sizeof(R), cudaMemcpyDeviceToHost, st_));
-        c += g.nk;
+    double* dst[7] = {o, b, v, w, mn, mx, iw};
+    const int k0[7] = {OX, B00, VX, WX, MNX, MXX, I00}, nk[7] = {3, 9, 3, 3, 3, 3, 9};
+    XferGroups G{};
+    size_t tot = 0;
+    int map[7];
+    for (int g = 0; g < 7; g++) {
+        if (!dst[g]) continue;
+        map[G.n] = g;
+        G.k0[G.n] = k0[g]; G.nk[G.n] = nk[g]; G.off[G.n] = tot;
+        tot += (size_t)nk[g] * N_;
+        G.n++;
     }
+    if (!N_ || !G.n) return;
+    xfer_.ensure(tot);
+    launch(K_MISC, grid(N_), k_state_pack<R>, bodies(), G, xfer_.p);
+    for (int q = 0; q < G.n; q++)
+        PE_CK(cudaMemcpyAsync(dst[map[q]], xfer_.p + G.off[q], (size_t)G.nk[q] * N_ * sizeof(double), cudaMemcpyDeviceToHost, st_));
     PE_CK(cudaStreamSynchronize(st_));
-    c = 0;
-    for (const G& g : groups) {
-        if (!g.dst) continue;
-        for (int k = 0; k < g.nk; k++) {
-            const R* col = h + (size_t)(c + k) * N_;
-            for (int i = 0; i < N_; i++) g.dst[(size_t)i * g.nk + k] = (double)col[i];
-        }
-        c += g.nk;
-    }
 }
 
 template <class R>
 void World<R>::set_state(const double* o, const double* b, const double* v, const double* w, const double* mn, const double* mx,
                          const double* iw) {
-    struct G { const double* src; int k0; int nk; };
-    const G groups[7] = {{o, OX, 3}, {b, B00, 9}, {v, VX, 3}, {w, WX, 3}, {mn, MNX, 3}, {mx, MXX, 3}, {iw, I00, 9}};
-    const bool scale = mn && mx && o;
-    int cols = scale ? 1 : 0;
-    for (const G& g : groups) if (g.src) cols += g.nk;
-    if (!N_ || !cols) return;
-    R* h = staging((size_t)cols * N_);
-    int c = 0;
-    for (const G& g : groups) {
-        if (!g.src) continue;
-        for (int k = 0; k < g.nk; k++) {
-            R* col = h + (size_t)(c + k) * N_;
-            for (int i = 0; i < N_; i++) col[i] = R(g.src[(size_t)i * g.nk + k]);
-        }
-        PE_CK(cudaMemcpyAsync(bf_.p + (size_t)g.k0 * bcap_, h + (size_t)c * N_, (size_t)g.nk * N_ * sizeof(R), cudaMemcpyHostToDevice, st_));
-        c += g.nk;
+    const double* src[7] = {o, b, v, w, mn, mx, iw};
+    const int k0[7] = {OX, B00, VX, WX, MNX, MXX, I00}, nk[7] = {3, 9, 3, 3, 3, 3, 9};
+    XferGroups G{};
+    size_t tot = 0;
+    int at[7] = {-1, -1, -1, -1, -1, -1, -1};
+    for (int g = 0; g < 7; g++) {
+        if (!src[g]) continue;
+        at[g] = G.n;
+        G.k0[G.n] = k0[g]; G.nk[G.n] = nk[g]; G.off[G.n] = tot;
+        tot += (size_t)nk[g] * N_;
+        G.n++;
     }
-    if (scale) {   // RigidBody::getAABBScale of the injected box
-        R* col = h + (size_t)c * N_;
-        for (int i = 0; i < N_; i++) {
-            const V3<R> a = V3<R>(R(mn[i * 3]), R(mn[i * 3 + 1]), R(mn[i * 3 + 2]));
-            const V3<R> d = V3<R>(R(mx[i * 3]), R(mx[i * 3 + 1]), R(mx[i * 3 + 2]));
-            const V3<R> org = V3<R>(R(o[i * 3]), R(o[i * 3 + 1]), R(o[i * 3 + 2]));
-            const R sc = norm(d - a), df = norm(d + a - org * R(2));
-            col[i] = (sc + df) * R(0.5);
-        }
-        PE_CK(cudaMemcpyAsync(bf_.p + (size_t)SCALE * bcap_, col, (size_t)N_ * sizeof(R), cudaMemcpyHostToDevice, st_));
-    }
+    if (!N_ || !G.n) return;
+    xfer_.ensure(tot);
+    for (int g = 0; g < 7; g++)
+        if (src[g])
+            PE_CK(cudaMemcpyAsync(xfer_.p + G.off[at[g]], src[g], (size_t)nk[g] * N_ * sizeof(double), cudaMemcpyHostToDevice, st_));
+    const bool scale = mn && mx && o;   // the injected box's AABB scale
+    launch(K_MISC, grid(N_), k_state_unpack<R>, bodies(), G, (const double*)xfer_.p, scale ? at[0] : -1, scale ? at[4] : -1,
+           scale ? at[5] : -1);
     PE_CK(cudaStreamSynchronize(st_));
 }
 

@@ -184,13 +184,21 @@ class GpuWorld:
     STATE_FIELDS = (("origin", 3), ("basis", 9), ("lin_vel", 3), ("ang_vel", 3), ("aabb_min", 3), ("aabb_max", 3),
                     ("world_inv_inertia", 9))
 
-    def state(self, fields=None):
-        """Body state as float64 arrays; ``fields`` limits the transfer to the named fields."""
+    def state(self, fields=None, out=None):
+        """Body state as float64 arrays; ``fields`` limits the transfer to the named fields.  With
+        ``out`` (a dict of C-contiguous float64 arrays of the fields' shapes, e.g. page-locked host
+        memory reused across steps) the fields are written there and ``out`` is returned."""
         N = self.n
-        out, ptrs = {}, []
+        dst, out, ptrs = out, {}, []
         for name, k in self.STATE_FIELDS:
             if fields is None or name in fields:
-                a = np.zeros((N, 3, 3) if k == 9 else (N, 3))
+                shape = (N, 3, 3) if k == 9 else (N, 3)
+                if dst is not None:
+                    a = dst[name]
+                    if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+                        raise ValueError(f"state: out[{name!r}] must be C-contiguous float64 of shape {shape}")
+                else:
+                    a = np.zeros(shape)
                 out[name] = a
                 ptrs.append(a.ctypes.data_as(C.c_void_p))
             else:
