@@ -21,6 +21,7 @@ template <class R> struct HullPrep {
     std::vector<R> e_a, e_b;          // [ne*3]
     M3<R> inertia;                    // per unit mass (divided by the volume)
     R volume = 0;
+    R inner = -1, outer = 0;          // balls about the local origin inside / around the hull (-1: none certified)
     std::vector<int> l_beg, l_cnt;    // concave meshes: face-tree leaves in tree order (face ranges)
     std::vector<R> l_min, l_max;      // [nl*3] leaf boxes
 };

@@ -1,5 +1,7 @@
 // Host preprocessing of shapes (see pe_host.h).
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cmath>
 #include <utility>
 #include "pe_host.h"
@@ -143,6 +145,131 @@ static void tree_leaves(int l, int r, int leaf, std::vector<std::pair<int, int>>
     const int mid = (l + r) / 2;
     tree_leaves(l, mid, leaf, out);
     tree_leaves(mid + 1, r, leaf, out);
+}
+
+// Radii of two balls about the hull's local origin, for the narrowphase's axis pruning: every
+// vertex lies within `outer`, and the ball of radius `inner` lies inside the vertices' convex hull.
+// `inner` is certified from the faces, in double precision on the stored coordinates: they must close
+// a surface (every directed edge once, its reverse once), every face vertex must lie on or behind
+// every face's plane (Newell normal; one global flip for inward windings), and the origin must lie
+// strictly inside.  Then that surface bounds the hull of the face vertices, the smallest plane
+// distance less each face's out-of-plane spread is a safe radius, and it is shrunk by 1e-6 of
+// `outer`.  Otherwise `inner` is -1 and no axis of the hull is pruned.
+template <class R> static void hull_radii(const std::vector<V3<R>>& v, const std::vector<HFace<R>>& faces, R& inner, R& outer) {
+    double ro = 0;
+    for (const auto& p : v) ro = std::max(ro, std::sqrt(double(p.x) * p.x + double(p.y) * p.y + double(p.z) * p.z));
+    outer = R(ro * (1 + 1e-6));
+    inner = R(-1);
+    if (faces.empty() || ro == 0) return;
+    std::map<std::pair<int, int>, int> dir;   // directed edge -> count
+    std::vector<int> used;
+    for (const auto& f : faces) {
+        const int n = (int)f.idx.size();
+        if (n < 3) return;
+        for (int i = 0; i < n; i++) {
+            dir[{f.idx[i], f.idx[(i + 1) % n]}]++;
+            used.push_back(f.idx[i]);
+        }
+    }
+    for (const auto& e : dir) {
+        if (e.second != 1) return;
+        auto back = dir.find({e.first.second, e.first.first});
+        if (back == dir.end() || back->second != 1) return;
+    }
+    std::sort(used.begin(), used.end());
+    used.erase(std::unique(used.begin(), used.end()), used.end());
+    const double tol = 1e-9 * ro;
+    const size_t F = faces.size();
+    std::vector<double> nrm(F * 3), dmin(F), dmax(F);
+    size_t pos = 0, neg = 0;
+    for (size_t k = 0; k < F; k++) {
+        const auto& f = faces[k];
+        const int n = (int)f.idx.size();
+        double nx = 0, ny = 0, nz = 0;
+        for (int i = 0; i < n; i++) {   // Newell's method
+            const V3<R>& a = v[f.idx[i]];
+            const V3<R>& b = v[f.idx[(i + 1) % n]];
+            nx += (double(a.y) - b.y) * (double(a.z) + b.z);
+            ny += (double(a.z) - b.z) * (double(a.x) + b.x);
+            nz += (double(a.x) - b.x) * (double(a.y) + b.y);
+        }
+        const double l = std::sqrt(nx * nx + ny * ny + nz * nz);
+        if (!(l > 0)) return;
+        nrm[3 * k] = nx / l; nrm[3 * k + 1] = ny / l; nrm[3 * k + 2] = nz / l;
+        double lo = 1e300, hi = -1e300;
+        for (int i = 0; i < n; i++) {
+            const V3<R>& a = v[f.idx[i]];
+            const double d = nrm[3 * k] * a.x + nrm[3 * k + 1] * a.y + nrm[3 * k + 2] * a.z;
+            lo = std::min(lo, d); hi = std::max(hi, d);
+        }
+        dmin[k] = lo; dmax[k] = hi;
+        if (lo > tol) pos++;
+        else if (hi < -tol) neg++;
+    }
+    if (neg == F) {   // inward winding
+        for (size_t k = 0; k < F; k++) {
+            for (int d = 0; d < 3; d++) nrm[3 * k + d] = -nrm[3 * k + d];
+            const double lo = -dmax[k];
+            dmax[k] = -dmin[k]; dmin[k] = lo;
+        }
+    } else if (pos != F) {
+        return;
+    }
+    double r = 1e300;
+    for (size_t k = 0; k < F; k++) {
+        for (int i : used) {
+            const V3<R>& a = v[i];
+            if (nrm[3 * k] * a.x + nrm[3 * k + 1] * a.y + nrm[3 * k + 2] * a.z > dmax[k] + tol) return;
+        }
+        r = std::min(r, dmin[k] - (dmax[k] - dmin[k]));
+    }
+    // The projection loop never takes vertex 0 as the maximum (convex_mesh_shape.cpp:171-175), so the
+    // radius must also hold for the hull of the other vertices.  Its facets are the faces without
+    // vertex 0 and new ones whose corners are neighbours of vertex 0 (vertices of its faces) or
+    // vertices on no face; every plane through three such candidates that supports the remaining
+    // vertices is a facet plane or lies farther out, so the smallest of these distances is that
+    // hull's radius.
+    const int nv = (int)v.size();
+    std::vector<char> cand(nv, 0), on_face(nv, 0);
+    for (int i : used) on_face[i] = 1;
+    for (size_t k = 0; k < F; k++) {
+        const auto& f = faces[k];
+        if (std::find(f.idx.begin(), f.idx.end(), 0) == f.idx.end()) continue;
+        for (int i : f.idx) cand[i] = 1;
+    }
+    if (on_face[0]) {
+        double r1 = 1e300;
+        for (size_t k = 0; k < F; k++)
+            if (std::find(faces[k].idx.begin(), faces[k].idx.end(), 0) == faces[k].idx.end())
+                r1 = std::min(r1, dmin[k] - (dmax[k] - dmin[k]));
+        std::vector<int> C;
+        for (int i = 1; i < nv; i++)
+            if (cand[i] || !on_face[i]) C.push_back(i);
+        auto dv = [&](int i) { return std::array<double, 3>{double(v[i].x), double(v[i].y), double(v[i].z)}; };
+        for (size_t a = 0; a < C.size(); a++)
+            for (size_t b = a + 1; b < C.size(); b++)
+                for (size_t c = b + 1; c < C.size(); c++) {
+                    const auto p0 = dv(C[a]), p1 = dv(C[b]), p2 = dv(C[c]);
+                    const double u[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+                    const double w[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+                    double n[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+                    const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+                    if (!(l > 1e-12 * ro * ro)) continue;
+                    for (double& x : n) x /= l;
+                    const double d = n[0] * p0[0] + n[1] * p0[1] + n[2] * p0[2];
+                    double lo = 1e300, hi = -1e300;
+                    for (int i = 1; i < nv; i++) {
+                        const auto q = dv(i);
+                        const double e = n[0] * q[0] + n[1] * q[1] + n[2] * q[2];
+                        lo = std::min(lo, e); hi = std::max(hi, e);
+                    }
+                    if (hi <= d + tol) r1 = std::min(r1, d);         // outward normal
+                    else if (lo >= d - tol) r1 = std::min(r1, -d);   // inward normal
+                }
+        r = std::min(r, r1);
+    }
+    r -= 1e-6 * ro;
+    if (r > 0) inner = R(r);
 }
 
 template <class R>
@@ -289,6 +416,7 @@ HullPrep<R> prepare_hull(const double* verts, int nv, const int* face_off, const
             for (int d = 0; d < 3; d++) { h.e_a.push_back(v[k0][d]); h.e_b.push_back(v[k1][d]); }
         }
     }
+    hull_radii(v, faces, h.inner, h.outer);
     return h;
 }
 

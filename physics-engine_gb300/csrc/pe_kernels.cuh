@@ -833,8 +833,83 @@ template <class R, int G> __device__ __forceinline__ V3<R> group_bcast3(const V3
     __syncthreads();
     return r;
 }
-// reals of per-group scratch after the staging area: G reduction values, G indices, 3 broadcast
+// reals of per-group scratch after the staging area: G reduction values, G indices, 3 broadcast,
+// the queue length
 template <class R> constexpr int sat_scratch_reals(int G) { return G == 1 ? 0 : 2 * G + 4; }
+// candidate axes per thread of one pruning pass, and the queue of surviving axis indices after the
+// scratch area
+constexpr int kSatQ = 8;
+template <class R> constexpr int sat_queue_reals(int G) { return (kSatQ * 32 * G * (int)sizeof(int) + (int)sizeof(R) - 1) / (int)sizeof(R); }
+
+// Pruning bound of one shape along a world axis: lo <= the computed maximum of its projection
+// interval, hi >= the computed minimum (a hull: its inner ball about the local origin; another
+// shape: its closed-form interval), and mag bounds the magnitudes entering their rounding.
+template <class R>
+__device__ __forceinline__ void prune_side(const ShapeView<R>& s, const Xf<R>& t, const V3<R>& ax, R& lo, R& hi, R& mag) {
+    if (s.type == ST_HULL) {
+        const R o = dot(t.o, ax);
+        lo = o + s.inner;
+        hi = o - s.inner;
+        mag = rabs(o) + s.outer;
+        return;
+    }
+    int i0, i1;
+    shape_interval(s, t, ax, (const R*)nullptr, hi, lo, i0, i1);
+    mag = rabs(hi) + rabs(lo);
+}
+// True when the axis's overlap depth min(maxA - minB, maxB - minA) is certainly above `best`, a
+// depth the SAT has already computed for one of the pair's axes (so best >= 0): such an axis can
+// neither separate the pair nor be its minimum (the reference keeps the first strict minimum), and
+// skipping it leaves the result unchanged.  The bound is lowered by 64 units of roundoff of the
+// magnitudes involved, which covers the rounding of the projections the SAT would compute.  `able`
+// is false when a hull of the pair has no certified inner ball.
+template <class R>
+__device__ __forceinline__ bool sat_prunable(const Pair<R>& c, bool able, const V3<R>& ax, R best) {
+    if (!able || !(best < Lim<R>::max())) return false;
+    R loA, hiA, mA, loB, hiB, mB;
+    prune_side(c.sa, c.ta(), ax, loA, hiA, mA);
+    prune_side(c.sb, c.tb(), ax, loB, hiB, mB);
+    const R d0 = loA - hiB, d1 = loB - hiA;
+    const R lb = d0 < d1 ? d0 : d1;
+    constexpr R u = sizeof(R) == 4 ? R(1.1920929e-7) : R(2.220446049250313e-16);
+    return lb > best + R(64) * u * (mA + mB + rabs(best));
+}
+// Compacts the candidate axes [base, base + span) ∩ [0, n) that `keep` accepts into the group's
+// queue and returns their count (the same in every thread of the group).  With one warp the queue
+// keeps ascending order; with several, warps append in any order.
+template <int G, class F>
+__device__ __forceinline__ int sat_queue(int base, int span, int n, int tid, int* q, int* qn, F&& keep) {
+    constexpr int T = 32 * G;
+    const unsigned lt = (1u << (tid & 31)) - 1u;
+    int cnt = 0;
+    for (int j = 0; j < span; j += T) {
+        const int f = base + j + tid;
+        const bool k = f < n && keep(f);
+        const unsigned m = __ballot_sync(0xffffffffu, k);
+        if (G == 1) {
+            if (k) q[cnt + __popc(m & lt)] = f;
+            cnt += __popc(m);
+        } else {
+            int b = 0;
+            if ((tid & 31) == 0 && m) b = atomicAdd(qn, __popc(m));
+            b = __shfl_sync(0xffffffffu, b, 0);
+            if (k) q[b + __popc(m & lt)] = f;
+        }
+    }
+    if (G == 1) {
+        __syncwarp();
+        return cnt;
+    }
+    __syncthreads();
+    cnt = *qn;
+    __syncthreads();
+    if (tid == 0) *qn = 0;   // visible to the next pass's appends after sat_queue_done
+    return cnt;
+}
+// the queue is read until here; the next pass may refill it
+template <int G> __device__ __forceinline__ void sat_queue_done() {
+    if (G == 1) __syncwarp(); else __syncthreads();
+}
 
 // Staged SAT of one pair by a group of G warps (tid in [0, 32 G)).  Each thread takes axes
 // f and f + 32 G of every 64 G-axis chunk, so a thread's axes ascend; the group stops at the
@@ -868,37 +943,58 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
     for (int e = tid; e < nb; e += T) { V3<R> b0, b1; c.sb.edge(e, b0, b1); st3(st.dB, e, mv(c.tb().b, normalized(b0 - b1))); }
     if (c.sa.type == ST_HULL) for (int i = tid; i < c.sa.nv; i += T) stv(st.vA, i, c.sa.vert(i));
     if (c.sb.type == ST_HULL) for (int i = tid; i < c.sb.nv; i += T) stv(st.vB, i, c.sb.vert(i));
+    int* queue = reinterpret_cast<int*>(smem + sat_stage_reals<R>() + sat_scratch_reals<R>(G));
+    int* qn = reinterpret_cast<int*>(rd + 2 * G + 3);   // several warps: the queue length
+    if (G > 1 && tid == 0) *qn = 0;
     if (G == 1) __syncwarp(); else __syncthreads();
     const V3<R> dc = c.ta().o - c.tb().o;
-    // ---- face axes of A, then of B (findSeparatingAxis :265-308)
+    const bool able = (c.sa.type != ST_HULL || c.sa.inner > 0) && (c.sb.type != ST_HULL || c.sb.inner > 0);
+    // ---- face axes of A, then of B (findSeparatingAxis :265-308).  Each pass compacts the axes
+    // that the running minimum does not rule out (sat_prunable) and projects those, two per thread;
+    // the first 2T axes run unpruned and give the bound.  A candidate compares by (depth, axis
+    // index), the reference's first strict minimum in any visiting order.
+    auto face_axis = [&](int f) {
+        V3<R> n = f < fa ? ld3(st.nA, f) : ld3(st.nB, f - fa);
+        if (dot(dc, n) < 0) n = n * R(-1.0);
+        return n;
+    };
     R bd = Lim<R>::max();
     int bf = 0x7fffffff, bside = 0, bia = -1, bib = -1;
-    for (int base = 0; base < fa + fb; base += 2 * T) {
-        V3<R> n[2];
-        bool ok[2];
-        for (int k = 0; k < 2; k++) {
-            const int f = base + T * k + tid;
-            ok[k] = f < fa + fb;
-            n[k] = !ok[k] ? V3<R>(0, 0, 0) : f < fa ? ld3(st.nA, f) : ld3(st.nB, f - fa);
-            if (ok[k] && dot(dc, n[k]) < 0) n[k] = n[k] * R(-1.0);
-        }
-        R min0[2], max0[2], min1[2], max1[2];
-        int a0[2], a1[2], b0[2], b1[2];
-        R best = bd;
-        warp_min(best);
-        pair_intervals2(c, n, ok, best, st.vA, st.vB, min0, max0, min1, max1, a0, a1, b0, b1);
-        bool sep = false;
-        for (int k = 0; k < 2; k++) sep |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
-        if (group_any<G>(sep)) return;
-        for (int k = 0; k < 2; k++) {
-            if (!ok[k]) continue;
-            const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
-            const R d = d0 < d1 ? d0 : d1;
-            if (d < bd) {
-                bd = d; bf = base + T * k + tid; bside = d0 < d1;
-                bia = d0 < d1 ? a1[k] : a0[k]; bib = d0 < d1 ? b0[k] : b1[k];
+    for (int pass = 0; pass < fa + fb;) {
+        const int span = pass == 0 ? 2 * T : kSatQ * T;
+        R pb = bd;
+        warp_min(pb);
+        const int cnt = sat_queue<G>(pass, span, fa + fb, tid, queue, qn, [&](int f) { return !sat_prunable(c, able, face_axis(f), pb); });
+        for (int base = 0; base < cnt; base += 2 * T) {
+            V3<R> n[2];
+            bool ok[2];
+            int fi[2];
+            for (int k = 0; k < 2; k++) {
+                const int qi = base + T * k + tid;
+                ok[k] = qi < cnt;
+                fi[k] = ok[k] ? queue[qi] : 0x7fffffff;
+                n[k] = ok[k] ? face_axis(fi[k]) : V3<R>(0, 0, 0);
+            }
+            R min0[2], max0[2], min1[2], max1[2];
+            int a0[2], a1[2], b0[2], b1[2];
+            R best = bd;
+            warp_min(best);
+            pair_intervals2(c, n, ok, best, st.vA, st.vB, min0, max0, min1, max1, a0, a1, b0, b1);
+            bool sep = false;
+            for (int k = 0; k < 2; k++) sep |= ok[k] && (max0[k] < min1[k] || max1[k] < min0[k]);
+            if (group_any<G>(sep)) return;
+            for (int k = 0; k < 2; k++) {
+                if (!ok[k]) continue;
+                const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
+                const R d = d0 < d1 ? d0 : d1;
+                if (d < bd || (d == bd && fi[k] < bf)) {
+                    bd = d; bf = fi[k]; bside = d0 < d1;
+                    bia = d0 < d1 ? a1[k] : a0[k]; bib = d0 < d1 ? b0[k] : b1[k];
+                }
             }
         }
+        sat_queue_done<G>();
+        pass += span;
     }
     R dmin = bd;
     int wf = bf;
@@ -937,22 +1033,31 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
     const bool boxA = c.sa.type == ST_BOX, boxB = c.sb.type == ST_BOX;
     const int ua = boxA ? 3 : na, ub = boxB ? 3 : nb;
     const int ne = ua * ub;
-    for (int base = 0; base < ne; base += 2 * T) {
+    auto edge_axis = [&](int q, V3<R>& a) {   // false for parallel edges
+        const int iu = q / ub, ju = q - iu * ub;
+        const V3<R> x = cross(ld3(st.dA, boxA ? 4 * iu : iu), ld3(st.dB, boxB ? 4 * ju : ju));
+        if (rabs(norm(x) - 0) < eps<R>()) return false;
+        a = normalized(x);
+        if (dot(dc, a) < 0) a = a * R(-1.0);
+        return true;
+    };
+    for (int pass = 0; pass < ne; pass += kSatQ * T) {
+      R pb = ed;
+      warp_min(pb);
+      const int cnt = sat_queue<G>(pass, kSatQ * T, ne, tid, queue, qn, [&](int q) {
+          V3<R> a;
+          return edge_axis(q, a) && !sat_prunable(c, able, a, pb);
+      });
+      for (int qb = 0; qb < cnt; qb += 2 * T) {
         V3<R> cr[2];
         bool ok[2];
+        int qa[2];
         for (int k = 0; k < 2; k++) {
-            const int q = base + T * k + tid;
-            ok[k] = false;
+            const int qi = qb + T * k + tid;
+            ok[k] = qi < cnt;
+            qa[k] = ok[k] ? queue[qi] : 0;
             cr[k] = V3<R>(0, 0, 0);
-            if (q < ne) {
-                const int iu = q / ub, ju = q - iu * ub;
-                const V3<R> x = cross(ld3(st.dA, boxA ? 4 * iu : iu), ld3(st.dB, boxB ? 4 * ju : ju));
-                if (!(rabs(norm(x) - 0) < eps<R>())) {
-                    ok[k] = true;
-                    cr[k] = normalized(x);
-                    if (dot(dc, cr[k]) < 0) cr[k] = cr[k] * R(-1.0);
-                }
-            }
+            if (ok[k]) edge_axis(qa[k], cr[k]);
         }
         R min0[2], max0[2], min1[2], max1[2];
         int a0[2], a1[2], b0[2], b1[2];
@@ -967,7 +1072,7 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
             const R d0 = max0[k] - min1[k], d1 = max1[k] - min0[k];
             const R dist = d0 < d1 ? d0 : d1;
             if (!(dist < ed || (dist == ed && ep != 0x7fffffff))) continue;
-            const int q = base + T * k + tid;
+            const int q = qa[k];
             const int iu = q / ub, ju = q - iu * ub;
             const bool side = d0 < d1;
             const V3<R> wa = shape_witness(c.sa, c.ta(), cr[k], side, side ? a1[k] : a0[k], st.vA);
@@ -989,6 +1094,8 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
             if (qref == 0x7fffffff || !(dist < ed || qref < ep)) continue;
             ed = dist; ep = qref; ewa = wa; ewb = wb; en = cr[k];
         }
+      }
+      sat_queue_done<G>();
     }
     R emin = ed;
     int wq = ep;
@@ -1159,7 +1266,9 @@ __device__ bool sat_warp(Pair<R>& c, int lane) {
 // (TA, TB; one launch per pairing); G = kSatGroup runs one heavy pair per block, any pairing (-1).
 // Only thread 0 holds the pair's contact cache.
 // per-group stride, a multiple of 4 reals so that every group's vertex rows stay 16-byte aligned
-template <class R> constexpr int sat_group_reals(int G) { return (sat_stage_reals<R>() + sat_scratch_reals<R>(G) + 3) & ~3; }
+template <class R> constexpr int sat_group_reals(int G) {
+    return (sat_stage_reals<R>() + sat_scratch_reals<R>(G) + sat_queue_reals<R>(G) + 3) & ~3;
+}
 static_assert(sat_group_reals<float>(1) % 4 == 0 && (3 * (2 * kSatF + 2 * kSatE)) % 4 == 0, "SAT staging alignment");
 template <class R, int G, int TA, int TB>
 __global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 4 : 2)

@@ -49,6 +49,7 @@ template <class R> struct ShapeView {
     const R* e_a;              // unique edge endpoints [ne*3]
     const R* e_b;
     int ne;
+    R inner, outer;            // hulls: balls about the local origin inside / around the vertices (inner < 0: none)
     // concave meshes: the face tree's leaves in tree order, each a face range and its box
     // (nl == 0 for convex meshes, whose leaves hold one face each)
     int nl;
@@ -105,6 +106,7 @@ template <class R> struct ShapeTable {
     const int* h_vbeg; const int* h_vcnt; const int* h_fbeg; const int* h_fcnt; const int* h_ebeg; const int* h_ecnt;
     const R* hv; const int* f_off; const int* f_idx; const R* f_n; const R* f_min; const R* f_max;
     const R* e_a; const R* e_b;
+    const R* h_rad;       // [H*2] per hull: inner and outer radius about the local origin
     // concave meshes (hull tables plus the face-tree leaves): leaves [h_lbeg[h], h_lbeg[h] + h_lcnt[h])
     const int* h_lbeg; const int* h_lcnt; const int* lf_beg; const int* lf_cnt; const R* lf_min; const R* lf_max;
     // compound shapes: children [c_beg[s], c_beg[s] + c_cnt[s]) of shape s, each a non-compound
@@ -131,11 +133,13 @@ template <class R> struct ShapeTable {
         v.r2 = p0 * 2;
         v.hv = nullptr; v.nv = 0; v.f_off = nullptr; v.f_idx = nullptr; v.f_n = nullptr; v.f_min = nullptr; v.f_max = nullptr;
         v.nf = 0; v.e_a = nullptr; v.e_b = nullptr; v.ne = 0;
+        v.inner = R(-1); v.outer = R(0);
         v.nl = 0; v.l_beg = nullptr; v.l_cnt = nullptr; v.l_min = nullptr; v.l_max = nullptr;
         if (v.type == ST_HULL || v.type == ST_CONCAVE) {
             const int h = hull[s];
             const int vb = h_vbeg[h], fb = h_fbeg[h], eb = h_ebeg[h];
             v.hv = hv + vb * 3; v.nv = h_vcnt[h];
+            v.inner = h_rad[2 * h]; v.outer = h_rad[2 * h + 1];
             v.f_off = f_off + fb; v.f_idx = f_idx; v.f_n = f_n + fb * 3; v.f_min = f_min + fb * 3; v.f_max = f_max + fb * 3;
             v.nf = h_fcnt[h];
             v.e_a = e_a + eb * 3; v.e_b = e_b + eb * 3; v.ne = h_ecnt[h];

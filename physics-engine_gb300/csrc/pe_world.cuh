@@ -254,13 +254,13 @@ private:
     // shapes
     int S_ = 0;
     DBuf<int> stype_, shull_, hvbeg_, hvcnt_, hfbeg_, hfcnt_, hebeg_, hecnt_, hfoff_, hfidx_;
-    DBuf<R> sparam_, hv_, hfn_, hfmin_, hfmax_, hea_, heb_;
+    DBuf<R> sparam_, hv_, hfn_, hfmin_, hfmax_, hea_, heb_, hrad_;
     std::vector<int> h_stype_;
     std::vector<R> h_sparam_;
     std::vector<M3<R>> h_sinertia_;
     // host copies of the shape tables (shapes are only ever appended after set_shapes)
     std::vector<int> h_shull_, h_hvb_, h_hvc_, h_hfb_, h_hfc_, h_heb_, h_hec_, h_foff_, h_fidx_;
-    std::vector<R> h_hv_, h_fn_, h_fmn_, h_fmx_, h_ea_, h_eb_;
+    std::vector<R> h_hv_, h_fn_, h_fmn_, h_fmx_, h_ea_, h_eb_, h_hrad_;   // h_hrad_: inner, outer radius per hull
     // concave meshes' face-tree leaves (per hull: first leaf and count; per leaf: face range and box)
     DBuf<int> hlbeg_, hlcnt_, lfbeg_, lfcnt_;
     DBuf<R> lfmin_, lfmax_;

@@ -62,6 +62,7 @@ template <class R> ShapeTable<R> World<R>::shapes() const {
     ShapeTable<R> t;
     t.type = stype_.p; t.param = sparam_.p; t.hull = shull_.p;
     t.h_vbeg = hvbeg_.p; t.h_vcnt = hvcnt_.p; t.h_fbeg = hfbeg_.p; t.h_fcnt = hfcnt_.p; t.h_ebeg = hebeg_.p; t.h_ecnt = hecnt_.p;
+    t.h_rad = hrad_.p;
     t.hv = hv_.p; t.f_off = hfoff_.p; t.f_idx = hfidx_.p; t.f_n = hfn_.p; t.f_min = hfmin_.p; t.f_max = hfmax_.p;
     t.e_a = hea_.p; t.e_b = heb_.p;
     t.c_beg = cbeg_.p; t.c_cnt = ccnt_.p; t.c_shape = cshape_.p; t.c_xf = cxf_.p;
@@ -105,7 +106,7 @@ void World<R>::set_shapes(int S, const int* type, const double* param, const int
     S_ = 0;
     h_stype_.clear(); h_sparam_.clear(); h_sinertia_.clear(); h_shull_.clear();
     h_hvb_.clear(); h_hvc_.clear(); h_hfb_.clear(); h_hfc_.clear(); h_heb_.clear(); h_hec_.clear(); h_foff_.clear(); h_fidx_.clear();
-    h_hv_.clear(); h_fn_.clear(); h_fmn_.clear(); h_fmx_.clear(); h_ea_.clear(); h_eb_.clear();
+    h_hv_.clear(); h_fn_.clear(); h_fmn_.clear(); h_fmx_.clear(); h_ea_.clear(); h_eb_.clear(); h_hrad_.clear();
     hull_by_content_.clear();
     h_cbeg_.clear(); h_ccnt_.clear(); h_cshape_.clear(); h_cready_.clear(); h_cxf_.clear();
     h_hlb_.clear(); h_hlc_.clear(); h_lfb_.clear(); h_lfc_.clear(); h_lfmn_.clear(); h_lfmx_.clear();
@@ -170,6 +171,7 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
             h_hvb_.push_back((int)h_hv_.size() / 3); h_hvc_.push_back(vcnt[s]);
             h_hfb_.push_back((int)h_fn_.size() / 3); h_hfc_.push_back(fcnt[s]);
             h_heb_.push_back((int)h_ea_.size() / 3); h_hec_.push_back((int)h.e_a.size() / 3);
+            h_hrad_.push_back(h.inner); h_hrad_.push_back(h.outer);
             const int ibase = (int)h_fidx_.size();
             if (h_foff_.empty()) h_foff_.push_back(0);
             for (int f = 0; f < fcnt[s]; f++) h_foff_.push_back(ibase + h.f_off[f + 1]);
@@ -201,7 +203,7 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
     upload_tail(hfcnt_, h_hfc_, o_h, st_); upload_tail(hebeg_, h_heb_, o_h, st_); upload_tail(hecnt_, h_hec_, o_h, st_);
     upload_tail(hv_, h_hv_, o_v, st_); upload_tail(hfoff_, h_foff_, o_fo, st_); upload_tail(hfidx_, h_fidx_, o_fi, st_);
     upload_tail(hfn_, h_fn_, o_f, st_); upload_tail(hfmin_, h_fmn_, o_f, st_); upload_tail(hfmax_, h_fmx_, o_f, st_);
-    upload_tail(hea_, h_ea_, o_e, st_); upload_tail(heb_, h_eb_, o_e, st_);
+    upload_tail(hea_, h_ea_, o_e, st_); upload_tail(heb_, h_eb_, o_e, st_); upload_tail(hrad_, h_hrad_, o_h * 2, st_);
     upload_tail(cbeg_, h_cbeg_, s0, st_); upload_tail(ccnt_, h_ccnt_, s0, st_);
     upload_tail(hlbeg_, h_hlb_, o_h, st_); upload_tail(hlcnt_, h_hlc_, o_h, st_);
     upload_tail(lfbeg_, h_lfb_, o_l, st_); upload_tail(lfcnt_, h_lfc_, o_l, st_);
