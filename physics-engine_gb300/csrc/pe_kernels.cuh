@@ -443,7 +443,7 @@ __global__ void k_bp_axis_combine(const int* scene_off, const int2* item, int n_
 // and the scheduling split of ConvexConvexCollisionAlgorithm pairs by estimated work: candidate
 // axes x projection cost (hull vertices; a box or cylinder projects in closed form).
 constexpr int kSatF = 128, kSatE = 192, kSatV = 64;
-constexpr int kSatWarps = 4;                 // pairs (one warp each) per block, light pairs
+constexpr int kSatWarps = 1;                 // pairs (one warp each) per block, light pairs
 constexpr int kSatGroup = 8;                 // warps per pair, heavy pairs (one block each)
 constexpr long long kSatHeavyCost = 200000;
 template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& s) {
@@ -1271,7 +1271,7 @@ template <class R> constexpr int sat_group_reals(int G) {
 }
 static_assert(sat_group_reals<float>(1) % 4 == 0 && (3 * (2 * kSatF + 2 * kSatE)) % 4 == 0, "SAT staging alignment");
 template <class R, int G, int TA, int TB>
-__global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 4 : 2)
+__global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 16 / kSatWarps : 2)
 k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, R* sat_out) {
     extern __shared__ __align__(16) unsigned char sat_smem[];
     const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
