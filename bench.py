@@ -244,6 +244,9 @@ def run_ours(args, rank, world, device):
         g.step(1, mode)
     for _ in range(args.warmup):
         g.step(1, mode)
+    # the state the timed steps start from: the end-to-end loop below replays the same steps
+    n_axes = len(offs) - 1 if offs is not None else 1
+    snapshot = (g.state(), g.results(), g.axes(n_axes))
     # device-resident timed region
     g.phase_times(reset=True)
     per_step, launches = [], 0
@@ -271,17 +274,20 @@ def run_ours(args, rank, world, device):
     peak, peak_kind = measured_peak()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = None   # ncu's per-kernel DRAM writes include write-backs of earlier kernels' dirty lines
-    # end to end through the C ABI with host buffers: each step copies the poses and velocities in
-    # from page-locked host arrays and reads the stepped ones back into them
+    # end to end through the C ABI with host buffers, over the same steps as the timed region
+    # (restored from the snapshot): each step copies the poses and velocities in from page-locked
+    # host arrays and reads the stepped ones back into them
     import torch   # page-locked host memory
     io = ("origin", "basis", "lin_vel", "ang_vel")
     st = {f: torch.empty((N, 3, 3) if f == "basis" else (N, 3), dtype=torch.float64, pin_memory=True).numpy() for f in io}
     g.state(fields=io, out=st)
     g.set_state(st)                      # one untimed pass through the host path
-    g.step(1, mode)
+    g.set_state(snapshot[0])
+    g.set_results(snapshot[1])
+    g.set_axes(snapshot[2])
     g.state(fields=io, out=st)
     e2e_times = []
-    for _ in range(max(3, args.steps // 2)):
+    for _ in range(args.steps):
         t0 = time.perf_counter()
         g.set_state(st)
         g.step(1, mode)
