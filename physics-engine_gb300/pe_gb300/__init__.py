@@ -204,7 +204,7 @@ class GpuWorld:
             else:
                 ptrs.append(None)
         self._ck(self.lib.pe_gpu_get_state(self.h, *ptrs))
-        return out
+        return dst if dst is not None else out
 
     def set_state(self, d):
         """Overwrite the given body-state fields (missing keys are left untouched)."""

@@ -329,6 +329,26 @@ def test_gpu_settled_piles_narrowphase_matches_oracle(bits, n_scenes):
     compare_results(g.results(), ro, what=f"settled piles narrowphase f{bits}")
 
 
+def test_gpu_state_into_caller_buffers():
+    """state(out=...) writes the requested fields into the caller's arrays (the end-to-end loop's
+    page-locked buffers) with the same values as a fresh read, leaves the other fields alone, and
+    refuses arrays of the wrong shape before touching the device."""
+    scene = sc.pile(200, seed=5, real_bits=32)
+    g = pg.GpuWorld(scene, 32)
+    g.step(20, pg.COLORED)
+    ref = g.state()
+    io = ("origin", "basis", "lin_vel", "ang_vel")
+    out = {f: np.full_like(ref[f], np.nan) for f in io}
+    got = g.state(fields=io, out=out)
+    assert got is out
+    for f in io:
+        np.testing.assert_array_equal(out[f], ref[f])
+    g.set_state(out)
+    np.testing.assert_array_equal(g.state()["origin"], ref["origin"])
+    with pytest.raises(ValueError):
+        g.state(fields=("origin",), out={"origin": np.zeros((3, 3))})
+
+
 def test_gpu_tower_serial_order_per_step_replay():
     """The 1,002-body tower in double precision: from identical state, one GPU step with the
     oracle's pair order (ties among the sort keys make the order a property of the host
