@@ -2003,14 +2003,6 @@ __global__ void k_gc_mask_reset(int lo, int m, const uint32_t* order, Results<R>
     mask[q.y] = 0ull;
 }
 template <class R>
-__global__ void k_gc_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, const int* color, int* claim) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= m || color[lo + j] >= 0) return;
-    const int2 q = item_bodies(order[lo + j], res, J);
-    claim[q.x] = 0x7fffffff;
-    claim[q.y] = 0x7fffffff;
-}
-template <class R>
 __global__ void k_gc_claim(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B, const int* color, int* claim) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m || color[lo + j] >= 0) return;
@@ -2120,12 +2112,6 @@ __global__ void __launch_bounds__(kBlock) k_gc_rounds(int lo, int m, const uint3
 // colour histogram (leftovers -> the last colour) and placement of every colour but the last
 __global__ void k_gc_count(int lo, int m, int* color, int* cnt);
 __global__ void k_gc_place(int lo, int m, const int* color, const uint32_t* order, int* cursor, uint32_t* corder);
-template <class R>
-__global__ void k_gc_pass(const uint32_t* list, int n, Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    iterate_item(list[j], res, J, B, rows, row_off);
-}
 // All iterations of a big island in one cooperative launch: colour after colour (the items of a
 // colour spread over the whole grid), a grid-wide barrier between colours, the leftover colour in
 // island order on one thread at the end of each iteration.  The same updates in the same order as
@@ -2151,15 +2137,6 @@ __global__ void __launch_bounds__(kBlock) k_gc_solve(const uint32_t* corder, con
                     if (color[lo + j] == kMaxColorsBig - 1) iterate_item(order[lo + j], res, J, B, rows, row_off);
             grid.sync();
         }
-    }
-}
-
-template <class R>
-__global__ void k_gc_last(int lo, int m, const uint32_t* order, const int* color, Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows,
-                          const int* row_off) {
-    for (int j = 0; j < m; j++) {
-        if (color[lo + j] != kMaxColorsBig - 1) continue;
-        iterate_item(order[lo + j], res, J, B, rows, row_off);
     }
 }
 
