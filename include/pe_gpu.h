@@ -134,7 +134,12 @@ int pe_gpu_narrowphase(pe_gpu_world* w);
 /* ConstraintSolver::setupSolver + solve (constraint_solver.h:14-28) on the current results. */
 int pe_gpu_solve(pe_gpu_world* w, int solver_mode);
 
-/* ---- state transfer (host arrays, doubles) ---- */
+/* ---- state transfer (host arrays, doubles) ----
+ * Each array is row-major per body (3 or 9 doubles); a null pointer skips that field.  One copy per
+ * field moves the caller's array to or from a device staging buffer, and a kernel changes the
+ * precision and layout on the device, so page-locked caller arrays make the transfers plain DMA.
+ * pe_gpu_set_state recomputes the AABB scale of every body when origin, aabb_min and aabb_max are
+ * all given.  Both return after the copies have completed. */
 int pe_gpu_n_bodies(const pe_gpu_world* w);
 int pe_gpu_get_state(pe_gpu_world* w, double* origin, double* basis, double* lin_vel, double* ang_vel, double* aabb_min,
                      double* aabb_max, double* world_inv_inertia);
