@@ -913,9 +913,9 @@ template <int G> __device__ __forceinline__ void sat_queue_done() {
     if (G == 1) __syncwarp(); else __syncthreads();
 }
 
-// Staged SAT of one pair by a group of G warps (tid in [0, 32 G)).  Each thread takes axes
-// f and f + 32 G of every 64 G-axis chunk, so a thread's axes ascend; the group stops at the
-// first chunk holding a separating axis.
+// Staged SAT of one pair by a group of G warps (tid in [0, 32 G)).  Per pass the group tests
+// candidate axes against the pruning bound, queues the survivors and projects them two per thread;
+// it stops at the first round holding a separating axis.
 // What the staged SAT leaves for the contact step (one record of kSatOut reals per pair, written by
 // thread 0): the face-stage point, the edge-stage point, the final axis and the clipping faces,
 // in the order the reference adds them (convex_convex_collision_algorithm.cpp:300-308, :363-395,
