@@ -87,3 +87,34 @@ def max_penetration(results):
     """Deepest contact (positive = penetration) over the valid points of all results."""
     d = [results["slots"][i, :n, 12].min() for i, n in enumerate(results["point_size"]) if n]
     return float(max(0.0, -min(d))) if d else 0.0
+
+
+def contact_residual(pre, post, results, scene, kerp=0.2, pen_th=0.3, rest_th=0.1):
+    """Velocity-level residual of the contact rows after a solve: for every valid point, how far its
+    normal relative velocity n . (v_a - v_b) at the contact falls short of the row's target
+    (restitution of the pre-solve approach speed, zeroed below rest_th, minus the Baumgarte term
+    kerp * max(depth, -pen_th) / dt), as FrictionContactConstraint::initSequentialImpulse sets it
+    up.  `pre` and `post` are the body states before and after the solve; returns (rms, max) of
+    max(0, target - n . v_rel) over the points."""
+    slots, ps = results["slots"], results["point_size"]
+    keep = np.arange(slots.shape[1])[None, :] < ps[:, None]
+    ia = np.repeat(results["res_a"], slots.shape[1]).reshape(keep.shape)[keep]
+    ib = np.repeat(results["res_b"], slots.shape[1]).reshape(keep.shape)[keep]
+    rest = np.repeat(results["restitution"], slots.shape[1]).reshape(keep.shape)[keep]
+    p = slots[keep]
+    n, la, lb, depth = p[:, 3:6], p[:, 6:9], p[:, 9:12], p[:, 12]
+    ra = np.einsum("nij,nj->ni", pre["basis"][ia], la)
+    rb = np.einsum("nij,nj->ni", pre["basis"][ib], lb)
+
+    def rel(s):
+        va = s["lin_vel"][ia] + np.cross(s["ang_vel"][ia], ra)
+        vb = s["lin_vel"][ib] + np.cross(s["ang_vel"][ib], rb)
+        return np.einsum("ni,ni->n", n, va - vb)
+
+    rev = -rel(pre)
+    rev = np.where(np.abs(rev) < rest_th, 0.0, rev) * rest
+    target = rev - kerp * np.maximum(depth, -pen_th) / scene.dt
+    short = np.maximum(0.0, target - rel(post))
+    if short.size == 0:
+        return 0.0, 0.0
+    return float(np.sqrt(np.mean(short ** 2))), float(short.max())
