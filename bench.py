@@ -21,8 +21,9 @@ Workloads (all synthetic, seeded):
 One "step" is one full World::step (integrate, broadphase, narrowphase, solver) of the whole
 workload.  `value` = body-steps per second of device time with the state resident in HBM
 (CUDA events on the library's stream, L2 flushed between steps); `e2e` = the same metric
-through the C ABI with host buffers: every step uploads body poses and velocities from host
-memory and reads them back.  `--impl reference` times the reference's CPU step (its
+through the C ABI with host buffers over the same steps (replayed from a snapshot of the state,
+contact results and sweep axes taken before the timed region): every step uploads body poses and
+velocities from page-locked host arrays and reads the stepped ones back into them.  `--impl reference` times the reference's CPU step (its
 algorithm restated in oracle/, multithreaded over the host cores like the reference's thread
 pool) on the same workload.
 """
