@@ -151,3 +151,83 @@ def test_uncertifiable_meshes_are_refused(radii_tool):
     for d in radii_tool([(v, faces), (Lv, Lf)]):
         for bits, (inner, outer, _) in d.items():
             assert inner == -1.0, (bits, inner)
+
+
+def _rot(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def _hull_interval(v, basis, origin, axis):
+    """The reference's hull projection in FP32 (convex_mesh_shape.cpp:160-183): the minimum over all
+    vertices, the maximum over the vertices that were not a running minimum when visited (so never
+    vertex 0), both offset by origin . axis."""
+    f = np.float32
+    la = (basis.T.astype(f) @ axis.astype(f)).astype(f)
+    p = (v[:, 0].astype(f) * la[0] + v[:, 1].astype(f) * la[1]).astype(f) + v[:, 2].astype(f) * la[2]
+    mn, mx = f(3.4e38), f(-1e30)
+    for x in p.astype(f):
+        if x < mn:
+            mn = x
+        elif x > mx:
+            mx = x
+    off = f(origin.astype(f) @ axis.astype(f))
+    return f(mn + off), f(mx + off), float(off)
+
+
+def test_prune_bound_never_exceeds_the_computed_depth(radii_tool):
+    """For hull pairs at random overlapping poses, along random axes and along the directions of each
+    hull's vertex 0 (the vertex the projection never takes as the maximum), the SAT's pruning bound
+    min(loA - hiB, loB - hiA) with [o - r, o + r] per hull stays below the FP32 depth the projection
+    computes, within the bound's roundoff allowance (64 units of the magnitudes).  A radius certified
+    for the whole hull instead of the hull without vertex 0 fails this along those directions."""
+    s = sc.batched_piles(n_scenes=8, seed=0)[0]
+    hulls = [d[32] for d in radii_tool(scene_meshes(s, 40))]
+    rng = np.random.default_rng(11)
+    u = 1.1920929e-7
+    checked = 0
+    for t in range(400):
+        (ra, oa_, va), (rb, ob_, vb) = hulls[rng.integers(len(hulls))], hulls[rng.integers(len(hulls))]
+        if ra <= 0 or rb <= 0:
+            continue
+        Ba, Bb = _rot(rng), _rot(rng)
+        oa = rng.uniform(-50, 50, 3)
+        ob = oa + rng.normal(size=3) * 0.3 * (oa_ + ob_)
+        axes = [a / np.linalg.norm(a) for a in rng.normal(size=(8, 3))]
+        axes += [Ba @ va[0] / np.linalg.norm(va[0]), Bb @ vb[0] / np.linalg.norm(vb[0])]
+        axes += [-(Bb @ vb[0]) / np.linalg.norm(vb[0]), -(Ba @ va[0]) / np.linalg.norm(va[0])]
+        for ax in axes:
+            mnA, mxA, cA = _hull_interval(va, Ba, oa, ax)
+            mnB, mxB, cB = _hull_interval(vb, Bb, ob, ax)
+            depth = min(float(mxA) - float(mnB), float(mxB) - float(mnA))
+            lb = min((cA + ra) - (cB - rb), (cB + rb) - (cA - ra))
+            slack = 64 * u * (abs(cA) + oa_ + abs(cB) + ob_)
+            assert lb - slack <= depth, (t, lb, depth, slack)
+            checked += 1
+    assert checked > 1000
+
+
+def test_ball_lies_within_each_computed_interval(radii_tool):
+    """Per hull, along every outward facet normal of the hull without vertex 0 (where the computed
+    maximum is smallest), along the vertex-0 directions and along random directions, at a random pose:
+    the computed FP32 interval [min, max] holds [o - r, o + r] within the bound's roundoff allowance.
+    Along those facet normals a radius certified for the whole hull falls outside on several hulls."""
+    s = sc.batched_piles(n_scenes=8, seed=0)[0]
+    hulls = [d[32] for d in radii_tool(scene_meshes(s, 40))]
+    rng = np.random.default_rng(5)
+    u = 1.1920929e-7
+    for r, outer, v in hulls:
+        assert r > 0
+        B, o = _rot(rng), rng.uniform(-50, 50, 3)
+        facets = spatial.ConvexHull(v[1:]).equations[:, :3]
+        dirs = [B @ n for n in facets] + [B @ v[0] / np.linalg.norm(v[0])]
+        dirs += [a / np.linalg.norm(a) for a in rng.normal(size=(16, 3))]
+        for ax in dirs:
+            for sgn in (1.0, -1.0):
+                mn, mx, c = _hull_interval(v, B, o, sgn * ax)
+                slack = 64 * u * (abs(c) + outer)
+                assert float(mx) >= c + r - slack and float(mn) <= c - r + slack, (r, float(mn), float(mx), c)
