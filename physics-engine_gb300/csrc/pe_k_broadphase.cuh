@@ -1,0 +1,385 @@
+// Kernels of the rigid-body step, part 2: scan, the LSD radix sort and the sweep-and-prune broadphase.
+#pragma once
+#include "pe_k_integrate.cuh"
+
+namespace pe {
+
+// ===================================================================== scan
+// exclusive scan of n ints, in place, three phases; totals of each tile in aux
+__global__ void k_scan_tiles(int* data, int n, int* aux);
+__global__ void k_scan_aux(int* aux, int m, int* total);
+__global__ void k_scan_add(int* data, int n, const int* aux);
+
+// ===================================================================== radix sort
+// Sort (key, value) pairs by a 64-bit key and then, more significantly, by a 32-bit
+// secondary key (scene id); stable, least-significant digit first, 8-bit digits.
+constexpr int kRadixItems = 16;                      // items per thread per tile
+constexpr int kRadixTile = kBlock * kRadixItems;     // 4096 items per tile
+__global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n, int shift, int use2, int* hist, int n_tiles);
+__global__ void k_radix_scatter(const uint64_t* key_in, const uint32_t* key2_in, const uint32_t* val_in, uint64_t* key_out,
+                                uint32_t* key2_out, uint32_t* val_out, int n, int shift, int use2, const int* hist, int n_tiles);
+
+__device__ inline uint64_t order_bits(float x) {
+    if (x == 0.0f) x = 0.0f;   // -0 and +0 compare equal: give them one key
+    const uint32_t u = __float_as_uint(x);
+    return (uint64_t)((u & 0x80000000u) ? ~u : (u | 0x80000000u));
+}
+__device__ inline uint64_t order_bits(double x) {
+    if (x == 0.0) x = 0.0;
+    const uint64_t u = (uint64_t)__double_as_longlong(x);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// sort key of each body: its AABB minimum along its scene's sweep axis
+template <class R>
+__global__ void k_bp_keys(Bodies<R> B, const int* scene_axis, uint64_t* key, uint32_t* key2, uint32_t* val) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.n) return;
+    const int ax = scene_axis[B.scene[i]];
+    key[i] = order_bits(B.at(MNX + ax, i));
+    key2[i] = (uint32_t)B.scene[i];
+    val[i] = (uint32_t)i;
+}
+
+// sorted copy of the sweep inputs (coalesced reads in the sweep)
+template <class R>
+__global__ void k_bp_gather(Bodies<R> B, const uint32_t* order, R* smn, R* smx, int* sflag, int* sscene) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= B.n) return;
+    const int i = (int)order[k];
+    for (int d = 0; d < 3; d++) {
+        smn[(size_t)d * B.n + k] = B.at(MNX + d, i);
+        smx[(size_t)d * B.n + k] = B.at(MXX + d, i);
+    }
+    sflag[k] = B.flags[i];
+    sscene[k] = B.scene[i];
+}
+
+// BroadPhaseSweepAndPrune::calcCollisionPairs sweep (broad_phase_sweep_and_prune.cpp:24-35)
+// with BroadPhaseBase::validateCollisionPair (broad_phase_base.cpp:5-19).
+//
+// One warp per sorted position i; the lanes test candidates j = i+1+lane, i+33+lane, ... with
+// coalesced loads of the sorted AABBs.  The reference stops at the first j whose minimum along
+// the axis exceeds i's maximum; minima are sorted, so the lanes still in range form a prefix and
+// the warp stops after the first chunk that is not full.  Overlapping partners are compacted in
+// ascending j with a ballot and a prefix popcount, which is the reference's pair order.
+// Pass 0 counts the pairs of each position and keeps its first kStage partners; pass 1 writes the
+// pairs at the scanned offsets, copying staged partners and re-sweeping only crowded positions.
+constexpr int kStage = 4;
+template <class R, bool WRITE>
+__device__ __forceinline__ int sweep_warp(int i, int n, int lane, const int* scene_axis, const R* smn, const R* smx,
+                                          const int* sflag, const int* sscene, int* stage, int2* out, const uint32_t* order,
+                                          const IgnoreLists& ign) {
+    const int sc = sscene[i];
+    const int ax = scene_axis[sc];
+    const R* amin = smn + (size_t)ax * n;
+    const R maxi_ax = smx[(size_t)ax * n + i];
+    const R mnx = smn[i], mny = smn[n + i], mnz = smn[2 * (size_t)n + i];
+    const R mxx = smx[i], mxy = smx[n + i], mxz = smx[2 * (size_t)n + i];
+    const int fi = sflag[i];
+    if (fi & BF_IGNORE) return 0;
+    const int a = WRITE ? (int)order[i] : 0;
+    const unsigned lt = (1u << lane) - 1u;
+    int c = 0;
+    for (int j0 = i + 1; j0 < n; j0 += 32) {
+        const int j = j0 + lane;
+        const bool in = j < n && !(amin[j] > maxi_ax) && sscene[j] == sc;
+        const unsigned live = __ballot_sync(0xffffffffu, in);
+        bool hit = false;
+        if (in) {
+            const int fj = sflag[j];
+            hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
+                  !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
+                  !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
+            if (hit && ign.off && ((fi | fj) & BF_IGN_LIST)) hit = !ign.ignored(i, j);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const int k = c + __popc(m & lt);
+            if (WRITE) out[k] = make_int2(a, (int)order[j]);
+            else if (k < kStage) stage[(size_t)i * kStage + k] = j;
+        }
+        c += __popc(m);
+        if (live != 0xffffffffu) break;
+    }
+    return c;
+}
+
+// A position whose window along the axis holds more than kBigWindow candidates (a floor or a wall
+// spanning the scene) is swept by a whole block instead of a warp: 256 candidates per iteration,
+// warp ballots plus a block prefix of the warp counts keep the pairs in ascending j.
+constexpr int kBigWindow = 32768;
+template <class R>
+__device__ __forceinline__ bool big_window(int i, int n, const int* scene_axis, const R* smn, const R* smx, const int* sscene) {
+    const int j = i + kBigWindow;
+    if (j >= n) return false;
+    const int sc = sscene[i], ax = scene_axis[sc];
+    return sscene[j] == sc && !(smn[(size_t)ax * n + j] > smx[(size_t)ax * n + i]);
+}
+template <class R, bool WRITE>
+__device__ int sweep_block(int i, int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                           int2* out, const uint32_t* order, int* wcnt, const IgnoreLists& ign) {
+    const int sc = sscene[i];
+    const int ax = scene_axis[sc];
+    const R* amin = smn + (size_t)ax * n;
+    const R maxi_ax = smx[(size_t)ax * n + i];
+    const R mnx = smn[i], mny = smn[n + i], mnz = smn[2 * (size_t)n + i];
+    const R mxx = smx[i], mxy = smx[n + i], mxz = smx[2 * (size_t)n + i];
+    const int fi = sflag[i];
+    if (fi & BF_IGNORE) return 0;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+    const int a = WRITE ? (int)order[i] : 0;
+    const unsigned lt = (1u << lane) - 1u;
+    int c = 0;
+    for (int j0 = i + 1; j0 < n; j0 += blockDim.x) {
+        const int j = j0 + tid;
+        const bool in = j < n && !(amin[j] > maxi_ax) && sscene[j] == sc;
+        bool hit = false;
+        if (in) {
+            const int fj = sflag[j];
+            hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
+                  !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
+                  !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
+            if (hit && ign.off && ((fi | fj) & BF_IGN_LIST)) hit = !ign.ignored(i, j);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) wcnt[w] = __popc(m);
+        const int all_in = __syncthreads_and(in);
+        int before = 0, total = 0;
+        for (int k = 0; k < nw; k++) { if (k < w) before += wcnt[k]; total += wcnt[k]; }
+        if (WRITE && hit) out[c + before + __popc(m & lt)] = make_int2(a, (int)order[j]);
+        c += total;
+        __syncthreads();   // wcnt is rewritten next iteration
+        if (!all_in) break;
+    }
+    return c;
+}
+
+// A crowded position's window (the candidates j > i of its scene whose minimum along the axis does
+// not exceed i's maximum: a prefix of the scene's sorted positions, found by binary search) swept in
+// up to kMaxChunks chunks of at least kChunk candidates, one block per chunk: chunk counts are summed
+// per position, and each chunk writes its pairs after those of the chunks before it, so the pairs
+// keep ascending j.
+constexpr int kChunk = 4096;
+constexpr int kMaxChunks = 32;
+template <class R, bool WRITE>
+__device__ int sweep_range_block(int i, int jb, int je, int n, const R* smn, const R* smx, const int* sflag, int2* out,
+                                 const uint32_t* order, int* wcnt, const IgnoreLists& ign) {
+    const R mnx = smn[i], mny = smn[n + i], mnz = smn[2 * (size_t)n + i];
+    const R mxx = smx[i], mxy = smx[n + i], mxz = smx[2 * (size_t)n + i];
+    const int fi = sflag[i];
+    if (fi & BF_IGNORE) return 0;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+    const int a = WRITE ? (int)order[i] : 0;
+    const unsigned lt = (1u << lane) - 1u;
+    int c = 0;
+    for (int j0 = jb; j0 < je; j0 += blockDim.x) {
+        const int j = j0 + tid;
+        bool hit = false;
+        if (j < je) {
+            const int fj = sflag[j];
+            hit = !(fj & BF_IGNORE) && !((fi & BF_KINEMATIC) && (fj & BF_KINEMATIC)) &&
+                  !(mnx > smx[j] || smn[j] > mxx) && !(mny > smx[n + j] || smn[n + j] > mxy) &&
+                  !(mnz > smx[2 * (size_t)n + j] || smn[2 * (size_t)n + j] > mxz);
+            if (hit && ign.off && ((fi | fj) & BF_IGN_LIST)) hit = !ign.ignored(i, j);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) wcnt[w] = __popc(m);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int k = 0; k < nw; k++) { if (k < w) before += wcnt[k]; total += wcnt[k]; }
+        if (WRITE && hit) out[c + before + __popc(m & lt)] = make_int2(a, (int)order[j]);
+        c += total;
+        __syncthreads();   // wcnt is rewritten next iteration
+    }
+    return c;
+}
+// per crowded position: window end, chunk size and chunk count
+template <class R>
+__global__ void k_bp_big_windows(int n, const int* scene_axis, const int* scene_off, const R* smn, const R* smx, const int* sscene,
+                                 const int* big, const int* n_big, int* wend, int* csize, int* nchunk) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < *n_big; b += gridDim.x * blockDim.x) {
+        const int i = big[b], sc = sscene[i];
+        const R* amin = smn + (size_t)scene_axis[sc] * n;
+        const R mx = smx[(size_t)scene_axis[sc] * n + i];
+        int lo = i + 1, hi = scene_off[sc + 1];   // first j with amin[j] > mx, else the scene's end
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (amin[mid] > mx) hi = mid;
+            else lo = mid + 1;
+        }
+        const int len = lo - (i + 1);
+        int cs = (len + kMaxChunks - 1) / kMaxChunks;
+        cs = cs < kChunk ? kChunk : cs;
+        wend[b] = lo;
+        csize[b] = cs;
+        nchunk[b] = (len + cs - 1) / cs;
+    }
+}
+__global__ void k_bp_chunk_offsets(const int* n_big, const int* nchunk, int* choff, int* total);
+__device__ __forceinline__ int chunk_owner(int c, const int* choff, int nb) {   // last b with choff[b] <= c
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (choff[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+template <class R>
+__global__ void k_bp_count_chunks(int n, const R* smn, const R* smx, const int* sflag, const int* big, const int* n_big, const int* wend,
+                                  const int* csize, const int* choff, const int* total, int* ccount, IgnoreLists ign) {
+    __shared__ int wcnt[32];
+    for (int c = blockIdx.x; c < *total; c += gridDim.x) {
+        const int b = chunk_owner(c, choff, *n_big), i = big[b];
+        const int jb = i + 1 + (c - choff[b]) * csize[b], je = jb + csize[b] < wend[b] ? jb + csize[b] : wend[b];
+        const int k = sweep_range_block<R, false>(i, jb, je, n, smn, smx, sflag, nullptr, nullptr, wcnt, ign);
+        if (threadIdx.x == 0) ccount[c] = k;
+    }
+}
+// per crowded position: its pair count and the offsets of its chunks' pairs
+__global__ void k_bp_chunk_sums(const int* big, const int* n_big, const int* choff, const int* nchunk, const int* ccount, int* cpref,
+                                int* count);
+template <class R>
+__global__ void k_bp_write_chunks(int n, const R* smn, const R* smx, const int* sflag, const uint32_t* order, const int* offset,
+                                  const int* big, const int* n_big, const int* wend, const int* csize, const int* choff, const int* total,
+                                  const int* cpref, int2* pairs, int pair_cap, int* status, IgnoreLists ign) {
+    __shared__ int wcnt[32];
+    for (int c = blockIdx.x; c < *total; c += gridDim.x) {
+        const int b = chunk_owner(c, choff, *n_big), i = big[b];
+        if (offset[i + 1] > pair_cap) {
+            if (threadIdx.x == 0) atomicOr(status, ST_PAIR_OVERFLOW);
+            continue;
+        }
+        const int jb = i + 1 + (c - choff[b]) * csize[b], je = jb + csize[b] < wend[b] ? jb + csize[b] : wend[b];
+        sweep_range_block<R, true>(i, jb, je, n, smn, smx, sflag, pairs + offset[i] + cpref[c], order, wcnt, ign);
+    }
+}
+
+template <class R>
+__global__ void k_bp_count(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene, int* count,
+                           int* stage, int* big, int* n_big, IgnoreLists ign) {
+    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    if (big_window(i, n, scene_axis, smn, smx, sscene)) {   // left to k_bp_count_big
+        if (lane == 0) big[atomicAdd(n_big, 1)] = i;
+        return;
+    }
+    const int c = sweep_warp<R, false>(i, n, lane, scene_axis, smn, smx, sflag, sscene, stage, nullptr, nullptr, ign);
+    if (lane == 0) count[i] = c;
+}
+// one block per listed position (blocks loop over the list)
+template <class R>
+__global__ void k_bp_count_big(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                               int* count, const int* big, const int* n_big, IgnoreLists ign) {
+    __shared__ int wcnt[32];
+    for (int b = blockIdx.x; b < *n_big; b += gridDim.x) {
+        const int i = big[b];
+        const int c = sweep_block<R, false>(i, n, scene_axis, smn, smx, sflag, sscene, nullptr, nullptr, wcnt, ign);
+        if (threadIdx.x == 0) count[i] = c;
+        __syncthreads();
+    }
+}
+template <class R>
+__global__ void k_bp_write_big(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                               const uint32_t* order, const int* offset, int2* pairs, int pair_cap, int* status, const int* big,
+                               const int* n_big, IgnoreLists ign) {
+    __shared__ int wcnt[32];
+    for (int b = blockIdx.x; b < *n_big; b += gridDim.x) {
+        const int i = big[b];
+        const int base = offset[i], c = offset[i + 1] - base;
+        if (c == 0) continue;   // uniform in the block
+        if (base + c > pair_cap) {
+            if (threadIdx.x == 0) atomicOr(status, ST_PAIR_OVERFLOW);
+            continue;
+        }
+        sweep_block<R, true>(i, n, scene_axis, smn, smx, sflag, sscene, pairs + base, order, wcnt, ign);
+        __syncthreads();
+    }
+}
+
+template <class R>
+__global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* smx, const int* sflag, const int* sscene,
+                           const uint32_t* order, const int* offset, const int* stage, int2* pairs, int pair_cap, int* status,
+                           IgnoreLists ign) {
+    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const int base = offset[i], c = offset[i + 1] - base;
+    if (c == 0 || big_window(i, n, scene_axis, smn, smx, sscene)) return;   // big windows: k_bp_write_big
+    if (base + c > pair_cap) {
+        if (lane == 0) atomicOr(status, ST_PAIR_OVERFLOW);
+        return;
+    }
+    if (c <= kStage) {
+        if (lane < c) pairs[base + lane] = make_int2((int)order[i], (int)order[stage[(size_t)i * kStage + lane]]);
+    } else {
+        sweep_warp<R, true>(i, n, lane, scene_axis, smn, smx, sflag, sscene, nullptr, pairs + base, order, ign);
+    }
+}
+
+// next sweep axis of each scene: the axis of largest AABB-centre variance (sweep_and_prune.cpp:37-40).
+// One block per scene sums the sorted centres in double, in an order fixed relative to the scene
+// (thread t takes positions t, t + blockDim, ... of the scene, then a fixed tree), so a scene gets
+// the same sums wherever it sits in a batch and run to run.  A scene below two bodies keeps its
+// axis, as the reference returns before updating it.
+constexpr int kAxisTile = 4096;   // scenes above this size sum scene-relative tiles in separate blocks
+template <class R>
+__global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, int* scene_axis) {
+    const int s = blockIdx.x;
+    const int lo = scene_off[s], hi = scene_off[s + 1];
+    const int cnt = hi - lo;
+    if (cnt < 2 || cnt > kAxisTile) return;   // whole block
+    __shared__ double red[6][kBlock];
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+        for (int d = 0; d < 3; d++) {
+            const double c = (double)((smn[(size_t)d * n + k] + smx[(size_t)d * n + k]) * R(0.5));
+            acc[d] += c;
+            acc[3 + d] += c * c;
+        }
+    }
+    for (int q = 0; q < 6; q++) red[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double v[3];
+        for (int d = 0; d < 3; d++) v[d] = red[3 + d][0] - red[d][0] * red[d][0] / (double)cnt;
+        int ax = 0;
+        if (v[1] > v[0]) ax = 1;
+        if (v[2] > v[ax]) ax = 2;
+        scene_axis[s] = ax;
+    }
+}
+
+// large scenes: block b sums tile item[b].y (positions lo + tile * kAxisTile, ...) of scene
+// item[b].x, in the same fixed order as k_bp_axis; then one thread per large scene adds its tiles
+// in tile order
+template <class R>
+__global__ void k_bp_axis_tiles(const R* smn, const R* smx, int n, const int* scene_off, const int2* item, double* part) {
+    const int s = item[blockIdx.x].x, t = item[blockIdx.x].y;
+    const int lo = scene_off[s] + t * kAxisTile, hi = min(scene_off[s + 1], lo + kAxisTile);
+    __shared__ double red[6][kBlock];
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+        for (int d = 0; d < 3; d++) {
+            const double c = (double)((smn[(size_t)d * n + k] + smx[(size_t)d * n + k]) * R(0.5));
+            acc[d] += c;
+            acc[3 + d] += c * c;
+        }
+    }
+    for (int q = 0; q < 6; q++) red[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) part[(size_t)blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
+}
+__global__ void k_bp_axis_combine(const int* scene_off, const int2* item, int n_item, const double* part, int* scene_axis);
+
+} // namespace pe
