@@ -245,6 +245,16 @@ def run_ours(args, rank, world, device):
         g.step(1, mode)
     for _ in range(args.warmup):
         g.step(1, mode)
+    if args.profile_one_step:
+        # one step between cudaProfilerStart and cudaProfilerStop (ncu --profile-from-start off
+        # captures exactly its launches), then stop: nothing is timed
+        rt = _cudart()
+        g.sync()
+        rt.cudaProfilerStart()
+        g.step(1, mode)
+        g.sync()
+        rt.cudaProfilerStop()
+        return None, scene, bits, offs
     # the state the timed steps start from: the end-to-end loop below replays the same steps
     n_axes = len(offs) - 1 if offs is not None else 1
     snapshot = (g.state(), g.results(), g.axes(n_axes))
@@ -458,6 +468,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scenes", type=int, default=4096, help="scene count of the batched workload")
     ap.add_argument("--no-per-scene", action="store_true", help="skip the one-scene-per-launch comparison")
+    ap.add_argument("--profile-one-step", action="store_true",
+                    help="after the pre-roll and warm-up, run one step inside cudaProfilerStart/Stop and exit (for ncu)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -471,8 +483,6 @@ def main():
                                                                 "the batched workload's reference arm")))
             return 0
         scene, bits, mode, offs, cfg = make_workload(args.workload, args.scenes)
-        if offs is not None:   # independent scenes: the reference steps one World per scene
-            pass
         cfg = dict(cfg, solver="serial (the reference's sequential impulse order)")
         k = max(1, min(args.steps, 8))
         if offs is None:
@@ -509,6 +519,9 @@ def main():
         dist.init_process_group("nccl")
         dist.barrier()
     res, scene, bits, offs = run_ours(args, rank, world, local)
+    if res is None:   # --profile-one-step
+        print(json.dumps(dict(profiled_step=True, workload=args.workload, bodies=scene.n_bodies)))
+        return 0
     dev_ms = res["dev_ms"]
     if dist is not None:
         import torch

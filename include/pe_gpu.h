@@ -209,7 +209,7 @@ int pe_gpu_server_create(const pe_gpu_config* cfg, double dt, double gx, double 
                          double hbm_budget_bytes, pe_gpu_server** out);
 int pe_gpu_server_destroy(pe_gpu_server* s);
 const char* pe_gpu_server_last_error(const pe_gpu_server* s);
-/* copies the scene; *id identifies the request */
+/* copies the scene; *id identifies the request.  n_steps must be at least 1 (PE_GPU_ERR_ARG otherwise). */
 int pe_gpu_server_submit(pe_gpu_server* s, const pe_gpu_scene* scene, int n_steps, long long* id);
 /* retire, admit, one batched step of all live scenes */
 int pe_gpu_server_step(pe_gpu_server* s, int* n_live, int* n_queued);
@@ -231,17 +231,22 @@ int pe_gpu_server_stats(pe_gpu_server* s, double* out10);
  *
  * All temporaries live in one fixed scratch array of about 1.4 MB per device, which limits n to
  * 16384 bodies; a larger n returns PE_GPU_ERR_CAPACITY with a message.  The first call on a device
- * looks the scratch up (cudaGetSymbolAddress, the device current) and caches it; make that first
- * call before any stream capture.  The device's context must already exist.  The scratch is
- * shared: calls on one device whose work overlaps (other streams, other threads) race on it, so
- * serialise them.  Nothing needs to start at zero: the call initialises every scratch value it
- * reads.
+ * looks the scratch up (cudaGetSymbolAddress, the device current) and caches it for the context
+ * that is current; make that first call before any stream capture.  A call in another context of
+ * the device (after cudaDeviceReset, or a context of the caller's own) looks it up again, and that
+ * call, too, must come before any capture.  Without a current context the call makes the device's
+ * primary context current.  The scratch is shared: calls on one device whose work overlaps (other
+ * streams, other threads) race on it, so serialise them.  Nothing needs to start at zero: the call
+ * initialises every scratch value it reads.
  *
  * Device pointers: aabb_min / aabb_max [3 n] floats (x, y, z per body), flags [n] PE_GPU_BODY_*
  * bits or NULL (all dynamic), pairs [2 pair_cap] ints (body indices, lower sweep position first),
- * n_pairs one int.  The work is queued on `stream` (a cudaStream_t, NULL for the default stream);
- * *n_pairs holds the pair count when it completes.  If that count exceeds pair_cap the output is
- * incomplete: call again with a larger buffer.  err (optional) receives a message on failure. */
+ * n_pairs one int.  pairs must be 8-byte aligned (pairs are stored as 8-byte words) and the other
+ * pointers 4-byte aligned; a misaligned pointer returns PE_GPU_ERR_ARG before any device work.
+ * The work is queued on `stream` (a cudaStream_t, NULL for the default stream); *n_pairs holds
+ * the pair count when it completes.  If that count exceeds pair_cap the output is incomplete:
+ * call again with a larger buffer.  The call clears the runtime's last-error state on entry, so a
+ * launch error it reports is its own.  err (optional) receives a message on failure. */
 int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min, const float* aabb_max, const int* flags, int axis,
                              int* pairs, int pair_cap, int* n_pairs, void* stream, char* err, int err_cap);
 

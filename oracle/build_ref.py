@@ -13,7 +13,8 @@ CMakeLists.txt:6-29 (-DPE_MULTI_THREAD, -DAMGCL_NO_BOOST, aligned storage on),
 compiled with g++ -std=c++14 -O2 like the reference's default build.
 
 Run:  python oracle/build_ref.py [--ref /path/to/reference] [--jobs N]
-Only this container has the reference sources; the GPU host never runs this.
+The reference tree is found by ``reference_dir()``: $PE_REFERENCE_DIR, else a directory named
+``reference`` beside this repository.  Where neither holds the sources, nothing is built.
 """
 import argparse
 import concurrent.futures as cf
@@ -25,6 +26,17 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 OBJ = Path(os.environ.get("TMPDIR", "/tmp")) / "pe_ref_obj"   # objects stay outside the repository
+
+
+def reference_dir():
+    """The reference engine's source tree: $PE_REFERENCE_DIR, else ``reference`` beside this
+    repository's root; None when neither holds the engine's sources."""
+    env = os.environ.get("PE_REFERENCE_DIR")
+    cands = ([Path(env)] if env else []) + [HERE.parent.parent / "reference"]
+    for c in cands:
+        if (c / "src" / "intf" / "world.cpp").exists():
+            return c
+    return None
 
 
 def sources(ref: Path):
@@ -88,7 +100,10 @@ def build(ref: Path, jobs: int, bits_list=(64, 32)):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference source tree (default: reference_dir())")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
-    build(Path(a.ref), a.jobs)
+    ref = Path(a.ref) if a.ref else reference_dir()
+    if ref is None:
+        raise SystemExit("reference sources not found: set PE_REFERENCE_DIR or pass --ref")
+    build(ref, a.jobs)

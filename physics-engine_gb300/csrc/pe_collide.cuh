@@ -18,12 +18,12 @@ template <class R> __device__ void ortho_units(V3<R> n, V3<R>& t1, V3<R>& t2) {
     n = normalized(n);
     if (rabs(n.z) > R(0.7071)) {
         const R a = n.y * n.y + n.z * n.z;
-        const R k = R(1.0) / rsqrt_(a);
+        const R k = R(1.0) / real_sqrt(a);
         t1 = V3<R>(0, -n.z * k, n.y * k);
         t2 = V3<R>(a * k, -n.x * t1.z, n.x * t1.y);
     } else {
         const R a = n.x * n.x + n.y * n.y;
-        const R k = R(1.0) / rsqrt_(a);
+        const R k = R(1.0) / real_sqrt(a);
         t1 = V3<R>(-n.y * k, n.x * k, 0);
         t2 = V3<R>(-n.z * t1.y, n.z * t1.x, a * k);
     }
@@ -202,7 +202,7 @@ template <class R> __device__ bool box_box(Pair<R>& c) {   // box_box_collision_
         s2 = rabs(ee) - (e2);                                                             \
         if (s2 > eps<R>()) return false;                                                  \
         const R a1 = (n1), a2 = (n2), a3 = (n3);                                          \
-        l = rsqrt_(a1 * a1 + a2 * a2 + a3 * a3);                                          \
+        l = real_sqrt(a1 * a1 + a2 * a2 + a3 * a3);                                          \
         if (l > eps<R>()) {                                                               \
             s2 /= l;                                                                      \
             if (s2 * fudge > s) {                                                         \
@@ -390,7 +390,7 @@ template <class R> __device__ bool sphere_cylinder(Pair<R>& c) {   // sphere_cyl
     bool ret = false;
     const R s_r = sph.radius, c_r = cyl.radius, c_h = cyl.height * R(0.5);
     const V3<R> s = tc.inv_apply(ts.o);
-    const R r = rsqrt_(s.x * s.x + s.z * s.z);
+    const R r = real_sqrt(s.x * s.x + s.z * s.z);
     const R d = rabs(s.y) - c_h;
     if (!(s.y < -c_h - s_r || s.y > c_h + s_r || r * r > (c_r + s_r) * (c_r + s_r) ||
           (d > 0 && r > c_r && (r - c_r) * (r - c_r) + d * d > s_r * s_r))) {
@@ -439,7 +439,7 @@ template <class R> __device__ void cyl_contact(const V3<R>& p, const V3<R>& pos,
                                                R margin, V3<R>& wn, V3<R>& wp, R& wd) {
     const V3<R> r = p - pos;
     const R dy = dot(r, axis);
-    const R dxz = rsqrt_(sqnorm(r) - dy * dy);
+    const R dxz = real_sqrt(sqnorm(r) - dy * dy);
     const R dside = radius - dxz, dtop = h - rabs(dy);
     V3<R> n;
     R dist;
@@ -501,7 +501,7 @@ template <class R> __device__ bool segment_cylinder(const V3<R>& s, const V3<R>&
     } else {
         R delta = b * b - a * cc;
         if (delta < 0) return false;
-        delta = rsqrt_(delta);
+        delta = real_sqrt(delta);
         tmin = (-b - delta) / a;
         tmax = (-b + delta) / a;
     }
@@ -656,7 +656,7 @@ template <class R> __device__ bool find_sep_axis(Pair<R>& c, V3<R>& sep) {
         V3<R> pts = tr - oa + ob;
         const R nl2 = sqnorm(pts);
         if (nl2 > eps<R>()) {
-            const R nl = rsqrt_(nl2);
+            const R nl = real_sqrt(nl2);
             pts = pts * (R(1.0) / nl);
             if (dot(pts, dc) < 0) pts = pts * R(-1.0);
             c.add(pts, wpb + ob - pts * margin, -nl + margin * 2);
@@ -770,7 +770,7 @@ template <class R> __device__ bool sphere_triangle(const V3<R>& ctr, R radius, c
     bool has = false;
     V3<R> cp;
     if (l2 >= eps<R>() * eps<R>()) {
-        n = n / rsqrt_(l2);
+        n = n / real_sqrt(l2);
         R dfp = dot(ctr - vs[0], n);
         if (dfp < 0) { dfp *= R(-1.); n = n * R(-1.); }
         if (dfp < radius) {
@@ -791,7 +791,7 @@ template <class R> __device__ bool sphere_triangle(const V3<R>& ctr, R radius, c
         const V3<R> cc = ctr - cp;
         const R ds = sqnorm(cc);
         if (ds < radius * radius) {
-            if (ds > eps<R>() * eps<R>()) { rn = normalized(cc); point = cp; depth = -(radius - rsqrt_(ds)); }
+            if (ds > eps<R>() * eps<R>()) { rn = normalized(cc); point = cp; depth = -(radius - real_sqrt(ds)); }
             else { rn = n; point = cp; depth = -radius; }
             return true;
         }

@@ -97,8 +97,8 @@ __device__ __forceinline__ void np_finish(int p, const int2* pairs, const Bodies
     res.a[p] = q.x;
     res.b[p] = q.y;
     res.npts[p] = np;
-    res.fr[p] = rsqrt_(B.at(FRIC, q.x) * B.at(FRIC, q.y));     // ContactResult::setObjects (contact_result.cpp:80-86)
-    res.re[p] = rsqrt_(B.at(REST, q.x) * B.at(REST, q.y));
+    res.fr[p] = real_sqrt(B.at(FRIC, q.x) * B.at(FRIC, q.y));     // ContactResult::setObjects (contact_result.cpp:80-86)
+    res.re[p] = real_sqrt(B.at(REST, q.x) * B.at(REST, q.y));
     for (int k = 0; k < kSlots; k++) res.dist[p * kSlots + k] = cache.dist[perm[k]];
     for (int k = 0; k < np; k++) {
         const int s = perm[k];

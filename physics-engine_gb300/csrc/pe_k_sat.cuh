@@ -87,7 +87,7 @@ __device__ __forceinline__ void shape_interval(const ShapeView<R>& s, const Xf<R
         if (rabs(la.x - 0) < eps<R>() && rabs(la.z - 0) < eps<R>()) { mnp = off - hh; mxp = off + hh; }
         else if (rabs(la.y - 0) < eps<R>()) { mnp = off - s.radius; mxp = off + s.radius; }
         else {
-            const R r = rsqrt_(la.x * la.x + la.z * la.z);
+            const R r = real_sqrt(la.x * la.x + la.z * la.z);
             const R x = s.radius * la.x / r, z = s.radius * la.z / r;
             const R y = hh * (la.y > 0 ? 1 : -1);
             const R el = dot(V3<R>(x, y, z), la);
@@ -527,7 +527,7 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
             V3<R> pts = tr - oa + ob;
             const R nl2 = sqnorm(pts);
             if (nl2 > eps<R>()) {
-                const R nl = rsqrt_(nl2);
+                const R nl = real_sqrt(nl2);
                 pts = pts * (R(1.0) / nl);
                 if (dot(pts, dc) < 0) pts = pts * R(-1.0);
                 out[SO_FLAGS] += R(2);
@@ -641,7 +641,7 @@ __device__ bool sat_warp(Pair<R>& c, int lane) {
             V3<R> pts = tr - oa + ob;
             const R nl2 = sqnorm(pts);
             if (nl2 > eps<R>()) {
-                const R nl = rsqrt_(nl2);
+                const R nl = real_sqrt(nl2);
                 pts = pts * (R(1.0) / nl);
                 if (dot(pts, dc) < 0) pts = pts * R(-1.0);
                 c.add(pts, wpb + ob - pts * margin, -nl + margin * 2);

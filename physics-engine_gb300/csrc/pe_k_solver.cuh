@@ -78,7 +78,7 @@ __device__ __forceinline__ void si_iterate_result(const Bodies<R>& B, const Rows
         nacc += ni;
         R tt0 = t0acc - dot(t0, vr) * rows.at(T0JMJ, r);
         R tt1 = t1acc - dot(t1, vr) * rows.at(T1JMJ, r);
-        const R scale = rows.at(MU, r) * nacc / rsqrt_(tt0 * tt0 + tt1 * tt1);
+        const R scale = rows.at(MU, r) * nacc / real_sqrt(tt0 * tt0 + tt1 * tt1);
         if (scale < 1) { tt0 *= scale; tt1 *= scale; }
         const V3<R> imp = ni * n + (tt0 - t0acc) * t0 + (tt1 - t1acc) * t1;
         rows.at(NACC, r) = nacc;

@@ -37,8 +37,8 @@ template <class R> PE_HD R eps() { return R(0.00001); }
 template <class R> PE_HD R pi() { return R(3.141592653589); }
 template <class R> PE_HD constexpr bool dbl() { return std::is_same<R, double>::value; }
 
-PE_HD float rsqrt_(float x) { return sqrtf(x); }
-PE_HD double rsqrt_(double x) { return sqrt(x); }
+PE_HD float real_sqrt(float x) { return sqrtf(x); }
+PE_HD double real_sqrt(double x) { return sqrt(x); }
 PE_HD float rabs(float x) { return fabsf(x); }
 PE_HD double rabs(double x) { return fabs(x); }
 template <class R> PE_HD R rmin(R a, R b) { return a < b ? a : b; }
@@ -66,10 +66,10 @@ template <class R> PE_HD V3<R> cross(const V3<R>& a, const V3<R>& b) {
 }
 template <class R> PE_HD R dot(const V3<R>& a, const V3<R>& b) { return sum3(a.x * b.x, a.y * b.y, a.z * b.z, dbl<R>()); }
 template <class R> PE_HD R sqnorm(const V3<R>& a) { return dot(a, a); }
-template <class R> PE_HD R norm(const V3<R>& a) { return rsqrt_(sqnorm(a)); }
+template <class R> PE_HD R norm(const V3<R>& a) { return real_sqrt(sqnorm(a)); }
 template <class R> PE_HD V3<R> normalized(const V3<R>& a) {
     const R n = sqnorm(a);
-    return n > R(0) ? a / rsqrt_(n) : a;
+    return n > R(0) ? a / real_sqrt(n) : a;
 }
 
 template <class R> struct M3 {
@@ -150,7 +150,7 @@ template <class R> PE_HD Quat<R> quat_from_basis(const M3<R>& m) {
     Quat<R> q;
     R t = m.m[0][0] + (m.m[1][1] + m.m[2][2]);
     if (t > R(0)) {
-        t = rsqrt_(t + R(1));
+        t = real_sqrt(t + R(1));
         q.w = R(0.5) * t;
         t = R(0.5) / t;
         q.x = (m.m[2][1] - m.m[1][2]) * t;
@@ -161,7 +161,7 @@ template <class R> PE_HD Quat<R> quat_from_basis(const M3<R>& m) {
         if (m.m[1][1] > m.m[0][0]) i = 1;
         if (m.m[2][2] > m.m[i][i]) i = 2;
         const int j = (i + 1) % 3, k = (j + 1) % 3;
-        t = rsqrt_(m.m[i][i] - m.m[j][j] - m.m[k][k] + R(1));
+        t = real_sqrt(m.m[i][i] - m.m[j][j] - m.m[k][k] + R(1));
         R c[3];
         c[i] = R(0.5) * t;
         t = R(0.5) / t;
@@ -192,7 +192,7 @@ template <class R> PE_HD Quat<R> quat_mul(const Quat<R>& a, const Quat<R>& b) {
 template <class R> PE_HD void quat_normalize(Quat<R>& q) {
     const R n2 = (q.x * q.x + q.z * q.z) + (q.y * q.y + q.w * q.w);
     if (n2 > R(0)) {
-        const R n = rsqrt_(n2);
+        const R n = real_sqrt(n2);
         q.x = q.x / n; q.y = q.y / n; q.z = q.z / n; q.w = q.w / n;
     }
 }

@@ -5,8 +5,11 @@
 // broad_phase_base.cpp:5-19) for one scene of at most kSapMaxBodies bodies, but every temporary
 // (sort keys, sorted AABBs, counts, scan totals) lives in one file-scope __device__ array.  The
 // array comes into existence when the CUDA module is loaded into the device's context; its
-// address is looked up once per device with cudaGetSymbolAddress and cached.
+// address is looked up with cudaGetSymbolAddress once per device and context and cached (a
+// cudaDeviceReset gives the device a new primary context, and the address is looked up again).
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -17,7 +20,9 @@ namespace pe {
 namespace {
 
 constexpr int kSapMaxBodies = 16384;
-constexpr int kSapBigBlocks = 64;   // blocks sharing the positions whose sweep window is crowded
+// no window of a scene this small can exceed the world's crowded-window threshold, so the warp
+// sweep alone gives the world's pairs (the block sweeps of crowded windows never have work here)
+static_assert(kSapMaxBodies <= kBigWindow, "crowded-window sweeps would be needed");
 constexpr size_t kAlign = 256;
 constexpr size_t al(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
 constexpr int kSapTiles = (kSapMaxBodies + kRadixTile - 1) / kRadixTile;
@@ -86,7 +91,25 @@ __global__ void k_sap_gather(int n, const float* mn, const float* mx, const int*
 __global__ void k_sap_total(const int* total, int* n_pairs) { *n_pairs = *total; }
 
 std::mutex g_setup_mu;
-void* g_scratch[64] = {};
+struct ScratchSlot {
+    void* ctx = nullptr;   // the context the address belongs to
+    void* ptr = nullptr;
+};
+ScratchSlot g_scratch[64];
+
+// the current context (driver API, reached through the runtime so the library needs no -lcuda)
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+CtxGetCurrent ctx_get_current() {
+    static CtxGetCurrent fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrent>(f);
+    }();
+    return fn;
+}
 
 void set_err(char* err, int cap, const char* msg) {
     if (err && cap > 0) {
@@ -107,6 +130,13 @@ extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min
         set_err(err, err_cap, "pe_gpu_sap_pairs_noalloc: bad argument");
         return PE_GPU_ERR_ARG;
     }
+    // the kernels store pairs as 8-byte (int2) words and read 4-byte words everywhere else
+    auto misaligned = [](const void* q, uintptr_t a) { return q && (reinterpret_cast<uintptr_t>(q) % a) != 0; };
+    if (misaligned(pairs, 8) || misaligned(aabb_min, 4) || misaligned(aabb_max, 4) || misaligned(flags, 4) ||
+        misaligned(n_pairs, 4)) {
+        set_err(err, err_cap, "pe_gpu_sap_pairs_noalloc: misaligned pointer (pairs needs 8 bytes, the others 4)");
+        return PE_GPU_ERR_ARG;
+    }
     if (n > kSapMaxBodies) {
         std::snprintf(msg, sizeof msg, "pe_gpu_sap_pairs_noalloc: %d bodies exceed the fixed scratch limit of %d", n, kSapMaxBodies);
         set_err(err, err_cap, msg);
@@ -115,29 +145,43 @@ extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min
     int prev = -1;
     if (cudaGetDevice(&prev) != cudaSuccess) { set_err(err, err_cap, "cudaGetDevice failed"); return PE_GPU_ERR_CUDA; }
     if (prev != device && cudaSetDevice(device) != cudaSuccess) { set_err(err, err_cap, "cudaSetDevice failed"); return PE_GPU_ERR_CUDA; }
-    auto done = [&](int rc, const char* what) {
+    auto done = [&](int rc, const char* what, cudaError_t e) {
         if (what) {
-            std::snprintf(msg, sizeof msg, "pe_gpu_sap_pairs_noalloc: %s: %s", what, cudaGetErrorString(cudaGetLastError()));
+            std::snprintf(msg, sizeof msg, "pe_gpu_sap_pairs_noalloc: %s: %s", what, cudaGetErrorString(e));
             set_err(err, err_cap, msg);
         }
         if (prev != device) cudaSetDevice(prev);
         return rc;
     };
-    // set-up, once per device, with that device current
+    // an error left by earlier, unrelated work would otherwise be reported as this call's
+    cudaGetLastError();
+    // set-up, once per device and context, with that device current
     unsigned char* base;
     {
         std::lock_guard<std::mutex> lk(g_setup_mu);
-        if (!g_scratch[device]) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_sap_scratch) != cudaSuccess || !p) return done(PE_GPU_ERR_CUDA, "cudaGetSymbolAddress");
-            g_scratch[device] = p;
+        CUcontext ctx = nullptr;
+        CtxGetCurrent get = ctx_get_current();
+        if (get && get(&ctx) == CUDA_SUCCESS && !ctx) {   // no context current yet: the device's primary context
+            const cudaError_t e = cudaSetDevice(device);
+            if (e != cudaSuccess) return done(PE_GPU_ERR_CUDA, "cudaSetDevice", e);
+            get(&ctx);
         }
-        base = static_cast<unsigned char*>(g_scratch[device]);
+        if (!get || !ctx) return done(PE_GPU_ERR_CUDA, "no current context", cudaErrorDeviceUninitialized);
+        ScratchSlot& slot = g_scratch[device];
+        if (!slot.ptr || slot.ctx != static_cast<void*>(ctx)) {
+            void* p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_sap_scratch);
+            if (e != cudaSuccess || !p) return done(PE_GPU_ERR_CUDA, "cudaGetSymbolAddress", e);
+            slot.ptr = p;
+            slot.ctx = static_cast<void*>(ctx);
+        }
+        base = static_cast<unsigned char*>(slot.ptr);
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (n < 2) {   // no pair (the world's broadphase returns before sorting below two bodies)
-        if (cudaMemsetAsync(n_pairs, 0, sizeof(int), st) != cudaSuccess) return done(PE_GPU_ERR_CUDA, "cudaMemsetAsync");
-        return done(PE_GPU_OK, nullptr);
+        const cudaError_t e = cudaMemsetAsync(n_pairs, 0, sizeof(int), st);
+        if (e != cudaSuccess) return done(PE_GPU_ERR_CUDA, "cudaMemsetAsync", e);
+        return done(PE_GPU_OK, nullptr, cudaSuccess);
     }
     uint64_t* key[2] = {reinterpret_cast<uint64_t*>(base + kL.key[0]), reinterpret_cast<uint64_t*>(base + kL.key[1])};
     uint32_t* key2[2] = {reinterpret_cast<uint32_t*>(base + kL.key2[0]), reinterpret_cast<uint32_t*>(base + kL.key2[1])};
@@ -176,16 +220,14 @@ extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min
     const int gw = (int)(((size_t)n * 32 + kBlock - 1) / kBlock);
     const IgnoreLists no_lists;   // this entry point takes no ignored-pair lists
     k_bp_count<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, stage, big, n_big, no_lists);
-    k_bp_count_big<float><<<kSapBigBlocks, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, count, big, n_big, no_lists);
     const int ct = (n + 1 + 1023) / 1024;
     k_scan_tiles<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
     k_scan_aux<<<1, kBlock, 0, st>>>(aux, ct, total);
     k_scan_add<<<ct, kBlock, 0, st>>>(count, n + 1, aux);
     k_bp_write<float><<<gw, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, order, count, stage, reinterpret_cast<int2*>(pairs),
                                              pair_cap, status, no_lists);
-    k_bp_write_big<float><<<kSapBigBlocks, kBlock, 0, st>>>(n, scene_axis, smn, smx, sflag, sscene, order, count,
-                                                          reinterpret_cast<int2*>(pairs), pair_cap, status, big, n_big, no_lists);
     k_sap_total<<<1, 1, 0, st>>>(total, n_pairs);
-    if (cudaGetLastError() != cudaSuccess) return done(PE_GPU_ERR_CUDA, "kernel launch");
-    return done(PE_GPU_OK, nullptr);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return done(PE_GPU_ERR_CUDA, "kernel launch", e);
+    return done(PE_GPU_OK, nullptr, cudaSuccess);
 }

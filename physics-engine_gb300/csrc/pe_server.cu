@@ -210,7 +210,9 @@ const char* pe_gpu_server_last_error(const pe_gpu_server* h) { return h ? h->err
 
 int pe_gpu_server_submit(pe_gpu_server* h, const pe_gpu_scene* sc, int n_steps, long long* id) {
     return sguard(h, [&](pe::Server& s) {
-        if (!sc || !id || n_steps < 0 || sc->n_shapes < 0 || sc->n_bodies < 0) return PE_GPU_ERR_ARG;
+        // a request steps its scene at least once: a zero-step request would still be advanced by
+        // the batched step that admits it
+        if (!sc || !id || n_steps < 1 || sc->n_shapes < 0 || sc->n_bodies < 0) return PE_GPU_ERR_ARG;
         pe::SceneData d;
         const int S = sc->n_shapes, N = sc->n_bodies;
         d.shape_type.assign(sc->shape_type, sc->shape_type + S);

@@ -167,9 +167,9 @@ template <class R> __device__ void shape_aabb(const ShapeView<R>& s, const Xf<R>
     if (s.type == ST_CYLINDER) {
         const V3<R> a = t.b.col(1);
         V3<R> e = V3<R>(rabs(a.x), rabs(a.y), rabs(a.z)) * (s.height * R(0.5));
-        e.y += s.radius * rsqrt_(a.x * a.x + a.z * a.z);
-        e.x += s.radius * rsqrt_(a.y * a.y + a.z * a.z);
-        e.z += s.radius * rsqrt_(a.x * a.x + a.y * a.y);
+        e.y += s.radius * real_sqrt(a.x * a.x + a.z * a.z);
+        e.x += s.radius * real_sqrt(a.y * a.y + a.z * a.z);
+        e.z += s.radius * real_sqrt(a.x * a.x + a.y * a.y);
         mn = t.o - e; mx = t.o + e;
         return;
     }
@@ -244,7 +244,7 @@ template <class R> __device__ void shape_project(const ShapeView<R>& s, const Xf
             mnpt = t.apply(-r); mxpt = t.apply(r);
             mnp = off - s.radius; mxp = off + s.radius;
         } else {
-            const R r = rsqrt_(la.x * la.x + la.z * la.z);
+            const R r = real_sqrt(la.x * la.x + la.z * la.z);
             const R x = s.radius * la.x / r, z = s.radius * la.z / r;
             const R y = hh * (la.y > 0 ? 1 : -1);
             const V3<R> ext(x, y, z);

@@ -59,7 +59,10 @@ for bits in (64, 32):
                                   bits, 120, [0, 1, 2, 30, 31, 45, 60, 61, 90, 91, 118, 119])
 # the reference's own sample scene (a bomb sphere at 70 m/s into a 15-box tower on a kinematic
 # ground), read by the scene-file loader; the sphere reaches the tower near step 57
-SAMPLES = Path("/root/reference/SampleScenes")
+REF = build_ref.reference_dir()
+if REF is None:
+    raise SystemExit("reference sources not found: set PE_REFERENCE_DIR")
+SAMPLES = REF / "SampleScenes"
 for bits in (64, 32):
     CASES[f"json_bomb_tower_smaller_f{bits}"] = (
         lambda bits=bits: load_scene_json(SAMPLES / "bomb_crash_tower_smaller.json", real_bits=bits)[0], bits, 120,
@@ -70,7 +73,7 @@ for bits in (64, 32):
 def obj_scene(bits):
     import json
     import tempfile
-    ref = Path("/root/reference/test")
+    ref = REF / "test"
     bodies = [{"type": "box", "kinematic": True, "position": [0, -0.5, 0], "scale": [40, 1, 40]},
               {"type": "concave", "kinematic": True, "mesh": str(ref / "utils/bvh/vase.obj"), "scale": [8, 8, 8],
                "position": [0, 4.2, 0]}]
@@ -126,7 +129,7 @@ def make(name, ref_dir):
 
 
 if __name__ == "__main__":
-    build_ref.build(Path("/root/reference"), 8)
+    build_ref.build(REF, 8)
     names = sys.argv[1:] or sorted(CASES)
     for name in names:
         p, c = make(name, build_ref.OUT)

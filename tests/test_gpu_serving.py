@@ -81,3 +81,17 @@ def test_serving_admission_by_budget():
     small = pg.Server(real_bits=32, hbm_budget_bytes=1e5)
     rid = small.submit(scenes[0], 5)
     assert small.result(rid)[0] == pg.REJECTED
+
+
+def test_serving_rejects_requests_without_steps():
+    scene = _scenes(1, seed=8, size_range=(20, 30))[0]
+    srv = pg.Server(real_bits=32)
+    for k in (0, -3):
+        with pytest.raises(pg.PeGpuError):
+            srv.submit(scene, k)
+    live, queued = srv.step()
+    assert (live, queued) == (0, 0)
+    rid = srv.submit(scene, 1)
+    srv.step()
+    srv.step()
+    assert srv.result(rid)[0] == pg.DONE

@@ -8,11 +8,13 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+import build_ref
 import orc
 from pe_gb300 import scene as sc
 from pe_gb300.scene_json import UnsupportedScene, load_scene_json
 
-SAMPLES = Path("/root/reference/SampleScenes")
+_REF = build_ref.reference_dir()
+SAMPLES = (_REF / "SampleScenes") if _REF is not None else Path("reference-sample-scenes-not-present")
 
 
 def write(tmp_path, doc):
