@@ -57,8 +57,8 @@ def make_workload(name, n_scenes=4096):
     if name == "tower":
         s = sc.tower(real_bits=64)
         return s, 64, 0, None, dict(workload="1,000-box 10x10x10 tower + ground + sphere at 30 m/s, full step, FP64, "
-                                             "20 SI iterations, serial-order solver", bodies=s.n_bodies, scenes=1,
-                                    solver="serial-order")
+                                             "20 SI iterations, contact margin 0.005, serial-order solver",
+                                    bodies=s.n_bodies, scenes=1, solver="serial-order", margin=0.005)
     if name == "batched":
         s, offs = sc.batched_piles(n_scenes=n_scenes, seed=4096, real_bits=32)
         return s, 32, 1, offs, dict(workload=f"{n_scenes:,} independent piles of 8..512 bodies (log-uniform; box/sphere/cylinder/"
@@ -238,7 +238,7 @@ KERNEL_GROUPS = {"integrate": ("integrate",), "bp_sort": ("radix_sort",), "bp_sw
 def run_ours(args, rank, world, device):
     import pe_gb300 as pg
     scene, bits, mode, offs, cfg = make_workload(args.workload, args.scenes)
-    g = pg.GpuWorld(scene, bits, device=device, scenes=offs)
+    g = pg.GpuWorld(scene, bits, device=device, scenes=offs, margin=cfg.get("margin", 0.0))
     flush = L2Flush()
     N = scene.n_bodies
     for _ in range(cfg.get("preroll_steps", 0)):   # untimed settling (part of the workload definition)
@@ -426,7 +426,7 @@ def run_serving(args, device):
                 gpu_launches=None, clocks=clk.summary())
 
 
-def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, steps=5):
+def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, steps=5, margin=0.0):
     """The reference's CPU step (its algorithm restated in oracle/) on a bounded sample, all host
     threads.  One scene: the reference's thread pool inside one world.  Independent scenes: one
     scene per host thread (a spawn process pool), a spread sample of the batch."""
@@ -434,7 +434,7 @@ def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, st
     import orc
     threads = os.cpu_count() or 1
     if offs is None:
-        w = orc.OracleWorld(scene, bits, threads=threads)
+        w = orc.OracleWorld(scene, bits, threads=threads, margin=margin)
         t = w.time_steps(1)
         n = 1
         while t < budget_s and n < 64:
@@ -489,7 +489,7 @@ def main():
             sys.path.insert(0, str(ROOT / "oracle"))
             import orc
             threads = os.cpu_count() or 1
-            w = orc.OracleWorld(scene, bits, threads=threads)
+            w = orc.OracleWorld(scene, bits, threads=threads, margin=cfg.get("margin", 0.0))
             for _ in range(args.warmup):   # untimed, like the GPU arm's warm-up
                 w.time_steps(1)
             t = w.time_steps(k)
@@ -545,7 +545,8 @@ def main():
                dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg, roofline=res["roofline"],
                e2e=res["e2e"], gpu_launches=res["launches"], clocks=res["clk"], kernels_ms_one_step=res["kernels"])
     if not args.no_cpu_baseline and world == 1:
-        out["cpu_baseline"] = cpu_baseline(scene, bits, offs, preroll=res["cfg"].get("preroll_steps", 0))
+        out["cpu_baseline"] = cpu_baseline(scene, bits, offs, preroll=res["cfg"].get("preroll_steps", 0),
+                                           margin=res["cfg"].get("margin", 0.0))
     print(json.dumps(out))
     return 0
 

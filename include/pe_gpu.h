@@ -120,6 +120,12 @@ int pe_gpu_set_scenes(pe_gpu_world* w, int n_scenes, const int* body_off);
 /* World::setDt / setGravity (world.h:24-25) and ConstraintSolver::setIteration (constraint_solver.h:72). */
 int pe_gpu_set_params(pe_gpu_world* w, double dt, double gx, double gy, double gz, int iterations);
 
+/* Contact margin of every pair algorithm: the reference's compile-time PE_MARGIN
+ * (src/rigid/phys_general.h:45, pe::Real(0) in its build), read into each algorithm's `margin`
+ * (e.g. convex_convex_collision_algorithm.cpp:23, its clipping window [-refScale, margin] at
+ * :426-429).  Default 0; a margin >= 0 reproduces the reference compiled with that PE_MARGIN. */
+int pe_gpu_set_contact_margin(pe_gpu_world* w, double margin);
+
 /* World::step (world.cpp:267-300): n_steps full steps on the device without host round trips
  * of body state. */
 int pe_gpu_step(pe_gpu_world* w, int n_steps, int solver_mode);

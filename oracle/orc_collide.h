@@ -116,6 +116,7 @@ template <class R> struct PairCtx {
     const Transform<R>* tb;
     BodyView<R> A, B;
     R ref_scale;
+    R margin = 0;   // PE_MARGIN (phys_general.h:45): 0 in the reference's build
     CResult<R>* res;
     void add(const V3<R>& n, const V3<R>& p, R d) { res->add(A, B, n, p, d); }
 };
@@ -207,7 +208,7 @@ template <class R> void cull_points(int n, const R p[], int m, int i0, int iret[
 
 // box_box_collision_algorithm.cpp:137-580
 template <class R> bool box_box(PairCtx<R>& c) {
-    const R margin = 0;
+    const R margin = c.margin;
     const R fudge = R(1.05);
     const V3<R>& p1 = c.ta->origin;
     const V3<R>& p2 = c.tb->origin;
@@ -413,7 +414,7 @@ template <class R> bool box_sphere(PairCtx<R>& c) {
     const Transform<R>& tbox = a_is_box ? *c.ta : *c.tb;
     const V3<R> center = tsph.origin;
     const R radius = sph->radius;
-    const R margin = 0;
+    const R margin = c.margin;
     c.res->swap = a_is_box;
     bool ret = false;
     {
@@ -443,7 +444,7 @@ template <class R> bool box_sphere(PairCtx<R>& c) {
 
 // sphere_sphere_collision_algorithm.cpp:23-37
 template <class R> bool sphere_sphere(PairCtx<R>& c) {
-    const R ra = c.sa->radius, rb = c.sb->radius, margin = 0;
+    const R ra = c.sa->radius, rb = c.sb->radius, margin = c.margin;
     const V3<R> rel = c.ta->origin - c.tb->origin;
     const R dist = norm(rel);
     if (dist > ra + rb || std::abs(dist - 0) < kEps<R>()) return false;
@@ -461,7 +462,7 @@ template <class R> bool sphere_cylinder(PairCtx<R>& c) {
     const Shape<R>* cyl = a_is_sph ? c.sb : c.sa;
     const Transform<R>& tsph = a_is_sph ? *c.ta : *c.tb;
     const Transform<R>& tcyl = a_is_sph ? *c.tb : *c.ta;
-    const R margin = 0;
+    const R margin = c.margin;
     c.res->swap = a_is_sph;
     bool ret = [&]() {
         const R s_r = sph->radius, c_r = cyl->radius, c_h = cyl->height * R(0.5);
@@ -612,7 +613,7 @@ template <class R> bool box_cylinder(PairCtx<R>& c) {
     const Shape<R>* cyl = a_is_box ? c.sb : c.sa;
     const Transform<R>& tbox = a_is_box ? *c.ta : *c.tb;
     const Transform<R>& tcyl = a_is_box ? *c.tb : *c.ta;
-    const R cyl_r = cyl->radius, cyl_h = cyl->height / R(2.0), margin = 0;
+    const R cyl_r = cyl->radius, cyl_h = cyl->height / R(2.0), margin = c.margin;
     const V3<R> he = box->size / R(2.0);
     c.res->swap = a_is_box;
     const Transform<R> rel = tbox.inverse() * tcyl;
@@ -729,7 +730,7 @@ template <class R> void seg_closest(V3<R>& pts, V3<R>& oa, V3<R>& ob, R& ta, R& 
 
 // :251-402
 template <class R> bool find_sep_axis(PairCtx<R>& c, V3<R>& sep) {
-    const R margin = 0;
+    const R margin = c.margin;
     const Shape<R>& A = *c.sa;
     const Shape<R>& B = *c.sb;
     const V3<R> dc = c.ta->origin - c.tb->origin;
@@ -798,7 +799,7 @@ template <class R> bool find_sep_axis(PairCtx<R>& c, V3<R>& sep) {
 
 // :63-170
 template <class R> void clip_hull_hull(PairCtx<R>& c, const V3<R>& sep, R min_dist, R max_dist) {
-    const R margin = 0;
+    const R margin = c.margin;
     const Shape<R>& A = *c.sa;
     const Shape<R>& B = *c.sb;
     int fb = -1;
@@ -850,7 +851,7 @@ template <class R> void clip_hull_hull(PairCtx<R>& c, const V3<R>& sep, R min_di
 template <class R> bool convex_convex(PairCtx<R>& c) {
     V3<R> sep;
     if (!find_sep_axis(c, sep)) return false;
-    clip_hull_hull(c, sep, -c.ref_scale, R(0));
+    clip_hull_hull(c, sep, -c.ref_scale, c.margin);   // :426-429: window [-refScale, margin]
     return true;
 }
 
@@ -926,7 +927,7 @@ template <class R> bool sphere_hull(PairCtx<R>& c) {   // also the concave mesh 
     const Shape<R>& sph = a_is_hull ? *c.sb : *c.sa;
     const Transform<R>& tm = a_is_hull ? *c.ta : *c.tb;
     const Transform<R>& ts = a_is_hull ? *c.tb : *c.ta;
-    const R margin = 0;
+    const R margin = c.margin;
     c.res->swap = a_is_hull;
     const V3<R> rel = tm.inv_apply(ts.origin);
     const R r = sph.radius;
@@ -996,7 +997,7 @@ template <class R> bool cylinder_hull(PairCtx<R>& c) {   // also the concave mes
     const Shape<R>& cyl = a_is_hull ? *c.sb : *c.sa;
     const Transform<R>& to = a_is_hull ? *c.ta : *c.tb;
     const Transform<R>& tc = a_is_hull ? *c.tb : *c.ta;
-    const R margin = 0;
+    const R margin = c.margin;
     c.res->swap = a_is_hull;
     const R cr = cyl.radius, ch = cyl.height / R(2.0);
     const Transform<R> rel = to.inverse() * tc;

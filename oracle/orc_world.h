@@ -105,6 +105,7 @@ public:
     V3<R> gravity = V3<R>(0, R(-9.8), 0);
     int iterations = 10;
     int axis = 0;                           // BroadPhaseSweepAndPrune::_target_axis
+    R margin = 0;                           // contact margin, PE_MARGIN (phys_general.h:45)
     std::vector<std::pair<int, int>> pairs;
     std::vector<CResult<R>> results;        // pooled: slots survive between steps (stale distances)
     std::vector<std::vector<Row<R>>> rows;
@@ -226,6 +227,7 @@ public:
             c.A = {&A.t, aabb_scale(A)};
             c.B = {&B.t, aabb_scale(B)};
             c.ref_scale = (c.A.aabb_scale + c.B.aabb_scale) * R(0.05);
+            c.margin = margin;
             c.res = &r;
             collide(c);
             r.sort();

@@ -10,6 +10,8 @@
 //
 // Usage: ref_harness <scene.pescene> <out.pedump> <steps> <threads> [dump_step ...]
 //        (no dump steps = dump every step; "-1" = dump none, time only)
+// With PE_TRAJ_OUT set, the body states after every step (origin 3, basis 9 row-major, linear
+// and angular velocity 3 + 3, as doubles, bodies in scene order) are also appended to that file.
 
 #include "intf/world.h"
 #include "rigid/shape/box_shape.h"
@@ -348,6 +350,7 @@ int main(int argc, char** argv) {
         fwrite(&real_bytes, sizeof(int), 1, g_dump.f);
     }
 
+    FILE* traj = getenv("PE_TRAJ_OUT") ? fopen(getenv("PE_TRAJ_OUT"), "wb") : nullptr;
     double total_s = 0;
     for (int k = 0; k < steps; k++) {
         g_dump.step = k;
@@ -357,7 +360,19 @@ int main(int argc, char** argv) {
         auto t1 = std::chrono::steady_clock::now();
         total_s += std::chrono::duration<double>(t1 - t0).count();
         if (g_dump.active) g_dump.write_step(world->getRigidBodies());
+        if (traj) {
+            std::vector<double> row(18);
+            for (auto* rb : rbs) {
+                const pe::Transform& t = rb->getTransform();
+                for (int d = 0; d < 3; d++) row[d] = (double)t.getOrigin()[d];
+                for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) row[3 + r * 3 + c] = (double)t.getBasis()(r, c);
+                for (int d = 0; d < 3; d++) row[12 + d] = (double)rb->getLinearVelocity()[d];
+                for (int d = 0; d < 3; d++) row[15 + d] = (double)rb->getAngularVelocity()[d];
+                fwrite(row.data(), sizeof(double), 18, traj);
+            }
+        }
     }
+    if (traj) fclose(traj);
     printf("{\"steps\": %d, \"bodies\": %d, \"threads\": %d, \"seconds\": %.6f, "
            "\"update_s\": %.6f, \"bp_s\": %.6f, \"np_s\": %.6f, \"solver_s\": %.6f, \"real_bytes\": %d}\n",
            steps, s.n_bodies, threads, total_s, (double)world->update_status_time, (double)world->broad_phase_time,

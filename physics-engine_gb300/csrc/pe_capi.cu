@@ -101,6 +101,11 @@ int pe_gpu_set_params(pe_gpu_world* h, double dt, double gx, double gy, double g
     return guard(h, [&](pe::WorldBase& w) { w.set_params(dt, gx, gy, gz, iterations); return PE_GPU_OK; });
 }
 
+int pe_gpu_set_contact_margin(pe_gpu_world* h, double margin) {
+    if (!(margin >= 0) || !(margin < 1e30)) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) { w.set_margin(margin); return PE_GPU_OK; });
+}
+
 int pe_gpu_step(pe_gpu_world* h, int n_steps, int mode) {
     if (n_steps < 0 || (mode != PE_GPU_SOLVER_SERIAL_ORDER && mode != PE_GPU_SOLVER_COLORED)) return PE_GPU_ERR_ARG;
     return guard(h, [&](pe::WorldBase& w) { w.step(n_steps, mode); return PE_GPU_OK; });

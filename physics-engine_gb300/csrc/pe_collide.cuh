@@ -4,8 +4,9 @@
 // Semantics follow the reference exactly (src/rigid/collision/narrow_phase/contact_result.cpp,
 // src/rigid/collision/collision_algorithm/*.cpp), including its quirks: the slot that a new
 // point replaces, the stale distances carried by invalid slots of a pooled result, the
-// "+y face uses half_extent.x" branch of box-sphere, the box-box edge-edge axis pair, the
-// hull projection that never lets a new minimum become the maximum, and margin 0.
+// "+y face uses half_extent.x" branch of box-sphere, the box-box edge-edge axis pair and the
+// hull projection that never lets a new minimum become the maximum.  The contact margin is the
+// world's (PE_MARGIN = 0 in the reference's build, phys_general.h:45).
 #pragma once
 #include "pe_shapes.cuh"
 
@@ -79,6 +80,7 @@ template <class R> struct Pair {
     ShapeView<R> sa, sb;
     Xf<R> xa, xb;
     R ref_scale;
+    R margin;       // the world's contact margin (ShapeTable::margin)
     Cache<R>* c;
     __device__ void add(const V3<R>& n, const V3<R>& p, R d) { c->add(n, p, d); }
     __device__ const Xf<R>& ta() const { return xa; }
@@ -166,7 +168,7 @@ template <class R> __device__ void cull_points(int n, const R p[], int m, int i0
 }
 
 template <class R> __device__ bool box_box(Pair<R>& c) {   // box_box_collision_algorithm.cpp:137-580
-    const R margin = 0, fudge = R(1.05);
+    const R margin = c.margin, fudge = R(1.05);
     const V3<R> p1 = c.ta().o, p2 = c.tb().o;
     const M3<R>& R1 = c.ta().b;
     const M3<R>& R2 = c.tb().b;
@@ -332,7 +334,7 @@ template <class R> __device__ bool box_sphere(Pair<R>& c) {   // box_sphere_coll
     const ShapeView<R>& box = a_box ? c.sa : c.sb;
     const Xf<R>& ts = a_box ? c.tb() : c.ta();
     const Xf<R>& tbx = a_box ? c.ta() : c.tb();
-    const R radius = sph.radius, margin = 0;
+    const R radius = sph.radius, margin = c.margin;
     c.c->swap = a_box;
     bool ret = false;
     const V3<R> he = box.size / R(2.0);
@@ -369,7 +371,7 @@ template <class R> __device__ bool box_sphere(Pair<R>& c) {   // box_sphere_coll
 }
 
 template <class R> __device__ bool sphere_sphere(Pair<R>& c) {   // sphere_sphere_collision_algorithm.cpp:23-37
-    const R ra = c.sa.radius, rb = c.sb.radius, margin = 0;
+    const R ra = c.sa.radius, rb = c.sb.radius, margin = c.margin;
     const V3<R> rel = c.ta().o - c.tb().o;
     const R dist = norm(rel);
     if (dist > ra + rb || rabs(dist - 0) < eps<R>()) return false;
@@ -385,7 +387,7 @@ template <class R> __device__ bool sphere_cylinder(Pair<R>& c) {   // sphere_cyl
     const ShapeView<R>& cyl = a_sph ? c.sb : c.sa;
     const Xf<R>& ts = a_sph ? c.ta() : c.tb();
     const Xf<R>& tc = a_sph ? c.tb() : c.ta();
-    const R margin = 0;
+    const R margin = c.margin;
     c.c->swap = a_sph;
     bool ret = false;
     const R s_r = sph.radius, c_r = cyl.radius, c_h = cyl.height * R(0.5);
@@ -529,7 +531,7 @@ template <class R> __device__ bool box_cylinder(Pair<R>& c) {   // box_cylinder_
     const ShapeView<R>& cyl = a_box ? c.sb : c.sa;
     const Xf<R>& tbx = a_box ? c.ta() : c.tb();
     const Xf<R>& tcy = a_box ? c.tb() : c.ta();
-    const R cr = cyl.radius, ch = cyl.height / R(2.0), margin = 0;
+    const R cr = cyl.radius, ch = cyl.height / R(2.0), margin = c.margin;
     const V3<R> he = box.size / R(2.0);
     c.c->swap = a_box;
     const Xf<R> rel = tbx.inverse() * tcy;
@@ -600,7 +602,7 @@ template <class R> __device__ bool on_line(const V3<R>& v0, const V3<R>& v1, con
 
 // findSeparatingAxis (:251-402), one thread
 template <class R> __device__ bool find_sep_axis(Pair<R>& c, V3<R>& sep) {
-    const R margin = 0;
+    const R margin = c.margin;
     const V3<R> dc = c.ta().o - c.tb().o;
     R dmin = Lim<R>::max();
     V3<R> dpt;
@@ -671,7 +673,7 @@ constexpr int kMaxClip = 64;   // clipped polygon capacity (incident face vertic
 // clipFaceAgainstHull (:63-131): the incident face fb of B clipped against the side planes of
 // the reference face fa of A; points whose depth under fa lies in [min_dist, max_dist] are kept
 template <class R> __device__ void clip_faces(Pair<R>& c, const V3<R>& sep, R min_dist, R max_dist, int fb, int fa) {
-    const R margin = 0;
+    const R margin = c.margin;
     V3<R> buf[2][kMaxClip];
     int n_in = 0;
     const int nbv = c.sb.face_size(fb);
@@ -746,7 +748,7 @@ template <class R> __device__ void clip_hull_hull(Pair<R>& c, const V3<R>& sep, 
 template <class R> __device__ bool convex_convex(Pair<R>& c) {   // :408-432
     V3<R> sep;
     if (!find_sep_axis(c, sep)) return false;
-    clip_hull_hull(c, sep, -c.ref_scale, R(0));
+    clip_hull_hull(c, sep, -c.ref_scale, c.margin);   // window [-refScale, margin] (:426-429)
     return true;
 }
 
@@ -835,7 +837,7 @@ template <class R> __device__ bool sphere_hull(Pair<R>& c) {   // sphere_convex_
     const ShapeView<R>& sp = a_hull ? c.sb : c.sa;
     const Xf<R>& tm = a_hull ? c.ta() : c.tb();
     const Xf<R>& ts = a_hull ? c.tb() : c.ta();
-    const R margin = 0;
+    const R margin = c.margin;
     c.c->swap = a_hull;
     const V3<R> rel = tm.inv_apply(ts.o);
     const R r = sp.radius;
@@ -899,7 +901,7 @@ template <class R> __device__ bool cylinder_hull(Pair<R>& c) {   // cylinder_con
     const ShapeView<R>& cy = a_hull ? c.sb : c.sa;
     const Xf<R>& to = a_hull ? c.ta() : c.tb();
     const Xf<R>& tc = a_hull ? c.tb() : c.ta();
-    const R margin = 0;
+    const R margin = c.margin;
     c.c->swap = a_hull;
     const R cr = cy.radius, ch = cy.height / R(2.0);
     const Xf<R> rel = to.inverse() * tc;

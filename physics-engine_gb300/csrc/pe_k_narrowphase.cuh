@@ -60,6 +60,7 @@ __device__ __forceinline__ void np_setup(int p, const int2* pairs, const Bodies<
     pr.sa = S.view(B.shape[ia]);
     pr.sb = S.view(B.shape[ib]);
     pr.ref_scale = (scale_a + scale_b) * R(0.05);
+    pr.margin = S.margin;
     pr.c = &cache;
     if (!load_cache) return;
     cache.valid = 0;

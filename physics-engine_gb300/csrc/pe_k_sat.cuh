@@ -335,7 +335,7 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
     if (tid == 0) out[SO_FLAGS] = R(0);
     if (TA >= 0) c.sa.type = TA;   // shape types known at compile time: the other branches fold away
     if (TB >= 0) c.sb.type = TB;
-    const R margin = 0;
+    const R margin = c.margin;
     SatStage<R> st;
     st.bind(smem);
     R* rd = smem + sat_stage_reals<R>();
@@ -563,7 +563,7 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
 
 template <class R>
 __device__ bool sat_warp(Pair<R>& c, int lane) {
-    const R margin = 0;
+    const R margin = c.margin;
     const V3<R> dc = c.ta().o - c.tb().o;
     const int fa = c.sa.face_count(), fb = c.sb.face_count();
     // face axes of A, then of B
@@ -664,7 +664,7 @@ __device__ bool sat_warp(Pair<R>& c, int lane) {
         if (d < dmn) { dmn = d; fabest = f; }
     }
     warp_argmin(dmn, fabest);
-    if (lane == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) clip_faces(c, sep, -c.ref_scale, R(0), fbest, fabest);
+    if (lane == 0 && fbest < 0x7fffffff && fabest < 0x7fffffff) clip_faces(c, sep, -c.ref_scale, c.margin, fbest, fabest);
     return true;
 }
 
@@ -690,6 +690,7 @@ k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, Shape
     pr.xb = B.xf(q.y);
     pr.sa = S.view(B.shape[q.x]);
     pr.sb = S.view(B.shape[q.y]);
+    pr.margin = S.margin;
     pr.c = nullptr;
     sat_staged<R, G, TA, TB>(pr, tid, reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G),
                              sat_out + (size_t)t * kSatOut);
@@ -711,7 +712,7 @@ __global__ void k_np_sat_finish(int lo, int hi, const int* order, const int2* pa
     const int fl = (int)o[SO_FLAGS];
     if (fl & 1) pr.add(so_get3(o, SO_FN), so_get3(o, SO_FP), o[SO_FD]);
     if (fl & 2) pr.add(so_get3(o, SO_EN), so_get3(o, SO_EP), o[SO_ED]);
-    if (fl & 4) clip_faces(pr, so_get3(o, SO_SEP), -pr.ref_scale, R(0), (int)o[SO_FB], (int)o[SO_FA]);
+    if (fl & 4) clip_faces(pr, so_get3(o, SO_SEP), -pr.ref_scale, pr.margin, (int)o[SO_FB], (int)o[SO_FA]);
     np_finish(p, pairs, B, res, cache);
 }
 
@@ -741,7 +742,7 @@ k_np_cyl_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, 
     const ShapeView<R>& cy = a_hull ? c.sb : c.sa;
     const Xf<R>& to = a_hull ? c.ta() : c.tb();
     const Xf<R>& tc = a_hull ? c.tb() : c.ta();
-    const R margin = 0;
+    const R margin = c.margin;
     if (lane == 0) cache.swap = a_hull;
     const R cr = cy.radius, ch = cy.height / R(2.0);
     const Xf<R> rel = to.inverse() * tc;

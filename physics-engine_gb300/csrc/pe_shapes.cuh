@@ -113,6 +113,8 @@ template <class R> struct ShapeTable {
     // shape c_shape[k] at local transform c_xf[12k..] (basis row-major, then origin), relocated by
     // CompoundShape::init()
     const int* c_beg; const int* c_cnt; const int* c_shape; const R* c_xf;
+    // contact margin of every pair algorithm (PE_MARGIN, phys_general.h:45; 0 in the reference's build)
+    R margin;
 
 #ifdef __CUDACC__
     __device__ Xf<R> child_xf(int k) const {

@@ -69,6 +69,7 @@ public:
     virtual void set_ignore_pairs(int n, const int* pairs) = 0;
     virtual void set_scenes(int n, const int* off) = 0;
     virtual void set_params(double dt, double gx, double gy, double gz, int iters) = 0;
+    virtual void set_margin(double m) = 0;
     virtual void step(int n, int mode) = 0;
     virtual void integrate() = 0;
     virtual int broadphase() = 0;
@@ -115,6 +116,7 @@ public:
     void set_ignore_pairs(int n, const int* pairs) override;
     void set_scenes(int n, const int* off) override;
     void set_params(double dt, double gx, double gy, double gz, int iters) override;
+    void set_margin(double m) override { margin_ = static_cast<R>(m); }
     void step(int n, int mode) override;
     void integrate() override;
     int broadphase() override;
@@ -251,6 +253,7 @@ private:
     bool ev_open_[5] = {false, false, false, false, false};
     double ms_[5] = {0, 0, 0, 0, 0};
     StepParams prm_{0.01, {0, -9.8, 0}, 10};
+    R margin_ = 0;   // contact margin of the pair algorithms (PE_MARGIN, phys_general.h:45)
     // shapes
     int S_ = 0;
     DBuf<int> stype_, shull_, hvbeg_, hvcnt_, hfbeg_, hfcnt_, hebeg_, hecnt_, hfoff_, hfidx_;

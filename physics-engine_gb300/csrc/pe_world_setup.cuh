@@ -68,6 +68,7 @@ template <class R> ShapeTable<R> World<R>::shapes() const {
     t.e_a = hea_.p; t.e_b = heb_.p;
     t.c_beg = cbeg_.p; t.c_cnt = ccnt_.p; t.c_shape = cshape_.p; t.c_xf = cxf_.p;
     t.h_lbeg = hlbeg_.p; t.h_lcnt = hlcnt_.p; t.lf_beg = lfbeg_.p; t.lf_cnt = lfcnt_.p; t.lf_min = lfmin_.p; t.lf_max = lfmax_.p;
+    t.margin = margin_;
     return t;
 }
 

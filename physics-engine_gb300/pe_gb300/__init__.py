@@ -49,6 +49,7 @@ def load(build_if_missing: bool = True):
         "pe_gpu_set_ignore_pairs": (I, [P, I, ip]),
         "pe_gpu_set_scenes": (I, [P, I, ip]),
         "pe_gpu_set_params": (I, [P, D, D, D, D, I]),
+        "pe_gpu_set_contact_margin": (I, [P, D]),
         "pe_gpu_step": (I, [P, I, I]),
         "pe_gpu_integrate": (I, [P]),
         "pe_gpu_broadphase": (I, [P, C.POINTER(I)]),
@@ -101,7 +102,7 @@ def _i32(a):
 class GpuWorld:
     """A device-resident world (or batch of independent scenes) on one GPU."""
 
-    def __init__(self, scene, real_bits=64, device=0, scenes=None):
+    def __init__(self, scene, real_bits=64, device=0, scenes=None, margin=0.0):
         self.lib = load()
         self.h = C.c_void_p()
         cfg = _Config(real_bits, device)
@@ -132,6 +133,8 @@ class GpuWorld:
         if len(s.ignore_pairs):
             self._ck(self.lib.pe_gpu_set_ignore_pairs(self.h, len(s.ignore_pairs), _i32(s.ignore_pairs).ravel()))
         self._ck(self.lib.pe_gpu_set_params(self.h, float(s.dt), *map(float, s.gravity), int(s.iterations)))
+        if margin:
+            self._ck(self.lib.pe_gpu_set_contact_margin(self.h, float(margin)))
         if scenes is not None:
             self.set_scenes(scenes)
 

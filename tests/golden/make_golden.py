@@ -107,19 +107,78 @@ for a in range(4):
 for a, b in ((0, 0), (0, 2), (2, 2), (2, 3), (3, 3)):
     CASES[f"zoo_{a}{b}_f32"] = (lambda a=a, b=b: sc.pair_zoo(a, b, m=48, seed=200 + 4 * a + b, real_bits=32), 32, 2, [0, 1])
 
+# contact margin 0.005 (the tower configuration's; the reference built with PE_MARGIN = 0.005
+# through oracle/ref_margin.h): every pair type, and a small tower over 60 steps
+MARGIN = build_ref.MARGIN_VARIANT
+MARGIN_CASES = set()
+for a in range(4):
+    for b in range(a, 4):
+        CASES[f"zoo_{a}{b}_m005_f64"] = (lambda a=a, b=b: sc.pair_zoo(a, b, m=48, seed=300 + 4 * a + b, real_bits=64), 64, 2, [0, 1])
+        MARGIN_CASES.add(f"zoo_{a}{b}_m005_f64")
+for a, b in ((0, 0), (0, 2), (2, 3), (3, 3)):
+    CASES[f"zoo_{a}{b}_m005_f32"] = (lambda a=a, b=b: sc.pair_zoo(a, b, m=48, seed=400 + 4 * a + b, real_bits=32), 32, 2, [0, 1])
+    MARGIN_CASES.add(f"zoo_{a}{b}_m005_f32")
+for bits in (64, 32):
+    CASES[f"tower3_m005_f{bits}"] = (lambda bits=bits: sc.tower(nx=3, ny=3, nz=3, real_bits=bits), bits, 60,
+                                     [0, 1, 2, 20, 21, 58, 59])
+    MARGIN_CASES.add(f"tower3_m005_f{bits}")
+# whole trajectories recorded as per-step digests of the body states: the 1,002-body tower of the
+# plain single-scene configuration (10 x 10 x 10 boxes, 50 kg sphere at 30 m/s, 20 iterations,
+# margin 0.005), 300 steps
+TRAJ = {"tower_m005_traj_f64": (lambda: sc.tower(real_bits=64), 64, 300, MARGIN, [149, 299])}
+
+
+def state_digests(traj):
+    """SHA-256 of each step's body states, rows of (origin 3, basis 9, v 3, w 3) doubles in scene
+    order: the layout the reference harness writes with PE_TRAJ_OUT."""
+    import hashlib
+    return np.array([np.frombuffer(hashlib.sha256(np.ascontiguousarray(t, "<f8").tobytes()).digest(), np.uint8)
+                     for t in traj])
+
+
+def make_traj(name, ref_dir):
+    import os
+    factory, bits, steps, margin, keep = TRAJ[name]
+    scene = factory()
+    with tempfile.TemporaryDirectory() as td:
+        sp = Path(td) / "s.pescene"
+        tp = Path(td) / "t.bin"
+        scene.write(sp)
+        exe = ref_dir / f"ref_harness{bits}{'m' if margin else ''}"
+        env = dict(os.environ, PE_TRAJ_OUT=str(tp))
+        subprocess.run([str(exe), str(sp), str(Path(td) / "d"), str(steps), "8", "-1"], check=True, capture_output=True, env=env)
+        traj = np.fromfile(tp, "<f8").reshape(steps, scene.n_bodies, 18)
+    arrays = {"scene": np.frombuffer(scene_bytes(scene), np.uint8), "bits": np.array(bits),
+              "steps": np.array(steps), "margin": np.array(margin), "digests": state_digests(traj),
+              "kept": np.array(keep)}
+    for k in keep:
+        arrays[f"state{k}"] = traj[k]
+    np.savez_compressed(OUT / f"{name}.npz", **arrays)
+    return steps, len(keep)
+
+
+def scene_bytes(scene):
+    with tempfile.TemporaryDirectory() as td:
+        sp = Path(td) / "s.pescene"
+        scene.write(sp)
+        return sp.read_bytes()
+
 
 def make(name, ref_dir):
+    if name in TRAJ:
+        return make_traj(name, ref_dir)
     factory, bits, steps, rec = CASES[name]
+    margin = MARGIN if name in MARGIN_CASES else 0.0
     scene = factory()
     with tempfile.TemporaryDirectory() as td:
         sp = Path(td) / "s.pescene"
         dp = Path(td) / "d.pedump"
         scene.write(sp)
-        exe = ref_dir / f"ref_harness{bits}"
+        exe = ref_dir / f"ref_harness{bits}{'m' if margin else ''}"
         subprocess.run([str(exe), str(sp), str(dp), str(steps), "2", *map(str, rec)], check=True, capture_output=True)
         dumps = pedump.read(dp)
         arrays = {"scene": np.frombuffer(sp.read_bytes(), np.uint8), "bits": np.array(bits), "steps": np.array(steps),
-                  "recorded": np.array([d["step"] for d in dumps])}
+                  "recorded": np.array([d["step"] for d in dumps]), "margin": np.array(margin)}
         for d in dumps:
             for f in FIELDS:
                 arrays[f"s{d['step']}_{f}"] = d[f]
@@ -130,7 +189,7 @@ def make(name, ref_dir):
 
 if __name__ == "__main__":
     build_ref.build(REF, 8)
-    names = sys.argv[1:] or sorted(CASES)
+    names = sys.argv[1:] or sorted(CASES) + sorted(TRAJ)
     for name in names:
         p, c = make(name, build_ref.OUT)
         print(f"{name}: pairs {p} contact points {c}")

@@ -12,20 +12,55 @@ RESULT_KEYS = ["res_a", "res_b", "point_size", "valid_mask", "friction", "restit
 
 
 def golden_names():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+    """Fixtures with phase records of chosen steps (the trajectory-digest fixtures are separate)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if "_traj_" not in p.stem)
 
 
-def load_golden(name):
-    z = np.load(GOLDEN / f"{name}.npz")
-    bits = int(z["bits"])
+def traj_names():
+    return sorted(p.stem for p in GOLDEN.glob("*_traj_*.npz"))
+
+
+def _scene_from_bytes(b, bits):
     import tempfile, os
     fd, path = tempfile.mkstemp(suffix=".pescene")
     os.close(fd)
     try:
-        Path(path).write_bytes(z["scene"].tobytes())
-        scene = Scene.read(path, real_bits=bits)
+        Path(path).write_bytes(b)
+        return Scene.read(path, real_bits=bits)
     finally:
         os.unlink(path)
+
+
+def load_traj(name):
+    """A trajectory fixture: the scene (with .margin), real bits, step count, the per-step SHA-256
+    digests of the body states and the full states of the kept steps ({step: [N, 18]})."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    bits = int(z["bits"])
+    scene = _scene_from_bytes(z["scene"].tobytes(), bits)
+    scene.margin = float(z["margin"])
+    return scene, bits, int(z["steps"]), z["digests"], {int(k): z[f"state{k}"] for k in z["kept"]}
+
+
+def state_rows(st):
+    """Body states as rows of (origin 3, basis 9 row-major, v 3, w 3) doubles: the layout of the
+    trajectory fixtures."""
+    n = len(st["origin"])
+    return np.concatenate([np.asarray(st["origin"], np.float64), np.asarray(st["basis"], np.float64).reshape(n, 9),
+                           np.asarray(st["lin_vel"], np.float64), np.asarray(st["ang_vel"], np.float64)], axis=1)
+
+
+def state_digest(st):
+    import hashlib
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(state_rows(st), "<f8").tobytes()).digest(), np.uint8)
+
+
+def load_golden(name):
+    """A phase-record fixture: the scene (its contact margin in scene.margin), real bits, step count
+    and the records of the chosen steps."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    bits = int(z["bits"])
+    scene = _scene_from_bytes(z["scene"].tobytes(), bits)
+    scene.margin = float(z["margin"]) if "margin" in z else 0.0
     steps = {}
     for k in z["recorded"]:
         d = {f: z[f"s{k}_{f}"] for f in STATE_KEYS + RESULT_KEYS + ["pairs", "lin_vel_post", "ang_vel_post"]}

@@ -10,7 +10,8 @@ import pytest
 import orc
 import pe_gb300 as pg
 from pe_gb300 import scene as sc
-from pe_testlib import compare_results, compare_state, dump_state, golden_names, load_golden, results_of
+from pe_testlib import (compare_results, compare_state, dump_state, golden_names, load_golden, load_traj, results_of,
+                        state_digest, state_rows, traj_names)
 
 pytestmark = pytest.mark.gpu
 
@@ -32,7 +33,7 @@ def keys_tie_free(d, axis):
 @pytest.mark.parametrize("name", golden_names())
 def test_gpu_phases_match_reference(name):
     scene, bits, steps, rec = load_golden(name)
-    g = pg.GpuWorld(scene, bits)
+    g = pg.GpuWorld(scene, bits, margin=scene.margin)
     for k in sorted(rec):
         d = rec[k]
         # broadphase: the pair set exactly; the order too when no two sort keys tie
@@ -79,7 +80,7 @@ def test_gpu_full_steps_serial_order_match_reference(name):
     """Whole steps on the device in serial-order mode reproduce the reference trajectory
     (scenes whose sort keys never tie, so the broadphase order is the reference's)."""
     scene, bits, steps, rec = load_golden(name)
-    g = pg.GpuWorld(scene, bits)
+    g = pg.GpuWorld(scene, bits, margin=scene.margin)
     done = 0
     for k in sorted(rec):
         g.step(k + 1 - done, pg.SERIAL_ORDER)
@@ -101,7 +102,7 @@ def test_gpu_scene_file_full_steps_match_reference(name):
     compounds landing from step 40 on).  The steps start from the reference's state after step 0,
     the one step whose sort keys tie (tied keys fix the pair set, not its order)."""
     scene, bits, steps, rec = load_golden(name)
-    g = pg.GpuWorld(scene, bits)
+    g = pg.GpuWorld(scene, bits, margin=scene.margin)
     d0 = rec[0]
     s0 = dump_state(d0)
     s0["lin_vel"], s0["ang_vel"] = d0["lin_vel_post"], d0["ang_vel_post"]
@@ -375,6 +376,37 @@ def test_gpu_tower_serial_order_per_step_replay():
         g.solve(pg.SERIAL_ORDER)
         o.solve()
         compare_state(g.state(), o.state(), keys=["lin_vel", "ang_vel"], what="tower solve")
+
+
+@pytest.mark.parametrize("name", traj_names())
+def test_gpu_tower_whole_trajectory_matches_reference(name):
+    """The plain single-scene configuration as stated: the 1,002-body tower hit by the sphere, FP64,
+    20 iterations, contact margin 0.005, serial order, 300 whole steps on the device.  Sort keys tie
+    all over the tower and the reference's std::sort orders tied keys its own way, so each step's
+    pair order is replayed from the oracle (whose order is the reference's; the GPU's own pair set
+    is checked against it).  Every step's body states equal the reference's bit for bit: per-step
+    digests of all states, and the kept full states."""
+    scene, bits, steps, digests, kept = load_traj(name)
+    o = orc.OracleWorld(scene, bits, threads=8, margin=scene.margin)
+    g = pg.GpuWorld(scene, bits, margin=scene.margin)
+    for k in range(steps):
+        g.axis = o.axis
+        g.integrate()
+        o.integrate()
+        g.broadphase()
+        o.broadphase()
+        ref_pairs = o.pairs()
+        got = g.pairs()
+        assert sorted(map(tuple, np.sort(got, axis=1))) == sorted(map(tuple, np.sort(ref_pairs, axis=1))), f"step {k}: pair sets differ"
+        g.set_pairs(ref_pairs)
+        g.narrowphase()
+        o.narrowphase()
+        g.solve(pg.SERIAL_ORDER)
+        o.solve()
+        st = g.state(fields=("origin", "basis", "lin_vel", "ang_vel"))
+        if k in kept:
+            np.testing.assert_array_equal(state_rows(st), kept[k], err_msg=f"{name} step {k}")
+        assert np.array_equal(state_digest(st), digests[k]), f"{name}: body states differ from the reference at step {k}"
 
 
 def test_gpu_batched_scenes_equal_scenes_alone():

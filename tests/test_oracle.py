@@ -6,7 +6,8 @@ import pytest
 
 import orc
 from pe_gb300 import scene as sc
-from pe_testlib import compare_results, compare_state, dump_state, golden_names, load_golden, results_of
+from pe_testlib import (compare_results, compare_state, dump_state, golden_names, load_golden, load_traj, results_of,
+                        state_digest, state_rows, traj_names)
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -14,7 +15,7 @@ def test_oracle_trajectory_matches_reference(name):
     """Stepping the oracle from the scene reproduces the reference bit for bit at every
     recorded step: poses, AABBs, world inertia, ordered pairs, contact caches, velocities."""
     scene, bits, steps, rec = load_golden(name)
-    w = orc.OracleWorld(scene, bits)
+    w = orc.OracleWorld(scene, bits, margin=scene.margin)
     done = 0
     for k in sorted(rec):
         w.step(k + 1 - done)
@@ -33,7 +34,7 @@ def test_oracle_trajectory_matches_reference(name):
 def test_oracle_phases_from_reference_state(name):
     """Each phase of the oracle, fed the reference's own inputs, gives the reference's outputs."""
     scene, bits, steps, rec = load_golden(name)
-    w = orc.OracleWorld(scene, bits)
+    w = orc.OracleWorld(scene, bits, margin=scene.margin)
     for k in sorted(rec):
         d = rec[k]
         # broadphase on the reference's AABBs and sweep axis
@@ -63,6 +64,36 @@ def test_oracle_phases_from_reference_state(name):
             w.set_state(s0)
             w.integrate()
             compare_state(w.state(), dump_state(d), what=f"{name} integrate step {k}")
+
+
+@pytest.mark.parametrize("name", traj_names())
+def test_oracle_whole_trajectory_matches_reference(name):
+    """Every step of a long trajectory of the reference (the 1,002-body tower at contact margin
+    0.005, 300 steps, the sphere's impact included) is reproduced bit for bit by the oracle: the
+    per-step digests of all body states agree, and the kept full states are equal."""
+    scene, bits, steps, digests, kept = load_traj(name)
+    w = orc.OracleWorld(scene, bits, threads=4, margin=scene.margin)
+    for k in range(steps):
+        w.step(1)
+        st = w.state()
+        if k in kept:
+            np.testing.assert_array_equal(state_rows(st), kept[k], err_msg=f"{name} step {k}")
+        assert np.array_equal(state_digest(st), digests[k]), f"{name}: body states differ from the reference at step {k}"
+
+
+def test_margin_changes_the_contacts():
+    """The margin fixtures are not the plain ones: contact margin 0.005 shifts every contact
+    point's depth by 2 margin (pt - n margin, depth + 2 margin in each pair algorithm)."""
+    _, _, _, rec = load_golden("zoo_00_m005_f64")
+    scene, bits, _, _ = load_golden("zoo_00_m005_f64")
+    assert scene.margin == 0.005
+    w0 = orc.OracleWorld(scene, bits)
+    w1 = orc.OracleWorld(scene, bits, margin=scene.margin)
+    for w in (w0, w1):
+        w.step(1)
+    r0, r1 = w0.results(), w1.results()
+    assert np.array_equal(r1["point_size"], rec[0]["point_size"])
+    assert not np.array_equal(r0["slots"], r1["slots"])
 
 
 # ------------------------------------------------------------------ reference unit-test answers
