@@ -162,17 +162,38 @@ private:
         if (g <= 0) return;
         klaunch_[id]++;
         step_launches_++;
+        cudaStream_t s = cur_ ? cur_ : st_;   // a side stream while a fork is open (fork_streams)
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (prof_) {
             if (ev_pool_.size() < 2) { cudaEvent_t a, b; PE_CK(cudaEventCreate(&a)); PE_CK(cudaEventCreate(&b)); ev_pool_.push_back(a); ev_pool_.push_back(b); }
             e0 = ev_pool_.back(); ev_pool_.pop_back();
             e1 = ev_pool_.back(); ev_pool_.pop_back();
-            PE_CK(cudaEventRecord(e0, st_));
+            PE_CK(cudaEventRecord(e0, s));
         }
-        kern<<<g, block, smem, st_>>>(args...);
+        kern<<<g, block, smem, s>>>(args...);
         if (prof_) {
-            PE_CK(cudaEventRecord(e1, st_));
+            PE_CK(cudaEventRecord(e1, s));
             pending_.push_back({id, e0, e1});
+        }
+    }
+    // Side streams for independent launches (the narrowphase's per-class kernels): fork_streams()
+    // makes every side stream wait for the work queued on the world's stream so far, use_stream(k)
+    // sends the following launches to side stream k, join_streams() makes the world's stream wait
+    // for all side streams and sends launches back to it.
+    static constexpr int kSideStreams = 4;
+    cudaStream_t side_[kSideStreams] = {};
+    cudaEvent_t fork_ev_ = nullptr, join_ev_[kSideStreams] = {};
+    cudaStream_t cur_ = nullptr;
+    void fork_streams() {
+        PE_CK(cudaEventRecord(fork_ev_, st_));
+        for (int k = 0; k < kSideStreams; k++) PE_CK(cudaStreamWaitEvent(side_[k], fork_ev_, 0));
+    }
+    void use_stream(int k) { cur_ = side_[k % kSideStreams]; }
+    void join_streams() {
+        cur_ = nullptr;
+        for (int k = 0; k < kSideStreams; k++) {
+            PE_CK(cudaEventRecord(join_ev_[k], side_[k]));
+            PE_CK(cudaStreamWaitEvent(st_, join_ev_[k], 0));
         }
     }
     // cooperative launch (all blocks resident; grid-wide barriers inside the kernel)

@@ -9,6 +9,11 @@ namespace pe {
 template <class R> World<R>::World(int device) : dev_(device) {
     PE_CK(cudaSetDevice(dev_));
     PE_CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    for (int k = 0; k < kSideStreams; k++) {
+        PE_CK(cudaStreamCreateWithFlags(&side_[k], cudaStreamNonBlocking));
+        PE_CK(cudaEventCreateWithFlags(&join_ev_[k], cudaEventDisableTiming));
+    }
+    PE_CK(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
     for (auto& e : ev_) { PE_CK(cudaEventCreate(&e[0])); PE_CK(cudaEventCreate(&e[1])); }
     UnitMeshes u;
     std::memset(&u, 0, sizeof(u));
@@ -26,6 +31,11 @@ template <class R> World<R>::~World() {
     for (auto& q : pending_) { cudaEventDestroy(q.e0); cudaEventDestroy(q.e1); }
     for (auto e : ev_pool_) cudaEventDestroy(e);
     for (auto& e : ev_) { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+    for (int k = 0; k < kSideStreams; k++) {
+        if (side_[k]) { cudaStreamSynchronize(side_[k]); cudaStreamDestroy(side_[k]); }
+        if (join_ev_[k]) cudaEventDestroy(join_ev_[k]);
+    }
+    if (fork_ev_) cudaEventDestroy(fork_ev_);
     if (st_) cudaStreamDestroy(st_);
 }
 

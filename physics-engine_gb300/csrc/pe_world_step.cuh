@@ -150,10 +150,27 @@ template <class R> void World<R>::narrowphase() {
                                        (int)(sat_group_reals<R>(kSatGroup) * sizeof(R))));
             sat_attr_ = true;
         }
+        // The classes' kernels touch disjoint pairs and results: they run side by side on the side
+        // streams, so the long tails of the serial per-pair kernels overlap the other classes.
+        // Streams are given greedily, largest estimated work first (pairs x a rough per-pair cost).
+        static_assert(PC_COUNT == 15, "one cost per pair class");
+        static constexpr double kClassCost[PC_COUNT] = {2, 1, 1, 1, 4, 20, 6, 12, 400, 40, 40, 60, 20, 30, 30};
+        int order_c[PC_COUNT], stream_of[PC_COUNT];
+        double load[kSideStreams] = {};
+        for (int c = 0; c < PC_COUNT; c++) order_c[c] = c;
+        std::sort(order_c, order_c + PC_COUNT, [&](int a, int b) { return cnt[a] * kClassCost[a] > cnt[b] * kClassCost[b]; });
+        for (int k = 0; k < PC_COUNT; k++) {
+            const int c = order_c[k];
+            const int best = (int)(std::min_element(load, load + kSideStreams) - load);
+            stream_of[c] = best;
+            load[best] += cnt[c] * kClassCost[c];
+        }
+        fork_streams();
         for (int c = 0; c < PC_COUNT; c++) {
             const int lo = cur[c], hi = cur[c] + cnt[c];
             if (hi == lo) continue;
             const int g = grid(hi - lo);
+            use_stream(stream_of[c]);
             switch (c) {
                 case PC_BOX_BOX: launch(K_NP, g, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_BOX_SPHERE: launch(K_NP, g, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
@@ -203,6 +220,7 @@ template <class R> void World<R>::narrowphase() {
                     break;
             }
         }
+        join_streams();
         PE_CK(cudaGetLastError());
     }
     PE_CK(cudaMemcpyAsync(res_scene_off_.p, pair_scene_off_.p, (NS_ + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));

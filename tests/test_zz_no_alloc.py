@@ -137,7 +137,7 @@ def test_noalloc_matches_oracle_at_the_size_limit_with_ignored_bodies():
     ign = set(np.flatnonzero(scene.body_flags & sc.IGNORE_COLLISION).tolist())
     assert not (set(got.ravel().tolist()) & ign)
     # the same bodies with no flags array: every body dynamic, so the ignored bodies pair again
-    count2, got2 = _noalloc_pairs(lib, rt, mn, mx, None, axis, cap=count + 4096)
+    count2, got2 = _noalloc_pairs(lib, rt, mn, mx, None, axis, cap=2 * count + 4096)
     plain = scene.body_flags & ~sc.IGNORE_COLLISION
     s2 = scene
     s2.body_flags = plain.astype(np.int32)
