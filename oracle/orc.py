@@ -26,7 +26,7 @@ def lib():
             "orc_create": (P, [C.c_char_p, I, I]),
             "orc_destroy": (None, [P]),
             "orc_n_bodies": (I, [P]), "orc_n_pairs": (I, [P]), "orc_n_results": (I, [P]),
-            "orc_get_axis": (I, [P]), "orc_set_axis": (None, [P, I]), "orc_set_margin": (None, [P, D]),
+            "orc_get_axis": (I, [P]), "orc_set_axis": (None, [P, I]), "orc_set_margin": (None, [P, D]), "orc_set_stable_ties": (None, [P, I]),
             "orc_step": (None, [P, I]), "orc_time_steps": (D, [P, I]),
             "orc_integrate": (None, [P]), "orc_broadphase": (I, [P]), "orc_narrowphase": (None, [P]),
             "orc_solve": (None, [P]),
@@ -44,7 +44,7 @@ def lib():
 
 
 class OracleWorld:
-    def __init__(self, scene, real_bits=64, threads=1, margin=0.0):
+    def __init__(self, scene, real_bits=64, threads=1, margin=0.0, stable_ties=False):
         L = lib()
         fd, path = tempfile.mkstemp(suffix=".pescene")
         os.close(fd)
@@ -58,6 +58,8 @@ class OracleWorld:
         self.real_bits = real_bits
         if margin:
             L.orc_set_margin(self.h, float(margin))
+        if stable_ties:
+            L.orc_set_stable_ties(self.h, 1)
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -187,6 +187,8 @@ int orc_get_axis(void* h) { return with(h, [](auto& W) { return W.axis; }); }
 void orc_set_axis(void* h, int a) { with(h, [a](auto& W) { W.axis = a; return 0; }); }
 // contact margin (PE_MARGIN, phys_general.h:45; the reference compiles it as 0)
 void orc_set_margin(void* h, double m) { with(h, [m](auto& W) { W.margin = static_cast<decltype(W.margin)>(m); return 0; }); }
+// broadphase sort ties in body order (std::stable_sort) instead of std::sort's order
+void orc_set_stable_ties(void* h, int on) { with(h, [on](auto& W) { W.stable_ties = on != 0; return 0; }); }
 
 void orc_step(void* h, int n) { with(h, [n](auto& W) { for (int i = 0; i < n; i++) W.step(); return 0; }); }
 

@@ -106,6 +106,7 @@ public:
     int iterations = 10;
     int axis = 0;                           // BroadPhaseSweepAndPrune::_target_axis
     R margin = 0;                           // contact margin, PE_MARGIN (phys_general.h:45)
+    bool stable_ties = false;               // broadphase ties in body order (std::stable_sort)
     std::vector<std::pair<int, int>> pairs;
     std::vector<CResult<R>> results;        // pooled: slots survive between steps (stale distances)
     std::vector<std::vector<Row<R>>> rows;
@@ -189,7 +190,11 @@ public:
         std::vector<int> order(n);
         for (int i = 0; i < n; i++) order[i] = i;
         const int ax = axis;
-        std::sort(order.begin(), order.end(), [&](int a, int b) { return bodies[a].aabb_min[ax] < bodies[b].aabb_min[ax]; });
+        auto by_min = [&](int a, int b) { return bodies[a].aabb_min[ax] < bodies[b].aabb_min[ax]; };
+        // the reference sorts with std::sort, whose order among equal keys is unspecified; the
+        // stable variant (ties in body order) is the other valid order this oracle can take
+        if (stable_ties) std::stable_sort(order.begin(), order.end(), by_min);
+        else std::sort(order.begin(), order.end(), by_min);
         V3<R> s(0, 0, 0), s2(0, 0, 0);
         for (int i = 0; i < n; i++) {
             const Body<R>& b1 = bodies[order[i]];

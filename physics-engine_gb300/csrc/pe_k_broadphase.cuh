@@ -319,67 +319,59 @@ __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* 
     }
 }
 
-// next sweep axis of each scene: the axis of largest AABB-centre variance (sweep_and_prune.cpp:37-40).
-// One block per scene sums the sorted centres in double, in an order fixed relative to the scene
-// (thread t takes positions t, t + blockDim, ... of the scene, then a fixed tree), so a scene gets
-// the same sums wherever it sits in a batch and run to run.  A scene below two bodies keeps its
-// axis, as the reference returns before updating it.
-constexpr int kAxisTile = 4096;   // scenes above this size sum scene-relative tiles in separate blocks
+// Next sweep axis of each scene (BroadPhaseSweepAndPrune::calcCollisionPairs,
+// broad_phase_sweep_and_prune.cpp:18-22, 37-40): the AABB centres (min + max) * 0.5 summed in the
+// scene's sorted order, in the world's real type, one running sum per component for the centres and
+// one for their squares, exactly as the reference accumulates them; then the variances
+// s2 - s * s / n and the reference's strict comparisons.  A float sum is not associative, so the
+// six sums run sequentially: one block of two warps per scene, warp 1 stages the next chunk of
+// centres in shared memory while six lanes of warp 0 add up the current one.  A scene below two
+// bodies keeps its axis (the reference returns before updating it).
+constexpr int kAxisChunk = 512;
 template <class R>
-__global__ void k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, int* scene_axis) {
-    const int s = blockIdx.x;
-    const int lo = scene_off[s], hi = scene_off[s + 1];
-    const int cnt = hi - lo;
-    if (cnt < 2 || cnt > kAxisTile) return;   // whole block
-    __shared__ double red[6][kBlock];
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
-        for (int d = 0; d < 3; d++) {
-            const double c = (double)((smn[(size_t)d * n + k] + smx[(size_t)d * n + k]) * R(0.5));
-            acc[d] += c;
-            acc[3 + d] += c * c;
-        }
-    }
-    for (int q = 0; q < 6; q++) red[q][threadIdx.x] = acc[q];
+__global__ void __launch_bounds__(64) k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, int* scene_axis) {
+    __shared__ R cbuf[2][3][kAxisChunk];
+    __shared__ R sums[6];
+    const int s = blockIdx.x, tid = threadIdx.x;
+    const int lo = scene_off[s], hi = scene_off[s + 1], cnt = hi - lo;
+    if (cnt < 2) return;   // whole block
+    auto stage = [&](int buf, int base, int t) {   // t in [0, 32): the staging warp's lane
+        const int e = min(kAxisChunk, hi - base);
+        for (int k = t; k < e; k += 32)
+            for (int d = 0; d < 3; d++) cbuf[buf][d][k] = (smn[(size_t)d * n + base + k] + smx[(size_t)d * n + base + k]) * R(0.5);
+    };
+    if (tid >= 32) stage(0, lo, tid - 32);
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+    R acc = 0;   // tid d < 3: running sum of centre component d; tid 3 + d: of its square
+    int buf = 0;
+    for (int base = lo; base < hi; base += kAxisChunk) {
+        if (tid >= 32) {
+            if (base + kAxisChunk < hi) stage(buf ^ 1, base + kAxisChunk, tid - 32);
+        } else if (tid < 6) {
+            const int e = min(kAxisChunk, hi - base);
+            const R* c = cbuf[buf][tid < 3 ? tid : tid - 3];
+            if (tid < 3) {
+                for (int k = 0; k < e; k++) acc = acc + c[k];
+            } else {
+                for (int k = 0; k < e; k++) { const R q = c[k] * c[k]; acc = acc + q; }
+            }
+        }
         __syncthreads();
+        buf ^= 1;
     }
-    if (threadIdx.x == 0) {
-        double v[3];
-        for (int d = 0; d < 3; d++) v[d] = red[3 + d][0] - red[d][0] * red[d][0] / (double)cnt;
+    if (tid < 6) sums[tid] = acc;
+    __syncthreads();
+    if (tid == 0) {
+        R v[3];
+        for (int d = 0; d < 3; d++) {
+            const R ss = sums[d] * sums[d];
+            v[d] = sums[3 + d] - ss / R(cnt);
+        }
         int ax = 0;
         if (v[1] > v[0]) ax = 1;
         if (v[2] > v[ax]) ax = 2;
         scene_axis[s] = ax;
     }
 }
-
-// large scenes: block b sums tile item[b].y (positions lo + tile * kAxisTile, ...) of scene
-// item[b].x, in the same fixed order as k_bp_axis; then one thread per large scene adds its tiles
-// in tile order
-template <class R>
-__global__ void k_bp_axis_tiles(const R* smn, const R* smx, int n, const int* scene_off, const int2* item, double* part) {
-    const int s = item[blockIdx.x].x, t = item[blockIdx.x].y;
-    const int lo = scene_off[s] + t * kAxisTile, hi = min(scene_off[s + 1], lo + kAxisTile);
-    __shared__ double red[6][kBlock];
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
-        for (int d = 0; d < 3; d++) {
-            const double c = (double)((smn[(size_t)d * n + k] + smx[(size_t)d * n + k]) * R(0.5));
-            acc[d] += c;
-            acc[3 + d] += c * c;
-        }
-    }
-    for (int q = 0; q < 6; q++) red[q][threadIdx.x] = acc[q];
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x < 6) part[(size_t)blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
-}
-__global__ void k_bp_axis_combine(const int* scene_off, const int2* item, int n_item, const double* part, int* scene_axis);
 
 } // namespace pe

@@ -525,6 +525,9 @@ __global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, co
 // bodies, so their order inside the colour does not matter; results left after kMaxColorsBig - 1
 // rounds run in island order in one thread.
 constexpr int kMaxColorsBig = 1024;
+// coloured mode: a big island whose exact level schedule needs at most this many levels runs it
+// (the reference's order); above, first-fit colours bound the colour count
+constexpr int kExactLevelsColored = 256;
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big);
 template <class R>
 __global__ void k_gc_mask_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, unsigned long long* mask) {
@@ -585,7 +588,7 @@ __global__ void k_gc_assign(int lo, int m, const uint32_t* order, Results<R> res
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_gc_rounds(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
                                                       unsigned long long* claim, int* color, unsigned long long* mask, int* left,
-                                                      int max_rounds, int* n_rounds) {
+                                                      int max_rounds, int* n_rounds, int* level) {
     cooperative_groups::grid_group grid = cooperative_groups::this_grid();
     __shared__ int bleft;
     const int t = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
@@ -617,6 +620,7 @@ __global__ void __launch_bounds__(kBlock) k_gc_rounds(int lo, int m, const uint3
                 if (!mask) {
                     color[lo + j] = r;
                 } else {
+                    if (level) level[lo + j] = r;   // the exact level, kept beside the first-fit colour
                     const unsigned long long used = (da ? mask[ia] : 0ull) | (db ? mask[ib] : 0ull);
                     const int c = used == ~0ull ? kMaxColorsBig - 1 : __ffsll((long long)~used) - 1;
                     color[lo + j] = c;

@@ -231,22 +231,5 @@ __global__ void k_bp_chunk_sums(const int* big, const int* n_big, const int* cho
     }
 }
 
-// axis of each large scene from its tile sums (items of a scene are consecutive, tile 0 first)
-__global__ void k_bp_axis_combine(const int* scene_off, const int2* item, int n_item, const double* part, int* scene_axis) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= n_item || item[b].y != 0) return;
-    const int s = item[b].x;
-    const int cnt = scene_off[s + 1] - scene_off[s];
-    const int tiles = (cnt + kAxisTile - 1) / kAxisTile;
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int t = 0; t < tiles; t++)
-        for (int q = 0; q < 6; q++) acc[q] += part[(size_t)(b + t) * 6 + q];
-    double v[3];
-    for (int d = 0; d < 3; d++) v[d] = acc[3 + d] - acc[d] * acc[d] / (double)cnt;
-    int ax = 0;
-    if (v[1] > v[0]) ax = 1;
-    if (v[2] > v[ax]) ax = 2;
-    scene_axis[s] = ax;
-}
 
 } // namespace pe

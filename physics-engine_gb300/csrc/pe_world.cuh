@@ -321,10 +321,6 @@ private:
     DBuf<R> smn_, smx_;
     DBuf<int> sflag_, ssc_, bp_stage_, bp_big_, bp_nbig_;
     DBuf<int> bp_wend_, bp_csize_, bp_nch_, bp_choff_, bp_ctot_, bp_ccount_, bp_cpref_;   // crowded windows in chunks
-    DBuf<int2> axis_items_;
-    DBuf<double> axis_part_;
-    int axis_items_n_ = 0;
-    void build_axis_items();
     static constexpr int kBigSweepBlocks = 152;   // blocks that share the crowded positions
     uint32_t* order_ = nullptr;   // sorted body order (points into val_)
     DBuf<int2> pairs_;
@@ -343,6 +339,7 @@ private:
     DBuf<unsigned long long> gc_mask_, gc_claim_;
     DBuf<double> xfer_;   // state transfers in the C ABI's layout
     DBuf<int> gc_left_;   // items left after each colouring round
+    DBuf<int> gc_level_;  // coloured mode: exact levels of a big island beside its first-fit colours
     void solve_big_islands(int NI, const uint32_t* order, bool exact);
     DBuf<R> rows_;
     int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0, n_islands_ = 0;

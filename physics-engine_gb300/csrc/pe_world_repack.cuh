@@ -137,7 +137,6 @@ void World<R>::repack(const int* keep, int n_keep, const SceneData* const* adds,
     NS_ = std::max(ns, 1);
     if (ns == 0) off = {0, 0};
     h_scene_off_ = off;
-    build_axis_items();
     std::vector<int> sc(std::max(N, 1), 0);
     for (int s = 0; s < ns; s++) for (int i = off[s]; i < off[s + 1]; i++) sc[i] = s;
     upload(bscene_, sc, st_);

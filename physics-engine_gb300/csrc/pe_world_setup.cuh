@@ -406,7 +406,6 @@ template <class R> void World<R>::set_scenes(int ns, const int* off) {
     for (int s = 0; s < ns; s++) if (so[s + 1] < so[s]) throw std::runtime_error("scene offsets must not decrease");
     NS_ = ns;
     h_scene_off_ = so;
-    build_axis_items();
     std::vector<int> sc(std::max(N_, 1), 0);
     for (int s = 0; s < ns; s++) for (int i = so[s]; i < so[s + 1]; i++) sc[i] = s;
     upload(bscene_, sc, st_);
@@ -422,17 +421,6 @@ template <class R> void World<R>::set_scenes(int ns, const int* off) {
     PE_CK(cudaStreamSynchronize(st_));
 }
 
-// (scene, tile) work items of the scenes above kAxisTile bodies, consecutive per scene
-template <class R> void World<R>::build_axis_items() {
-    std::vector<int2> it;
-    for (size_t s = 0; s + 1 < h_scene_off_.size(); s++) {
-        const int cnt = h_scene_off_[s + 1] - h_scene_off_[s];
-        if (cnt <= kAxisTile) continue;
-        for (int t = 0; t * kAxisTile < cnt; t++) it.push_back(make_int2((int)s, t));
-    }
-    axis_items_n_ = (int)it.size();
-    if (axis_items_n_) upload(axis_items_, it, st_);
-}
 
 template <class R> void World<R>::set_params(double dt, double gx, double gy, double gz, int iters) {
     prm_.dt = dt; prm_.g[0] = gx; prm_.g[1] = gy; prm_.g[2] = gz; prm_.iterations = iters;

@@ -107,14 +107,7 @@ template <class R> int World<R>::broadphase() {
            (const int*)bp_csize_.p, (const int*)bp_choff_.p, (const int*)bp_ctot_.p, (const int*)bp_cpref_.p, pairs_.p, pair_cap_,
            status_.p, ign);
     launch(K_MISC, grid(NS_ + 1), k_scene_pair_off, NS_, scene_off_.p, count_.p, n, pair_scene_off_.p);
-    launch(K_BP_AXIS, NS_, k_bp_axis<R>, smn_.p, smx_.p, n, scene_off_.p, scene_axis_.p);
-    if (axis_items_n_ > 0) {   // scenes above kAxisTile bodies
-        axis_part_.ensure((size_t)axis_items_n_ * 6);
-        launch(K_BP_AXIS, axis_items_n_, k_bp_axis_tiles<R>, (const R*)smn_.p, (const R*)smx_.p, n, (const int*)scene_off_.p,
-               (const int2*)axis_items_.p, axis_part_.p);
-        launch(K_BP_AXIS, grid(axis_items_n_), k_bp_axis_combine, (const int*)scene_off_.p, (const int2*)axis_items_.p,
-               axis_items_n_, (const double*)axis_part_.p, scene_axis_.p);
-    }
+    launch_block(K_BP_AXIS, NS_, 64, k_bp_axis<R>, (const R*)smn_.p, (const R*)smx_.p, n, (const int*)scene_off_.p, scene_axis_.p);
     PE_CK(cudaGetLastError());
     P_ = P;
     return P;
@@ -349,12 +342,29 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         gc_left_.ensure(kMaxColorsBig);
         PE_CK(cudaMemsetAsync(gc_left_.p, 0, kMaxColorsBig * sizeof(int), st_));
         gc_claim_.ensure(N_ + 1);
+        int* level = nullptr;   // coloured mode: the exact levels beside the first-fit colours
+        if (!exact) {
+            gc_level_.ensure((size_t)(lo + m));
+            level = gc_level_.p;
+            PE_CK(cudaMemsetAsync(level + lo, 0xff, (size_t)m * sizeof(int), st_));
+        }
         launch_coop(K_GC_COLOR, coop_blocks_, kBlock, k_gc_rounds<R>, lo, m, order, rs, jt, bd, gc_claim_.p, color_.p, mask, gc_left_.p,
-                    kMaxColorsBig - 1, gc_n_.p + 1);
+                    kMaxColorsBig - 1, gc_n_.p + 1, level);
         int ncol = 0;
         PE_CK(cudaMemcpyAsync(&ncol, gc_n_.p + 1, sizeof(int), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaStreamSynchronize(st_));
+        // Coloured mode keeps the exact levels (the reference's order, as in serial-order mode) when
+        // the island needs few of them; first-fit colours only bound the colour count of islands
+        // with long dependency chains (hundreds of levels), where one grid barrier per level and
+        // iteration would dominate.
+        int* col = color_.p;
+        if (!exact && ncol <= kExactLevelsColored) {
+            int left_last = 0;
+            PE_CK(cudaMemcpy(&left_last, gc_left_.p + ncol - 1, sizeof(int), cudaMemcpyDeviceToHost));
+            if (left_last == 0) col = level;
+        }
         PE_CK(cudaMemsetAsync(gc_cnt_.p, 0, (kMaxColorsBig + 1) * sizeof(int), st_));
-        launch(K_GC_COLOR, g, k_gc_count, lo, m, color_.p, gc_cnt_.p);
+        launch(K_GC_COLOR, g, k_gc_count, lo, m, col, gc_cnt_.p);
         PE_CK(cudaMemcpyAsync(cnt.data(), gc_cnt_.p, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, st_));
         PE_CK(cudaStreamSynchronize(st_));
         if (exact && cnt[kMaxColorsBig] > 0) {   // out of levels: the island in order on one thread
@@ -367,7 +377,7 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
             if (cnt[c + 1]) used = c + 1;
         }
         PE_CK(cudaMemcpyAsync(gc_cursor_.p, cur.data(), cur.size() * sizeof(int), cudaMemcpyHostToDevice, st_));
-        launch(K_GC_COLOR, g, k_gc_place, lo, m, (const int*)color_.p, order, gc_cursor_.p, isl_corder_.p);
+        launch(K_GC_COLOR, g, k_gc_place, lo, m, (const int*)col, order, gc_cursor_.p, isl_corder_.p);
         const bool last = cnt[kMaxColorsBig] > 0;
         n_colors_ = std::max(n_colors_, std::min(used, ncol) + (last ? 1 : 0));
         // every iteration in one cooperative launch: colour lists, then the grid-wide passes
@@ -377,7 +387,7 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         upload(gc_cstart_, cs, st_);
         upload(gc_ccount_, cc, st_);
         launch_coop(K_GC_SOLVE, coop_blocks_, kBlock, k_gc_solve<R>, (const uint32_t*)isl_corder_.p, (const int*)gc_cstart_.p,
-                    (const int*)gc_ccount_.p, top, prm_.iterations, lo, m, order, (const int*)color_.p, last ? 1 : 0, rs, jt, bd, rw,
+                    (const int*)gc_ccount_.p, top, prm_.iterations, lo, m, order, (const int*)col, last ? 1 : 0, rs, jt, bd, rw,
                     (const int*)row_off_.p);
     }
 }

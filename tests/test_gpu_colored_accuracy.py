@@ -1,15 +1,22 @@
-"""Accuracy of the coloured Gauss-Seidel solver (GPU, FP32) against the oracle's serial-order runs
-(the reference's sequential impulse order) in FP64 and FP32, on a pour: 4,096 bodies (boxes,
-spheres, convex hulls) dropped into a 10 x 10 m walled container from random, partly overlapping
-positions, 240 steps of 1/120 s.  Colouring changes the Gauss-Seidel order, so trajectories differ
-body by body; the gates are on aggregate physics:
+"""Accuracy of the coloured Gauss-Seidel solver (GPU, FP32) against the oracle, the reference's
+sequential-impulse solver in its own order.
 
-* total mechanical energy, sampled every 20 steps, stays within max(3 x the largest FP32-vs-FP64
-  oracle spread, 0.5 %) of the FP64 oracle, relative to the initial energy;
-* the largest penetration seen stays within 1.25 x the larger of the two oracle runs' largest;
+Pour: 4,096 bodies (boxes, spheres, convex hulls) dropped into a 10 x 10 m walled container from
+random, partly overlapping positions, 240 steps of 1/120 s.  The tolerance is the spread of the
+oracle's own runs of the scene: the FP64 build and the FP32 build, each at two thread counts, and
+each with both orders the reference's broadphase may give equal sort keys (its std::sort leaves
+that order unspecified; the oracle takes std::sort's or body order).  Thread counts change no bit
+(asserted).  For each metric m, spread = max over the runs of |m(run) - m(FP64)|, and the coloured
+GPU run must satisfy |m(GPU) - m(FP64)| <= spread, with no extra factor or floor:
+
+* energy: total mechanical energy sampled every 20 steps, the largest deviation from the FP64 run
+  over the samples, relative to the initial energy;
+* the largest penetration seen over the samples;
 * the contact rows' velocity residual after the next solve (RMS over the points of how far the
-  normal relative velocity falls short of the row's target) stays within 1.25 x the larger of the
-  two oracle runs' (measured: 0.444 m/s against 0.455 / 0.433 m/s).
+  normal relative velocity falls short of the row's target).
+
+Batched piles (the benchmark's workload): there the coloured solver's islands keep the exact level
+schedule, so a coloured step equals a serial-order step bit for bit.
 """
 import numpy as np
 import pytest
@@ -39,29 +46,56 @@ def _trace(world, scene, step):
     return np.array(energy), max(pen)
 
 
-def test_gpu_colored_energy_and_penetration_within_oracle_spread():
+def _residual(w, scene, solve):
+    """The next step by phases, with the body state read before and after the solve."""
+    w.integrate()
+    w.broadphase()
+    w.narrowphase()
+    pre, res = w.state(), w.results()
+    solve()
+    return contact_residual(pre, w.state(), res, scene)[0]
+
+
+def test_gpu_colored_within_oracle_spread():
     s64, s32 = _pour(64), _pour(32)
-    o64, o32 = orc.OracleWorld(s64, 64, threads=16), orc.OracleWorld(s32, 32, threads=16)
-    e64, p64 = _trace(o64, s64, lambda: o64.step(1))
-    e32, p32 = _trace(o32, s32, lambda: o32.step(1))
+    runs = {}
+    for bits, scene in ((64, s64), (32, s32)):
+        for stable in (False, True):
+            for threads in (4, 16):
+                o = orc.OracleWorld(scene, bits, threads=threads, stable_ties=stable)
+                e, p = _trace(o, scene, lambda: o.step(1))
+                r = _residual(o, scene, lambda: o.solve())
+                runs[(bits, stable, threads)] = (e, p, r)
+    for bits in (64, 32):
+        for stable in (False, True):
+            a, b = runs[(bits, stable, 4)], runs[(bits, stable, 16)]
+            assert np.array_equal(a[0], b[0]) and a[1] == b[1] and a[2] == b[2], "the thread count changed the oracle's result"
     g = pg.GpuWorld(s32, 32)
     eg, pgpu = _trace(g, s32, lambda: g.step(1, pg.COLORED))
+    rg = _residual(g, s32, lambda: g.solve(pg.COLORED))
+    assert np.all(np.isfinite(eg))
     dyn = s64.mass > 0
     e0 = float((s64.mass[dyn] * 9.8 * s64.origin[dyn, 1]).sum())
-    spread = float(np.max(np.abs(e32 - e64))) / e0
-    dev = float(np.max(np.abs(eg - e64))) / e0
-    tol = max(3.0 * spread, 0.005)
-    assert dev <= tol, f"energy deviation {dev:.4%} of E0 > tolerance {tol:.4%} (oracle FP32/FP64 spread {spread:.4%})"
-    assert pgpu <= 1.25 * max(p64, p32), f"max penetration {pgpu:.4f} m vs oracle {p64:.4f} / {p32:.4f} m"
-    assert np.all(np.isfinite(eg))
-    # the next step by phases, with the body state read before and after the solve
-    r = {}
-    for name, w, scene, solve in (("o64", o64, s64, lambda: o64.solve()), ("o32", o32, s32, lambda: o32.solve()),
-                                  ("gpu", g, s32, lambda: g.solve(pg.COLORED))):
-        w.integrate()
-        w.broadphase()
-        w.narrowphase()
-        pre, res = w.state(), w.results()
-        solve()
-        r[name] = contact_residual(pre, w.state(), res, scene)[0]
-    assert r["gpu"] <= 1.25 * max(r["o64"], r["o32"]), f"contact residual {r['gpu']:.4f} m/s vs oracle {r['o64']:.4f} / {r['o32']:.4f} m/s"
+    e64, p64, r64 = runs[(64, False, 16)]
+    members = [v for k, v in runs.items() if k[2] == 16]
+    spread_e = max(float(np.max(np.abs(e - e64))) / e0 for e, _, _ in members)
+    spread_p = max(abs(p - p64) for _, p, _ in members)
+    spread_r = max(abs(r - r64) for _, _, r in members)
+    dev_e = float(np.max(np.abs(eg - e64))) / e0
+    assert dev_e <= spread_e, f"energy deviation {dev_e:.4%} of E0 > oracle spread {spread_e:.4%}"
+    assert abs(pgpu - p64) <= spread_p, f"max penetration {pgpu:.4f} m vs FP64 {p64:.4f} m, oracle spread {spread_p:.4f} m"
+    assert abs(rg - r64) <= spread_r, f"contact residual {rg:.4f} m/s vs FP64 {r64:.4f} m/s, oracle spread {spread_r:.4f} m/s"
+
+
+def test_gpu_colored_equals_serial_order_on_batched_piles():
+    merged, offs = sc.batched_piles(n_scenes=96, seed=77, real_bits=32)
+    a = pg.GpuWorld(merged, 32, scenes=offs)
+    b = pg.GpuWorld(merged, 32, scenes=offs)
+    for k in range(90):
+        a.step(1, pg.COLORED)
+        b.step(1, pg.SERIAL_ORDER)
+        assert a.last_counts()["colors"] < 63   # no island left items after the block path's rounds
+        if (k + 1) % 30 == 0:
+            sa, sb = a.state(), b.state()
+            for f in ("origin", "basis", "lin_vel", "ang_vel"):
+                np.testing.assert_array_equal(sa[f], sb[f], err_msg=f"step {k}: {f}")
