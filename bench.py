@@ -209,29 +209,54 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def algorithmic_bytes(counts, n_bodies, iters, real_bytes):
-    """Algorithmic HBM bytes of one step (per kernel group), from the per-unit figures:
-    body 268 B, pair 104 B (+12 B per hull vertex), manifold 8 B, contact point 184 B plus
-    200 B per point and solver iteration (FP32; FP64 doubles every real field)."""
+def hull_vertices_per_pair(scene, pairs):
+    """Sum over the step's pairs of (V_A + V_B), the vertex counts of the pair's convex hulls (0 for
+    boxes, spheres, cylinders): the hull term of the pair bytes."""
+    from pe_gb300 import scene as sc
+    st = np.asarray(scene.shape_type)
+    vc = np.where(st == sc.HULL, np.asarray(scene.hull_vcnt), 0)
+    per_body = vc[np.asarray(scene.body_shape)]
+    p = np.asarray(pairs).reshape(-1, 2)
+    return int(per_body[p[:, 0]].sum() + per_body[p[:, 1]].sum()) if len(p) else 0
+
+
+def algorithmic_bytes(counts, n_bodies, iters, real_bytes, hull_verts=0):
+    """Algorithmic HBM bytes of one step (per phase), from the per-unit figures:
+    body 268 B, pair 104 B plus 12 B per hull vertex of the pair (hull_verts = sum of V_A + V_B over
+    the pairs), manifold 8 B, contact point 184 B plus 200 B per point and solver iteration (FP32;
+    FP64 doubles every real field)."""
     k = real_bytes / 4.0
     P, M, C = counts["pairs"], counts["active"], counts["rows"]
     return {
-        "integrate": n_bodies * 124 * k,                   # read state 72 + write pose 28 + write AABB 24
-        "bp_sort": n_bodies * (8 + 64),                    # keys/indices + 4-pass radix of 8 B records
-        "bp_sweep": n_bodies * 24 * k + P * 8,             # sorted AABB gather reads + pair writes
-        "narrowphase": P * 104 * k + C * 52 * k + M * 8,   # pair + two bodies' pose/shape; point writes
-        "si_setup": C * (52 + 80) * k,                     # point reads + row writes
-        "si_colored": C * iters * 200 * k,                 # row 80 + accumulators 24 + two bodies' v,w 96
-        "si_serial": C * iters * 200 * k,
-        "step": (n_bodies * 268 + P * 104 + M * 8 + C * (184 + iters * 200)) * k,
+        "integrate": n_bodies * 124 * k,                                          # read state 72 + write pose 28 + AABB 24
+        "broadphase": n_bodies * (8 + 64 + 24 * k) + P * 8,                       # sort records + sorted AABB gather + pairs
+        "narrowphase": (P * 104 + 12 * hull_verts + C * 52) * k + M * 8,          # pairs, bodies, hull vertices; points
+        "solver": (n_bodies * 48 + C * (52 + 80) + C * iters * 200) * k,          # v, w; setup; row 80 + acc 24 + bodies 96
+        "step": (n_bodies * 268 + P * 104 + 12 * hull_verts + M * 8 + C * (184 + iters * 200)) * k,
     }
 
 
-# kernel groups (as reported by pe_gpu_kernel_stats) whose algorithmic bytes are one entry above;
-# the narrowphase's per-class thread kernels and its warp-per-pair SAT kernel share the pair bytes
-KERNEL_GROUPS = {"integrate": ("integrate",), "bp_sort": ("radix_sort",), "bp_sweep": ("bp_sweep",),
-                 "narrowphase": ("narrowphase", "np_sat"), "si_setup": ("si_setup",), "si_colored": ("si_colored",),
-                 "si_serial": ("si_serial",)}
+# The roofline is taken per phase: the narrowphase's class kernels run side by side on several
+# streams, so a phase's duration (events on the world's stream around the phase) is the time its
+# kernels take together; the phase with the longest duration is the dominant one.
+PHASES = ("integrate", "broadphase", "narrowphase", "solver")
+
+
+def ncu_traffic(phase):
+    """DRAM bytes (read + write) per step of a phase's kernels from the committed ncu launch list
+    of the batched workload (profiles/launches_batched_dram.md), scaled to the full workload by the
+    bodies processed; None when the summary is absent."""
+    f = ROOT / "profiles" / "launches_batched_dram.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        m = line.strip().split("|")
+        if len(m) > 4 and m[1].strip() == f"phase:{phase}":
+            try:
+                return float(m[4])   # bytes per step at the full workload
+            except ValueError:
+                return None
+    return None
 
 
 # ------------------------------------------------------------------ our arm
@@ -270,21 +295,33 @@ def run_ours(args, rank, world, device):
             launches += g.last_counts()["launches"]
     counts = g.last_counts()
     dev_ms = float(sum(per_step))
-    # dominant kernel: one profiled step (events around every launch; not part of the timed region)
+    hull_verts = hull_vertices_per_pair(scene, g.pairs())
+    # per-phase durations over the timed steps: the dominant phase and its roofline
+    g.phase_times(reset=True)
+    for _ in range(args.steps):
+        flush()
+        g.step(1, mode)
+    ph = g.phase_times(reset=True)
+    dom = max(PHASES, key=lambda k: ph[k])
+    dom_ms = ph[dom] / args.steps
+    alg = algorithmic_bytes(counts, N, scene.iterations, bits // 8, hull_verts)
+    dom_bytes = alg[dom]   # bytes of the whole phase in one step
+    peak, peak_kind = measured_peak()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(dom) if args.workload == "batched" and args.scenes == 4096 else None
+    # latency sample: more steps, each timed alone (no flush between them), for p50/p99
+    lat = []
+    for _ in range(args.latency_steps):
+        before = g.phase_times()["step"]
+        g.step(1, mode)
+        lat.append(g.phase_times()["step"] - before)
+    # per-kernel device time of one profiled step (events around every launch; the narrowphase's
+    # kernels overlap on side streams, so their times add up to more than the phase)
     g.set_profiling(True)
     flush()
     g.step(1, mode)
     g.set_profiling(False)
     ks = g.kernel_stats()
-    grp = {g: (sum(ks.get(k, (0.0, 0))[0] for k in m), sum(ks.get(k, (0.0, 0))[1] for k in m))
-           for g, m in KERNEL_GROUPS.items()}
-    dom = max(grp, key=lambda g: grp[g][0])
-    dom_ms, dom_n = grp[dom]
-    alg = algorithmic_bytes(counts, N, scene.iterations, bits // 8)
-    dom_bytes = alg[dom]   # bytes of the whole group in one step
-    peak, peak_kind = measured_peak()
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = None   # ncu's per-kernel DRAM writes include write-backs of earlier kernels' dirty lines
     # end to end through the C ABI with host buffers, over the same steps as the timed region
     # (restored from the snapshot): each step copies the poses and velocities in from page-locked
     # host arrays and reads the stepped ones back into them
@@ -307,14 +344,40 @@ def run_ours(args, rank, world, device):
     io_bytes = N * 18 * 8   # float64 poses and velocities through the C ABI, each way
     per_scene = per_scene_gpu(pg, scene, offs, g.state(fields=("origin", "basis", "lin_vel", "ang_vel")), bits, mode,
                               device, args.steps) if offs is not None and not args.no_per_scene else None
-    res = dict(dev_ms=dev_ms, per_step=per_step, N=N, launches=launches, counts=counts, cfg=cfg, bits=bits, clk=clk.summary(),
-               roofline=dict(kernel=dom, bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
-                             traffic=traffic, algorithmic_bytes=dom_bytes, launches=dom_n, avg_launch_ms=dom_ms / max(dom_n, 1),
-                             peak_source=peak_kind, step_frac=alg["step"] / (dev_ms / args.steps * 1e-3) / 1e9 / peak),
+    res = dict(dev_ms=dev_ms, per_step=per_step, lat=lat, N=N, launches=launches, counts=counts, cfg=cfg, bits=bits,
+               clk=clk.summary(),
+               roofline=dict(kernel=f"{dom} phase", bound="hbm", achieved=achieved, peak=peak, unit="GB/s", frac=achieved / peak,
+                             traffic=traffic, algorithmic_bytes=dom_bytes, phase_ms=dom_ms, hull_vertices_in_pairs=hull_verts,
+                             peak_source=peak_kind, step_bytes=alg["step"],
+                             step_frac=alg["step"] / (dev_ms / args.steps * 1e-3) / 1e9 / peak,
+                             phases_ms={k: ph[k] / args.steps for k in PHASES}),
                e2e=dict(value=N * len(e2e_times) / sum(e2e_times), unit=UNIT, h2d_bytes_per_step=io_bytes,
                         d2h_bytes_per_step=io_bytes),
                kernels={k: round(v[0], 4) for k, v in ks.items() if v[1]}, per_scene=per_scene)
     return res, scene, bits, offs
+
+
+def run_leg(name, steps, warmup, device):
+    """One of the other configurations on the GPU, device-timed like the main line (L2 flushed
+    between steps): body-steps/s, p50/p99 step time, pairs and contact points of the last step."""
+    import pe_gb300 as pg
+    scene, bits, mode, offs, cfg = make_workload(name)
+    g = pg.GpuWorld(scene, bits, device=device, scenes=offs, margin=cfg.get("margin", 0.0))
+    flush = L2Flush()
+    for _ in range(cfg.get("preroll_steps", 0) + warmup):
+        g.step(1, mode)
+    per = []
+    for _ in range(steps):
+        flush()
+        before = g.phase_times()["step"]
+        g.step(1, mode)
+        per.append(g.phase_times()["step"] - before)
+    c = g.last_counts()
+    g.close()
+    per_sorted = sorted(per)
+    return dict(value=scene.n_bodies * steps / (sum(per) * 1e-3), unit=UNIT, ms_per_step=sum(per) / steps, steps=steps,
+                p50_step_ms=per_sorted[len(per) // 2], p99_step_ms=per_sorted[min(len(per) - 1, int(0.99 * len(per)))],
+                pairs=c["pairs"], contact_points=c["rows"], dtype="f64" if bits == 64 else "f32", **cfg)
 
 
 def per_scene_gpu(pg, scene, offs, state, bits, mode, device, steps, sample=64, warmup=3):
@@ -342,17 +405,6 @@ def per_scene_gpu(pg, scene, offs, state, bits, mode, device, steps, sample=64, 
     return dict(value=bodies / (ms * 1e-3), unit=UNIT, scenes=len(picks),
                 sample=f"{len(picks)} scenes spread over the batch, each stepped alone {steps} times after {warmup} warm-up steps",
                 p50_step_ms=per_step[len(per_step) // 2], p99_step_ms=per_step[min(len(per_step) - 1, int(0.99 * len(per_step)))])
-
-
-def _cpu_scene_worker(job):
-    """One scene on one host thread: untimed pre-roll, then timed steps (oracle process pool)."""
-    scene, bits, preroll, steps = job
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import orc
-    w = orc.OracleWorld(scene, bits, threads=1)
-    if preroll:
-        w.time_steps(preroll)
-    return scene.n_bodies * steps, w.time_steps(steps)
 
 
 def run_serving(args, device):
@@ -426,6 +478,30 @@ def run_serving(args, device):
                 gpu_launches=None, clocks=clk.summary())
 
 
+def cpu_scenes_wall(scene, bits, offs, preroll, steps, sample=256, threads=None):
+    """The reference's CPU step (its algorithm restated in oracle/) on a spread sample of the batch's
+    scenes, one World per scene (World is not thread-safe; the reference's pool is a process
+    singleton), the scenes spread over all host threads.  The pre-roll runs first, untimed; the
+    timed region is the wall time of `steps` steps of every sampled scene, all threads busy."""
+    import concurrent.futures as cf
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import orc
+    from pe_gb300 import scene as sc
+    threads = threads or os.cpu_count() or 1
+    S = len(offs) - 1
+    picks = np.unique(np.linspace(0, S - 1, min(sample, S)).astype(int))
+    worlds = [orc.OracleWorld(sc.extract(scene, offs, int(k)), bits, threads=1) for k in picks]
+    bodies = sum(w.n for w in worlds)
+    with cf.ThreadPoolExecutor(threads) as ex:   # the oracle's step releases the interpreter lock
+        list(ex.map(lambda w: w.step(preroll), worlds))
+        t0 = time.perf_counter()
+        list(ex.map(lambda w: w.step(steps), worlds))
+        wall = time.perf_counter() - t0
+    return dict(value=bodies * steps / wall, unit=UNIT, cores=threads, kind="port", ms_per_step=wall / steps * 1e3,
+                sample=f"{len(picks)} of the {S:,} scenes ({bodies:,} bodies) spread over the batch, one World per scene on "
+                       f"{threads} host threads, {steps} timed steps after {preroll} untimed; wall time {wall:.2f} s")
+
+
 def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, steps=5, margin=0.0):
     """The reference's CPU step (its algorithm restated in oracle/) on a bounded sample, all host
     threads.  One scene: the reference's thread pool inside one world.  Independent scenes: one
@@ -443,18 +519,7 @@ def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, st
             n += k
         return dict(value=scene.n_bodies * n / t, unit=UNIT, cores=threads, kind="port",
                     sample=f"{n} full steps of the same workload from its initial state ({t:.1f} s, {threads} threads)")
-    import multiprocessing as mp
-    from pe_gb300 import scene as sc
-    S = len(offs) - 1
-    picks = np.unique(np.linspace(0, S - 1, min(sample, S)).astype(int))
-    jobs = [(sc.extract(scene, offs, int(k)), bits, preroll, steps) for k in picks]
-    with mp.get_context("spawn").Pool(threads) as pool:
-        out = pool.map(_cpu_scene_worker, jobs, chunksize=1)
-    body_steps = sum(o[0] for o in out)
-    t = sum(o[1] for o in out)
-    return dict(value=body_steps / (t / threads), unit=UNIT, cores=threads, kind="port",
-                sample=f"{len(picks)} scenes spread over the batch, one per host thread, {steps} timed steps each after "
-                       f"{preroll} untimed; summed per-scene time / {threads} threads ({t:.1f} s of CPU time)")
+    return cpu_scenes_wall(scene, bits, offs, preroll, steps)
 
 
 def main():
@@ -470,6 +535,9 @@ def main():
     ap.add_argument("--no-per-scene", action="store_true", help="skip the one-scene-per-launch comparison")
     ap.add_argument("--profile-one-step", action="store_true",
                     help="after the pre-roll and warm-up, run one step inside cudaProfilerStart/Stop and exit (for ncu)")
+    ap.add_argument("--latency-steps", type=int, default=200, help="extra steps timed one by one for p50/p99")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="skip the other configurations (stress, large, tower, 10 s of serving) reported beside the main line")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -483,8 +551,8 @@ def main():
                                                                 "the batched workload's reference arm")))
             return 0
         scene, bits, mode, offs, cfg = make_workload(args.workload, args.scenes)
-        cfg = dict(cfg, solver="serial (the reference's sequential impulse order)")
-        k = max(1, min(args.steps, 8))
+        cfg = dict(cfg, solver="serial: the reference's sequential impulse order (it has no coloured solver)")
+        k = max(1, args.steps)
         if offs is None:
             sys.path.insert(0, str(ROOT / "oracle"))
             import orc
@@ -492,15 +560,20 @@ def main():
             w = orc.OracleWorld(scene, bits, threads=threads, margin=cfg.get("margin", 0.0))
             for _ in range(args.warmup):   # untimed, like the GPU arm's warm-up
                 w.time_steps(1)
-            t = w.time_steps(k)
-            cb = dict(value=scene.n_bodies * k / t, unit=UNIT, cores=threads, kind="port",
-                      sample=f"{k} full steps from the initial state, {threads} host threads")
+            t, done = 0.0, 0
+            while done < k and (done == 0 or t < 120.0):   # a bounded sample of the K steps
+                t += w.time_steps(1)
+                done += 1
+            cb = dict(value=scene.n_bodies * done / t, unit=UNIT, cores=threads, kind="port", ms_per_step=t / done * 1e3,
+                      sample=f"{done} full steps after {args.warmup} untimed, the whole scene, the reference's thread pool "
+                             f"with {threads} host threads")
         else:
-            # the GPU arm's untimed pre-roll and warm-up steps, then the timed ones
-            cb = cpu_baseline(scene, bits, offs, preroll=cfg.get("preroll_steps", 0) + args.warmup, steps=k)
+            # the GPU arm's untimed pre-roll and warm-up steps, then its K timed steps
+            cb = cpu_scenes_wall(scene, bits, offs, cfg.get("preroll_steps", 0) + args.warmup, k)
+            done = k
         v = cb["value"]
-        print(json.dumps(dict(metric=METRIC, value=v, unit=UNIT, n_gpus=args.gpus, steps=k, warmup=args.warmup,
-                              ms_per_step=scene.n_bodies / v * 1e3, higher_is_better=True, scaling="weak",
+        print(json.dumps(dict(metric=METRIC, value=v, unit=UNIT, n_gpus=args.gpus, steps=done, warmup=args.warmup,
+                              ms_per_step=cb["ms_per_step"], higher_is_better=True, scaling="weak",
                               vs_baseline=None, dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg,
                               impl="reference", cpu_baseline=cb,
                               e2e=dict(value=v, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))))
@@ -531,11 +604,12 @@ def main():
         dist.barrier()
     if rank != 0:
         return 0
-    per = sorted(res["per_step"])
+    per = sorted(res["per_step"] + res["lat"])
     value = res["N"] * args.steps * world / (dev_ms * 1e-3)
     cfg = dict(res["cfg"], l2="flushed between timed steps (256 MiB memset)", pairs_last_step=res["counts"]["pairs"],
                contact_points_last_step=res["counts"]["rows"], colors_last_step=res["counts"]["colors"],
                p50_step_ms=per[len(per) // 2], p99_step_ms=per[min(len(per) - 1, int(0.99 * len(per)))],
+               latency_sample=f"{len(per)} steps: the {args.steps} timed ones and {len(res['lat'])} more timed one by one",
                contacts_per_s=res["counts"]["rows"] * args.steps * world / (dev_ms * 1e-3), parallelism=f"replicas x{world}")
     if res["per_scene"] is not None:
         cfg["per_scene_gpu"] = res["per_scene"]
@@ -545,8 +619,17 @@ def main():
                dtype="f64" if bits == 64 else "f32", data="synthetic", config=cfg, roofline=res["roofline"],
                e2e=res["e2e"], gpu_launches=res["launches"], clocks=res["clk"], kernels_ms_one_step=res["kernels"])
     if not args.no_cpu_baseline and world == 1:
-        out["cpu_baseline"] = cpu_baseline(scene, bits, offs, preroll=res["cfg"].get("preroll_steps", 0),
-                                           margin=res["cfg"].get("margin", 0.0))
+        out["cpu_baseline"] = cpu_baseline(scene, bits, offs, preroll=res["cfg"].get("preroll_steps", 0) + args.warmup,
+                                           steps=args.steps, margin=res["cfg"].get("margin", 0.0))
+    if not args.no_legs and world == 1 and args.workload == "batched" and not args.profile_one_step:
+        legs = {}
+        for name, k in (("stress", 10), ("large", 10), ("tower", 20)):
+            legs[name] = run_leg(name, k, 3, local)
+        sv = run_serving(argparse.Namespace(serve_seconds=10.0), local)
+        legs["serving"] = dict(value=sv["value"], unit=UNIT, **{k: sv["config"][k] for k in (
+            "workload", "requests", "finished", "p50_step_ms", "p99_step_ms", "mean_step_ms", "p50_request_s", "p99_request_s",
+            "peak_footprint_gb", "batched_steps", "wall_s")})
+        out["config"]["other_configs"] = legs
     print(json.dumps(out))
     return 0
 

@@ -41,6 +41,44 @@ __global__ void k_bp_keys(Bodies<R> B, const int* scene_axis, uint64_t* key, uin
     val[i] = (uint32_t)i;
 }
 
+// Sort of every scene's bodies by the AABB minimum along the scene's axis, one block per scene of
+// at most kSceneSortMax bodies: a bitonic sort in shared memory of (key, body index) pairs, whose
+// order, ties by body index, is the stable LSD radix sort's.  Replaces the radix passes (four
+// per key byte plus one per scene-id byte, five launches each) when every scene fits a block.
+constexpr int kSceneSortMax = 2048;
+constexpr int kSceneSortBlock = 512;
+template <class R>
+__global__ void __launch_bounds__(kSceneSortBlock) k_bp_sort_scenes(Bodies<R> B, const int* scene_axis, const int* scene_off,
+                                                                   uint32_t* order) {
+    __shared__ uint64_t key[kSceneSortMax];
+    __shared__ uint32_t idx[kSceneSortMax];
+    const int s = blockIdx.x;
+    const int lo = scene_off[s], cnt = scene_off[s + 1] - lo;
+    if (cnt <= 0) return;   // whole block
+    int P = 1;
+    while (P < cnt) P <<= 1;
+    const int ax = scene_axis[s];
+    for (int k = threadIdx.x; k < P; k += blockDim.x) {
+        if (k < cnt) { key[k] = order_bits(B.at(MNX + ax, lo + k)); idx[k] = (uint32_t)k; }
+        else { key[k] = ~0ull; idx[k] = 0xffffffffu; }   // padding sorts last
+    }
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+                const int i = 2 * t - (t & (stride - 1)), j = i + stride;   // the t-th pair of this stage
+                const bool up = (i & size) == 0;
+                const uint64_t ki = key[i], kj = key[j];
+                const uint32_t ii = idx[i], ij = idx[j];
+                const bool gt = ki > kj || (ki == kj && ii > ij);
+                if (gt == up) { key[i] = kj; key[j] = ki; idx[i] = ij; idx[j] = ii; }
+            }
+            __syncthreads();
+        }
+    }
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) order[lo + k] = (uint32_t)lo + idx[k];
+}
+
 // sorted copy of the sweep inputs (coalesced reads in the sweep)
 template <class R>
 __global__ void k_bp_gather(Bodies<R> B, const uint32_t* order, R* smn, R* smx, int* sflag, int* sscene) {

@@ -73,10 +73,18 @@ template <class R> int World<R>::broadphase() {
     for (int k = 0; k < 2; k++) { key_[k].ensure(n); key2_[k].ensure(n); val_[k].ensure(n); }
     smn_.ensure((size_t)3 * n); smx_.ensure((size_t)3 * n); sflag_.ensure(n); ssc_.ensure(n);
     count_.ensure(n + 1);
-    launch(K_BP_KEYS, grid(n), k_bp_keys<R>, bodies(), scene_axis_.p, key_[0].p, key2_[0].p, val_[0].p);
-    int scene_passes = 0;
-    for (int m = NS_ - 1; m > 0; m >>= 8) scene_passes++;
-    radix_sort(n, scene_passes);
+    int max_scene = 0;
+    for (int s = 0; s < NS_; s++) max_scene = std::max(max_scene, h_scene_off_[s + 1] - h_scene_off_[s]);
+    if (max_scene <= kSceneSortMax) {   // every scene sorted inside one block
+        launch_block(K_RADIX, NS_, kSceneSortBlock, k_bp_sort_scenes<R>, bodies(), (const int*)scene_axis_.p, (const int*)scene_off_.p,
+                     val_[0].p);
+        order_ = val_[0].p;
+    } else {
+        launch(K_BP_KEYS, grid(n), k_bp_keys<R>, bodies(), scene_axis_.p, key_[0].p, key2_[0].p, val_[0].p);
+        int scene_passes = 0;
+        for (int m = NS_ - 1; m > 0; m >>= 8) scene_passes++;
+        radix_sort(n, scene_passes);
+    }
     launch(K_BP_GATHER, grid(n), k_bp_gather<R>, bodies(), order_, smn_.p, smx_.p, sflag_.p, ssc_.p);
     bp_stage_.ensure((size_t)n * kStage);
     bp_big_.ensure(n + 1);
