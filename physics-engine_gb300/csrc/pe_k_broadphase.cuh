@@ -365,33 +365,47 @@ __global__ void k_bp_write(int n, const int* scene_axis, const R* smn, const R* 
 // six sums run sequentially: one block of two warps per scene, warp 1 stages the next chunk of
 // centres in shared memory while six lanes of warp 0 add up the current one.  A scene below two
 // bodies keeps its axis (the reference returns before updating it).
-constexpr int kAxisChunk = 512;
+template <class R> constexpr int axis_chunk() { return sizeof(R) == 4 ? 1024 : 512; }   // centres per staged chunk
 template <class R>
 __global__ void __launch_bounds__(64) k_bp_axis(const R* smn, const R* smx, int n, const int* scene_off, int* scene_axis) {
-    __shared__ R cbuf[2][3][kAxisChunk];
+    constexpr int CH = axis_chunk<R>(), PAD = CH + 1;   // the padding puts the three rows in different banks
+    __shared__ R cbuf[2][3 * PAD];
     __shared__ R sums[6];
     const int s = blockIdx.x, tid = threadIdx.x;
     const int lo = scene_off[s], hi = scene_off[s + 1], cnt = hi - lo;
     if (cnt < 2) return;   // whole block
     auto stage = [&](int buf, int base, int t) {   // t in [0, 32): the staging warp's lane
-        const int e = min(kAxisChunk, hi - base);
+        const int e = min(CH, hi - base);
         for (int k = t; k < e; k += 32)
-            for (int d = 0; d < 3; d++) cbuf[buf][d][k] = (smn[(size_t)d * n + base + k] + smx[(size_t)d * n + base + k]) * R(0.5);
+            for (int d = 0; d < 3; d++)
+                cbuf[buf][d * PAD + k] = (smn[(size_t)d * n + base + k] + smx[(size_t)d * n + base + k]) * R(0.5);
     };
     if (tid >= 32) stage(0, lo, tid - 32);
     __syncthreads();
     R acc = 0;   // tid d < 3: running sum of centre component d; tid 3 + d: of its square
     int buf = 0;
-    for (int base = lo; base < hi; base += kAxisChunk) {
+    for (int base = lo; base < hi; base += CH) {
         if (tid >= 32) {
-            if (base + kAxisChunk < hi) stage(buf ^ 1, base + kAxisChunk, tid - 32);
+            if (base + CH < hi) stage(buf ^ 1, base + CH, tid - 32);
         } else if (tid < 6) {
-            const int e = min(kAxisChunk, hi - base);
-            const R* c = cbuf[buf][tid < 3 ? tid : tid - 3];
-            if (tid < 3) {
-                for (int k = 0; k < e; k++) acc = acc + c[k];
-            } else {
-                for (int k = 0; k < e; k++) { const R q = c[k] * c[k]; acc = acc + q; }
+            const int e = min(CH, hi - base);
+            const R* c = cbuf[buf] + (tid < 3 ? tid : tid - 3) * PAD;
+            const bool sq = tid >= 3;
+            int k = 0;
+            for (; k + 8 <= e; k += 8) {   // loads ahead of the dependent adds, which stay in order
+                R v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    v[u] = c[k + u];
+                    if (sq) v[u] = v[u] * v[u];
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) acc = acc + v[u];
+            }
+            for (; k < e; k++) {
+                R v = c[k];
+                if (sq) v = v * v;
+                acc = acc + v;
             }
         }
         __syncthreads();

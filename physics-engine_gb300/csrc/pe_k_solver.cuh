@@ -59,12 +59,10 @@ __global__ void k_si_setup(int P, Results<R> res, Bodies<R> B, Rows<R> rows, con
 
 // FrictionContactConstraint::iterateSequentialImpulse (friction_contact_constraint.cpp:75-108)
 // for all points of one result; temporary velocities live in the body arrays
+// The rows of one result applied to the two bodies' temporary velocities, held by the caller.
 template <class R>
-__device__ __forceinline__ void si_iterate_result(const Bodies<R>& B, const Rows<R>& rows, int ia, int ib, int r0, int np) {
-    const bool ka = (B.flags[ia] & BF_KINEMATIC) != 0, kb = (B.flags[ib] & BF_KINEMATIC) != 0;
-    V3<R> tva = B.vec(TVX, ia), twa = B.vec(TWX, ia), tvb = B.vec(TVX, ib), twb = B.vec(TWX, ib);
-    const R ima = B.at(INVM, ia), imb = B.at(INVM, ib);
-    const M3<R> Ia = B.mat(I00, ia), Ib = B.mat(I00, ib);
+__device__ __forceinline__ void si_result_rows(const Rows<R>& rows, int r0, int np, bool ka, bool kb, V3<R>& tva, V3<R>& twa,
+                                               V3<R>& tvb, V3<R>& twb, R ima, R imb, const M3<R>& Ia, const M3<R>& Ib) {
     for (int r = r0; r < r0 + np; r++) {
         const V3<R> ra(rows.at(RAX, r), rows.at(RAY, r), rows.at(RAZ, r));
         const V3<R> rb(rows.at(RBX, r), rows.at(RBY, r), rows.at(RBZ, r));
@@ -89,6 +87,14 @@ __device__ __forceinline__ void si_iterate_result(const Bodies<R>& B, const Rows
         if (!kb) { tvb = tvb + nimp * imb; twb = twb + mv(Ib, cross(rb, nimp)); }
         // the same body can sit on both sides only through distinct results, never here
     }
+}
+template <class R>
+__device__ __forceinline__ void si_iterate_result(const Bodies<R>& B, const Rows<R>& rows, int ia, int ib, int r0, int np) {
+    const bool ka = (B.flags[ia] & BF_KINEMATIC) != 0, kb = (B.flags[ib] & BF_KINEMATIC) != 0;
+    V3<R> tva = B.vec(TVX, ia), twa = B.vec(TWX, ia), tvb = B.vec(TVX, ib), twb = B.vec(TWX, ib);
+    const R ima = B.at(INVM, ia), imb = B.at(INVM, ib);
+    const M3<R> Ia = B.mat(I00, ia), Ib = B.mat(I00, ib);
+    si_result_rows(rows, r0, np, ka, kb, tva, twa, tvb, twb, ima, imb, Ia, Ib);
     if (!ka) { B.set_vec(TVX, ia, tva); B.set_vec(TWX, ia, twa); }
     if (!kb) { B.set_vec(TVX, ib, tvb); B.set_vec(TWX, ib, twb); }
 }
@@ -342,17 +348,67 @@ __global__ void k_isl_keys(int A, const int* active, Results<R> res, Bodies<R> B
 __global__ void k_isl_flags(int A, const uint64_t* key, int* flag);
 __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out);
 
-// serial order inside each island: one thread per island (all islands in serial-order mode,
-// islands up to `max_len` results in coloured mode)
+// serial order inside each island of min_len..max_len items, one thread per island.  An island of
+// contact results whose results touch at most two dynamic bodies (a body resting on static ones, a
+// pair of touching bodies: most small islands) keeps those bodies' temporary velocities, inverse
+// masses and inertias in registers through all iterations and writes them back once; the rows are
+// applied in the same order with the same arithmetic, so the velocities are the same bit for bit.
+// Other islands go through the body arrays item by item.
 template <class R>
-__global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
-                             Rows<R> rows, const int* row_off, int iterations, int min_len, int max_len) {
+__global__ void __launch_bounds__(64) k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res,
+                                                   Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off, int iterations,
+                                                   int min_len, int max_len) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= *n_isl) return;
     const int lo = isl_off[s], hi = isl_off[s + 1];
     if (hi - lo < min_len || hi - lo > max_len) return;
+    int d0 = -1, d1 = -1;   // the island's dynamic bodies when there are at most two
+    bool two = true;
+    for (int k = lo; k < hi && two; k++) {
+        const uint32_t item = order[k];
+        if (item & kJointItem) { two = false; break; }
+        const int q[2] = {res.a[item], res.b[item]};
+        for (int e = 0; e < 2; e++) {
+            const int b = q[e];
+            if (B.flags[b] & BF_KINEMATIC) continue;
+            if (b == d0 || b == d1) continue;
+            if (d0 < 0) d0 = b;
+            else if (d1 < 0) d1 = b;
+            else two = false;
+        }
+    }
+    if (!two || d0 < 0) {
+        for (int it = 0; it < iterations; it++)
+            for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
+        return;
+    }
+    V3<R> v0 = B.vec(TVX, d0), w0 = B.vec(TWX, d0), v1, w1;
+    const R m0 = B.at(INVM, d0);
+    const M3<R> I0 = B.mat(I00, d0);
+    R m1 = 0;
+    M3<R> I1;
+    if (d1 >= 0) { v1 = B.vec(TVX, d1); w1 = B.vec(TWX, d1); m1 = B.at(INVM, d1); I1 = B.mat(I00, d1); }
     for (int it = 0; it < iterations; it++)
-        for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
+        for (int k = lo; k < hi; k++) {
+            const int p = (int)order[k];
+            const int ia = res.a[p], ib = res.b[p], r0 = row_off[p], np = res.npts[p];
+            if (ia == d0 && ib == d1) {
+                si_result_rows(rows, r0, np, false, false, v0, w0, v1, w1, m0, m1, I0, I1);
+            } else if (ia == d1 && ib == d0) {
+                si_result_rows(rows, r0, np, false, false, v1, w1, v0, w0, m1, m0, I1, I0);
+            } else {   // one dynamic body against a kinematic one, whose temporary velocity never changes
+                const int kin = (ia == d0 || ia == d1) ? ib : ia;
+                V3<R> kv = B.vec(TVX, kin), kw = B.vec(TWX, kin);
+                const R km = B.at(INVM, kin);
+                const M3<R> kI = B.mat(I00, kin);
+                if (ia == d0) si_result_rows(rows, r0, np, false, true, v0, w0, kv, kw, m0, km, I0, kI);
+                else if (ia == d1) si_result_rows(rows, r0, np, false, true, v1, w1, kv, kw, m1, km, I1, kI);
+                else if (ib == d0) si_result_rows(rows, r0, np, true, false, kv, kw, v0, w0, km, m0, kI, I0);
+                else si_result_rows(rows, r0, np, true, false, kv, kw, v1, w1, km, m1, kI, I1);
+            }
+        }
+    B.set_vec(TVX, d0, v0); B.set_vec(TWX, d0, w0);
+    if (d1 >= 0) { B.set_vec(TVX, d1, v1); B.set_vec(TWX, d1, w1); }
 }
 
 constexpr int kSmallResults = 8;   // islands up to this size run in the reference order, one thread each
@@ -360,9 +416,10 @@ constexpr int kSmallResults = 8;   // islands up to this size run in the referen
 // coloured Gauss-Seidel of one island per block: greedy colouring in rounds (a result takes
 // colour c when it holds the smallest position among the uncoloured results on each of its
 // dynamic bodies), then every iteration runs the colours in turn, all results of a colour in
-// parallel.  Results still uncoloured after kMaxColors - 1 rounds form a last colour that one
-// thread runs in order.
-constexpr int kMaxColors = 64;
+// parallel.  Colour c is then the item's level in the serial order's level schedule, so an island
+// coloured in at most kMaxColors - 1 rounds runs exactly the reference's order.  Results still
+// uncoloured after kMaxColors - 1 rounds form a last colour that one thread runs in order.
+constexpr int kMaxColors = 512;
 constexpr int kColorBlock = 64;   // threads per island block: islands run tens of results per colour
 constexpr int kBigIsland = 4096;  // larger islands are coloured and solved by the whole grid (k_gc_*)
 template <class R>
@@ -374,6 +431,7 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
     const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
     if (m <= min_len || m > kBigIsland) return;
     __shared__ int cnt[kMaxColors + 1];
+    __shared__ int fill[kMaxColors];
     __shared__ int remaining;
     __shared__ int ncol;
     for (int j = threadIdx.x; j < m; j += blockDim.x) color[lo + j] = -1;
@@ -422,11 +480,19 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
         atomicMax(n_colors_out, ncol + (cnt[kMaxColors] > cnt[kMaxColors - 1] ? 1 : 0));
     }
     __syncthreads();
-    // placement by colour keeping the island order within each colour
-    if (threadIdx.x == 0) {
-        int fill[kMaxColors];
-        for (int k = 0; k < kMaxColors; k++) fill[k] = cnt[k];
-        for (int j = 0; j < m; j++) corder[lo + fill[color[lo + j]]++] = order[lo + j];
+    // placement by colour: the results of a colour touch disjoint dynamic bodies, so their order
+    // inside the colour does not matter and they are placed in parallel; the last colour's (run in
+    // island order by one thread) in order
+    for (int k = threadIdx.x; k < kMaxColors; k += blockDim.x) fill[k] = cnt[k];
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        const int c = color[lo + j];
+        if (c < kMaxColors - 1) corder[lo + atomicAdd(&fill[c], 1)] = order[lo + j];
+    }
+    if (threadIdx.x == 0 && cnt[kMaxColors] > cnt[kMaxColors - 1]) {
+        int f = cnt[kMaxColors - 1];
+        for (int j = 0; j < m; j++)
+            if (color[lo + j] == kMaxColors - 1) corder[lo + f++] = order[lo + j];
     }
     __syncthreads();
     for (int it = 0; it < iterations; it++) {
@@ -527,7 +593,7 @@ __global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, co
 constexpr int kMaxColorsBig = 1024;
 // coloured mode: a big island whose exact level schedule needs at most this many levels runs it
 // (the reference's order); above, first-fit colours bound the colour count
-constexpr int kExactLevelsColored = 256;
+constexpr int kExactLevelsColored = 512;
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big);
 template <class R>
 __global__ void k_gc_mask_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, unsigned long long* mask) {

@@ -280,8 +280,8 @@ template <class R> void World<R>::solve(int mode) {
         launch(K_ISLAND, grid(M + 1), k_isl_offsets, M, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
         const int NI = n_islands_;
         // islands of up to kSmallResults items: one thread each
-        launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(), row_off_.p,
-               prm_.iterations, 0, kSmallResults);
+        launch_block(K_SI_SERIAL, (NI + 63) / 64, 64, k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
+                     row_off_.p, prm_.iterations, 0, kSmallResults);
         if (mode == 0) {
             // serial order, larger islands: the exact level schedule, a block per island up to
             // kBigIsland items, grid-wide above
