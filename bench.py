@@ -263,7 +263,9 @@ def ncu_traffic(phase):
 def run_ours(args, rank, world, device):
     import pe_gb300 as pg
     scene, bits, mode, offs, cfg = make_workload(args.workload, args.scenes)
-    g = pg.GpuWorld(scene, bits, device=device, scenes=offs, margin=cfg.get("margin", 0.0))
+    g = pg.GpuWorld(scene, bits, device=device, scenes=offs, margin=cfg.get("margin", 0.0), tuning="auto")
+    cfg = dict(cfg, tuning=dict(g.tuning(), source="pe_gb300/tuning table for this GPU" if pg.autotune_table_present(device, bits)
+                                else "defaults (no tuning table for this GPU)"))
     flush = L2Flush()
     N = scene.n_bodies
     for _ in range(cfg.get("preroll_steps", 0)):   # untimed settling (part of the workload definition)
@@ -362,7 +364,7 @@ def run_leg(name, steps, warmup, device):
     between steps): body-steps/s, p50/p99 step time, pairs and contact points of the last step."""
     import pe_gb300 as pg
     scene, bits, mode, offs, cfg = make_workload(name)
-    g = pg.GpuWorld(scene, bits, device=device, scenes=offs, margin=cfg.get("margin", 0.0))
+    g = pg.GpuWorld(scene, bits, device=device, scenes=offs, margin=cfg.get("margin", 0.0), tuning="auto")
     flush = L2Flush()
     for _ in range(cfg.get("preroll_steps", 0) + warmup):
         g.step(1, mode)

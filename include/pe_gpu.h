@@ -126,6 +126,27 @@ int pe_gpu_set_params(pe_gpu_world* w, double dt, double gx, double gy, double g
  * :426-429).  Default 0; a margin >= 0 reproduces the reference compiled with that PE_MARGIN. */
 int pe_gpu_set_contact_margin(pe_gpu_world* w, double margin);
 
+/* Scheduling settings of the step: which kernel takes which work, with how many threads.  They
+ * replace the reference's fixed work split of its thread pool (batch = count / threads / 2 + 1,
+ * src/utils/thread_pool.h:85-102).  In serial-order mode no valid setting changes a result bit; in
+ * coloured mode none does while every island needs at most exact_levels_colored levels (above, a
+ * big island is coloured first-fit).  pe_gb300.autotune picks them by timing a small batched case;
+ * the defaults are those below. */
+typedef struct pe_gpu_tuning {
+    int sat_heavy_cost;       /* SAT pairs whose estimated work reaches this run on a block of warps (200000) */
+    int small_island_items;   /* islands up to this many items run on one thread each, 0..64 (8) */
+    int big_island_items;     /* islands above this many items are coloured and solved grid-wide (4096) */
+    int color_block;          /* threads per island block in coloured mode, 32..256, multiple of 32 (64) */
+    int level_block;          /* threads per island block in serial-order mode, 32..256, multiple of 32 (256) */
+    int exact_levels_colored; /* coloured mode keeps a big island's exact levels up to this many, 0..1023 (512) */
+    int scene_sort_max;       /* scenes up to this many bodies are sorted inside one block, 0..2048 (2048) */
+    int side_streams;         /* streams for the narrowphase's per-class kernels, 1..4 (4) */
+} pe_gpu_tuning;
+int pe_gpu_get_tuning(pe_gpu_world* w, pe_gpu_tuning* out);
+int pe_gpu_set_tuning(pe_gpu_world* w, const pe_gpu_tuning* t);
+/* the name of CUDA device `device` (cudaGetDeviceProperties), the key of the autotuner's tables */
+int pe_gpu_device_name(int device, char* name, int cap);
+
 /* World::step (world.cpp:267-300): n_steps full steps on the device without host round trips
  * of body state. */
 int pe_gpu_step(pe_gpu_world* w, int n_steps, int solver_mode);

@@ -1,5 +1,6 @@
 // C ABI (include/pe_gpu.h): status codes, argument checks, exception barrier.
 #include <cuda_runtime.h>
+#include <cstdio>
 #include <new>
 #include <string>
 #include "../../include/pe_gpu.h"
@@ -104,6 +105,40 @@ int pe_gpu_set_params(pe_gpu_world* h, double dt, double gx, double gy, double g
 int pe_gpu_set_contact_margin(pe_gpu_world* h, double margin) {
     if (!(margin >= 0) || !(margin < 1e30)) return PE_GPU_ERR_ARG;
     return guard(h, [&](pe::WorldBase& w) { w.set_margin(margin); return PE_GPU_OK; });
+}
+
+int pe_gpu_device_name(int device, char* name, int cap) {
+    if (!name || cap < 1) return PE_GPU_ERR_ARG;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return PE_GPU_ERR_CUDA;
+    std::snprintf(name, (size_t)cap, "%s", prop.name);
+    return PE_GPU_OK;
+}
+
+int pe_gpu_get_tuning(pe_gpu_world* h, pe_gpu_tuning* out) {
+    if (!out) return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) {
+        const pe::Tuning& t = w.tuning();
+        *out = pe_gpu_tuning{t.sat_heavy_cost, t.small_island_items, t.big_island_items, t.color_block, t.level_block,
+                             t.exact_levels_colored, t.scene_sort_max, t.side_streams};
+        return PE_GPU_OK;
+    });
+}
+
+int pe_gpu_set_tuning(pe_gpu_world* h, const pe_gpu_tuning* t) {
+    if (!t || t->sat_heavy_cost < 1 || t->small_island_items < 0 || t->small_island_items > 64 ||
+        t->big_island_items <= t->small_island_items || t->big_island_items > (1 << 24) || t->color_block < 32 ||
+        t->color_block > 256 || t->color_block % 32 || t->level_block < 32 || t->level_block > 256 || t->level_block % 32 ||
+        t->exact_levels_colored < 0 || t->exact_levels_colored > 1023 || t->scene_sort_max < 0 || t->scene_sort_max > 2048 ||
+        t->side_streams < 1 || t->side_streams > 4)
+        return PE_GPU_ERR_ARG;
+    return guard(h, [&](pe::WorldBase& w) {
+        pe::Tuning& u = w.tuning();
+        u.sat_heavy_cost = t->sat_heavy_cost; u.small_island_items = t->small_island_items; u.big_island_items = t->big_island_items;
+        u.color_block = t->color_block; u.level_block = t->level_block; u.exact_levels_colored = t->exact_levels_colored;
+        u.scene_sort_max = t->scene_sort_max; u.side_streams = t->side_streams;
+        return PE_GPU_OK;
+    });
 }
 
 int pe_gpu_step(pe_gpu_world* h, int n_steps, int mode) {

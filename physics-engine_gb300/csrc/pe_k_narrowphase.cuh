@@ -13,30 +13,30 @@ namespace pe {
 constexpr int kSatF = 128, kSatE = 192, kSatV = 64;
 constexpr int kSatWarps = 1;                 // pairs (one warp each) per block, light pairs
 constexpr int kSatGroup = 8;                 // warps per pair, heavy pairs (one block each)
-constexpr long long kSatHeavyCost = 200000;
 template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& s) {
     return s.face_count() <= kSatF && s.edge_count() <= kSatE && (s.type != ST_HULL || s.nv <= kSatV);
 }
-template <class R> __device__ __forceinline__ int sat_class(const ShapeView<R>& a, const ShapeView<R>& b) {
+// heavy: estimated work (axes x projection cost) from which a pair gets a block of warps
+template <class R> __device__ __forceinline__ int sat_class(const ShapeView<R>& a, const ShapeView<R>& b, long long heavy) {
     if (!sat_fits(a) || !sat_fits(b)) return PC_CONVEX_BIG;
     auto w = [](const ShapeView<R>& s) { return s.type == ST_HULL ? s.nv : s.type == ST_CYLINDER ? 12 : s.type == ST_BOX ? 8 : 2; };
     auto ue = [](const ShapeView<R>& s) { return s.type == ST_BOX ? 3 : s.edge_count(); };   // distinct edge axes
     const long long axes = (long long)a.face_count() + b.face_count() + (long long)ue(a) * ue(b);
-    if (axes * (w(a) + w(b)) >= kSatHeavyCost) return PC_CONVEX_HEAVY;
+    if (axes * (w(a) + w(b)) >= heavy) return PC_CONVEX_HEAVY;
     if (a.type == ST_HULL && b.type == ST_HULL) return PC_CONVEX_HULL_HULL;
     if (a.type == ST_CYLINDER) return PC_CONVEX_CYL_CYL;
     return a.type == ST_BOX ? PC_CONVEX : PC_CONVEX_HULL_BOX;
 }
 
 template <class R>
-__global__ void k_np_classify(int P, const int2* pairs, Bodies<R> B, ShapeTable<R> S, int* cls, int* cls_count) {
+__global__ void k_np_classify(int P, const int2* pairs, Bodies<R> B, ShapeTable<R> S, int* cls, int* cls_count, long long heavy) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     int c = -1 - (int)(threadIdx.x & 31);   // lanes past the end never match a class
     if (p < P) {
         const int2 q = pairs[p];
         const ShapeView<R> sa = S.view(B.shape[q.x]), sb = S.view(B.shape[q.y]);
         c = pair_class(sa.type, sb.type);
-        if (c == PC_CONVEX) c = sat_class(sa, sb);
+        if (c == PC_CONVEX) c = sat_class(sa, sb, heavy);
         cls[p] = c;
     }
     // one atomic per class present in the warp

@@ -865,6 +865,85 @@ k_np_cyl_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, 
     }
 }
 
+// SphereConvexCollisionAlgorithm (sphere_convex_collision_algorithm.cpp:185-210) for a convex hull,
+// one warp per pair: in rounds of 32 faces (the face tree's order for a hull, descending face
+// index; lane i takes the i-th face of the round) each lane tests its face's box and runs the
+// sphere-triangle test on its face's fan triangles; lane 0 then adds the points to the pair's cache
+// in face order and, inside a face, in triangle order, as the reference's query callback does.  A
+// face with more than kSphereHullCand triangles is left to lane 0 in its turn.
+constexpr int kSphereHullCand = 8;
+template <class R> constexpr int sphere_hull_warps() { return sizeof(R) == 4 ? 4 : 2; }
+template <class R>
+__global__ void __launch_bounds__(32 * sphere_hull_warps<R>())
+k_np_sphere_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                 const int* pair_scene_off, const int* prev_off) {
+    constexpr int W = sphere_hull_warps<R>(), K = kSphereHullCand;
+    __shared__ R cand[W][32 * K][7];
+    __shared__ int ccnt[W][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = lo + blockIdx.x * W + warp;
+    if (t >= hi) return;   // whole warps
+    const int p = order[t];
+    Cache<R> cache;
+    Pair<R> c;
+    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, c, lane == 0);
+    const bool a_hull = c.sa.type == ST_HULL;
+    const ShapeView<R>& m = a_hull ? c.sa : c.sb;
+    const ShapeView<R>& sp = a_hull ? c.sb : c.sa;
+    const Xf<R>& tm = a_hull ? c.ta() : c.tb();
+    const Xf<R>& ts = a_hull ? c.tb() : c.ta();
+    const R margin = c.margin;
+    if (lane == 0) cache.swap = a_hull;
+    const V3<R> rel = tm.inv_apply(ts.o);
+    const R r = sp.radius;
+    const V3<R> aa = rel - V3<R>(r, r, r), bb = rel + V3<R>(r, r, r);
+    // the points of face f's fan triangles, in order, through emit
+    auto face_points = [&](int f, auto&& emit) {
+        const int n = m.face_size(f);
+        for (int i = 0; i < n - 2; i++) {
+            const V3<R> vs[3] = {m.vert(m.face_vert(f, 0)), m.vert(m.face_vert(f, i + 1)), m.vert(m.face_vert(f, i + 2))};
+            V3<R> point, normal;
+            R depth = 0;
+            if (sphere_triangle(rel, r, vs, point, normal, depth)) {
+                normal = mv(tm.b, normal);
+                point = tm.apply(point);
+                emit(normal, point - normal * margin, depth + 2 * margin);
+            }
+        }
+    };
+    for (int base = 0; base < m.nf; base += 32) {
+        const int f = m.nf - 1 - base - lane;
+        int k = 0;
+        if (f >= 0 && face_hit(m, f, aa, bb)) {
+            if (m.face_size(f) - 2 > K) k = -1;
+            else
+                face_points(f, [&](const V3<R>& n, const V3<R>& pt, R d) {
+                    R* e = cand[warp][lane * K + k];
+                    e[0] = n.x; e[1] = n.y; e[2] = n.z; e[3] = pt.x; e[4] = pt.y; e[5] = pt.z; e[6] = d;
+                    k++;
+                });
+        }
+        ccnt[warp][lane] = k;
+        __syncwarp();
+        if (lane == 0)
+            for (int l = 0; l < 32; l++) {
+                if (ccnt[warp][l] >= 0) {
+                    for (int q = 0; q < ccnt[warp][l]; q++) {
+                        const R* e = cand[warp][l * K + q];
+                        c.add(V3<R>(e[0], e[1], e[2]), V3<R>(e[3], e[4], e[5]), e[6]);
+                    }
+                } else {
+                    face_points(m.nf - 1 - base - l, [&](const V3<R>& n, const V3<R>& pt, R d) { c.add(n, pt, d); });
+                }
+            }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        cache.swap = false;
+        np_finish(p, pairs, B, res, cache);
+    }
+}
+
 // SAT pairs with a shape beyond the staging limits (PC_CONVEX_BIG): one warp each, unstaged
 template <class R>
 __global__ void k_np_sat_big(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,

@@ -354,14 +354,16 @@ __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* 
 // masses and inertias in registers through all iterations and writes them back once; the rows are
 // applied in the same order with the same arithmetic, so the velocities are the same bit for bit.
 // Other islands go through the body arrays item by item.
+// The islands come from `list` (the small islands by descending work, k_isl_work*), so the longest
+// serial chains start in the first wave instead of holding the last one.
 template <class R>
-__global__ void __launch_bounds__(64) k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res,
-                                                   Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off, int iterations,
-                                                   int min_len, int max_len) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= *n_isl) return;
+__global__ void __launch_bounds__(64) k_isl_serial(const int* list, const int* n_list, const int* isl_off, const uint32_t* order,
+                                                   Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off,
+                                                   int iterations) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= *n_list) return;
+    const int s = list[t];
     const int lo = isl_off[s], hi = isl_off[s + 1];
-    if (hi - lo < min_len || hi - lo > max_len) return;
     int d0 = -1, d1 = -1;   // the island's dynamic bodies when there are at most two
     bool two = true;
     for (int k = lo; k < hi && two; k++) {
@@ -411,7 +413,6 @@ __global__ void __launch_bounds__(64) k_isl_serial(const int* n_isl, const int* 
     if (d1 >= 0) { B.set_vec(TVX, d1, v1); B.set_vec(TWX, d1, w1); }
 }
 
-constexpr int kSmallResults = 8;   // islands up to this size run in the reference order, one thread each
 
 // coloured Gauss-Seidel of one island per block: greedy colouring in rounds (a result takes
 // colour c when it holds the smallest position among the uncoloured results on each of its
@@ -420,16 +421,14 @@ constexpr int kSmallResults = 8;   // islands up to this size run in the referen
 // coloured in at most kMaxColors - 1 rounds runs exactly the reference's order.  Results still
 // uncoloured after kMaxColors - 1 rounds form a last colour that one thread runs in order.
 constexpr int kMaxColors = 512;
-constexpr int kColorBlock = 64;   // threads per island block: islands run tens of results per colour
-constexpr int kBigIsland = 4096;  // larger islands are coloured and solved by the whole grid (k_gc_*)
 template <class R>
-__global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
-                              Rows<R> rows, const int* row_off, int iterations, int min_len, int* claim, int* color, uint32_t* corder,
-                              int* n_colors_out) {
+__global__ void __launch_bounds__(256) k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
+                              Rows<R> rows, const int* row_off, int iterations, int min_len, int max_len, int* claim, int* color,
+                              uint32_t* corder, int* n_colors_out) {
     const int s = blockIdx.x;
     if (s >= *n_isl) return;
     const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
-    if (m <= min_len || m > kBigIsland) return;
+    if (m <= min_len || m > max_len) return;
     __shared__ int cnt[kMaxColors + 1];
     __shared__ int fill[kMaxColors];
     __shared__ int remaining;
@@ -468,47 +467,49 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
         __syncthreads();
         if (rem == 0) break;
     }
-    // leftovers (pathological degree): one last colour, run in order by one thread
+    // leftovers (pathological degree): colour nc after the nc rounds' colours, run in island order
+    // by one thread; only the colours in use are counted, placed and run
+    const int nc = ncol;
     for (int j = threadIdx.x; j < m; j += blockDim.x)
-        if (color[lo + j] < 0) color[lo + j] = kMaxColors - 1;
-    for (int k = threadIdx.x; k <= kMaxColors; k += blockDim.x) cnt[k] = 0;
+        if (color[lo + j] < 0) color[lo + j] = nc;
+    for (int k = threadIdx.x; k <= nc + 1; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
     for (int j = threadIdx.x; j < m; j += blockDim.x) atomicAdd(&cnt[color[lo + j] + 1], 1);
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int k = 0; k < kMaxColors; k++) cnt[k + 1] += cnt[k];   // cnt[c] = first slot of colour c
-        atomicMax(n_colors_out, ncol + (cnt[kMaxColors] > cnt[kMaxColors - 1] ? 1 : 0));
+        for (int k = 0; k <= nc; k++) cnt[k + 1] += cnt[k];   // cnt[c] = first slot of colour c
+        atomicMax(n_colors_out, nc + (cnt[nc + 1] > cnt[nc] ? 1 : 0));
     }
     __syncthreads();
+    const bool left = cnt[nc + 1] > cnt[nc];
     // placement by colour: the results of a colour touch disjoint dynamic bodies, so their order
-    // inside the colour does not matter and they are placed in parallel; the last colour's (run in
-    // island order by one thread) in order
-    for (int k = threadIdx.x; k < kMaxColors; k += blockDim.x) fill[k] = cnt[k];
+    // inside the colour does not matter and they are placed in parallel; the leftovers in order
+    for (int k = threadIdx.x; k < nc; k += blockDim.x) fill[k] = cnt[k];
     __syncthreads();
     for (int j = threadIdx.x; j < m; j += blockDim.x) {
         const int c = color[lo + j];
-        if (c < kMaxColors - 1) corder[lo + atomicAdd(&fill[c], 1)] = order[lo + j];
+        if (c < nc) corder[lo + atomicAdd(&fill[c], 1)] = order[lo + j];
     }
-    if (threadIdx.x == 0 && cnt[kMaxColors] > cnt[kMaxColors - 1]) {
-        int f = cnt[kMaxColors - 1];
+    if (threadIdx.x == 0 && left) {
+        int f = cnt[nc];
         for (int j = 0; j < m; j++)
-            if (color[lo + j] == kMaxColors - 1) corder[lo + f++] = order[lo + j];
+            if (color[lo + j] == nc) corder[lo + f++] = order[lo + j];
     }
     __syncthreads();
     for (int it = 0; it < iterations; it++) {
-        for (int c = 0; c < kMaxColors - 1; c++) {
-            const int a = cnt[c], b = cnt[c + 1];
-            if (a == b) continue;
-            for (int j = a + threadIdx.x; j < b; j += blockDim.x) iterate_item(corder[lo + j], res, J, B, rows, row_off);
+        for (int c = 0; c < nc; c++) {
+            for (int j = cnt[c] + threadIdx.x; j < cnt[c + 1]; j += blockDim.x) iterate_item(corder[lo + j], res, J, B, rows, row_off);
             __syncthreads();
         }
-        if (threadIdx.x == 0)
-            for (int j = cnt[kMaxColors - 1]; j < cnt[kMaxColors]; j++) iterate_item(corder[lo + j], res, J, B, rows, row_off);
-        __syncthreads();
+        if (left) {
+            if (threadIdx.x == 0)
+                for (int j = cnt[nc]; j < cnt[nc + 1]; j++) iterate_item(corder[lo + j], res, J, B, rows, row_off);
+            __syncthreads();
+        }
     }
 }
 
-// Serial-order mode for an island of up to kBigIsland items, in parallel and exact: levels in rounds
+// Serial-order mode for an island of min_len + 1 .. max_len items, in parallel and exact: levels in rounds
 // (an item takes level r in the round where it holds the smallest position among the unleveled
 // items on each of its dynamic bodies), so every item runs after all lower-position items that
 // share a dynamic body with it and before all higher-position ones: each body receives its updates
@@ -516,15 +517,15 @@ __global__ void k_isl_colored(const int* n_isl, const int* isl_off, const uint32
 // iteration runs the levels in turn with a block barrier between them.  An island that needs more
 // than kMaxLevels levels runs in order on one thread instead.
 constexpr int kMaxLevels = 256;
-constexpr int kLevelBlock = 256;
+constexpr int kLevelBlock = 256;   // the largest block of k_isl_levels
 template <class R>
 __global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res,
                                                             Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off, int iterations,
-                                                            int min_len, int* claim, int* level, uint32_t* lorder) {
+                                                            int min_len, int max_len, int* claim, int* level, uint32_t* lorder) {
     const int s = blockIdx.x;
     if (s >= *n_isl) return;
     const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
-    if (m <= min_len || m > kBigIsland) return;
+    if (m <= min_len || m > max_len) return;
     __shared__ int cnt[kMaxLevels + 1];
     __shared__ int remaining;
     for (int j = threadIdx.x; j < m; j += blockDim.x) level[lo + j] = -1;
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, co
         }
 }
 
-// ---- islands above kBigIsland results: k_isl_colored's colouring rule in grid-wide kernels (round
+// ---- islands above Tuning::big_island_items results: k_isl_colored's colouring rule in grid-wide kernels (round
 // c gives colour c to every uncoloured result that holds the smallest island position among the
 // uncoloured results on each of its dynamic bodies, so the colour classes follow the island order,
 // i.e. the reference's solve order, as closely as colouring allows), with up to kMaxColorsBig
@@ -591,10 +592,12 @@ __global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, co
 // bodies, so their order inside the colour does not matter; results left after kMaxColorsBig - 1
 // rounds run in island order in one thread.
 constexpr int kMaxColorsBig = 1024;
-// coloured mode: a big island whose exact level schedule needs at most this many levels runs it
-// (the reference's order); above, first-fit colours bound the colour count
-constexpr int kExactLevelsColored = 512;
-__global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big);
+__global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big, int big_items);
+constexpr int kWorkBuckets = 64;
+__global__ void k_isl_work(const int* n_isl, const int* isl_off, const uint32_t* order, const int* npts, int max_len, int* bucket_of,
+                           int* count);
+__global__ void k_isl_work_scan(int* count);
+__global__ void k_isl_work_place(const int* n_isl, const int* bucket_of, int* cursor, int* list);
 template <class R>
 __global__ void k_gc_mask_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, unsigned long long* mask) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;

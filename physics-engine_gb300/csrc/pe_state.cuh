@@ -110,6 +110,21 @@ struct StepParams {
     int iterations;
 };
 
+// Scheduling settings of the step: which kernel takes which work and with how many threads.  In
+// serial-order mode no setting changes a result bit.  In coloured mode none does either while every
+// island needs at most exact_levels_colored levels (above, a big island takes first-fit colours and
+// a block-path island runs its leftover items last): the autotuner leaves that one setting alone.
+struct Tuning {
+    int sat_heavy_cost = 200000;      // SAT pairs whose estimated work reaches this run on a block of warps
+    int small_island_items = 8;       // islands up to this many items run on one thread each
+    int big_island_items = 4096;      // islands above this many items are coloured and solved grid-wide
+    int color_block = 64;             // threads per island block, coloured mode
+    int level_block = 256;            // threads per island block, serial-order mode
+    int exact_levels_colored = 512;   // coloured mode keeps a big island's exact levels up to this many
+    int scene_sort_max = 2048;        // scenes up to this many bodies are sorted inside one block
+    int side_streams = 4;             // streams the narrowphase's per-class kernels are spread over
+};
+
 // device status word bits
 enum StatusBits { ST_PAIR_OVERFLOW = 1, ST_ROW_OVERFLOW = 2, ST_COLOR_OVERFLOW = 4 };
 

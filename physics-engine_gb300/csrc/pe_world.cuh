@@ -70,6 +70,7 @@ public:
     virtual void set_scenes(int n, const int* off) = 0;
     virtual void set_params(double dt, double gx, double gy, double gz, int iters) = 0;
     virtual void set_margin(double m) = 0;
+    virtual Tuning& tuning() = 0;
     virtual void step(int n, int mode) = 0;
     virtual void integrate() = 0;
     virtual int broadphase() = 0;
@@ -117,6 +118,7 @@ public:
     void set_scenes(int n, const int* off) override;
     void set_params(double dt, double gx, double gy, double gz, int iters) override;
     void set_margin(double m) override { margin_ = static_cast<R>(m); }
+    Tuning& tuning() override { return tun_; }
     void step(int n, int mode) override;
     void integrate() override;
     int broadphase() override;
@@ -275,6 +277,7 @@ private:
     double ms_[5] = {0, 0, 0, 0, 0};
     StepParams prm_{0.01, {0, -9.8, 0}, 10};
     R margin_ = 0;   // contact margin of the pair algorithms (PE_MARGIN, phys_general.h:45)
+    Tuning tun_;     // scheduling settings
     // shapes
     int S_ = 0;
     DBuf<int> stype_, shull_, hvbeg_, hvcnt_, hfbeg_, hfcnt_, hebeg_, hecnt_, hfoff_, hfidx_;
@@ -339,6 +342,7 @@ private:
     DBuf<unsigned long long> gc_mask_, gc_claim_;
     DBuf<double> xfer_;   // state transfers in the C ABI's layout
     DBuf<int> gc_left_;   // items left after each colouring round
+    DBuf<int> isl_work_;  // small islands by descending work: bucket per island, list, bucket counts
     DBuf<int> gc_level_;  // coloured mode: exact levels of a big island beside its first-fit colours
     void solve_big_islands(int NI, const uint32_t* order, bool exact);
     DBuf<R> rows_;

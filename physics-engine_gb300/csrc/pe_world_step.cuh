@@ -75,7 +75,7 @@ template <class R> int World<R>::broadphase() {
     count_.ensure(n + 1);
     int max_scene = 0;
     for (int s = 0; s < NS_; s++) max_scene = std::max(max_scene, h_scene_off_[s + 1] - h_scene_off_[s]);
-    if (max_scene <= kSceneSortMax) {   // every scene sorted inside one block
+    if (max_scene <= std::min(tun_.scene_sort_max, kSceneSortMax)) {   // every scene sorted inside one block
         launch_block(K_RADIX, NS_, kSceneSortBlock, k_bp_sort_scenes<R>, bodies(), (const int*)scene_axis_.p, (const int*)scene_off_.p,
                      val_[0].p);
         order_ = val_[0].p;
@@ -130,7 +130,8 @@ template <class R> void World<R>::narrowphase() {
     if (P > 0) {
         cls_count_.ensure(2 * PC_COUNT);
         PE_CK(cudaMemsetAsync(cls_count_.p, 0, 2 * PC_COUNT * sizeof(int), st_));
-        launch(K_NP_BUCKET, grid(P), k_np_classify<R>, P, pairs_.p, bodies(), shapes(), cls_.p, cls_count_.p);
+        launch(K_NP_BUCKET, grid(P), k_np_classify<R>, P, pairs_.p, bodies(), shapes(), cls_.p, cls_count_.p,
+               (long long)tun_.sat_heavy_cost);
         int cnt[PC_COUNT];
         PE_CK(cudaMemcpyAsync(cnt, cls_count_.p, sizeof(cnt), cudaMemcpyDeviceToHost, st_));
         PE_CK(cudaStreamSynchronize(st_));
@@ -171,14 +172,19 @@ template <class R> void World<R>::narrowphase() {
             const int lo = cur[c], hi = cur[c] + cnt[c];
             if (hi == lo) continue;
             const int g = grid(hi - lo);
-            use_stream(stream_of[c]);
+            use_stream(stream_of[c] % tun_.side_streams);
             switch (c) {
                 case PC_BOX_BOX: launch(K_NP, g, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_BOX_SPHERE: launch(K_NP, g, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_SPHERE_SPHERE: launch(K_NP, g, k_np_class<R, PC_SPHERE_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_SPHERE_CYL: launch(K_NP, g, k_np_class<R, PC_SPHERE_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_BOX_CYL: launch(K_NP, g, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_SPHERE_HULL: launch(K_NP, g, k_np_class<R, PC_SPHERE_HULL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_HULL: {
+                    const int w = sphere_hull_warps<R>();
+                    launch_block(K_NP, (hi - lo + w - 1) / w, 32 * w, k_np_sphere_hull<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,
+                                 pair_scene_off_.p, prev_res_off_.p);
+                    break;
+                }
                 case PC_CYL_HULL: {
                     const int w = cyl_hull_warps<R>();
                     launch_block(K_NP, (hi - lo + w - 1) / w, 32 * w, k_np_cyl_hull<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,
@@ -279,24 +285,35 @@ template <class R> void World<R>::solve(int mode) {
         n_islands_ = scan(isl_flag_.p, M + 1);
         launch(K_ISLAND, grid(M + 1), k_isl_offsets, M, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
         const int NI = n_islands_;
-        // islands of up to kSmallResults items: one thread each
-        launch_block(K_SI_SERIAL, (NI + 63) / 64, 64, k_isl_serial<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
-                     row_off_.p, prm_.iterations, 0, kSmallResults);
+        // islands of up to small_island_items items: one thread each, listed by descending work so
+        // that the longest serial chains start first
+        isl_work_.ensure((size_t)2 * NI + kWorkBuckets + 1);
+        int* bucket_of = isl_work_.p;
+        int* wlist = bucket_of + NI;
+        int* wcount = wlist + NI;
+        PE_CK(cudaMemsetAsync(wcount, 0, (kWorkBuckets + 1) * sizeof(int), st_));
+        launch(K_SI_SERIAL, grid(NI), k_isl_work, (const int*)isl_n_.p, (const int*)isl_off_.p, order, (const int*)results().npts,
+               tun_.small_island_items, bucket_of, wcount);
+        launch_block(K_SI_SERIAL, 1, kWorkBuckets, k_isl_work_scan, wcount);
+        launch(K_SI_SERIAL, grid(NI), k_isl_work_place, (const int*)isl_n_.p, (const int*)bucket_of, wcount, wlist);
+        launch_block(K_SI_SERIAL, (NI + 63) / 64, 64, k_isl_serial<R>, (const int*)wlist, (const int*)(wcount + kWorkBuckets),
+                     (const int*)isl_off_.p, order, results(), jt, bodies(), rows(), (const int*)row_off_.p, prm_.iterations);
         if (mode == 0) {
             // serial order, larger islands: the exact level schedule, a block per island up to
-            // kBigIsland items, grid-wide above
+            // big_island_items items, grid-wide above
             isl_corder_.ensure(M);
             color_.ensure(M + 1);
-            launch_block(K_SI_SERIAL, NI, kLevelBlock, k_isl_levels<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
-                         row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p);
+            launch_block(K_SI_SERIAL, NI, tun_.level_block, k_isl_levels<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
+                         row_off_.p, prm_.iterations, tun_.small_island_items, tun_.big_island_items, claim_.p, color_.p, isl_corder_.p);
             solve_big_islands(NI, order, true);
         } else {
             isl_corder_.ensure(M);
             color_.ensure(M + 1);
             ncol_.ensure(1);
             PE_CK(cudaMemsetAsync(ncol_.p, 0, sizeof(int), st_));
-            launch_block(K_SI_COLOR, NI, kColorBlock, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
-                         row_off_.p, prm_.iterations, kSmallResults, claim_.p, color_.p, isl_corder_.p, ncol_.p);
+            launch_block(K_SI_COLOR, NI, tun_.color_block, k_isl_colored<R>, isl_n_.p, isl_off_.p, order, results(), jt, bodies(), rows(),
+                         row_off_.p, prm_.iterations, tun_.small_island_items, tun_.big_island_items, claim_.p, color_.p, isl_corder_.p,
+                         ncol_.p);
             PE_CK(cudaMemcpyAsync(&n_colors_, ncol_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
             solve_big_islands(NI, order, false);
         }
@@ -305,13 +322,13 @@ template <class R> void World<R>::solve(int mode) {
     PE_CK(cudaGetLastError());
 }
 
-// islands above kBigIsland results (coloured mode): grid-wide colouring rounds, then one launch per
+// islands above big_island_items results: grid-wide colouring rounds, then one launch per
 // colour and iteration (see k_gc_*)
 template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* order, bool exact) {
     gc_big_.ensure(NI + 1);
     gc_n_.ensure(2);
     PE_CK(cudaMemsetAsync(gc_n_.p, 0, sizeof(int), st_));
-    launch(K_SI_COLOR, grid(NI), k_isl_big, (const int*)isl_n_.p, (const int*)isl_off_.p, gc_big_.p, gc_n_.p);
+    launch(K_SI_COLOR, grid(NI), k_isl_big, (const int*)isl_n_.p, (const int*)isl_off_.p, gc_big_.p, gc_n_.p, tun_.big_island_items);
     int nb = 0;
     PE_CK(cudaMemcpyAsync(&nb, gc_n_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
     PE_CK(cudaStreamSynchronize(st_));
@@ -366,7 +383,7 @@ template <class R> void World<R>::solve_big_islands(int NI, const uint32_t* orde
         // with long dependency chains (hundreds of levels), where one grid barrier per level and
         // iteration would dominate.
         int* col = color_.p;
-        if (!exact && ncol <= kExactLevelsColored) {
+        if (!exact && ncol <= tun_.exact_levels_colored) {
             int left_last = 0;
             PE_CK(cudaMemcpy(&left_last, gc_left_.p + ncol - 1, sizeof(int), cudaMemcpyDeviceToHost));
             if (left_last == 0) col = level;

@@ -50,6 +50,8 @@ def load(build_if_missing: bool = True):
         "pe_gpu_set_scenes": (I, [P, I, ip]),
         "pe_gpu_set_params": (I, [P, D, D, D, D, I]),
         "pe_gpu_set_contact_margin": (I, [P, D]),
+        "pe_gpu_get_tuning": (I, [P, C.c_void_p]), "pe_gpu_set_tuning": (I, [P, C.c_void_p]),
+        "pe_gpu_device_name": (I, [I, C.c_char_p, I]),
         "pe_gpu_step": (I, [P, I, I]),
         "pe_gpu_integrate": (I, [P]),
         "pe_gpu_broadphase": (I, [P, C.POINTER(I)]),
@@ -90,6 +92,29 @@ class _Config(C.Structure):
     _fields_ = [("real_bits", C.c_int), ("device", C.c_int)]
 
 
+TUNING_FIELDS = ("sat_heavy_cost", "small_island_items", "big_island_items", "color_block", "level_block",
+                 "exact_levels_colored", "scene_sort_max", "side_streams")
+
+
+class _Tuning(C.Structure):
+    _fields_ = [(f, C.c_int) for f in TUNING_FIELDS]
+
+
+def autotune_table_present(device=0, real_bits=32):
+    """Whether the autotuner stored settings for this GPU model and real type."""
+    from .autotune import load_table
+    return bool(load_table(device_name(device), real_bits))
+
+
+def device_name(device=0):
+    """The CUDA device's name (cudaGetDeviceProperties), e.g. "NVIDIA GB300"."""
+    buf = C.create_string_buffer(256)
+    rc = load().pe_gpu_device_name(int(device), buf, 256)
+    if rc != 0:
+        raise PeGpuError(f"pe_gpu_device_name failed ({rc})")
+    return buf.value.decode()
+
+
 def _f64(a, shape=None):
     a = np.ascontiguousarray(a, np.float64)
     return a.reshape(shape) if shape is not None else a
@@ -102,7 +127,7 @@ def _i32(a):
 class GpuWorld:
     """A device-resident world (or batch of independent scenes) on one GPU."""
 
-    def __init__(self, scene, real_bits=64, device=0, scenes=None, margin=0.0):
+    def __init__(self, scene, real_bits=64, device=0, scenes=None, margin=0.0, tuning=None):
         self.lib = load()
         self.h = C.c_void_p()
         cfg = _Config(real_bits, device)
@@ -135,8 +160,28 @@ class GpuWorld:
         self._ck(self.lib.pe_gpu_set_params(self.h, float(s.dt), *map(float, s.gravity), int(s.iterations)))
         if margin:
             self._ck(self.lib.pe_gpu_set_contact_margin(self.h, float(margin)))
+        if tuning is not None:   # a dict of scheduling settings, or "auto": the stored table for this GPU
+            if tuning == "auto":
+                from .autotune import load_table
+                tuning = load_table(device_name(device), real_bits)
+            if tuning:
+                self.set_tuning(**tuning)
         if scenes is not None:
             self.set_scenes(scenes)
+
+    def tuning(self):
+        t = _Tuning()
+        self._ck(self.lib.pe_gpu_get_tuning(self.h, C.byref(t)))
+        return {f: getattr(t, f) for f in TUNING_FIELDS}
+
+    def set_tuning(self, **kw):
+        """Scheduling settings (pe_gpu_tuning); unknown names are refused, unnamed ones keep their value."""
+        cur = self.tuning()
+        bad = set(kw) - set(TUNING_FIELDS)
+        if bad:
+            raise ValueError(f"unknown tuning settings {sorted(bad)}")
+        cur.update({k: int(v) for k, v in kw.items()})
+        self._ck(self.lib.pe_gpu_set_tuning(self.h, C.byref(_Tuning(**cur))))
 
     def _ck(self, rc):
         if rc != 0:
