@@ -354,7 +354,8 @@ def run_ours(args, rank, world, device):
                              step_frac=alg["step"] / (dev_ms / args.steps * 1e-3) / 1e9 / peak,
                              phases_ms={k: ph[k] / args.steps for k in PHASES}),
                e2e=dict(value=N * len(e2e_times) / sum(e2e_times), unit=UNIT, h2d_bytes_per_step=io_bytes,
-                        d2h_bytes_per_step=io_bytes),
+                        d2h_bytes_per_step=io_bytes, p50_step_ms=sorted(e2e_times)[len(e2e_times) // 2] * 1e3,
+                        max_step_ms=max(e2e_times) * 1e3),
                kernels={k: round(v[0], 4) for k, v in ks.items() if v[1]}, per_scene=per_scene)
     return res, scene, bits, offs
 

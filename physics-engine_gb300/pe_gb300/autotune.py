@@ -14,7 +14,7 @@ so far) on a reduced batched workload, every candidate over the same steps from 
 state, and keeps the fastest; save_table() stores the winners per GPU model and real type in
 tuning/<gpu>.json beside this module, where GpuWorld(..., tuning="auto") finds them.
 
-    python -m pe_gb300.autotune [--scenes 1024] [--steps 8] [--bits 32] [--mode colored]
+    python -m pe_gb300.autotune [--scenes 4096] [--steps 8] [--bits 32] [--mode colored]
 """
 import argparse
 import json
@@ -76,7 +76,7 @@ def _time_steps(g, snapshot, steps, mode, repeats):
     return best
 
 
-def tune(device=0, real_bits=32, mode=None, scenes=1024, steps=8, preroll=60, repeats=3, seed=4096, log=print):
+def tune(device=0, real_bits=32, mode=None, scenes=4096, steps=8, preroll=60, repeats=3, seed=4096, log=print):
     """Coordinate descent over CANDIDATES on `scenes` piles of the batched workload; returns
     (settings, detail) with the winners and every timing."""
     import pe_gb300 as pg
@@ -121,7 +121,7 @@ def main(argv=None):
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--bits", type=int, default=32, choices=(32, 64))
     ap.add_argument("--mode", default="colored", choices=("colored", "serial"))
-    ap.add_argument("--scenes", type=int, default=1024)
+    ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--out", default=None, help="write the table here instead of beside the module")
     a = ap.parse_args(argv)
