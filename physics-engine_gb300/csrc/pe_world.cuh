@@ -267,6 +267,7 @@ private:
     void check_status();
     void ev_begin(int phase);
     void ev_end(int phase);
+    void ev_collect();
     int grid(int n) const { return (n + kBlock - 1) / kBlock; }
     int grid_warps(int n) const { return (int)(((size_t)n * 32 + kBlock - 1) / kBlock); }   // one warp per item
 

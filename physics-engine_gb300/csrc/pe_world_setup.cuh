@@ -45,11 +45,16 @@ template <class R> void World<R>::ev_begin(int k) {
 }
 template <class R> void World<R>::ev_end(int k) {
     PE_CK(cudaEventRecord(ev_[k][1], st_));
-    PE_CK(cudaEventSynchronize(ev_[k][1]));
-    float ms = 0;
-    PE_CK(cudaEventElapsedTime(&ms, ev_[k][0], ev_[k][1]));
-    ms_[k] += ms;
     ev_open_[k] = false;
+}
+// the phases' durations, once the step's last event has completed (one wait per step)
+template <class R> void World<R>::ev_collect() {
+    PE_CK(cudaEventSynchronize(ev_[4][1]));
+    for (int k = 0; k < 5; k++) {
+        float ms = 0;
+        PE_CK(cudaEventElapsedTime(&ms, ev_[k][0], ev_[k][1]));
+        ms_[k] += ms;
+    }
 }
 template <class R> void World<R>::phase_times(double* ms, bool reset) {
     for (int k = 0; k < 5; k++) ms[k] = ms_[k];
@@ -63,6 +68,7 @@ template <class R> void World<R>::check_status() {
     int s = 0;
     PE_CK(cudaMemcpyAsync(&s, status_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
     PE_CK(cudaStreamSynchronize(st_));
+    ev_collect();
     if (s) {
         PE_CK(cudaMemsetAsync(status_.p, 0, sizeof(int), st_));
         throw std::runtime_error("device capacity overflow (status " + std::to_string(s) + ")");
