@@ -76,7 +76,7 @@ def _time_steps(g, snapshot, steps, mode, repeats):
     return best
 
 
-def tune(device=0, real_bits=32, mode=None, scenes=4096, steps=8, preroll=60, repeats=3, seed=4096, log=print):
+def tune(device=0, real_bits=32, mode=None, scenes=4096, steps=8, preroll=120, repeats=3, seed=4096, log=print):
     """Coordinate descent over CANDIDATES on `scenes` piles of the batched workload; returns
     (settings, detail) with the winners and every timing."""
     import pe_gb300 as pg
