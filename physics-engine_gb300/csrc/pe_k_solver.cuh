@@ -348,69 +348,20 @@ __global__ void k_isl_keys(int A, const int* active, Results<R> res, Bodies<R> B
 __global__ void k_isl_flags(int A, const uint64_t* key, int* flag);
 __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out);
 
-// serial order inside each island of min_len..max_len items, one thread per island.  An island of
-// contact results whose results touch at most two dynamic bodies (a body resting on static ones, a
-// pair of touching bodies: most small islands) keeps those bodies' temporary velocities, inverse
-// masses and inertias in registers through all iterations and writes them back once; the rows are
-// applied in the same order with the same arithmetic, so the velocities are the same bit for bit.
-// Other islands go through the body arrays item by item.
-// The islands come from `list` (the small islands by descending work, k_isl_work*), so the longest
-// serial chains start in the first wave instead of holding the last one.
+// serial order inside each island of up to max_len items, one thread per island, islands in their
+// natural order (the island of the smallest body first): consecutive threads take neighbouring
+// islands, whose bodies and rows lie close in memory.  (Keeping an island's bodies in registers
+// through the iterations, or ordering islands by descending work, both measured slower: the
+// first lowers occupancy, the second scatters the threads' memory accesses.)
 template <class R>
-__global__ void __launch_bounds__(64) k_isl_serial(const int* list, const int* n_list, const int* isl_off, const uint32_t* order,
-                                                   Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off,
-                                                   int iterations) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= *n_list) return;
-    const int s = list[t];
+__global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
+                             Rows<R> rows, const int* row_off, int iterations, int max_len) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *n_isl) return;
     const int lo = isl_off[s], hi = isl_off[s + 1];
-    int d0 = -1, d1 = -1;   // the island's dynamic bodies when there are at most two
-    bool two = true;
-    for (int k = lo; k < hi && two; k++) {
-        const uint32_t item = order[k];
-        if (item & kJointItem) { two = false; break; }
-        const int q[2] = {res.a[item], res.b[item]};
-        for (int e = 0; e < 2; e++) {
-            const int b = q[e];
-            if (B.flags[b] & BF_KINEMATIC) continue;
-            if (b == d0 || b == d1) continue;
-            if (d0 < 0) d0 = b;
-            else if (d1 < 0) d1 = b;
-            else two = false;
-        }
-    }
-    if (!two || d0 < 0) {
-        for (int it = 0; it < iterations; it++)
-            for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
-        return;
-    }
-    V3<R> v0 = B.vec(TVX, d0), w0 = B.vec(TWX, d0), v1, w1;
-    const R m0 = B.at(INVM, d0);
-    const M3<R> I0 = B.mat(I00, d0);
-    R m1 = 0;
-    M3<R> I1;
-    if (d1 >= 0) { v1 = B.vec(TVX, d1); w1 = B.vec(TWX, d1); m1 = B.at(INVM, d1); I1 = B.mat(I00, d1); }
+    if (hi - lo > max_len) return;
     for (int it = 0; it < iterations; it++)
-        for (int k = lo; k < hi; k++) {
-            const int p = (int)order[k];
-            const int ia = res.a[p], ib = res.b[p], r0 = row_off[p], np = res.npts[p];
-            if (ia == d0 && ib == d1) {
-                si_result_rows(rows, r0, np, false, false, v0, w0, v1, w1, m0, m1, I0, I1);
-            } else if (ia == d1 && ib == d0) {
-                si_result_rows(rows, r0, np, false, false, v1, w1, v0, w0, m1, m0, I1, I0);
-            } else {   // one dynamic body against a kinematic one, whose temporary velocity never changes
-                const int kin = (ia == d0 || ia == d1) ? ib : ia;
-                V3<R> kv = B.vec(TVX, kin), kw = B.vec(TWX, kin);
-                const R km = B.at(INVM, kin);
-                const M3<R> kI = B.mat(I00, kin);
-                if (ia == d0) si_result_rows(rows, r0, np, false, true, v0, w0, kv, kw, m0, km, I0, kI);
-                else if (ia == d1) si_result_rows(rows, r0, np, false, true, v1, w1, kv, kw, m1, km, I1, kI);
-                else if (ib == d0) si_result_rows(rows, r0, np, true, false, kv, kw, v0, w0, km, m0, kI, I0);
-                else si_result_rows(rows, r0, np, true, false, kv, kw, v1, w1, km, m1, kI, I1);
-            }
-        }
-    B.set_vec(TVX, d0, v0); B.set_vec(TWX, d0, w0);
-    if (d1 >= 0) { B.set_vec(TVX, d1, v1); B.set_vec(TWX, d1, w1); }
+        for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
 }
 
 
@@ -593,11 +544,6 @@ __global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, co
 // rounds run in island order in one thread.
 constexpr int kMaxColorsBig = 1024;
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big, int big_items);
-constexpr int kWorkBuckets = 64;
-__global__ void k_isl_work(const int* n_isl, const int* isl_off, const uint32_t* order, const int* npts, int max_len, int* bucket_of,
-                           int* count);
-__global__ void k_isl_work_scan(int* count);
-__global__ void k_isl_work_place(const int* n_isl, const int* bucket_of, int* cursor, int* list);
 template <class R>
 __global__ void k_gc_mask_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, unsigned long long* mask) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;

@@ -177,45 +177,6 @@ __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* 
     if (k == A) { isl_off[scan[A]] = A; *n_isl_out = scan[A]; }
 }
 
-// Small islands (max_len items or fewer) in buckets of descending work: bucket kWorkBuckets - 1 - rows
-// (rows capped), so that a walk over the buckets lists the islands with the longest serial chains
-// first.  Other islands get no bucket.
-__global__ void k_isl_work(const int* n_isl, const int* isl_off, const uint32_t* order, const int* npts, int max_len, int* bucket_of,
-                           int* count) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= *n_isl) return;
-    const int lo = isl_off[s], hi = isl_off[s + 1];
-    if (hi - lo > max_len) { bucket_of[s] = -1; return; }
-    int rows = 0;
-    for (int k = lo; k < hi; k++) {
-        const uint32_t item = order[k];
-        rows += (item & 0x80000000u) ? 3 : npts[item];   // a joint counts as three rows
-    }
-    const int b = kWorkBuckets - 1 - (rows < kWorkBuckets - 1 ? rows : kWorkBuckets - 1);
-    bucket_of[s] = b;
-    atomicAdd(&count[b], 1);
-}
-// exclusive scan of the bucket counts (one block of kWorkBuckets threads); count[kWorkBuckets] = total
-__global__ void k_isl_work_scan(int* count) {
-    __shared__ int c[kWorkBuckets];
-    const int t = threadIdx.x;
-    c[t] = count[t];
-    __syncthreads();
-    if (t == 0) {
-        int run = 0;
-        for (int b = 0; b < kWorkBuckets; b++) { const int v = c[b]; c[b] = run; run += v; }
-        count[kWorkBuckets] = run;
-    }
-    __syncthreads();
-    count[t] = c[t];
-}
-__global__ void k_isl_work_place(const int* n_isl, const int* bucket_of, int* cursor, int* list) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= *n_isl) return;
-    const int b = bucket_of[s];
-    if (b >= 0) list[atomicAdd(&cursor[b], 1)] = s;
-}
-
 // islands with more than big_items results
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big, int big_items) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;

@@ -343,7 +343,6 @@ private:
     DBuf<unsigned long long> gc_mask_, gc_claim_;
     DBuf<double> xfer_;   // state transfers in the C ABI's layout
     DBuf<int> gc_left_;   // items left after each colouring round
-    DBuf<int> isl_work_;  // small islands by descending work: bucket per island, list, bucket counts
     DBuf<int> gc_level_;  // coloured mode: exact levels of a big island beside its first-fit colours
     void solve_big_islands(int NI, const uint32_t* order, bool exact);
     DBuf<R> rows_;

@@ -285,19 +285,9 @@ template <class R> void World<R>::solve(int mode) {
         n_islands_ = scan(isl_flag_.p, M + 1);
         launch(K_ISLAND, grid(M + 1), k_isl_offsets, M, skey, isl_flag_.p, isl_off_.p, isl_n_.p);
         const int NI = n_islands_;
-        // islands of up to small_island_items items: one thread each, listed by descending work so
-        // that the longest serial chains start first
-        isl_work_.ensure((size_t)2 * NI + kWorkBuckets + 1);
-        int* bucket_of = isl_work_.p;
-        int* wlist = bucket_of + NI;
-        int* wcount = wlist + NI;
-        PE_CK(cudaMemsetAsync(wcount, 0, (kWorkBuckets + 1) * sizeof(int), st_));
-        launch(K_SI_SERIAL, grid(NI), k_isl_work, (const int*)isl_n_.p, (const int*)isl_off_.p, order, (const int*)results().npts,
-               tun_.small_island_items, bucket_of, wcount);
-        launch_block(K_SI_SERIAL, 1, kWorkBuckets, k_isl_work_scan, wcount);
-        launch(K_SI_SERIAL, grid(NI), k_isl_work_place, (const int*)isl_n_.p, (const int*)bucket_of, wcount, wlist);
-        launch_block(K_SI_SERIAL, (NI + 63) / 64, 64, k_isl_serial<R>, (const int*)wlist, (const int*)(wcount + kWorkBuckets),
-                     (const int*)isl_off_.p, order, results(), jt, bodies(), rows(), (const int*)row_off_.p, prm_.iterations);
+        // islands of up to small_island_items items: one thread each
+        launch(K_SI_SERIAL, grid(NI), k_isl_serial<R>, (const int*)isl_n_.p, (const int*)isl_off_.p, order, results(), jt, bodies(),
+               rows(), (const int*)row_off_.p, prm_.iterations, tun_.small_island_items);
         if (mode == 0) {
             // serial order, larger islands: the exact level schedule, a block per island up to
             // big_island_items items, grid-wide above
