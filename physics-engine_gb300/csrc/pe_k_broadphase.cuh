@@ -9,6 +9,7 @@ namespace pe {
 __global__ void k_scan_tiles(int* data, int n, int* aux);
 __global__ void k_scan_aux(int* aux, int m, int* total);
 __global__ void k_scan_add(int* data, int n, const int* aux);
+constexpr int kSmallScanTiles = 16;   // scans of up to 16 tiles of 1024 run in one block (k_scan_aux in place)
 
 // ===================================================================== radix sort
 // Sort (key, value) pairs by a 64-bit key and then, more significantly, by a 32-bit
@@ -16,6 +17,9 @@ __global__ void k_scan_add(int* data, int n, const int* aux);
 constexpr int kRadixItems = 16;                      // items per thread per tile
 constexpr int kRadixTile = kBlock * kRadixItems;     // 4096 items per tile
 __global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n, int shift, int use2, int* hist, int n_tiles);
+// a sort of n <= kSceneSortMax (key, value) pairs inside one block (bitonic over (key, position)): the
+// order of the stable LSD radix sort, in one launch instead of five per pass, for small inputs
+__global__ void k_sort_pairs_block(const uint64_t* key, const uint32_t* val, int n, uint64_t* key_out, uint32_t* val_out);
 __global__ void k_radix_scatter(const uint64_t* key_in, const uint32_t* key2_in, const uint32_t* val_in, uint64_t* key_out,
                                 uint32_t* key2_out, uint32_t* val_out, int n, int shift, int use2, const int* hist, int n_tiles);
 

@@ -67,6 +67,33 @@ __global__ void k_scan_add(int* data, int n, const int* aux) {
     for (int k = 0; k < kScanItems; k++) if (base + k < n) data[base + k] += add;
 }
 
+// ---------------------------------------------------------------- small sorts
+__global__ void __launch_bounds__(kSceneSortBlock) k_sort_pairs_block(const uint64_t* key, const uint32_t* val, int n, uint64_t* key_out,
+                                                                     uint32_t* val_out) {
+    __shared__ uint64_t k[kSceneSortMax];
+    __shared__ uint32_t pos[kSceneSortMax];
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        if (i < n) { k[i] = key[i]; pos[i] = (uint32_t)i; }
+        else { k[i] = ~0ull; pos[i] = 0xffffffffu; }   // padding sorts last
+    }
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < P / 2; t += blockDim.x) {
+                const int i = 2 * t - (t & (stride - 1)), j = i + stride;
+                const bool up = (i & size) == 0;
+                const uint64_t ki = k[i], kj = k[j];
+                const uint32_t pi = pos[i], pj = pos[j];
+                const bool gt = ki > kj || (ki == kj && pi > pj);
+                if (gt == up) { k[i] = kj; k[j] = ki; pos[i] = pj; pos[j] = pi; }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { key_out[i] = k[i]; val_out[i] = val[pos[i]]; }
+}
+
 // ---------------------------------------------------------------- radix sort
 __device__ __forceinline__ int digit_of(const uint64_t* key, const uint32_t* key2, int i, int shift, int use2) {
     return use2 ? (int)((key2[i] >> shift) & 0xffu) : (int)((key[i] >> shift) & 0xffull);

@@ -8,10 +8,14 @@ namespace pe {
 // ------------------------------------------------------------------ utilities
 template <class R> int World<R>::scan(int* data, int n) {
     const int tiles = (n + 1023) / 1024;
-    aux_.ensure(tiles + 1);
-    launch(K_SCAN, tiles, k_scan_tiles, data, n, aux_.p);
-    launch(K_SCAN, 1, k_scan_aux, aux_.p, tiles, total_.p);
-    launch(K_SCAN, tiles, k_scan_add, data, n, aux_.p);
+    if (tiles <= kSmallScanTiles) {   // small: one block scans in place (one launch instead of three)
+        launch(K_SCAN, 1, k_scan_aux, data, n, total_.p);
+    } else {
+        aux_.ensure(tiles + 1);
+        launch(K_SCAN, tiles, k_scan_tiles, data, n, aux_.p);
+        launch(K_SCAN, 1, k_scan_aux, aux_.p, tiles, total_.p);
+        launch(K_SCAN, tiles, k_scan_add, data, n, aux_.p);
+    }
     int tot = 0;
     PE_CK(cudaMemcpyAsync(&tot, total_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
     PE_CK(cudaStreamSynchronize(st_));
@@ -23,6 +27,11 @@ template <class R> void World<R>::radix_sort(int n, int scene_passes) {
 }
 
 template <class R> int World<R>::radix_sort_keys(int n, int key_passes, int scene_passes) {
+    if (scene_passes == 0 && n <= kSceneSortMax) {   // small: one block, one launch
+        launch_block(K_RADIX, 1, kSceneSortBlock, k_sort_pairs_block, (const uint64_t*)key_[0].p, (const uint32_t*)val_[0].p, n,
+                     key_[1].p, val_[1].p);
+        return 1;
+    }
     const int tiles = (n + kRadixTile - 1) / kRadixTile;
     hist_.ensure((size_t)256 * tiles + 1);
     aux_.ensure((256 * tiles + 1023) / 1024 + 1);
@@ -31,9 +40,13 @@ template <class R> int World<R>::radix_sort_keys(int n, int key_passes, int scen
         launch(K_RADIX, tiles, k_radix_hist, key_[cur].p, key2_[cur].p, n, shift, use2, hist_.p, tiles);
         const int m = 256 * tiles;
         const int st = (m + 1023) / 1024;
-        launch(K_SCAN, st, k_scan_tiles, hist_.p, m, aux_.p);
-        launch(K_SCAN, 1, k_scan_aux, aux_.p, st, total_.p);
-        launch(K_SCAN, st, k_scan_add, hist_.p, m, aux_.p);
+        if (st <= kSmallScanTiles) {
+            launch(K_SCAN, 1, k_scan_aux, hist_.p, m, total_.p);
+        } else {
+            launch(K_SCAN, st, k_scan_tiles, hist_.p, m, aux_.p);
+            launch(K_SCAN, 1, k_scan_aux, aux_.p, st, total_.p);
+            launch(K_SCAN, st, k_scan_add, hist_.p, m, aux_.p);
+        }
         launch(K_RADIX, tiles, k_radix_scatter, key_[cur].p, key2_[cur].p, val_[cur].p, key_[cur ^ 1].p, key2_[cur ^ 1].p,
                                                   val_[cur ^ 1].p, n, shift, use2, hist_.p, tiles);
         cur ^= 1;
@@ -94,23 +107,25 @@ template <class R> int World<R>::broadphase() {
     if (n_ign_ > 0) { ign.off = ign_off_.p; ign.ids = ign_ids_.p; ign.order = order_; }
     launch(K_BP_SWEEP, grid_warps(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p,
            bp_big_.p, bp_nbig_.p, ign);
-    // crowded positions: windows in chunks of one block each (at most kMaxChunks per position)
+    // crowded positions: windows in chunks of one block each (at most kMaxChunks per position); a
+    // window holds at most n - 1 candidates, so with at most kBigWindow bodies there are none
+    const bool crowded = n > kBigWindow;
     bp_wend_.ensure(n + 1); bp_csize_.ensure(n + 1); bp_nch_.ensure(n + 1); bp_choff_.ensure(n + 1); bp_ctot_.ensure(1);
     bp_ccount_.ensure((size_t)kMaxChunks * n + 1); bp_cpref_.ensure((size_t)kMaxChunks * n + 1);
-    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_big_windows<R>, n, (const int*)scene_axis_.p, (const int*)scene_off_.p, (const R*)smn_.p,
+    if (crowded) launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_big_windows<R>, n, (const int*)scene_axis_.p, (const int*)scene_off_.p, (const R*)smn_.p,
            (const R*)smx_.p, (const int*)ssc_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p, bp_wend_.p, bp_csize_.p, bp_nch_.p);
-    launch_block(K_BP_SWEEP, 1, 32, k_bp_chunk_offsets, (const int*)bp_nbig_.p, (const int*)bp_nch_.p, bp_choff_.p, bp_ctot_.p);
-    launch(K_BP_SWEEP, 2 * kBigSweepBlocks, k_bp_count_chunks<R>, n, (const R*)smn_.p, (const R*)smx_.p, (const int*)sflag_.p,
+    if (crowded) launch_block(K_BP_SWEEP, 1, 32, k_bp_chunk_offsets, (const int*)bp_nbig_.p, (const int*)bp_nch_.p, bp_choff_.p, bp_ctot_.p);
+    if (crowded) launch(K_BP_SWEEP, 2 * kBigSweepBlocks, k_bp_count_chunks<R>, n, (const R*)smn_.p, (const R*)smx_.p, (const int*)sflag_.p,
            (const int*)bp_big_.p, (const int*)bp_nbig_.p, (const int*)bp_wend_.p, (const int*)bp_csize_.p, (const int*)bp_choff_.p,
            (const int*)bp_ctot_.p, bp_ccount_.p, ign);
-    launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_chunk_sums, (const int*)bp_big_.p, (const int*)bp_nbig_.p, (const int*)bp_choff_.p,
+    if (crowded) launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_chunk_sums, (const int*)bp_big_.p, (const int*)bp_nbig_.p, (const int*)bp_choff_.p,
            (const int*)bp_nch_.p, (const int*)bp_ccount_.p, bp_cpref_.p, count_.p);
     PE_CK(cudaMemsetAsync(count_.p + n, 0, sizeof(int), st_));
     const int P = scan(count_.p, n + 1);
     ensure_pair_capacity(P);
     launch(K_BP_SWEEP, grid_warps(n), k_bp_write<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, order_, count_.p, bp_stage_.p,
            pairs_.p, pair_cap_, status_.p, ign);
-    launch(K_BP_SWEEP, 2 * kBigSweepBlocks, k_bp_write_chunks<R>, n, (const R*)smn_.p, (const R*)smx_.p, (const int*)sflag_.p,
+    if (crowded) launch(K_BP_SWEEP, 2 * kBigSweepBlocks, k_bp_write_chunks<R>, n, (const R*)smn_.p, (const R*)smx_.p, (const int*)sflag_.p,
            (const uint32_t*)order_, (const int*)count_.p, (const int*)bp_big_.p, (const int*)bp_nbig_.p, (const int*)bp_wend_.p,
            (const int*)bp_csize_.p, (const int*)bp_choff_.p, (const int*)bp_ctot_.p, (const int*)bp_cpref_.p, pairs_.p, pair_cap_,
            status_.p, ign);
