@@ -108,8 +108,8 @@ template <class R> int World<R>::broadphase() {
     launch(K_BP_SWEEP, grid_warps(n), k_bp_count<R>, n, scene_axis_.p, smn_.p, smx_.p, sflag_.p, ssc_.p, count_.p, bp_stage_.p,
            bp_big_.p, bp_nbig_.p, ign);
     // crowded positions: windows in chunks of one block each (at most kMaxChunks per position); a
-    // window holds at most n - 1 candidates, so with at most kBigWindow bodies there are none
-    const bool crowded = n > kBigWindow;
+    // window holds at most the scene's other bodies, so scenes of at most kBigWindow bodies have none
+    const bool crowded = max_scene > kBigWindow;
     bp_wend_.ensure(n + 1); bp_csize_.ensure(n + 1); bp_nch_.ensure(n + 1); bp_choff_.ensure(n + 1); bp_ctot_.ensure(1);
     bp_ccount_.ensure((size_t)kMaxChunks * n + 1); bp_cpref_.ensure((size_t)kMaxChunks * n + 1);
     if (crowded) launch(K_BP_SWEEP, kBigSweepBlocks, k_bp_big_windows<R>, n, (const int*)scene_axis_.p, (const int*)scene_off_.p, (const R*)smn_.p,
@@ -187,13 +187,14 @@ template <class R> void World<R>::narrowphase() {
             const int lo = cur[c], hi = cur[c] + cnt[c];
             if (hi == lo) continue;
             const int g = grid(hi - lo);
+            const int cb = np_cache_block<R>(), gc = (hi - lo + cb - 1) / cb;   // thread-per-pair kernels with caches in shared memory
             use_stream(stream_of[c] % tun_.side_streams);
             switch (c) {
-                case PC_BOX_BOX: launch(K_NP, g, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_BOX_SPHERE: launch(K_NP, g, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_SPHERE_SPHERE: launch(K_NP, g, k_np_class<R, PC_SPHERE_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_SPHERE_CYL: launch(K_NP, g, k_np_class<R, PC_SPHERE_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_BOX_CYL: launch(K_NP, g, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_BOX: launch_block(K_NP, gc, cb, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_SPHERE: launch_block(K_NP, gc, cb, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_SPHERE: launch_block(K_NP, gc, cb, k_np_class<R, PC_SPHERE_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_CYL: launch_block(K_NP, gc, cb, k_np_class<R, PC_SPHERE_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_CYL: launch_block(K_NP, gc, cb, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_SPHERE_HULL: {
                     const int w = sphere_hull_warps<R>();
                     launch_block(K_NP, (hi - lo + w - 1) / w, 32 * w, k_np_sphere_hull<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,
@@ -217,7 +218,7 @@ template <class R> void World<R>::narrowphase() {
                               : c == PC_CONVEX_HULL_HULL ? k_np_sat<R, 1, ST_HULL, ST_HULL>
                               : k_np_sat<R, 1, ST_CYLINDER, ST_CYLINDER>;
                     launch_smem(K_NP_SAT, gb, bs, smem, kern, lo, hi, order_np_.p, pairs_.p, bd, sh, sat_out_.p);
-                    launch(K_NP_SAT, grid(hi - lo), k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                    launch_block(K_NP_SAT, gc, cb, k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
                            prev_res_off_.p, (const R*)sat_out_.p);
                     break;
                 }
@@ -225,7 +226,7 @@ template <class R> void World<R>::narrowphase() {
                     const size_t smem = (size_t)sat_group_reals<R>(kSatGroup) * sizeof(R);
                     launch_smem(K_NP_SAT, hi - lo, 32 * kSatGroup, smem, k_np_sat<R, kSatGroup, -1, -1>, lo, hi, order_np_.p, pairs_.p, bd,
                                 sh, sat_out_.p);
-                    launch(K_NP_SAT, grid(hi - lo), k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                    launch_block(K_NP_SAT, gc, cb, k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
                            prev_res_off_.p, (const R*)sat_out_.p);
                     break;
                 }
@@ -233,7 +234,7 @@ template <class R> void World<R>::narrowphase() {
                     launch(K_NP, g, k_np_compound<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
                     break;
                 case PC_CONCAVE:
-                    launch(K_NP, g, k_np_class<R, PC_CONCAVE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                    launch_block(K_NP, gc, cb, k_np_class<R, PC_CONCAVE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
                            prev_res_off_.p);
                     break;
                 default:   // PC_CONVEX_BIG
