@@ -352,7 +352,12 @@ def run_ours(args, rank, world, device):
                              traffic=traffic, algorithmic_bytes=dom_bytes, phase_ms=dom_ms, hull_vertices_in_pairs=hull_verts,
                              peak_source=peak_kind, step_bytes=alg["step"],
                              step_frac=alg["step"] / (dev_ms / args.steps * 1e-3) / 1e9 / peak,
-                             phases_ms={k: ph[k] / args.steps for k in PHASES}),
+                             phases_ms={k: ph[k] / args.steps for k in PHASES},
+                             phases_algorithmic_bytes={k: alg[k] for k in PHASES},
+                             phases_dram_bytes_ncu={k: ncu_traffic(k) for k in PHASES}
+                             if args.workload == "batched" and args.scenes == 4096 else None,
+                             traffic_source="profiles/launches_batched_dram.md (ncu, one step of this workload)"
+                             if traffic is not None else None),
                e2e=dict(value=N * len(e2e_times) / sum(e2e_times), unit=UNIT, h2d_bytes_per_step=io_bytes,
                         d2h_bytes_per_step=io_bytes, p50_step_ms=sorted(e2e_times)[len(e2e_times) // 2] * 1e3,
                         max_step_ms=max(e2e_times) * 1e3),
