@@ -1,7 +1,6 @@
 // Kernels of the rigid-body step, part 3: narrowphase classification, bucketing and the
 // closed-form pair kernels.
 #pragma once
-#include <new>
 #include "pe_k_broadphase.cuh"
 
 namespace pe {
@@ -112,25 +111,14 @@ __device__ __forceinline__ void np_finish(int p, const int2* pairs, const Bodies
     }
 }
 
-// The thread-per-pair kernels keep each thread's contact cache (Cache, about 0.5 KB in FP32) in
-// shared memory: in local memory, tens of warps' caches per SM overflowed L1 and went to L2 and DRAM
-// on every slot update.  np_cache_block threads per block keep a block's caches within the 48 KB of
-// static shared memory.
-template <class R> constexpr int np_cache_block() { return sizeof(R) == 4 ? 64 : 32; }
-template <class R> __device__ __forceinline__ Cache<R>& np_cache_slot(unsigned char* mem) {
-    return *new (mem + threadIdx.x * sizeof(Cache<R>)) Cache<R>();
-}
-
 // one thread per pair of one algorithm class; `order[lo..hi)` holds that class's pairs
 template <class R, int CLS>
-__global__ void __launch_bounds__(np_cache_block<R>()) k_np_class(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B,
-                                                                 ShapeTable<R> S, Results<R> res, const int* pair_scene_off,
-                                                                 const int* prev_off) {
-    __shared__ __align__(16) unsigned char cache_mem[np_cache_block<R>() * sizeof(Cache<R>)];
+__global__ void k_np_class(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                           const int* pair_scene_off, const int* prev_off) {
     const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= hi) return;
     const int p = order[t];
-    Cache<R>& cache = np_cache_slot<R>(cache_mem);
+    Cache<R> cache;
     Pair<R> pr;
     np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
     collide(pr, CLS);

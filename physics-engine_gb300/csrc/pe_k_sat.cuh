@@ -700,14 +700,12 @@ k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, Shape
 // recorded face-stage and edge-stage points are added and the faces clipped, in the reference's
 // order, and the result is sorted and written out
 template <class R>
-__global__ void __launch_bounds__(np_cache_block<R>()) k_np_sat_finish(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B,
-                                                                      ShapeTable<R> S, Results<R> res, const int* pair_scene_off,
-                                                                      const int* prev_off, const R* sat_out) {
-    __shared__ __align__(16) unsigned char cache_mem[np_cache_block<R>() * sizeof(Cache<R>)];
+__global__ void k_np_sat_finish(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                                const int* pair_scene_off, const int* prev_off, const R* sat_out) {
     const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= hi) return;
     const int p = order[t];
-    Cache<R>& cache = np_cache_slot<R>(cache_mem);
+    Cache<R> cache;
     Pair<R> pr;
     np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
     const R* o = sat_out + (size_t)t * kSatOut;

@@ -187,14 +187,13 @@ template <class R> void World<R>::narrowphase() {
             const int lo = cur[c], hi = cur[c] + cnt[c];
             if (hi == lo) continue;
             const int g = grid(hi - lo);
-            const int cb = np_cache_block<R>(), gc = (hi - lo + cb - 1) / cb;   // thread-per-pair kernels with caches in shared memory
             use_stream(stream_of[c] % tun_.side_streams);
             switch (c) {
-                case PC_BOX_BOX: launch_block(K_NP, gc, cb, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_BOX_SPHERE: launch_block(K_NP, gc, cb, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_SPHERE_SPHERE: launch_block(K_NP, gc, cb, k_np_class<R, PC_SPHERE_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_SPHERE_CYL: launch_block(K_NP, gc, cb, k_np_class<R, PC_SPHERE_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
-                case PC_BOX_CYL: launch_block(K_NP, gc, cb, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_BOX: launch(K_NP, g, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_SPHERE: launch(K_NP, g, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_SPHERE: launch(K_NP, g, k_np_class<R, PC_SPHERE_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_SPHERE_CYL: launch(K_NP, g, k_np_class<R, PC_SPHERE_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
+                case PC_BOX_CYL: launch(K_NP, g, k_np_class<R, PC_BOX_CYL>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_SPHERE_HULL: {
                     const int w = sphere_hull_warps<R>();
                     launch_block(K_NP, (hi - lo + w - 1) / w, 32 * w, k_np_sphere_hull<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs,
@@ -218,7 +217,7 @@ template <class R> void World<R>::narrowphase() {
                               : c == PC_CONVEX_HULL_HULL ? k_np_sat<R, 1, ST_HULL, ST_HULL>
                               : k_np_sat<R, 1, ST_CYLINDER, ST_CYLINDER>;
                     launch_smem(K_NP_SAT, gb, bs, smem, kern, lo, hi, order_np_.p, pairs_.p, bd, sh, sat_out_.p);
-                    launch_block(K_NP_SAT, gc, cb, k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                    launch(K_NP_SAT, grid(hi - lo), k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
                            prev_res_off_.p, (const R*)sat_out_.p);
                     break;
                 }
@@ -226,7 +225,7 @@ template <class R> void World<R>::narrowphase() {
                     const size_t smem = (size_t)sat_group_reals<R>(kSatGroup) * sizeof(R);
                     launch_smem(K_NP_SAT, hi - lo, 32 * kSatGroup, smem, k_np_sat<R, kSatGroup, -1, -1>, lo, hi, order_np_.p, pairs_.p, bd,
                                 sh, sat_out_.p);
-                    launch_block(K_NP_SAT, gc, cb, k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                    launch(K_NP_SAT, grid(hi - lo), k_np_sat_finish<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
                            prev_res_off_.p, (const R*)sat_out_.p);
                     break;
                 }
@@ -234,7 +233,7 @@ template <class R> void World<R>::narrowphase() {
                     launch(K_NP, g, k_np_compound<R>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p);
                     break;
                 case PC_CONCAVE:
-                    launch_block(K_NP, gc, cb, k_np_class<R, PC_CONCAVE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
+                    launch(K_NP, g, k_np_class<R, PC_CONCAVE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p,
                            prev_res_off_.p);
                     break;
                 default:   // PC_CONVEX_BIG
