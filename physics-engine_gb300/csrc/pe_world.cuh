@@ -259,6 +259,11 @@ private:
     Results<R> results();
     Rows<R> rows();
     int scan(int* data, int n);   // exclusive scan in place; returns the total (synchronises)
+    void scan_async(int* data, int n, int* total);   // exclusive scan in place, total to device memory
+    DBuf<int> rows_total_;
+    int* h_rows_ = nullptr;       // pinned: the last solve's row total, read at the step's end
+    bool rows_pending_ = false;
+    void take_rows() { if (rows_pending_) { PE_CK(cudaStreamSynchronize(st_)); n_rows_ = *h_rows_; rows_pending_ = false; } }
     R* staging(size_t n);         // pinned host buffer of at least n reals
     R* stage_ = nullptr;
     size_t stage_n_ = 0;

@@ -22,12 +22,15 @@ template <class R> World<R>::World(int device) : dev_(device) {
     status_.ensure(1);
     PE_CK(cudaMemset(status_.p, 0, sizeof(int)));
     total_.ensure(1);
+    rows_total_.ensure(1);
+    PE_CK(cudaMallocHost(&h_rows_, sizeof(int)));
     set_scenes(1, nullptr);
 }
 
 template <class R> World<R>::~World() {
     if (st_) cudaStreamSynchronize(st_);
     if (stage_) cudaFreeHost(stage_);
+    if (h_rows_) cudaFreeHost(h_rows_);
     for (auto& q : pending_) { cudaEventDestroy(q.e0); cudaEventDestroy(q.e1); }
     for (auto e : ev_pool_) cudaEventDestroy(e);
     for (auto& e : ev_) { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
@@ -61,6 +64,7 @@ template <class R> void World<R>::phase_times(double* ms, bool reset) {
     if (reset) for (double& m : ms_) m = 0;
 }
 template <class R> void World<R>::last_counts(int* c) {
+    take_rows();
     c[0] = P_; c[1] = n_active_; c[2] = n_rows_; c[3] = n_colors_; c[4] = (int)last_step_launches_; c[5] = n_islands_;
 }
 
@@ -69,6 +73,7 @@ template <class R> void World<R>::check_status() {
     PE_CK(cudaMemcpyAsync(&s, status_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
     PE_CK(cudaStreamSynchronize(st_));
     ev_collect();
+    take_rows();
     if (s) {
         PE_CK(cudaMemsetAsync(status_.p, 0, sizeof(int), st_));
         throw std::runtime_error("device capacity overflow (status " + std::to_string(s) + ")");

@@ -6,6 +6,18 @@
 namespace pe {
 
 // ------------------------------------------------------------------ utilities
+template <class R> void World<R>::scan_async(int* data, int n, int* total) {
+    const int tiles = (n + 1023) / 1024;
+    if (tiles <= kSmallScanTiles) {
+        launch(K_SCAN, 1, k_scan_aux, data, n, total);
+    } else {
+        aux_.ensure(tiles + 1);
+        launch(K_SCAN, tiles, k_scan_tiles, data, n, aux_.p);
+        launch(K_SCAN, 1, k_scan_aux, aux_.p, tiles, total);
+        launch(K_SCAN, tiles, k_scan_add, data, n, aux_.p);
+    }
+}
+
 template <class R> int World<R>::scan(int* data, int n) {
     const int tiles = (n + 1023) / 1024;
     if (tiles <= kSmallScanTiles) {   // small: one block scans in place (one launch instead of three)
@@ -262,11 +274,15 @@ template <class R> void World<R>::solve(int mode) {
         // rows: one per contact point, results' rows contiguous in result order
         PE_CK(cudaMemcpyAsync(row_off_.p, res_np_.p, P * sizeof(int), cudaMemcpyDeviceToDevice, st_));
         PE_CK(cudaMemsetAsync(row_off_.p + P, 0, sizeof(int), st_));
-        n_rows_ = scan(row_off_.p, P + 1);
-        if (n_rows_ > rows_cap_) {
-            rows_cap_ = std::max(n_rows_ + n_rows_ / 2, 1024);
+        // a result has at most kSlots points, so kSlots * P rows always fit: the row total is read
+        // back with the step's status at its end instead of in a host wait here
+        if ((long long)kSlots * P > rows_cap_) {
+            rows_cap_ = std::max(kSlots * P + kSlots * P / 4, 1024);
             rows_.ensure((size_t)NRF * rows_cap_);
         }
+        scan_async(row_off_.p, P + 1, rows_total_.p);
+        PE_CK(cudaMemcpyAsync(h_rows_, rows_total_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
+        rows_pending_ = true;
         launch(K_SI_SETUP, grid(P), k_si_setup<R>, P, results(), bodies(), rows(), row_off_.p, prm_, status_.p);
         // results with points, in result order
         launch(K_SI_MISC, grid(P + 1), k_active_flags, P, res_np_.p, active_.p);
