@@ -183,7 +183,6 @@ private:
     // sends the following launches to side stream k, join_streams() makes the world's stream wait
     // for all side streams and sends launches back to it.
     static constexpr int kSideStreams = 4;
-    static constexpr int kForkMinPairs = 4096;   // fewer pairs: the classes run on the world's stream
     cudaStream_t side_[kSideStreams] = {};
     cudaEvent_t fork_ev_ = nullptr, join_ev_[kSideStreams] = {};
     cudaStream_t cur_ = nullptr;

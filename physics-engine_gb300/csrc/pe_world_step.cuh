@@ -194,14 +194,12 @@ template <class R> void World<R>::narrowphase() {
             stream_of[c] = best;
             load[best] += cnt[c] * kClassCost[c];
         }
-        // a small step's classes are short: the stream fork and join would cost more than they overlap
-        const bool fork = P >= kForkMinPairs;
-        if (fork) fork_streams();
+        fork_streams();
         for (int c = 0; c < PC_COUNT; c++) {
             const int lo = cur[c], hi = cur[c] + cnt[c];
             if (hi == lo) continue;
             const int g = grid(hi - lo);
-            if (fork) use_stream(stream_of[c] % tun_.side_streams);
+            use_stream(stream_of[c] % tun_.side_streams);
             switch (c) {
                 case PC_BOX_BOX: launch(K_NP, g, k_np_class<R, PC_BOX_BOX>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
                 case PC_BOX_SPHERE: launch(K_NP, g, k_np_class<R, PC_BOX_SPHERE>, lo, hi, order_np_.p, pairs_.p, bd, sh, rs, pair_scene_off_.p, prev_res_off_.p); break;
@@ -256,7 +254,7 @@ template <class R> void World<R>::narrowphase() {
                     break;
             }
         }
-        if (fork) join_streams();
+        join_streams();
         PE_CK(cudaGetLastError());
     }
     PE_CK(cudaMemcpyAsync(res_scene_off_.p, pair_scene_off_.p, (NS_ + 1) * sizeof(int), cudaMemcpyDeviceToDevice, st_));
