@@ -206,6 +206,13 @@ const char* pe_gpu_kernel_name(int k);
 int pe_gpu_kernel_stats(pe_gpu_world* w, double* ms, long long* launches);
 /* blocks until all work on the world's stream finished */
 int pe_gpu_sync(pe_gpu_world* w);
+/* Steps through CUDA graphs (on by default).  A step waits on the host twice: for the pair count
+ * (the pair capacity follows it) and for its counters at the end.  Between the two, the pair list,
+ * the narrowphase and the solver size every grid from device-side counts, so that part is captured
+ * once as a CUDA graph per solver mode and replayed while the world's sizes, capacities, parameters
+ * and settings stay the same; off, the same kernels are launched one by one from the host.  Results
+ * are identical either way.  With profiling on (pe_gpu_set_profiling) steps launch one by one. */
+int pe_gpu_set_step_graphs(pe_gpu_world* w, int on);
 
 /* Serving (no counterpart in the reference, which steps one World per caller): a request loop over
  * one device-resident world.  A request is a scene (the arrays of pe_gpu_set_shapes and

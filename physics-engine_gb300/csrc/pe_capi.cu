@@ -107,6 +107,10 @@ int pe_gpu_set_contact_margin(pe_gpu_world* h, double margin) {
     return guard(h, [&](pe::WorldBase& w) { w.set_margin(margin); return PE_GPU_OK; });
 }
 
+int pe_gpu_set_step_graphs(pe_gpu_world* h, int on) {
+    return guard(h, [&](pe::WorldBase& w) { w.set_step_graphs(on != 0); return PE_GPU_OK; });
+}
+
 int pe_gpu_device_name(int device, char* name, int cap) {
     if (!name || cap < 1) return PE_GPU_ERR_ARG;
     cudaDeviceProp prop;

@@ -16,12 +16,19 @@ constexpr int kSmallScanTiles = 16;   // scans of up to 16 tiles of 1024 run in 
 // secondary key (scene id); stable, least-significant digit first, 8-bit digits.
 constexpr int kRadixItems = 16;                      // items per thread per tile
 constexpr int kRadixTile = kBlock * kRadixItems;     // 4096 items per tile
-__global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n, int shift, int use2, int* hist, int n_tiles);
+// The item count is n, or *nd when nd is set (a count the device computed: the grid then covers an
+// upper bound, tiles past the count do nothing, and with `small` >= 0 the passes do nothing at all
+// when the count is at most `small`, the inputs that k_sort_pairs_block sorts instead).
+__global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n, const int* nd, int small, int shift, int use2, int* hist,
+                             int n_tiles);
 // a sort of n <= kSceneSortMax (key, value) pairs inside one block (bitonic over (key, position)): the
-// order of the stable LSD radix sort, in one launch instead of five per pass, for small inputs
-__global__ void k_sort_pairs_block(const uint64_t* key, const uint32_t* val, int n, uint64_t* key_out, uint32_t* val_out);
+// order of the stable LSD radix sort, in one launch instead of five per pass, for small inputs.  With
+// nd set the count is *nd and the kernel does nothing when it is above kSceneSortMax; the output
+// may be the input (all reads precede all writes).
+__global__ void k_sort_pairs_block(const uint64_t* key, const uint32_t* val, int n, const int* nd, uint64_t* key_out, uint32_t* val_out);
 __global__ void k_radix_scatter(const uint64_t* key_in, const uint32_t* key2_in, const uint32_t* val_in, uint64_t* key_out,
-                                uint32_t* key2_out, uint32_t* val_out, int n, int shift, int use2, const int* hist, int n_tiles);
+                                uint32_t* key2_out, uint32_t* val_out, int n, const int* nd, int small, int shift, int use2,
+                                const int* hist, int n_tiles);
 
 __device__ inline uint64_t order_bits(float x) {
     if (x == 0.0f) x = 0.0f;   // -0 and +0 compare equal: give them one key

@@ -28,22 +28,60 @@ template <class R> __device__ __forceinline__ int sat_class(const ShapeView<R>& 
     return a.type == ST_BOX ? PC_CONVEX : PC_CONVEX_HULL_BOX;
 }
 
+// The pair count is on the device (*Pd); whole warps stride over it, so that every lane takes part
+// in the warp votes.
 template <class R>
-__global__ void k_np_classify(int P, const int2* pairs, Bodies<R> B, ShapeTable<R> S, int* cls, int* cls_count, long long heavy) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int c = -1 - (int)(threadIdx.x & 31);   // lanes past the end never match a class
-    if (p < P) {
-        const int2 q = pairs[p];
-        const ShapeView<R> sa = S.view(B.shape[q.x]), sb = S.view(B.shape[q.y]);
-        c = pair_class(sa.type, sb.type);
-        if (c == PC_CONVEX) c = sat_class(sa, sb, heavy);
-        cls[p] = c;
+__global__ void k_np_classify(const int* Pd, const int2* pairs, Bodies<R> B, ShapeTable<R> S, int* cls, int* cls_count, long long heavy) {
+    const int P = *Pd;
+    for (int base = blockIdx.x * blockDim.x; base < P; base += gridDim.x * blockDim.x) {
+        const int p = base + threadIdx.x;
+        int c = -1 - (int)(threadIdx.x & 31);   // lanes past the end never match a class
+        if (p < P) {
+            const int2 q = pairs[p];
+            const ShapeView<R> sa = S.view(B.shape[q.x]), sb = S.view(B.shape[q.y]);
+            c = pair_class(sa.type, sb.type);
+            if (c == PC_CONVEX) c = sat_class(sa, sb, heavy);
+            cls[p] = c;
+        }
+        // one atomic per class present in the warp
+        const unsigned peers = __match_any_sync(0xffffffffu, c);
+        if (c >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cls_count[c], __popc(peers));
     }
-    // one atomic per class present in the warp
-    const unsigned peers = __match_any_sync(0xffffffffu, c);
-    if (c >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cls_count[c], __popc(peers));
 }
-__global__ void k_np_bucket(int P, const int* cls, int* cursor, int* order);
+__global__ void k_np_bucket(const int* Pd, const int* cls, int* cursor, int* order);
+__global__ void k_np_ranges(const int* count, int* cursor, int2* range, int* work);
+
+// Work loops over a class's range [rng.x, rng.y) of the bucketed order, whose size only the device
+// knows: the grids are sized by an upper bound, at most the GPU's resident blocks.
+// thread_items: one item per thread, grid-strided.
+template <class F> __device__ __forceinline__ void thread_items(int2 rng, F&& f) {
+    for (int t = rng.x + blockIdx.x * blockDim.x + threadIdx.x; t < rng.y; t += gridDim.x * blockDim.x) f(t);
+}
+// warp_items: one item per warp, handed out by an atomic cursor (which starts at rng.x), so that
+// the warps that finish early take the next items while a long pair holds another warp
+template <class F> __device__ __forceinline__ void warp_items(int2 rng, int* cursor, F&& f) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(cursor, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= rng.y) break;
+        f(t);
+        __syncwarp();
+    }
+}
+// block_items: one item per block, from an atomic cursor
+template <class F> __device__ __forceinline__ void block_items(int2 rng, int* cursor, int* slot, F&& f) {
+    for (;;) {
+        if (threadIdx.x == 0) *slot = atomicAdd(cursor, 1);
+        __syncthreads();
+        const int t = *slot;
+        __syncthreads();
+        if (t >= rng.y) break;
+        f(t);
+        __syncthreads();
+    }
+}
 
 // Pair setup of SimpleNarrowPhase::calcContactResults (simple_narrow_phase.cpp:24-38): the pooled
 // result is reset, keeping the distances its slots had after the previous step's sort when the
@@ -111,18 +149,18 @@ __device__ __forceinline__ void np_finish(int p, const int2* pairs, const Bodies
     }
 }
 
-// one thread per pair of one algorithm class; `order[lo..hi)` holds that class's pairs
+// one thread per pair of one algorithm class; `order[rng)` holds that class's pairs
 template <class R, int CLS>
-__global__ void k_np_class(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+__global__ void k_np_class(const int2* rng, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
                            const int* pair_scene_off, const int* prev_off) {
-    const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= hi) return;
-    const int p = order[t];
-    Cache<R> cache;
-    Pair<R> pr;
-    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
-    collide(pr, CLS);
-    np_finish(p, pairs, B, res, cache);
+    thread_items(*rng, [&](int t) {
+        const int p = order[t];
+        Cache<R> cache;
+        Pair<R> pr;
+        np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
+        collide(pr, CLS);
+        np_finish(p, pairs, B, res, cache);
+    });
 }
 
 // CompoundCompoundCollisionAlgorithm::processCollision (compound_compound_collision_algorithm.cpp:8-46),
@@ -133,11 +171,8 @@ __global__ void k_np_class(int lo, int hi, const int* order, const int2* pairs, 
 // cache at the child's world transform (body transform * local transform).  Local contact
 // positions stay relative to the bodies.
 template <class R>
-__global__ void k_np_compound(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
-                              const int* pair_scene_off, const int* prev_off) {
-    const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= hi) return;
-    const int p = order[t];
+__device__ __forceinline__ void compound_pair(int p, const int2* pairs, const Bodies<R>& B, const ShapeTable<R>& S, const Results<R>& res,
+                                              const int* pair_scene_off, const int* prev_off) {
     Cache<R> cache;
     Pair<R> pr;
     np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
@@ -168,6 +203,12 @@ __global__ void k_np_compound(int lo, int hi, const int* order, const int2* pair
         }
     }
     np_finish(p, pairs, B, res, cache, swapped);
+}
+
+template <class R>
+__global__ void k_np_compound(const int2* rng, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+                              const int* pair_scene_off, const int* prev_off) {
+    thread_items(*rng, [&](int t) { compound_pair(order[t], pairs, B, S, res, pair_scene_off, prev_off); });
 }
 
 } // namespace pe

@@ -678,42 +678,48 @@ template <class R> constexpr int sat_group_reals(int G) {
 static_assert(sat_group_reals<float>(1) % 4 == 0 && (3 * (2 * kSatF + 2 * kSatE)) % 4 == 0, "SAT staging alignment");
 template <class R, int G, int TA, int TB>
 __global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 16 / kSatWarps : 2)
-k_np_sat(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, R* sat_out) {
+k_np_sat(const int2* rng, int* cursor, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, R* sat_out) {
     extern __shared__ __align__(16) unsigned char sat_smem[];
     const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
     const int tid = G == 1 ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
-    const int t = lo + blockIdx.x * (G == 1 ? kSatWarps : 1) + grp;
-    if (t >= hi) return;   // whole groups leave together
-    const int2 q = pairs[order[t]];
-    Pair<R> pr;
-    pr.xa = B.xf(q.x);
-    pr.xb = B.xf(q.y);
-    pr.sa = S.view(B.shape[q.x]);
-    pr.sb = S.view(B.shape[q.y]);
-    pr.margin = S.margin;
-    pr.c = nullptr;
-    sat_staged<R, G, TA, TB>(pr, tid, reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G),
-                             sat_out + (size_t)t * kSatOut);
+    R* smem = reinterpret_cast<R*>(sat_smem) + (size_t)grp * sat_group_reals<R>(G);
+    auto one = [&](int t) {
+        const int2 q = pairs[order[t]];
+        Pair<R> pr;
+        pr.xa = B.xf(q.x);
+        pr.xb = B.xf(q.y);
+        pr.sa = S.view(B.shape[q.x]);
+        pr.sb = S.view(B.shape[q.y]);
+        pr.margin = S.margin;
+        pr.c = nullptr;
+        sat_staged<R, G, TA, TB>(pr, tid, smem, sat_out + (size_t)t * kSatOut);
+    };
+    if (G == 1) {
+        warp_items(*rng, cursor, one);
+    } else {
+        __shared__ int slot;
+        block_items(*rng, cursor, &slot, one);
+    }
 }
 
 // contact step of the staged SAT pairs, one thread per pair: the pooled result is set up, the
 // recorded face-stage and edge-stage points are added and the faces clipped, in the reference's
 // order, and the result is sorted and written out
 template <class R>
-__global__ void k_np_sat_finish(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+__global__ void k_np_sat_finish(const int2* rng, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
                                 const int* pair_scene_off, const int* prev_off, const R* sat_out) {
-    const int t = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= hi) return;
-    const int p = order[t];
-    Cache<R> cache;
-    Pair<R> pr;
-    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
-    const R* o = sat_out + (size_t)t * kSatOut;
-    const int fl = (int)o[SO_FLAGS];
-    if (fl & 1) pr.add(so_get3(o, SO_FN), so_get3(o, SO_FP), o[SO_FD]);
-    if (fl & 2) pr.add(so_get3(o, SO_EN), so_get3(o, SO_EP), o[SO_ED]);
-    if (fl & 4) clip_faces(pr, so_get3(o, SO_SEP), -pr.ref_scale, pr.margin, (int)o[SO_FB], (int)o[SO_FA]);
-    np_finish(p, pairs, B, res, cache);
+    thread_items(*rng, [&](int t) {
+        const int p = order[t];
+        Cache<R> cache;
+        Pair<R> pr;
+        np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
+        const R* o = sat_out + (size_t)t * kSatOut;
+        const int fl = (int)o[SO_FLAGS];
+        if (fl & 1) pr.add(so_get3(o, SO_FN), so_get3(o, SO_FP), o[SO_FD]);
+        if (fl & 2) pr.add(so_get3(o, SO_EN), so_get3(o, SO_EP), o[SO_ED]);
+        if (fl & 4) clip_faces(pr, so_get3(o, SO_SEP), -pr.ref_scale, pr.margin, (int)o[SO_FB], (int)o[SO_FA]);
+        np_finish(p, pairs, B, res, cache);
+    });
 }
 
 // CylinderConvexCollisionAlgorithm (cylinder_convex_collision_algorithm.cpp:109-203), one warp
@@ -725,14 +731,13 @@ constexpr int kCylHullCand = 12;   // points a face can give: 6 cylinder segment
 template <class R> constexpr int cyl_hull_warps() { return sizeof(R) == 4 ? 4 : 2; }
 template <class R>
 __global__ void __launch_bounds__(32 * cyl_hull_warps<R>())
-k_np_cyl_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+k_np_cyl_hull(const int2* rng, int* cursor, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
               const int* pair_scene_off, const int* prev_off) {
     constexpr int W = cyl_hull_warps<R>(), K = kCylHullCand;
     __shared__ R cand[W][32 * K][7];
     __shared__ int ccnt[W][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t = lo + blockIdx.x * W + warp;
-    if (t >= hi) return;   // whole warps
+    warp_items(*rng, cursor, [&](int t) {
     const int p = order[t];
     Cache<R> cache;
     Pair<R> c;
@@ -863,6 +868,7 @@ k_np_cyl_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, 
         cache.swap = false;
         np_finish(p, pairs, B, res, cache);
     }
+    });
 }
 
 // SphereConvexCollisionAlgorithm (sphere_convex_collision_algorithm.cpp:185-210) for a convex hull,
@@ -875,14 +881,13 @@ constexpr int kSphereHullCand = 8;
 template <class R> constexpr int sphere_hull_warps() { return sizeof(R) == 4 ? 4 : 2; }
 template <class R>
 __global__ void __launch_bounds__(32 * sphere_hull_warps<R>())
-k_np_sphere_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
+k_np_sphere_hull(const int2* rng, int* cursor, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
                  const int* pair_scene_off, const int* prev_off) {
     constexpr int W = sphere_hull_warps<R>(), K = kSphereHullCand;
     __shared__ R cand[W][32 * K][7];
     __shared__ int ccnt[W][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int t = lo + blockIdx.x * W + warp;
-    if (t >= hi) return;   // whole warps
+    warp_items(*rng, cursor, [&](int t) {
     const int p = order[t];
     Cache<R> cache;
     Pair<R> c;
@@ -942,21 +947,22 @@ k_np_sphere_hull(int lo, int hi, const int* order, const int2* pairs, Bodies<R> 
         cache.swap = false;
         np_finish(p, pairs, B, res, cache);
     }
+    });
 }
 
 // SAT pairs with a shape beyond the staging limits (PC_CONVEX_BIG): one warp each, unstaged
 template <class R>
-__global__ void k_np_sat_big(int lo, int hi, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, Results<R> res,
-                             const int* pair_scene_off, const int* prev_off) {
-    const int t = lo + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+__global__ void k_np_sat_big(const int2* rng, int* cursor, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S,
+                             Results<R> res, const int* pair_scene_off, const int* prev_off) {
     const int lane = threadIdx.x & 31;
-    if (t >= hi) return;
-    const int p = order[t];
-    Cache<R> cache;
-    Pair<R> pr;
-    np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
-    sat_warp(pr, lane);
-    if (lane == 0) np_finish(p, pairs, B, res, cache);
+    warp_items(*rng, cursor, [&](int t) {
+        const int p = order[t];
+        Cache<R> cache;
+        Pair<R> pr;
+        np_setup(p, pairs, B, S, res, pair_scene_off, prev_off, cache, pr);
+        sat_warp(pr, lane);
+        if (lane == 0) np_finish(p, pairs, B, res, cache);
+    });
 }
 
 } // namespace pe

@@ -8,9 +8,8 @@ namespace pe {
 // ===================================================================== solver
 // FrictionContactConstraint::initSequentialImpulse (friction_contact_constraint.cpp:9-73), one thread per result
 template <class R>
-__global__ void k_si_setup(int P, Results<R> res, Bodies<R> B, Rows<R> rows, const int* row_off, StepParams prm, int* status) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
+__device__ __forceinline__ void si_setup_result(int p, const Results<R>& res, const Bodies<R>& B, const Rows<R>& rows, const int* row_off,
+                                                const StepParams& prm, int* status) {
     const int np = res.npts[p];
     if (np == 0) return;
     const int ia = res.a[p], ib = res.b[p];
@@ -55,6 +54,11 @@ __global__ void k_si_setup(int P, Results<R> res, Bodies<R> B, Rows<R> rows, con
         rows.at(T0ACC, r) = 0;
         rows.at(T1ACC, r) = 0;
     }
+}
+template <class R>
+__global__ void k_si_setup(const int* Rd, Results<R> res, Bodies<R> B, Rows<R> rows, const int* row_off, StepParams prm, int* status) {
+    const int P = *Rd;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) si_setup_result(p, res, B, rows, row_off, prm, status);
 }
 
 // FrictionContactConstraint::iterateSequentialImpulse (friction_contact_constraint.cpp:75-108)
@@ -303,13 +307,14 @@ __device__ __forceinline__ void uf_union(int* parent, int a, int b) {
 
 __global__ void k_isl_init(int n, int* parent);
 template <class R>
-__global__ void k_isl_union(int A, const int* active, Results<R> res, Bodies<R> B, int* parent) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A) return;
-    const int p = active[t];
-    const int ia = res.a[p], ib = res.b[p];
-    if ((B.flags[ia] & BF_KINEMATIC) || (B.flags[ib] & BF_KINEMATIC)) return;
-    uf_union(parent, ia, ib);
+__global__ void k_isl_union(const int* Ad, const int* active, Results<R> res, Bodies<R> B, int* parent) {
+    const int A = *Ad;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < A; t += gridDim.x * blockDim.x) {
+        const int p = active[t];
+        const int ia = res.a[p], ib = res.b[p];
+        if ((B.flags[ia] & BF_KINEMATIC) || (B.flags[ib] & BF_KINEMATIC)) continue;
+        uf_union(parent, ia, ib);
+    }
 }
 // joints link their bodies like contact results do
 template <class R>
@@ -323,9 +328,10 @@ __global__ void k_isl_union_joints(Joints<R> J, Bodies<R> B, int* parent) {
 // sort keys of the joints, after the A active results: the island label of a dynamic body; a joint
 // between two kinematic bodies (which moves nothing) gets the label n_bodies, an island of its own
 template <class R>
-__global__ void k_isl_keys_joints(Joints<R> J, Bodies<R> B, const int* parent, int A, uint64_t* key, uint32_t* key2, uint32_t* val) {
+__global__ void k_isl_keys_joints(Joints<R> J, Bodies<R> B, const int* parent, const int* Ad, uint64_t* key, uint32_t* key2, uint32_t* val) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= J.n) return;
+    const int A = *Ad;
     const int ia = J.body[j].x, ib = J.body[j].y;
     const bool ka = (B.flags[ia] & BF_KINEMATIC) != 0, kb = (B.flags[ib] & BF_KINEMATIC) != 0;
     key[A + j] = ka && kb ? (uint64_t)B.n : (uint64_t)uf_find(parent, ka ? ib : ia);
@@ -334,19 +340,22 @@ __global__ void k_isl_keys_joints(Joints<R> J, Bodies<R> B, const int* parent, i
 }
 // sort keys: island label (smallest body index of the island) of each active result
 template <class R>
-__global__ void k_isl_keys(int A, const int* active, Results<R> res, Bodies<R> B, const int* parent, uint64_t* key, uint32_t* key2,
+__global__ void k_isl_keys(const int* Ad, const int* active, Results<R> res, Bodies<R> B, const int* parent, uint64_t* key, uint32_t* key2,
                            uint32_t* val) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A) return;
-    const int p = active[t];
-    const int ia = res.a[p], ib = res.b[p];
-    const int dyn = (B.flags[ia] & BF_KINEMATIC) ? ib : ia;
-    key[t] = (uint64_t)uf_find(parent, dyn);
-    key2[t] = 0;
-    val[t] = (uint32_t)p;
+    const int A = *Ad;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < A; t += gridDim.x * blockDim.x) {
+        const int p = active[t];
+        const int ia = res.a[p], ib = res.b[p];
+        const int dyn = (B.flags[ia] & BF_KINEMATIC) ? ib : ia;
+        key[t] = (uint64_t)uf_find(parent, dyn);
+        key2[t] = 0;
+        val[t] = (uint32_t)p;
+    }
 }
-__global__ void k_isl_flags(int A, const uint64_t* key, int* flag);
-__global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out);
+// M = *Md sorted items (active results, then joints): island starts, and the islands' first slots
+__global__ void k_isl_flags(const int* Md, int bound, const uint64_t* key, int* flag);
+__global__ void k_isl_offsets(const int* Md, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out);
+__global__ void k_count_add(const int* a, int add, int* out);
 
 // serial order inside each island of up to max_len items, one thread per island, islands in their
 // natural order (the island of the smallest body first): consecutive threads take neighbouring
@@ -356,16 +365,18 @@ __global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* 
 template <class R>
 __global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
                              Rows<R> rows, const int* row_off, int iterations, int max_len) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= *n_isl) return;
-    const int lo = isl_off[s], hi = isl_off[s + 1];
-    if (hi - lo > max_len) return;
-    for (int it = 0; it < iterations; it++)
-        for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
+    const int NI = *n_isl;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < NI; s += gridDim.x * blockDim.x) {
+        const int lo = isl_off[s], hi = isl_off[s + 1];
+        if (hi - lo > max_len) continue;
+        for (int it = 0; it < iterations; it++)
+            for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
+    }
 }
 
 
-// coloured Gauss-Seidel of one island per block: greedy colouring in rounds (a result takes
+// coloured Gauss-Seidel of one island at a time per block (the islands of `list`, taken in turn
+// through an atomic cursor): greedy colouring in rounds (a result takes
 // colour c when it holds the smallest position among the uncoloured results on each of its
 // dynamic bodies), then every iteration runs the colours in turn, all results of a colour in
 // parallel.  Colour c is then the item's level in the serial order's level schedule, so an island
@@ -373,90 +384,99 @@ __global__ void k_isl_serial(const int* n_isl, const int* isl_off, const uint32_
 // uncoloured after kMaxColors - 1 rounds form a last colour that one thread runs in order.
 constexpr int kMaxColors = 512;
 template <class R>
-__global__ void __launch_bounds__(256) k_isl_colored(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B,
-                              Rows<R> rows, const int* row_off, int iterations, int min_len, int max_len, int* claim, int* color,
-                              uint32_t* corder, int* n_colors_out) {
-    const int s = blockIdx.x;
-    if (s >= *n_isl) return;
-    const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
-    if (m <= min_len || m > max_len) return;
+__global__ void __launch_bounds__(256) k_isl_colored(const int* list, const int* n_list, int* cursor, const int* isl_off, const uint32_t* order,
+                                                     Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off,
+                                                     int iterations, int min_len, int max_len, int* claim, int* color, uint32_t* corder,
+                                                     int* n_colors_out) {
     __shared__ int cnt[kMaxColors + 1];
     __shared__ int fill[kMaxColors];
     __shared__ int remaining;
     __shared__ int ncol;
-    for (int j = threadIdx.x; j < m; j += blockDim.x) color[lo + j] = -1;
-    if (threadIdx.x == 0) ncol = 0;
-    __syncthreads();
-    for (int c = 0; c < kMaxColors - 1; c++) {
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-            if (color[lo + j] >= 0) continue;
-            const int2 q = item_bodies(order[lo + j], res, J);
-            claim[q.x] = 0x7fffffff;
-            claim[q.y] = 0x7fffffff;
-        }
-        if (threadIdx.x == 0) remaining = 0;
+    __shared__ int slot;
+    for (;;) {   // islands from the list, one at a time per block
+        if (threadIdx.x == 0) slot = atomicAdd(cursor, 1);
         __syncthreads();
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-            if (color[lo + j] >= 0) continue;
-            const int2 q = item_bodies(order[lo + j], res, J);
-            const int ia = q.x, ib = q.y;
-            if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
-            if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
-        }
+        const int li = slot;
         __syncthreads();
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-            if (color[lo + j] >= 0) continue;
-            const int2 q = item_bodies(order[lo + j], res, J);
-            const int ia = q.x, ib = q.y;
-            const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
-            if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) color[lo + j] = c;
-            else atomicAdd(&remaining, 1);
-        }
+        if (li >= *n_list) break;
+        const int s = list[li];
+        const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
+        if (m <= min_len || m > max_len) continue;
+        for (int j = threadIdx.x; j < m; j += blockDim.x) color[lo + j] = -1;
+        if (threadIdx.x == 0) ncol = 0;
         __syncthreads();
-        if (threadIdx.x == 0) ncol = c + 1;
-        const int rem = remaining;
-        __syncthreads();
-        if (rem == 0) break;
-    }
-    // leftovers (pathological degree): colour nc after the nc rounds' colours, run in island order
-    // by one thread; only the colours in use are counted, placed and run
-    const int nc = ncol;
-    for (int j = threadIdx.x; j < m; j += blockDim.x)
-        if (color[lo + j] < 0) color[lo + j] = nc;
-    for (int k = threadIdx.x; k <= nc + 1; k += blockDim.x) cnt[k] = 0;
-    __syncthreads();
-    for (int j = threadIdx.x; j < m; j += blockDim.x) atomicAdd(&cnt[color[lo + j] + 1], 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 0; k <= nc; k++) cnt[k + 1] += cnt[k];   // cnt[c] = first slot of colour c
-        atomicMax(n_colors_out, nc + (cnt[nc + 1] > cnt[nc] ? 1 : 0));
-    }
-    __syncthreads();
-    const bool left = cnt[nc + 1] > cnt[nc];
-    // placement by colour: the results of a colour touch disjoint dynamic bodies, so their order
-    // inside the colour does not matter and they are placed in parallel; the leftovers in order
-    for (int k = threadIdx.x; k < nc; k += blockDim.x) fill[k] = cnt[k];
-    __syncthreads();
-    for (int j = threadIdx.x; j < m; j += blockDim.x) {
-        const int c = color[lo + j];
-        if (c < nc) corder[lo + atomicAdd(&fill[c], 1)] = order[lo + j];
-    }
-    if (threadIdx.x == 0 && left) {
-        int f = cnt[nc];
-        for (int j = 0; j < m; j++)
-            if (color[lo + j] == nc) corder[lo + f++] = order[lo + j];
-    }
-    __syncthreads();
-    for (int it = 0; it < iterations; it++) {
-        for (int c = 0; c < nc; c++) {
-            for (int j = cnt[c] + threadIdx.x; j < cnt[c + 1]; j += blockDim.x) iterate_item(corder[lo + j], res, J, B, rows, row_off);
+        for (int c = 0; c < kMaxColors - 1; c++) {
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                if (color[lo + j] >= 0) continue;
+                const int2 q = item_bodies(order[lo + j], res, J);
+                claim[q.x] = 0x7fffffff;
+                claim[q.y] = 0x7fffffff;
+            }
+            if (threadIdx.x == 0) remaining = 0;
             __syncthreads();
-        }
-        if (left) {
-            if (threadIdx.x == 0)
-                for (int j = cnt[nc]; j < cnt[nc + 1]; j++) iterate_item(corder[lo + j], res, J, B, rows, row_off);
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                if (color[lo + j] >= 0) continue;
+                const int2 q = item_bodies(order[lo + j], res, J);
+                const int ia = q.x, ib = q.y;
+                if (!(B.flags[ia] & BF_KINEMATIC)) atomicMin(&claim[ia], j);
+                if (!(B.flags[ib] & BF_KINEMATIC)) atomicMin(&claim[ib], j);
+            }
             __syncthreads();
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                if (color[lo + j] >= 0) continue;
+                const int2 q = item_bodies(order[lo + j], res, J);
+                const int ia = q.x, ib = q.y;
+                const bool da = !(B.flags[ia] & BF_KINEMATIC), db = !(B.flags[ib] & BF_KINEMATIC);
+                if ((!da || claim[ia] == j) && (!db || claim[ib] == j)) color[lo + j] = c;
+                else atomicAdd(&remaining, 1);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) ncol = c + 1;
+            const int rem = remaining;
+            __syncthreads();
+            if (rem == 0) break;
         }
+        // leftovers (pathological degree): colour nc after the nc rounds' colours, run in island order
+        // by one thread; only the colours in use are counted, placed and run
+        const int nc = ncol;
+        for (int j = threadIdx.x; j < m; j += blockDim.x)
+            if (color[lo + j] < 0) color[lo + j] = nc;
+        for (int k = threadIdx.x; k <= nc + 1; k += blockDim.x) cnt[k] = 0;
+        __syncthreads();
+        for (int j = threadIdx.x; j < m; j += blockDim.x) atomicAdd(&cnt[color[lo + j] + 1], 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 0; k <= nc; k++) cnt[k + 1] += cnt[k];   // cnt[c] = first slot of colour c
+            atomicMax(n_colors_out, nc + (cnt[nc + 1] > cnt[nc] ? 1 : 0));
+        }
+        __syncthreads();
+        const bool left = cnt[nc + 1] > cnt[nc];
+        // placement by colour: the results of a colour touch disjoint dynamic bodies, so their order
+        // inside the colour does not matter and they are placed in parallel; the leftovers in order
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) fill[k] = cnt[k];
+        __syncthreads();
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            const int c = color[lo + j];
+            if (c < nc) corder[lo + atomicAdd(&fill[c], 1)] = order[lo + j];
+        }
+        if (threadIdx.x == 0 && left) {
+            int f = cnt[nc];
+            for (int j = 0; j < m; j++)
+                if (color[lo + j] == nc) corder[lo + f++] = order[lo + j];
+        }
+        __syncthreads();
+        for (int it = 0; it < iterations; it++) {
+            for (int c = 0; c < nc; c++) {
+                for (int j = cnt[c] + threadIdx.x; j < cnt[c + 1]; j += blockDim.x) iterate_item(corder[lo + j], res, J, B, rows, row_off);
+                __syncthreads();
+            }
+            if (left) {
+                if (threadIdx.x == 0)
+                    for (int j = cnt[nc]; j < cnt[nc + 1]; j++) iterate_item(corder[lo + j], res, J, B, rows, row_off);
+                __syncthreads();
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -470,69 +490,78 @@ __global__ void __launch_bounds__(256) k_isl_colored(const int* n_isl, const int
 constexpr int kMaxLevels = 256;
 constexpr int kLevelBlock = 256;   // the largest block of k_isl_levels
 template <class R>
-__global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, const int* isl_off, const uint32_t* order, Results<R> res,
-                                                            Joints<R> J, Bodies<R> B, Rows<R> rows, const int* row_off, int iterations,
-                                                            int min_len, int max_len, int* claim, int* level, uint32_t* lorder) {
-    const int s = blockIdx.x;
-    if (s >= *n_isl) return;
-    const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
-    if (m <= min_len || m > max_len) return;
+__global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* list, const int* n_list, int* cursor, const int* isl_off,
+                                                            const uint32_t* order, Results<R> res, Joints<R> J, Bodies<R> B, Rows<R> rows,
+                                                            const int* row_off, int iterations, int min_len, int max_len, int* claim,
+                                                            int* level, uint32_t* lorder) {
     __shared__ int cnt[kMaxLevels + 1];
     __shared__ int remaining;
-    for (int j = threadIdx.x; j < m; j += blockDim.x) level[lo + j] = -1;
-    __syncthreads();
-    int rem = m;
-    for (int r = 0; r < kMaxLevels && rem > 0; r++) {
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-            if (level[lo + j] >= 0) continue;
-            const int2 q = item_bodies(order[lo + j], res, J);
-            claim[q.x] = 0x7fffffff;
-            claim[q.y] = 0x7fffffff;
-        }
-        if (threadIdx.x == 0) remaining = 0;
+    __shared__ int slot;
+    for (;;) {   // islands from the list, one at a time per block
+        if (threadIdx.x == 0) slot = atomicAdd(cursor, 1);
         __syncthreads();
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-            if (level[lo + j] >= 0) continue;
-            const int2 q = item_bodies(order[lo + j], res, J);
-            if (!(B.flags[q.x] & BF_KINEMATIC)) atomicMin(&claim[q.x], j);
-            if (!(B.flags[q.y] & BF_KINEMATIC)) atomicMin(&claim[q.y], j);
-        }
+        const int li = slot;
         __syncthreads();
-        for (int j = threadIdx.x; j < m; j += blockDim.x) {
-            if (level[lo + j] >= 0) continue;
-            const int2 q = item_bodies(order[lo + j], res, J);
-            const bool da = !(B.flags[q.x] & BF_KINEMATIC), db = !(B.flags[q.y] & BF_KINEMATIC);
-            if ((!da || claim[q.x] == j) && (!db || claim[q.y] == j)) level[lo + j] = r;
-            else atomicAdd(&remaining, 1);
-        }
+        if (li >= *n_list) break;
+        const int s = list[li];
+        const int lo = isl_off[s], hi = isl_off[s + 1], m = hi - lo;
+        if (m <= min_len || m > max_len) continue;
+        for (int j = threadIdx.x; j < m; j += blockDim.x) level[lo + j] = -1;
         __syncthreads();
-        rem = remaining;
-        __syncthreads();
-    }
-    if (rem > 0) {   // too many levels: the island in order on one thread
-        if (threadIdx.x == 0)
-            for (int it = 0; it < iterations; it++)
-                for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
-        return;
-    }
-    for (int k = threadIdx.x; k <= kMaxLevels; k += blockDim.x) cnt[k] = 0;
-    __syncthreads();
-    int nl = 0;
-    for (int j = threadIdx.x; j < m; j += blockDim.x) atomicAdd(&cnt[level[lo + j] + 1], 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < kMaxLevels; k++) cnt[k + 1] += cnt[k];   // cnt[l] = first slot of level l
-        int fill[kMaxLevels];
-        for (int k = 0; k < kMaxLevels; k++) fill[k] = cnt[k];
-        for (int j = 0; j < m; j++) lorder[lo + fill[level[lo + j]]++] = order[lo + j];
-    }
-    __syncthreads();
-    for (int k = 0; k < kMaxLevels; k++) if (cnt[k + 1] > cnt[k]) nl = k + 1;
-    for (int it = 0; it < iterations; it++)
-        for (int l = 0; l < nl; l++) {
-            for (int j = cnt[l] + threadIdx.x; j < cnt[l + 1]; j += blockDim.x) iterate_item(lorder[lo + j], res, J, B, rows, row_off);
+        int rem = m;
+        for (int r = 0; r < kMaxLevels && rem > 0; r++) {
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                if (level[lo + j] >= 0) continue;
+                const int2 q = item_bodies(order[lo + j], res, J);
+                claim[q.x] = 0x7fffffff;
+                claim[q.y] = 0x7fffffff;
+            }
+            if (threadIdx.x == 0) remaining = 0;
+            __syncthreads();
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                if (level[lo + j] >= 0) continue;
+                const int2 q = item_bodies(order[lo + j], res, J);
+                if (!(B.flags[q.x] & BF_KINEMATIC)) atomicMin(&claim[q.x], j);
+                if (!(B.flags[q.y] & BF_KINEMATIC)) atomicMin(&claim[q.y], j);
+            }
+            __syncthreads();
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                if (level[lo + j] >= 0) continue;
+                const int2 q = item_bodies(order[lo + j], res, J);
+                const bool da = !(B.flags[q.x] & BF_KINEMATIC), db = !(B.flags[q.y] & BF_KINEMATIC);
+                if ((!da || claim[q.x] == j) && (!db || claim[q.y] == j)) level[lo + j] = r;
+                else atomicAdd(&remaining, 1);
+            }
+            __syncthreads();
+            rem = remaining;
             __syncthreads();
         }
+        if (rem > 0) {   // too many levels: the island in order on one thread
+            if (threadIdx.x == 0)
+                for (int it = 0; it < iterations; it++)
+                    for (int k = lo; k < hi; k++) iterate_item(order[k], res, J, B, rows, row_off);
+            continue;
+        }
+        for (int k = threadIdx.x; k <= kMaxLevels; k += blockDim.x) cnt[k] = 0;
+        __syncthreads();
+        int nl = 0;
+        for (int j = threadIdx.x; j < m; j += blockDim.x) atomicAdd(&cnt[level[lo + j] + 1], 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < kMaxLevels; k++) cnt[k + 1] += cnt[k];   // cnt[l] = first slot of level l
+            int fill[kMaxLevels];
+            for (int k = 0; k < kMaxLevels; k++) fill[k] = cnt[k];
+            for (int j = 0; j < m; j++) lorder[lo + fill[level[lo + j]]++] = order[lo + j];
+        }
+        __syncthreads();
+        for (int k = 0; k < kMaxLevels; k++) if (cnt[k + 1] > cnt[k]) nl = k + 1;
+        for (int it = 0; it < iterations; it++)
+            for (int l = 0; l < nl; l++) {
+                for (int j = cnt[l] + threadIdx.x; j < cnt[l + 1]; j += blockDim.x) iterate_item(lorder[lo + j], res, J, B, rows, row_off);
+                __syncthreads();
+            }
+        __syncthreads();
+    }
 }
 
 // ---- islands above Tuning::big_island_items results: k_isl_colored's colouring rule in grid-wide kernels (round
@@ -544,6 +573,9 @@ __global__ void __launch_bounds__(kLevelBlock) k_isl_levels(const int* n_isl, co
 // rounds run in island order in one thread.
 constexpr int kMaxColorsBig = 1024;
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big, int big_items);
+__global__ void k_isl_pick(const int* n_isl, const int* isl_off, int min_len, int max_len, int* list, int* n_list);
+__global__ void k_step_counters(const int* status, const int* rows, const int* active, const int* islands, const int* big, const int* colors,
+                                const int* cls, int* out);
 template <class R>
 __global__ void k_gc_mask_reset(int lo, int m, const uint32_t* order, Results<R> res, Joints<R> J, unsigned long long* mask) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -712,8 +744,9 @@ __global__ void k_si_clear(Bodies<R> B) {
 // first sorted position of each scene -> offset of its first pair
 __global__ void k_scene_pair_off(int n_scenes, const int* scene_off, const int* pair_scan, int n, int* pair_scene_off);
 // results with at least one point, compacted
-__global__ void k_active_flags(int P, const int* npts, int* flag);
-__global__ void k_active_compact(int P, const int* npts, const int* scan, int* active);
+__global__ void k_rows_init(const int* Rd, int bound, const int* npts, int* row_off);
+__global__ void k_active_flags(const int* Rd, int bound, const int* npts, int* flag);
+__global__ void k_active_compact(const int* Rd, const int* npts, const int* scan, int* active);
 
 // RigidBody::syncTempVelocity (rigidbody.cpp:154-158)
 template <class R>

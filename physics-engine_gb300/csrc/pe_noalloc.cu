@@ -206,12 +206,12 @@ extern "C" int pe_gpu_sap_pairs_noalloc(int device, int n, const float* aabb_min
     const int tiles = (n + kRadixTile - 1) / kRadixTile;
     int cur = 0;
     for (int shift = 0; shift < 32; shift += 8) {
-        k_radix_hist<<<tiles, kBlock, 0, st>>>(key[cur], key2[cur], n, shift, 0, hist, tiles);
+        k_radix_hist<<<tiles, kBlock, 0, st>>>(key[cur], key2[cur], n, nullptr, -1, shift, 0, hist, tiles);
         const int m = 256 * tiles, ht = (m + 1023) / 1024;
         k_scan_tiles<<<ht, kBlock, 0, st>>>(hist, m, aux);
         k_scan_aux<<<1, kBlock, 0, st>>>(aux, ht, total);
         k_scan_add<<<ht, kBlock, 0, st>>>(hist, m, aux);
-        k_radix_scatter<<<tiles, kBlock, 0, st>>>(key[cur], key2[cur], val[cur], key[cur ^ 1], key2[cur ^ 1], val[cur ^ 1], n, shift, 0,
+        k_radix_scatter<<<tiles, kBlock, 0, st>>>(key[cur], key2[cur], val[cur], key[cur ^ 1], key2[cur ^ 1], val[cur ^ 1], n, nullptr, -1, shift, 0,
                                                  hist, tiles);
         cur ^= 1;
     }

@@ -68,10 +68,12 @@ __global__ void k_scan_add(int* data, int n, const int* aux) {
 }
 
 // ---------------------------------------------------------------- small sorts
-__global__ void __launch_bounds__(kSceneSortBlock) k_sort_pairs_block(const uint64_t* key, const uint32_t* val, int n, uint64_t* key_out,
-                                                                     uint32_t* val_out) {
+__global__ void __launch_bounds__(kSceneSortBlock) k_sort_pairs_block(const uint64_t* key, const uint32_t* val, int n0, const int* nd,
+                                                                     uint64_t* key_out, uint32_t* val_out) {
     __shared__ uint64_t k[kSceneSortMax];
     __shared__ uint32_t pos[kSceneSortMax];
+    const int n = nd ? *nd : n0;
+    if (n > kSceneSortMax) return;   // the radix passes sort this count
     int P = 1;
     while (P < n) P <<= 1;
     for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -91,7 +93,9 @@ __global__ void __launch_bounds__(kSceneSortBlock) k_sort_pairs_block(const uint
             }
             __syncthreads();
         }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) { key_out[i] = k[i]; val_out[i] = val[pos[i]]; }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) pos[i] = val[pos[i]];   // every read of the input before any write
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { key_out[i] = k[i]; val_out[i] = pos[i]; }
 }
 
 // ---------------------------------------------------------------- radix sort
@@ -100,8 +104,11 @@ __device__ __forceinline__ int digit_of(const uint64_t* key, const uint32_t* key
 }
 
 // per-tile digit histogram, stored digit-major: hist[d * n_tiles + tile]
-__global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n, int shift, int use2, int* hist, int n_tiles) {
+__global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n0, const int* nd, int small, int shift, int use2, int* hist,
+                             int n_tiles) {
     __shared__ int cnt[256];
+    const int n = nd ? *nd : n0;
+    if (n <= small) return;
     cnt[threadIdx.x] = 0;
     __syncthreads();
     const int base = blockIdx.x * kRadixTile;
@@ -115,8 +122,11 @@ __global__ void k_radix_hist(const uint64_t* key, const uint32_t* key2, int n, i
 
 // stable scatter: items of a tile keep their order within each digit
 __global__ void k_radix_scatter(const uint64_t* key_in, const uint32_t* key2_in, const uint32_t* val_in, uint64_t* key_out,
-                                uint32_t* key2_out, uint32_t* val_out, int n, int shift, int use2, const int* hist, int n_tiles) {
+                                uint32_t* key2_out, uint32_t* val_out, int n0, const int* nd, int small, int shift, int use2,
+                                const int* hist, int n_tiles) {
     __shared__ int base_d[256];          // running output position of each digit for this tile
+    const int n = nd ? *nd : n0;
+    if (n <= small) return;
     __shared__ int warp_cnt[kBlock / 32][256];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     base_d[threadIdx.x] = hist[threadIdx.x * n_tiles + blockIdx.x];
@@ -152,17 +162,35 @@ __global__ void k_radix_scatter(const uint64_t* key_in, const uint32_t* key2_in,
 
 // ---------------------------------------------------------------- narrowphase bucketing
 // pairs grouped by class (order inside a class is free: every pair's result has its own slot);
-// one atomic per class present in a warp
-__global__ void k_np_bucket(int P, const int* cls, int* cursor, int* order) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+// one atomic per class present in a warp.  The pair count is on the device; whole warps stride
+// over it (the loop bound is block-uniform, so every lane takes part in the warp votes).
+__global__ void k_np_bucket(const int* Pd, const int* cls, int* cursor, int* order) {
+    const int P = *Pd;
     const int lane = threadIdx.x & 31;
-    const int c = p < P ? cls[p] : -1 - lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, c);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (c >= 0 && lane == leader) base = atomicAdd(&cursor[c], __popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (c >= 0) order[base + __popc(peers & ((1u << lane) - 1u))] = p;
+    for (int base = blockIdx.x * blockDim.x; base < P; base += gridDim.x * blockDim.x) {
+        const int p = base + threadIdx.x;
+        const int c = p < P ? cls[p] : -1 - lane;
+        const unsigned peers = __match_any_sync(0xffffffffu, c);
+        const int leader = __ffs(peers) - 1;
+        int b = 0;
+        if (c >= 0 && lane == leader) b = atomicAdd(&cursor[c], __popc(peers));
+        b = __shfl_sync(0xffffffffu, b, leader);
+        if (c >= 0) order[b + __popc(peers & ((1u << lane) - 1u))] = p;
+    }
+}
+
+// class ranges from the class counts (one thread): range[c] = [first, end) of class c in the
+// bucketed order, the bucketing cursors at each class's first slot, and the work cursors of the
+// kernels that hand pairs out one at a time (they start at the class's first slot)
+__global__ void k_np_ranges(const int* count, int* cursor, int2* range, int* work) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int run = 0;
+    for (int c = 0; c < PC_COUNT; c++) {
+        range[c] = make_int2(run, run + count[c]);
+        cursor[c] = run;
+        work[c] = run;
+        run += count[c];
+    }
 }
 
 } // namespace pe
@@ -175,15 +203,27 @@ __global__ void k_scene_pair_off(int n_scenes, const int* scene_off, const int* 
     pair_scene_off[s] = pair_scan[scene_off[s]];
 }
 
-__global__ void k_active_flags(int P, const int* npts, int* flag) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < P) flag[p] = npts[p] > 0 ? 1 : 0;
-    else if (p == P) flag[p] = 0;
+// rows of each result before the scan: its point count; zero from the result count up to `bound`
+__global__ void k_rows_init(const int* Rd, int bound, const int* npts, int* row_off) {
+    const int P = *Rd;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= bound; p += gridDim.x * blockDim.x) row_off[p] = p < P ? npts[p] : 0;
 }
 
-__global__ void k_active_compact(int P, const int* npts, const int* scan, int* active) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < P && npts[p] > 0) active[scan[p]] = p;
+// 1 for the results with points, 0 from the result count up to `bound`
+__global__ void k_active_flags(const int* Rd, int bound, const int* npts, int* flag) {
+    const int P = *Rd;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= bound; p += gridDim.x * blockDim.x) flag[p] = p < P && npts[p] > 0 ? 1 : 0;
+}
+
+__global__ void k_active_compact(const int* Rd, const int* npts, const int* scan, int* active) {
+    const int P = *Rd;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x)
+        if (npts[p] > 0) active[scan[p]] = p;
+}
+
+// *out = *a + add (one thread)
+__global__ void k_count_add(const int* a, int add, int* out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = *a + add;
 }
 
 __global__ void k_isl_init(int n, int* parent) {
@@ -191,24 +231,50 @@ __global__ void k_isl_init(int n, int* parent) {
     if (i < n) parent[i] = i;
 }
 
-__global__ void k_isl_flags(int A, const uint64_t* key, int* flag) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < A) flag[k] = (k == 0 || key[k] != key[k - 1]) ? 1 : 0;
-    else if (k == A) flag[k] = 0;
+// island starts among the M = *Md sorted items; 0 from M up to `bound`
+__global__ void k_isl_flags(const int* Md, int bound, const uint64_t* key, int* flag) {
+    const int M = *Md;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= bound; k += gridDim.x * blockDim.x)
+        flag[k] = k < M && (k == 0 || key[k] != key[k - 1]) ? 1 : 0;
 }
 
 // after an exclusive scan of the flags: island id = scan value at each island's first slot
-__global__ void k_isl_offsets(int A, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < A && (k == 0 || key[k] != key[k - 1])) isl_off[scan[k]] = k;
-    if (k == A) { isl_off[scan[A]] = A; *n_isl_out = scan[A]; }
+__global__ void k_isl_offsets(const int* Md, const uint64_t* key, const int* scan, int* isl_off, int* n_isl_out) {
+    const int M = *Md;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= M; k += gridDim.x * blockDim.x) {
+        if (k < M && (k == 0 || key[k] != key[k - 1])) isl_off[scan[k]] = k;
+        if (k == M) { isl_off[scan[M]] = M; *n_isl_out = scan[M]; }
+    }
 }
 
 // islands with more than big_items results
 __global__ void k_isl_big(const int* n_isl, const int* isl_off, int* big, int* n_big, int big_items) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= *n_isl) return;
-    if (isl_off[s + 1] - isl_off[s] > big_items) big[atomicAdd(n_big, 1)] = s;
+    const int NI = *n_isl;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < NI; s += gridDim.x * blockDim.x)
+        if (isl_off[s + 1] - isl_off[s] > big_items) big[atomicAdd(n_big, 1)] = s;
+}
+
+// the step's counters gathered for one copy to the host (World::HostStat order; colours may be absent)
+__global__ void k_step_counters(const int* status, const int* rows, const int* active, const int* islands, const int* big, const int* colors,
+                                const int* cls, int* out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    out[0] = *status;
+    out[1] = *rows;
+    out[2] = *active;
+    out[3] = *islands;
+    out[4] = *big;
+    out[5] = colors ? *colors : 0;
+    out[6] = 0;
+    for (int c = 0; c < PC_COUNT; c++) out[7 + c] = cls[c];
+}
+
+// islands of min_len + 1 .. max_len results (any order: islands share no dynamic body)
+__global__ void k_isl_pick(const int* n_isl, const int* isl_off, int min_len, int max_len, int* list, int* n_list) {
+    const int NI = *n_isl;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < NI; s += gridDim.x * blockDim.x) {
+        const int m = isl_off[s + 1] - isl_off[s];
+        if (m > min_len && m <= max_len) list[atomicAdd(n_list, 1)] = s;
+    }
 }
 
 // colour histogram of an island (cnt[c + 1] counts colour c); uncoloured results join the last colour

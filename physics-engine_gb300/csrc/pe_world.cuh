@@ -1,7 +1,9 @@
 // Host orchestration of the device-resident world (the GB300 counterpart of pe_intf::World).
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
+#include <map>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -23,6 +25,12 @@ struct CudaError : std::runtime_error {
         if (e_ != cudaSuccess) throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));    \
     } while (0)
 
+// Counts device-array reallocations in this process: a captured step graph holds the addresses it
+// was captured with, so any reallocation since then sends the step back through a new capture.
+inline std::atomic<unsigned long long>& dbuf_generation() {
+    static std::atomic<unsigned long long> g{0};
+    return g;
+}
 template <class T> struct DBuf {   // device array that grows on demand
     T* p = nullptr;
     size_t n = 0;
@@ -39,6 +47,7 @@ template <class T> struct DBuf {   // device array that grows on demand
         if (p) cudaFree(p);
         p = q;
         n = cap;
+        dbuf_generation()++;
     }
 };
 
@@ -92,6 +101,9 @@ public:
     virtual void phase_times(double* ms, bool reset) = 0;
     virtual void last_counts(int* c) = 0;
     virtual void sync() = 0;
+    // steps replay a captured CUDA graph of their device part (on by default)
+    virtual void set_step_graphs(bool on) = 0;
+    virtual bool step_graphs() const = 0;
     // serving: replace the scene list by the kept scenes (old indices, in the new order) followed by
     // the added ones, keeping the kept scenes' bodies, sweep axes and contact-result pools on the device
     virtual void repack(const int* keep, int n_keep, const SceneData* const* adds, int n_add) = 0;
@@ -140,6 +152,8 @@ public:
     void phase_times(double* ms, bool reset) override;
     void last_counts(int* c) override;
     void sync() override { PE_CK(cudaStreamSynchronize(st_)); }
+    void set_step_graphs(bool on) override { graphs_ = on; }
+    bool step_graphs() const override { return graphs_; }
     void repack(const int* keep, int n_keep, const SceneData* const* adds, int n_add) override;
     const std::vector<int>& scene_body_offsets() const override { return h_scene_off_; }
     void get_state_range(int first, int count, double* o, double* b, double* v, double* w) override;
@@ -260,16 +274,76 @@ private:
     int scan(int* data, int n);   // exclusive scan in place; returns the total (synchronises)
     void scan_async(int* data, int n, int* total);   // exclusive scan in place, total to device memory
     DBuf<int> rows_total_;
-    int* h_rows_ = nullptr;       // pinned: the last solve's row total, read at the step's end
-    bool rows_pending_ = false;
-    void take_rows() { if (rows_pending_) { PE_CK(cudaStreamSynchronize(st_)); n_rows_ = *h_rows_; rows_pending_ = false; } }
+
+    // ---- the step without host waits between its phases.  The device holds the sizes the phases
+    // pass on (pairs, results, active results, island items, medium islands); kernels read them
+    // there, and their grids come from upper bounds (the pair capacity), at most the GPU's resident
+    // blocks.  The host waits twice per step: for the pair count (the capacities follow it) and for
+    // the step's counters at its end.
+    enum DevCount { DC_P = 0, DC_R, DC_A, DC_M, DC_NMED, DC_MEDCUR, DC_COUNT };
+    DBuf<int> dcnt_;
+    DBuf<int2> cls_rng_;   // [first, end) of each pair class in the bucketed order
+    DBuf<int> cls_work_;   // per-class work cursors of the pair-at-a-time kernels
+    DBuf<int> isl_med_;    // islands above small_island_items and up to big_island_items results
+    const uint32_t* isl_order_ = nullptr;   // island items sorted by island (points into val_)
+    // counters read back at the step's end, one copy into page-locked memory
+    // (k_step_counters writes them in this order)
+    enum HostStat { HS_STATUS = 0, HS_ROWS, HS_ACTIVE, HS_ISLANDS, HS_BIG, HS_COLORS, HS_P, HS_CLS, HS_COUNT = HS_CLS + PC_COUNT };
+    DBuf<int> dstat_;
+    int* hstat_ = nullptr;
+    int h_cls_[PC_COUNT] = {};   // the last step's pair-class counts (the side-stream plan)
+    int stream_of_[PC_COUNT] = {};
+    void plan_streams(int* plan) const;
+    int bp_count();                 // integrate's successor up to the pair count (waits for it)
+    void prepare_tail(int P);       // every capacity the rest of the step needs, before any launch of it
+    void bp_tail();                 // pair list, scene pair offsets, sweep axes
+    void np_enqueue();              // narrowphase, no host waits
+    void solve_enqueue(int mode);   // solver up to the velocity sync and the counters' copy, no host waits
+    void finish(int mode);          // waits for the counters; big islands; status
+    void run_tail(int mode);        // bp_tail .. solve_enqueue, replayed from a CUDA graph when enabled
+    int radix_sort_dev(int bound, int key_passes, const int* nd);
+    // resident blocks of a kernel at a block size and dynamic shared memory (cached), and a grid for
+    // `items` items of `per_block` items per block, at most those
+    std::map<std::tuple<const void*, int, size_t>, int> resident_;
+    int sms_ = 0;
+    template <class Kern> int resident(Kern kern, int block, size_t smem) {
+        const auto key = std::make_tuple((const void*)kern, block, smem);
+        auto it = resident_.find(key);
+        if (it != resident_.end()) return it->second;
+        if (sms_ == 0) PE_CK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev_));
+        int b = 0;
+        PE_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, block, smem));
+        const int r = std::max(b, 1) * sms_;
+        resident_[key] = r;
+        return r;
+    }
+    template <class Kern> int pgrid(long long items, int per_block, Kern kern, int block = kBlock, size_t smem = 0) {
+        const long long g = std::max((items + per_block - 1) / per_block, 1ll);
+        return (int)std::min<long long>(g, resident(kern, block, smem));
+    }
+    // captured step graphs, by solver mode and contact-distance generation, with what they baked in
+    struct GraphSig {
+        unsigned long long gen;
+        const void* order;
+        int n, ns, pair_cap, rows_cap, nj, n_ign, s, side;
+        int plan[PC_COUNT];
+        StepParams prm;
+        R margin;
+        Tuning tun;
+    };
+    void graph_sig(GraphSig& g) const;
+    cudaGraphExec_t gexec_[2][2] = {};
+    GraphSig gsig_[2][2];
+    GraphSig last_sig_;     // the previous step's (a capture waits for one repeat)
+    long long glaunch_[2][2] = {};
+    bool graphs_ = true, capturing_ = false;
+    long long steps_since_plan_ = 0;
     R* staging(size_t n);         // pinned host buffer of at least n reals
     R* stage_ = nullptr;
     size_t stage_n_ = 0;
     void radix_sort(int n, int n_scene_passes);
     int radix_sort_keys(int n, int key_passes, int scene_passes);   // returns the buffer holding the result
     void ensure_pair_capacity(int P);
-    void check_status();
     void ev_begin(int phase);
     void ev_end(int phase);
     void ev_collect();
@@ -332,6 +406,7 @@ private:
     DBuf<int> bp_wend_, bp_csize_, bp_nch_, bp_choff_, bp_ctot_, bp_ccount_, bp_cpref_;   // crowded windows in chunks
     static constexpr int kBigSweepBlocks = 152;   // blocks that share the crowded positions
     uint32_t* order_ = nullptr;   // sorted body order (points into val_)
+    int max_scene_ = 0;           // bodies of the largest scene (the crowded-window kernels run above kBigWindow)
     DBuf<int2> pairs_;
     int P_ = 0, pair_cap_ = 0;
     // narrowphase
@@ -349,7 +424,7 @@ private:
     DBuf<double> xfer_;   // state transfers in the C ABI's layout
     DBuf<int> gc_left_;   // items left after each colouring round
     DBuf<int> gc_level_;  // coloured mode: exact levels of a big island beside its first-fit colours
-    void solve_big_islands(int NI, const uint32_t* order, bool exact);
+    void solve_big_islands(int nb, const uint32_t* order, bool exact);
     DBuf<R> rows_;
     int rows_cap_ = 0, n_rows_ = 0, n_active_ = 0, n_colors_ = 0, n_islands_ = 0;
     bool sat_attr_ = false;

@@ -104,6 +104,7 @@ template <class R> void World<R>::set_pairs(int n, const int* p) {
     if (n) PE_CK(cudaMemcpyAsync(pairs_.p, p, (size_t)n * sizeof(int2), cudaMemcpyHostToDevice, st_));
     h_pair_scene_off_ = scene_offsets(n, p, h_scene_off_);
     PE_CK(cudaMemcpyAsync(pair_scene_off_.p, h_pair_scene_off_.data(), (NS_ + 1) * sizeof(int), cudaMemcpyHostToDevice, st_));
+    PE_CK(cudaMemcpyAsync(dcnt_.p + DC_P, &n, sizeof(int), cudaMemcpyHostToDevice, st_));
     PE_CK(cudaStreamSynchronize(st_));
     P_ = n;
 }
@@ -177,6 +178,7 @@ void World<R>::set_results(int n, const int* a, const int* b, const int* ps, con
         PE_CK(cudaMemcpyAsync(res_pts_.p, pts.data(), pts.size() * sizeof(R), cudaMemcpyHostToDevice, st_));
     }
     PE_CK(cudaMemcpyAsync(res_scene_off_.p, off.data(), (NS_ + 1) * sizeof(int), cudaMemcpyHostToDevice, st_));
+    PE_CK(cudaMemcpyAsync(dcnt_.p + DC_R, &n, sizeof(int), cudaMemcpyHostToDevice, st_));
     PE_CK(cudaStreamSynchronize(st_));
     R_ = n;
 }

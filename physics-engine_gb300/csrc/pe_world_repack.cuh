@@ -150,6 +150,7 @@ void World<R>::repack(const int* keep, int n_keep, const SceneData* const* adds,
     h_pair_scene_off_ = zero;
     P_ = 0;
     R_ = 0;
+    PE_CK(cudaMemsetAsync(dcnt_.p, 0, DC_COUNT * sizeof(int), st_));
     PE_CK(cudaStreamSynchronize(st_));
 }
 

@@ -23,14 +23,21 @@ template <class R> World<R>::World(int device) : dev_(device) {
     PE_CK(cudaMemset(status_.p, 0, sizeof(int)));
     total_.ensure(1);
     rows_total_.ensure(1);
-    PE_CK(cudaMallocHost(&h_rows_, sizeof(int)));
+    dcnt_.ensure(DC_COUNT);
+    PE_CK(cudaMemset(dcnt_.p, 0, DC_COUNT * sizeof(int)));
+    std::memset(gsig_, 0, sizeof gsig_);
+    std::memset(&last_sig_, 0xff, sizeof last_sig_);
+    dstat_.ensure(HS_COUNT);
+    PE_CK(cudaMallocHost(&hstat_, HS_COUNT * sizeof(int)));
+    std::memset(hstat_, 0, HS_COUNT * sizeof(int));
     set_scenes(1, nullptr);
 }
 
 template <class R> World<R>::~World() {
     if (st_) cudaStreamSynchronize(st_);
     if (stage_) cudaFreeHost(stage_);
-    if (h_rows_) cudaFreeHost(h_rows_);
+    if (hstat_) cudaFreeHost(hstat_);
+    for (auto& m : gexec_) for (auto& g : m) if (g) cudaGraphExecDestroy(g);
     for (auto& q : pending_) { cudaEventDestroy(q.e0); cudaEventDestroy(q.e1); }
     for (auto e : ev_pool_) cudaEventDestroy(e);
     for (auto& e : ev_) { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
@@ -42,12 +49,13 @@ template <class R> World<R>::~World() {
     if (st_) cudaStreamDestroy(st_);
 }
 
+// phase events; inside a graph capture they become event-record nodes of the graph
 template <class R> void World<R>::ev_begin(int k) {
-    PE_CK(cudaEventRecord(ev_[k][0], st_));
+    PE_CK(cudaEventRecordWithFlags(ev_[k][0], st_, capturing_ ? cudaEventRecordExternal : cudaEventRecordDefault));
     ev_open_[k] = true;
 }
 template <class R> void World<R>::ev_end(int k) {
-    PE_CK(cudaEventRecord(ev_[k][1], st_));
+    PE_CK(cudaEventRecordWithFlags(ev_[k][1], st_, capturing_ ? cudaEventRecordExternal : cudaEventRecordDefault));
     ev_open_[k] = false;
 }
 // the phases' durations, once the step's last event has completed (one wait per step)
@@ -64,20 +72,7 @@ template <class R> void World<R>::phase_times(double* ms, bool reset) {
     if (reset) for (double& m : ms_) m = 0;
 }
 template <class R> void World<R>::last_counts(int* c) {
-    take_rows();
     c[0] = P_; c[1] = n_active_; c[2] = n_rows_; c[3] = n_colors_; c[4] = (int)last_step_launches_; c[5] = n_islands_;
-}
-
-template <class R> void World<R>::check_status() {
-    int s = 0;
-    PE_CK(cudaMemcpyAsync(&s, status_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-    PE_CK(cudaStreamSynchronize(st_));
-    ev_collect();
-    take_rows();
-    if (s) {
-        PE_CK(cudaMemsetAsync(status_.p, 0, sizeof(int), st_));
-        throw std::runtime_error("device capacity overflow (status " + std::to_string(s) + ")");
-    }
 }
 
 template <class R> ShapeTable<R> World<R>::shapes() const {
@@ -429,6 +424,7 @@ template <class R> void World<R>::set_scenes(int ns, const int* off) {
     h_pair_scene_off_ = zero;
     P_ = 0;
     R_ = 0;
+    PE_CK(cudaMemsetAsync(dcnt_.p, 0, DC_COUNT * sizeof(int), st_));
     PE_CK(cudaStreamSynchronize(st_));
 }
 

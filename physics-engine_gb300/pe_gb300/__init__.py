@@ -68,6 +68,7 @@ def load(build_if_missing: bool = True):
         "pe_gpu_last_counts": (I, [P, ip]),
         "pe_gpu_sync": (I, [P]),
         "pe_gpu_set_profiling": (I, [P, I]),
+        "pe_gpu_set_step_graphs": (I, [P, I]),
         "pe_gpu_kernel_count": (I, []),
         "pe_gpu_kernel_name": (C.c_char_p, [I]),
         "pe_gpu_kernel_stats": (I, [P, dp, np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]),
@@ -200,6 +201,10 @@ class GpuWorld:
             pass
 
     # ---------------------------------------------------------------- stepping
+    def set_params(self, dt, gravity=(0.0, -9.8, 0.0), iterations=10):
+        """World::setDt / setGravity and the solver's iteration count."""
+        self._ck(self.lib.pe_gpu_set_params(self.h, float(dt), *map(float, gravity), int(iterations)))
+
     def set_scenes(self, body_off):
         off = _i32(body_off)
         self._ck(self.lib.pe_gpu_set_scenes(self.h, len(off) - 1, off))
@@ -324,6 +329,10 @@ class GpuWorld:
 
     def set_profiling(self, on=True):
         self._ck(self.lib.pe_gpu_set_profiling(self.h, int(bool(on))))
+
+    def set_step_graphs(self, on=True):
+        """Replay each step's device part from a captured CUDA graph (default) or launch it kernel by kernel."""
+        self._ck(self.lib.pe_gpu_set_step_graphs(self.h, int(bool(on))))
 
     def kernel_stats(self):
         """{kernel group: (device ms, launches)} accumulated while profiling was on."""
