@@ -59,6 +59,11 @@ def make_workload(name, n_scenes=4096):
         return s, 64, 0, None, dict(workload="1,000-box 10x10x10 tower + ground + sphere at 30 m/s, full step, FP64, "
                                              "20 SI iterations, contact margin 0.005, serial-order solver",
                                     bodies=s.n_bodies, scenes=1, solver="serial-order", margin=0.005)
+    if name == "tower_colored":
+        s = sc.tower(real_bits=32)
+        return s, 32, 1, None, dict(workload="the same tower (1,000 boxes, ground, sphere at 30 m/s), FP32, 20 SI iterations, "
+                                             "contact margin 0.005, coloured Gauss-Seidel",
+                                    bodies=s.n_bodies, scenes=1, solver="coloured", margin=0.005)
     if name == "batched":
         s, offs = sc.batched_piles(n_scenes=n_scenes, seed=4096, real_bits=32)
         return s, 32, 1, offs, dict(workload=f"{n_scenes:,} independent piles of 8..512 bodies (log-uniform; box/sphere/cylinder/"
@@ -365,9 +370,11 @@ def run_ours(args, rank, world, device):
     return res, scene, bits, offs
 
 
-def run_leg(name, steps, warmup, device):
+def run_leg(name, steps, warmup, device, cpu=False):
     """One of the other configurations on the GPU, device-timed like the main line (L2 flushed
-    between steps): body-steps/s, p50/p99 step time, pairs and contact points of the last step."""
+    between steps): body-steps/s, p50/p99 step time, pairs and contact points of the last step;
+    with `cpu`, the reference's CPU step (the oracle port, all host threads, serial order) on the
+    same scene and precision from its initial state, a few seconds' sample."""
     import pe_gb300 as pg
     scene, bits, mode, offs, cfg = make_workload(name)
     g = pg.GpuWorld(scene, bits, device=device, scenes=offs, margin=cfg.get("margin", 0.0), tuning="auto")
@@ -383,9 +390,12 @@ def run_leg(name, steps, warmup, device):
     c = g.last_counts()
     g.close()
     per_sorted = sorted(per)
-    return dict(value=scene.n_bodies * steps / (sum(per) * 1e-3), unit=UNIT, ms_per_step=sum(per) / steps, steps=steps,
-                p50_step_ms=per_sorted[len(per) // 2], p99_step_ms=per_sorted[min(len(per) - 1, int(0.99 * len(per)))],
-                pairs=c["pairs"], contact_points=c["rows"], dtype="f64" if bits == 64 else "f32", **cfg)
+    out = dict(value=scene.n_bodies * steps / (sum(per) * 1e-3), unit=UNIT, ms_per_step=sum(per) / steps, steps=steps,
+               p50_step_ms=per_sorted[len(per) // 2], p99_step_ms=per_sorted[min(len(per) - 1, int(0.99 * len(per)))],
+               pairs=c["pairs"], contact_points=c["rows"], dtype="f64" if bits == 64 else "f32", **cfg)
+    if cpu:
+        out["cpu_reference"] = cpu_baseline(scene, bits, None, budget_s=4.0, margin=cfg.get("margin", 0.0))
+    return out
 
 
 def per_scene_gpu(pg, scene, offs, state, bits, mode, device, steps, sample=64, warmup=3):
@@ -536,7 +546,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["batched", "stress", "tower", "large", "serving"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "stress", "tower", "tower_colored", "large", "serving"])
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window of the serving workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scenes", type=int, default=4096, help="scene count of the batched workload")
@@ -631,8 +641,8 @@ def main():
                                            steps=args.steps, margin=res["cfg"].get("margin", 0.0))
     if not args.no_legs and world == 1 and args.workload == "batched" and not args.profile_one_step:
         legs = {}
-        for name, k in (("stress", 10), ("large", 10), ("tower", 20)):
-            legs[name] = run_leg(name, k, 3, local)
+        for name, k in (("stress", 10), ("large", 10), ("tower", 20), ("tower_colored", 20)):
+            legs[name] = run_leg(name, k, 3, local, cpu=name.startswith("tower") and not args.no_cpu_baseline)
         sv = run_serving(argparse.Namespace(serve_seconds=10.0), local)
         legs["serving"] = dict(value=sv["value"], unit=UNIT, **{k: sv["config"][k] for k in (
             "workload", "requests", "finished", "p50_step_ms", "p99_step_ms", "mean_step_ms", "p50_request_s", "p99_request_s",

@@ -13,6 +13,9 @@ namespace pe {
 constexpr int kSatF = 128, kSatE = 192, kSatV = 64;
 constexpr int kSatWarps = 1;                 // pairs (one warp each) per block, light pairs
 constexpr int kSatGroup = 8;                 // warps per pair, heavy pairs (one block each)
+// resident light SAT blocks per SM the registers are sized for: 12 leaves the warp loop unspilled
+// (16, at most 128 registers, spilled: the batched step measured 0.16 ms slower)
+constexpr int kSatBlocksPerSm = 12 / kSatWarps;
 template <class R> __device__ __forceinline__ bool sat_fits(const ShapeView<R>& s) {
     return s.face_count() <= kSatF && s.edge_count() <= kSatE && (s.type != ST_HULL || s.nv <= kSatV);
 }

@@ -677,7 +677,7 @@ template <class R> constexpr int sat_group_reals(int G) {
 }
 static_assert(sat_group_reals<float>(1) % 4 == 0 && (3 * (2 * kSatF + 2 * kSatE)) % 4 == 0, "SAT staging alignment");
 template <class R, int G, int TA, int TB>
-__global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? 16 / kSatWarps : 2)
+__global__ void __launch_bounds__(G == 1 ? 32 * kSatWarps : 32 * G, G == 1 ? kSatBlocksPerSm : 2)
 k_np_sat(const int2* rng, int* cursor, const int* order, const int2* pairs, Bodies<R> B, ShapeTable<R> S, R* sat_out) {
     extern __shared__ __align__(16) unsigned char sat_smem[];
     const int grp = G == 1 ? (int)(threadIdx.x >> 5) : 0;
