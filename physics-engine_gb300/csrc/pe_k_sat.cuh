@@ -280,6 +280,35 @@ __device__ __forceinline__ bool sat_prunable(const Pair<R>& c, bool able, const 
     constexpr R u = sizeof(R) == 4 ? R(1.1920929e-7) : R(2.220446049250313e-16);
     return lb > best + R(64) * u * (mA + mB + rabs(best));
 }
+// The same test on an unnormalised axis x of length nx (computed as the reference's norm): every
+// projection scales by nx, so the bound and the slack are scaled by nx instead of dividing x by
+// it.  The normalisation the test skips changes each projection by a few units of roundoff, well
+// inside the 64-unit slack.  For boxes and hulls only (a cylinder's closed form branches on
+// near-zero components of the normalised axis).
+template <class R>
+__device__ __forceinline__ void prune_side_scaled(const ShapeView<R>& s, const Xf<R>& t, const V3<R>& x, R nx, R& lo, R& hi, R& mag) {
+    if (s.type == ST_HULL) {
+        const R o = dot(t.o, x);
+        lo = o + s.inner * nx;
+        hi = o - s.inner * nx;
+        mag = rabs(o) + s.outer * nx;
+        return;
+    }
+    int i0, i1;
+    shape_interval(s, t, x, (const R*)nullptr, hi, lo, i0, i1);
+    mag = rabs(hi) + rabs(lo);
+}
+template <class R>
+__device__ __forceinline__ bool sat_prunable_scaled(const Pair<R>& c, bool able, const V3<R>& x, R nx, R best) {
+    if (!able || !(best < Lim<R>::max())) return false;
+    R loA, hiA, mA, loB, hiB, mB;
+    prune_side_scaled(c.sa, c.ta(), x, nx, loA, hiA, mA);
+    prune_side_scaled(c.sb, c.tb(), x, nx, loB, hiB, mB);
+    const R d0 = loA - hiB, d1 = loB - hiA;
+    const R lb = d0 < d1 ? d0 : d1;
+    constexpr R u = sizeof(R) == 4 ? R(1.1920929e-7) : R(2.220446049250313e-16);
+    return lb > nx * best + R(64) * u * (mA + mB + nx * rabs(best));
+}
 // Compacts the candidate axes [base, base + span) ∩ [0, n) that `keep` accepts into the group's
 // queue and returns their count (the same in every thread of the group).  With one warp the queue
 // keeps ascending order; with several, warps append in any order.
@@ -438,6 +467,7 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
     V3<R> ewa, ewb, en;
     const bool boxA = c.sa.type == ST_BOX, boxB = c.sb.type == ST_BOX;
     const int ua = boxA ? 3 : na, ub = boxB ? 3 : nb;
+    const bool cyl = c.sa.type == ST_CYLINDER || c.sb.type == ST_CYLINDER;
     const int ne = ua * ub;
     auto edge_axis = [&](int q, V3<R>& a) {   // false for parallel edges
         const int iu = q / ub, ju = q - iu * ub;
@@ -451,8 +481,14 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
       R pb = ed;
       warp_min(pb);
       const int cnt = sat_queue<G>(pass, kSatQ * T, ne, tid, queue, qn, [&](int q) {
-          V3<R> a;
-          return edge_axis(q, a) && !sat_prunable(c, able, a, pb);
+          if (cyl) {
+              V3<R> a;
+              return edge_axis(q, a) && !sat_prunable(c, able, a, pb);
+          }
+          const int iu = q / ub, ju = q - iu * ub;
+          const V3<R> x = cross(ld3(st.dA, boxA ? 4 * iu : iu), ld3(st.dB, boxB ? 4 * ju : ju));
+          const R nx = norm(x);
+          return !(rabs(nx - 0) < eps<R>()) && !sat_prunable_scaled(c, able, x, nx, pb);   // parallel edges: no axis
       });
       for (int qb = 0; qb < cnt; qb += 2 * T) {
         V3<R> cr[2];
