@@ -1002,7 +1002,7 @@ template <class R> __device__ bool concave_convex(Pair<R>& c) {
         face.type = ST_HULL;
         face.hv = fv; face.nv = n;
         face.f_off = foff; face.f_idx = fidx; face.f_n = fn; face.f_min = fmn; face.f_max = fmx; face.nf = 1;
-        face.e_a = nullptr; face.e_b = nullptr; face.ne = 0;
+        face.e_a = nullptr; face.e_b = nullptr; face.e_d = nullptr; face.ne = 0;
         face.nl = 0;
         Pair<R> s = c;
         s.sa = cv; s.sb = face; s.xa = tcv; s.xb = tcc;

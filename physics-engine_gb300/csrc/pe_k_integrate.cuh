@@ -56,4 +56,15 @@ __global__ void k_integrate(Bodies<R> B, ShapeTable<R> S, StepParams P, int do_m
     B.at(SCALE, i) = (sc + df) * R(0.5);
 }
 
+// unit direction of every hull edge, normalized(a - b) in the world's real type: the staged SAT
+// reads these instead of normalising each edge of both shapes for every pair
+template <class R>
+__global__ void k_hull_edge_dirs(int n, const R* ea, const R* eb, R* ed) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const V3<R> a(ea[3 * e], ea[3 * e + 1], ea[3 * e + 2]), b(eb[3 * e], eb[3 * e + 1], eb[3 * e + 2]);
+    const V3<R> d = normalized(a - b);
+    ed[3 * e] = d.x; ed[3 * e + 1] = d.y; ed[3 * e + 2] = d.z;
+}
+
 } // namespace pe

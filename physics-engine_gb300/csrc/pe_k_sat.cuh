@@ -374,8 +374,15 @@ __device__ void sat_staged(Pair<R>& c, int tid, R* smem, R* out) {
     const int na = c.sa.edge_count(), nb = c.sb.edge_count();
     for (int f = tid; f < fa; f += T) st3(st.nA, f, mv(c.ta().b, c.sa.face_normal(f)));
     for (int f = tid; f < fb; f += T) st3(st.nB, f, mv(c.tb().b, c.sb.face_normal(f)));
-    for (int e = tid; e < na; e += T) { V3<R> a0, a1; c.sa.edge(e, a0, a1); st3(st.dA, e, mv(c.ta().b, normalized(a0 - a1))); }
-    for (int e = tid; e < nb; e += T) { V3<R> b0, b1; c.sb.edge(e, b0, b1); st3(st.dB, e, mv(c.tb().b, normalized(b0 - b1))); }
+    // unit edge directions: a hull's come precomputed (k_hull_edge_dirs, the same arithmetic)
+    auto edge_unit = [](const ShapeView<R>& sh, int e) {
+        if (sh.type == ST_HULL) return sh.edge_dir(e);
+        V3<R> a0, a1;
+        sh.edge(e, a0, a1);
+        return normalized(a0 - a1);
+    };
+    for (int e = tid; e < na; e += T) st3(st.dA, e, mv(c.ta().b, edge_unit(c.sa, e)));
+    for (int e = tid; e < nb; e += T) st3(st.dB, e, mv(c.tb().b, edge_unit(c.sb, e)));
     if (c.sa.type == ST_HULL) for (int i = tid; i < c.sa.nv; i += T) stv(st.vA, i, c.sa.vert(i));
     if (c.sb.type == ST_HULL) for (int i = tid; i < c.sb.nv; i += T) stv(st.vB, i, c.sb.vert(i));
     int* queue = reinterpret_cast<int*>(smem + sat_stage_reals<R>() + sat_scratch_reals<R>(G));

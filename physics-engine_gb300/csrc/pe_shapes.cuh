@@ -48,6 +48,7 @@ template <class R> struct ShapeView {
     int nf;
     const R* e_a;              // unique edge endpoints [ne*3]
     const R* e_b;
+    const R* e_d;              // unit edge directions normalized(e_a - e_b), computed once per hull
     int ne;
     R inner, outer;            // hulls: balls about the local origin inside / around the vertices (inner < 0: none)
     // concave meshes: the face tree's leaves in tree order, each a face range and its box
@@ -83,6 +84,8 @@ template <class R> struct ShapeView {
         if (type == ST_CYLINDER) return V3<R>(R(g_unit.cyl_n[f][0]), R(g_unit.cyl_n[f][1]), R(g_unit.cyl_n[f][2]));
         return V3<R>(f_n[f * 3], f_n[f * 3 + 1], f_n[f * 3 + 2]);
     }
+    // unit direction of hull edge e: normalized(a - b) of edge(e, a, b), as stored by k_hull_edge_dirs
+    __device__ V3<R> edge_dir(int e) const { return V3<R>(e_d[e * 3], e_d[e * 3 + 1], e_d[e * 3 + 2]); }
     __device__ void edge(int e, V3<R>& a, V3<R>& b) const {
         if (type == ST_BOX) {
             a = cmul(V3<R>(R(g_unit.box_e[e][0]), R(g_unit.box_e[e][1]), R(g_unit.box_e[e][2])), size);
@@ -106,6 +109,7 @@ template <class R> struct ShapeTable {
     const int* h_vbeg; const int* h_vcnt; const int* h_fbeg; const int* h_fcnt; const int* h_ebeg; const int* h_ecnt;
     const R* hv; const int* f_off; const int* f_idx; const R* f_n; const R* f_min; const R* f_max;
     const R* e_a; const R* e_b;
+    const R* e_d;         // [E*3] unit directions of the hull edges (k_hull_edge_dirs)
     const R* h_rad;       // [H*2] per hull: inner and outer radius about the local origin
     // concave meshes (hull tables plus the face-tree leaves): leaves [h_lbeg[h], h_lbeg[h] + h_lcnt[h])
     const int* h_lbeg; const int* h_lcnt; const int* lf_beg; const int* lf_cnt; const R* lf_min; const R* lf_max;
@@ -134,7 +138,7 @@ template <class R> struct ShapeTable {
         v.height = p1;
         v.r2 = p0 * 2;
         v.hv = nullptr; v.nv = 0; v.f_off = nullptr; v.f_idx = nullptr; v.f_n = nullptr; v.f_min = nullptr; v.f_max = nullptr;
-        v.nf = 0; v.e_a = nullptr; v.e_b = nullptr; v.ne = 0;
+        v.nf = 0; v.e_a = nullptr; v.e_b = nullptr; v.e_d = nullptr; v.ne = 0;
         v.inner = R(-1); v.outer = R(0);
         v.nl = 0; v.l_beg = nullptr; v.l_cnt = nullptr; v.l_min = nullptr; v.l_max = nullptr;
         if (v.type == ST_HULL || v.type == ST_CONCAVE) {
@@ -144,7 +148,7 @@ template <class R> struct ShapeTable {
             v.inner = h_rad[2 * h]; v.outer = h_rad[2 * h + 1];
             v.f_off = f_off + fb; v.f_idx = f_idx; v.f_n = f_n + fb * 3; v.f_min = f_min + fb * 3; v.f_max = f_max + fb * 3;
             v.nf = h_fcnt[h];
-            v.e_a = e_a + eb * 3; v.e_b = e_b + eb * 3; v.ne = h_ecnt[h];
+            v.e_a = e_a + eb * 3; v.e_b = e_b + eb * 3; v.e_d = e_d + eb * 3; v.ne = h_ecnt[h];
             if (v.type == ST_CONCAVE) {
                 const int lb = h_lbeg[h];
                 v.nl = h_lcnt[h];

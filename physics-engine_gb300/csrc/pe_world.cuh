@@ -363,7 +363,7 @@ private:
     // shapes
     int S_ = 0;
     DBuf<int> stype_, shull_, hvbeg_, hvcnt_, hfbeg_, hfcnt_, hebeg_, hecnt_, hfoff_, hfidx_;
-    DBuf<R> sparam_, hv_, hfn_, hfmin_, hfmax_, hea_, heb_, hrad_;
+    DBuf<R> sparam_, hv_, hfn_, hfmin_, hfmax_, hea_, heb_, hed_, hrad_;
     std::vector<int> h_stype_;
     std::vector<R> h_sparam_;
     std::vector<M3<R>> h_sinertia_;

@@ -81,7 +81,7 @@ template <class R> ShapeTable<R> World<R>::shapes() const {
     t.h_vbeg = hvbeg_.p; t.h_vcnt = hvcnt_.p; t.h_fbeg = hfbeg_.p; t.h_fcnt = hfcnt_.p; t.h_ebeg = hebeg_.p; t.h_ecnt = hecnt_.p;
     t.h_rad = hrad_.p;
     t.hv = hv_.p; t.f_off = hfoff_.p; t.f_idx = hfidx_.p; t.f_n = hfn_.p; t.f_min = hfmin_.p; t.f_max = hfmax_.p;
-    t.e_a = hea_.p; t.e_b = heb_.p;
+    t.e_a = hea_.p; t.e_b = heb_.p; t.e_d = hed_.p;
     t.c_beg = cbeg_.p; t.c_cnt = ccnt_.p; t.c_shape = cshape_.p; t.c_xf = cxf_.p;
     t.h_lbeg = hlbeg_.p; t.h_lcnt = hlcnt_.p; t.lf_beg = lfbeg_.p; t.lf_cnt = lfcnt_.p; t.lf_min = lfmin_.p; t.lf_max = lfmax_.p;
     t.margin = margin_;
@@ -226,6 +226,9 @@ int World<R>::append_shapes(int S, const int* type, const double* param, const i
     upload_tail(hlbeg_, h_hlb_, o_h, st_); upload_tail(hlcnt_, h_hlc_, o_h, st_);
     upload_tail(lfbeg_, h_lfb_, o_l, st_); upload_tail(lfcnt_, h_lfc_, o_l, st_);
     upload_tail(lfmin_, h_lfmn_, o_l * 3, st_); upload_tail(lfmax_, h_lfmx_, o_l * 3, st_);
+    const int n_edges = (int)(h_ea_.size() / 3);
+    hed_.ensure((size_t)std::max(n_edges, 1) * 3);
+    if (n_edges > 0) launch(K_MISC, grid(n_edges), k_hull_edge_dirs<R>, n_edges, (const R*)hea_.p, (const R*)heb_.p, hed_.p);
     PE_CK(cudaStreamSynchronize(st_));
     return s0;
 }
