@@ -196,7 +196,7 @@ int pe_gpu_set_results(pe_gpu_world* w, int n, const int* a, const int* b, const
  * ms[0] integrate, ms[1] broadphase, ms[2] narrowphase, ms[3] solver, ms[4] whole steps. */
 int pe_gpu_phase_times(pe_gpu_world* w, double* ms, int reset);
 /* counts6: pairs, non-empty results, contact points (solver rows), colours, kernel launches of the
- * last pe_gpu_step step, 0 */
+ * last pe_gpu_step step (a replayed step graph counts its kernel nodes), contact islands */
 int pe_gpu_last_counts(pe_gpu_world* w, int* counts6);
 /* Per-kernel-group device time: with profiling on, every kernel launch is bracketed by CUDA events
  * on the world's stream.  ms[k] / launches[k] for k < pe_gpu_kernel_count() (cumulative). */

@@ -325,7 +325,7 @@ class GpuWorld:
     def last_counts(self):
         c = np.zeros(6, np.int32)
         self._ck(self.lib.pe_gpu_last_counts(self.h, c))
-        return dict(pairs=int(c[0]), active=int(c[1]), rows=int(c[2]), colors=int(c[3]), launches=int(c[4]))
+        return dict(pairs=int(c[0]), active=int(c[1]), rows=int(c[2]), colors=int(c[3]), launches=int(c[4]), islands=int(c[5]))
 
     def set_profiling(self, on=True):
         self._ck(self.lib.pe_gpu_set_profiling(self.h, int(bool(on))))
