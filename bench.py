@@ -23,7 +23,8 @@ workload.  `value` = body-steps per second of device time with the state residen
 (CUDA events on the library's stream, L2 flushed between steps); `e2e` = the same metric
 through the C ABI with host buffers over the same steps (replayed from a snapshot of the state,
 contact results and sweep axes taken before the timed region): every step uploads body poses and
-velocities from page-locked host arrays and reads the stepped ones back into them.  `--impl reference` times the reference's CPU step (its
+velocities (in the world's real type) from page-locked host arrays and reads the stepped ones back
+into them.  `--impl reference` times the reference's CPU step (its
 algorithm restated in oracle/, multithreaded over the host cores like the reference's thread
 pool) on the same workload.
 """
@@ -331,10 +332,12 @@ def run_ours(args, rank, world, device):
     ks = g.kernel_stats()
     # end to end through the C ABI with host buffers, over the same steps as the timed region
     # (restored from the snapshot): each step copies the poses and velocities in from page-locked
-    # host arrays and reads the stepped ones back into them
+    # host arrays and reads the stepped ones back into them, in the world's real type (float32 for
+    # an FP32 world: the reference's default pe::Real)
     import torch   # page-locked host memory
     io = ("origin", "basis", "lin_vel", "ang_vel")
-    st = {f: torch.empty((N, 3, 3) if f == "basis" else (N, 3), dtype=torch.float64, pin_memory=True).numpy() for f in io}
+    tdt = torch.float32 if bits == 32 else torch.float64
+    st = {f: torch.empty((N, 3, 3) if f == "basis" else (N, 3), dtype=tdt, pin_memory=True).numpy() for f in io}
     g.state(fields=io, out=st)
     g.set_state(st)                      # one untimed pass through the host path
     g.set_state(snapshot[0])
@@ -348,7 +351,7 @@ def run_ours(args, rank, world, device):
         g.step(1, mode)
         g.state(fields=io, out=st)
         e2e_times.append(time.perf_counter() - t0)
-    io_bytes = N * 18 * 8   # float64 poses and velocities through the C ABI, each way
+    io_bytes = N * 18 * (4 if bits == 32 else 8)   # poses and velocities through the C ABI, each way
     per_scene = per_scene_gpu(pg, scene, offs, g.state(fields=("origin", "basis", "lin_vel", "ang_vel")), bits, mode,
                               device, args.steps) if offs is not None and not args.no_per_scene else None
     res = dict(dev_ms=dev_ms, per_step=per_step, lat=lat, N=N, launches=launches, counts=counts, cfg=cfg, bits=bits,

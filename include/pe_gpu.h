@@ -173,6 +173,13 @@ int pe_gpu_get_state(pe_gpu_world* w, double* origin, double* basis, double* lin
 int pe_gpu_set_state(pe_gpu_world* w, const double* origin, const double* basis, const double* lin_vel,
                      const double* ang_vel, const double* aabb_min, const double* aabb_max,
                      const double* world_inv_inertia);
+/* The same with float arrays: the state as the reference's default build holds it (pe::Real is
+ * float unless PE_USE_DOUBLE, src/rigid/phys_general.h:79-83), half the bytes of the double calls. */
+int pe_gpu_get_state_f32(pe_gpu_world* w, float* origin, float* basis, float* lin_vel, float* ang_vel, float* aabb_min,
+                         float* aabb_max, float* world_inv_inertia);
+int pe_gpu_set_state_f32(pe_gpu_world* w, const float* origin, const float* basis, const float* lin_vel,
+                         const float* ang_vel, const float* aabb_min, const float* aabb_max,
+                         const float* world_inv_inertia);
 /* sweep axis of each scene (BroadPhaseSweepAndPrune::_target_axis) */
 int pe_gpu_get_axes(pe_gpu_world* w, int* axes);
 int pe_gpu_set_axes(pe_gpu_world* w, const int* axes);

@@ -174,6 +174,13 @@ int pe_gpu_set_state(pe_gpu_world* h, const double* o, const double* b, const do
                      const double* mx, const double* iw) {
     return guard(h, [&](pe::WorldBase& W) { W.set_state(o, b, v, w, mn, mx, iw); return PE_GPU_OK; });
 }
+int pe_gpu_get_state_f32(pe_gpu_world* h, float* o, float* b, float* v, float* w, float* mn, float* mx, float* iw) {
+    return guard(h, [&](pe::WorldBase& W) { W.get_state(o, b, v, w, mn, mx, iw); return PE_GPU_OK; });
+}
+int pe_gpu_set_state_f32(pe_gpu_world* h, const float* o, const float* b, const float* v, const float* w, const float* mn,
+                         const float* mx, const float* iw) {
+    return guard(h, [&](pe::WorldBase& W) { W.set_state(o, b, v, w, mn, mx, iw); return PE_GPU_OK; });
+}
 int pe_gpu_get_axes(pe_gpu_world* h, int* a) {
     if (!a) return PE_GPU_ERR_ARG;
     return guard(h, [&](pe::WorldBase& w) { w.get_axes(a); return PE_GPU_OK; });

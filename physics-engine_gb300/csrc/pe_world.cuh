@@ -89,6 +89,10 @@ public:
     virtual void get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) = 0;
     virtual void set_state(const double* o, const double* b, const double* v, const double* w, const double* mn,
                            const double* mx, const double* iw) = 0;
+    // the same in single precision (pe::Real of the reference's default build)
+    virtual void get_state(float* o, float* b, float* v, float* w, float* mn, float* mx, float* iw) = 0;
+    virtual void set_state(const float* o, const float* b, const float* v, const float* w, const float* mn,
+                           const float* mx, const float* iw) = 0;
     virtual void get_axes(int* a) = 0;
     virtual void set_axes(const int* a) = 0;
     virtual int n_pairs() const = 0;
@@ -137,9 +141,20 @@ public:
     void narrowphase() override;
     void solve(int mode) override;
     int n_bodies() const override { return N_; }
-    void get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) override;
+    void get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) override {
+        get_state_t(o, b, v, w, mn, mx, iw);
+    }
     void set_state(const double* o, const double* b, const double* v, const double* w, const double* mn, const double* mx,
-                   const double* iw) override;
+                   const double* iw) override {
+        set_state_t(o, b, v, w, mn, mx, iw);
+    }
+    void get_state(float* o, float* b, float* v, float* w, float* mn, float* mx, float* iw) override { get_state_t(o, b, v, w, mn, mx, iw); }
+    void set_state(const float* o, const float* b, const float* v, const float* w, const float* mn, const float* mx,
+                   const float* iw) override {
+        set_state_t(o, b, v, w, mn, mx, iw);
+    }
+    template <class T> void get_state_t(T* o, T* b, T* v, T* w, T* mn, T* mx, T* iw);
+    template <class T> void set_state_t(const T* o, const T* b, const T* v, const T* w, const T* mn, const T* mx, const T* iw);
     void get_axes(int* a) override;
     void set_axes(const int* a) override;
     int n_pairs() const override { return P_; }

@@ -21,9 +21,9 @@ template <class R> R* World<R>::staging(size_t n) {
     return stage_;
 }
 
-template <class R>
-void World<R>::get_state(double* o, double* b, double* v, double* w, double* mn, double* mx, double* iw) {
-    double* dst[7] = {o, b, v, w, mn, mx, iw};
+template <class R> template <class T>
+void World<R>::get_state_t(T* o, T* b, T* v, T* w, T* mn, T* mx, T* iw) {
+    T* dst[7] = {o, b, v, w, mn, mx, iw};
     const int k0[7] = {OX, B00, VX, WX, MNX, MXX, I00}, nk[7] = {3, 9, 3, 3, 3, 3, 9};
     XferGroups G{};
     size_t tot = 0;
@@ -36,17 +36,17 @@ void World<R>::get_state(double* o, double* b, double* v, double* w, double* mn,
         G.n++;
     }
     if (!N_ || !G.n) return;
-    xfer_.ensure(tot);
-    launch(K_MISC, grid(N_), k_state_pack<R>, bodies(), G, xfer_.p);
+    xfer_.ensure((tot * sizeof(T) + sizeof(double) - 1) / sizeof(double));
+    T* x = reinterpret_cast<T*>(xfer_.p);
+    launch(K_MISC, grid(N_), k_state_pack<R, T>, bodies(), G, x);
     for (int q = 0; q < G.n; q++)
-        PE_CK(cudaMemcpyAsync(dst[map[q]], xfer_.p + G.off[q], (size_t)G.nk[q] * N_ * sizeof(double), cudaMemcpyDeviceToHost, st_));
+        PE_CK(cudaMemcpyAsync(dst[map[q]], x + G.off[q], (size_t)G.nk[q] * N_ * sizeof(T), cudaMemcpyDeviceToHost, st_));
     PE_CK(cudaStreamSynchronize(st_));
 }
 
-template <class R>
-void World<R>::set_state(const double* o, const double* b, const double* v, const double* w, const double* mn, const double* mx,
-                         const double* iw) {
-    const double* src[7] = {o, b, v, w, mn, mx, iw};
+template <class R> template <class T>
+void World<R>::set_state_t(const T* o, const T* b, const T* v, const T* w, const T* mn, const T* mx, const T* iw) {
+    const T* src[7] = {o, b, v, w, mn, mx, iw};
     const int k0[7] = {OX, B00, VX, WX, MNX, MXX, I00}, nk[7] = {3, 9, 3, 3, 3, 3, 9};
     XferGroups G{};
     size_t tot = 0;
@@ -59,12 +59,13 @@ void World<R>::set_state(const double* o, const double* b, const double* v, cons
         G.n++;
     }
     if (!N_ || !G.n) return;
-    xfer_.ensure(tot);
+    xfer_.ensure((tot * sizeof(T) + sizeof(double) - 1) / sizeof(double));
+    T* x = reinterpret_cast<T*>(xfer_.p);
     for (int g = 0; g < 7; g++)
         if (src[g])
-            PE_CK(cudaMemcpyAsync(xfer_.p + G.off[at[g]], src[g], (size_t)nk[g] * N_ * sizeof(double), cudaMemcpyHostToDevice, st_));
+            PE_CK(cudaMemcpyAsync(x + G.off[at[g]], src[g], (size_t)nk[g] * N_ * sizeof(T), cudaMemcpyHostToDevice, st_));
     const bool scale = mn && mx && o;   // the injected box's AABB scale
-    launch(K_MISC, grid(N_), k_state_unpack<R>, bodies(), G, (const double*)xfer_.p, scale ? at[0] : -1, scale ? at[4] : -1,
+    launch(K_MISC, grid(N_), k_state_unpack<R, T>, bodies(), G, (const T*)x, scale ? at[0] : -1, scale ? at[4] : -1,
            scale ? at[5] : -1);
     PE_CK(cudaStreamSynchronize(st_));
 }

@@ -69,6 +69,8 @@ def load(build_if_missing: bool = True):
         "pe_gpu_sync": (I, [P]),
         "pe_gpu_set_profiling": (I, [P, I]),
         "pe_gpu_set_step_graphs": (I, [P, I]),
+        "pe_gpu_get_state_f32": (I, [P] + [P] * 7),
+        "pe_gpu_set_state_f32": (I, [P] + [P] * 7),
         "pe_gpu_kernel_count": (I, []),
         "pe_gpu_kernel_name": (C.c_char_p, [I]),
         "pe_gpu_kernel_stats": (I, [P, dp, np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]),
@@ -237,39 +239,50 @@ class GpuWorld:
     STATE_FIELDS = (("origin", 3), ("basis", 9), ("lin_vel", 3), ("ang_vel", 3), ("aabb_min", 3), ("aabb_max", 3),
                     ("world_inv_inertia", 9))
 
-    def state(self, fields=None, out=None):
-        """Body state as float64 arrays; ``fields`` limits the transfer to the named fields.  With
-        ``out`` (a dict of C-contiguous float64 arrays of the fields' shapes, e.g. page-locked host
-        memory reused across steps) the fields are written there and ``out`` is returned."""
+    def state(self, fields=None, out=None, dtype=np.float64):
+        """Body state as arrays of ``dtype`` (float64, or float32: the reference's default pe::Real);
+        ``fields`` limits the transfer to the named fields.  With ``out`` (a dict of C-contiguous
+        arrays of the fields' shapes and one dtype, e.g. page-locked host memory reused across steps)
+        the fields are written there and ``out`` is returned."""
         N = self.n
         dst, out, ptrs = out, {}, []
+        if dst is not None and dst:
+            dtype = next(iter(dst.values())).dtype
+        dtype = np.dtype(dtype)
+        if dtype not in (np.dtype(np.float64), np.dtype(np.float32)):
+            raise ValueError("state: dtype must be float64 or float32")
         for name, k in self.STATE_FIELDS:
             if fields is None or name in fields:
                 shape = (N, 3, 3) if k == 9 else (N, 3)
                 if dst is not None:
                     a = dst[name]
-                    if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
-                        raise ValueError(f"state: out[{name!r}] must be C-contiguous float64 of shape {shape}")
+                    if a.shape != shape or a.dtype != dtype or not a.flags.c_contiguous:
+                        raise ValueError(f"state: out[{name!r}] must be C-contiguous {dtype} of shape {shape}")
                 else:
-                    a = np.zeros(shape)
+                    a = np.zeros(shape, dtype)
                 out[name] = a
                 ptrs.append(a.ctypes.data_as(C.c_void_p))
             else:
                 ptrs.append(None)
-        self._ck(self.lib.pe_gpu_get_state(self.h, *ptrs))
+        fn = self.lib.pe_gpu_get_state if dtype == np.float64 else self.lib.pe_gpu_get_state_f32
+        self._ck(fn(self.h, *ptrs))
         return dst if dst is not None else out
 
     def set_state(self, d):
-        """Overwrite the given body-state fields (missing keys are left untouched)."""
+        """Overwrite the given body-state fields (missing keys are left untouched).  All-float32
+        arrays go through the single-precision entry point, anything else as float64."""
+        given = [d[name] for name, _ in self.STATE_FIELDS if name in d and d[name] is not None]
+        f32 = bool(given) and all(isinstance(a, np.ndarray) and a.dtype == np.float32 for a in given)
         keep, ptrs = [], []
         for name, k in self.STATE_FIELDS:
             if name in d and d[name] is not None:
-                a = _f64(d[name]).reshape(-1)
+                a = np.ascontiguousarray(d[name], np.float32).reshape(-1) if f32 else _f64(d[name]).reshape(-1)
                 keep.append(a)
                 ptrs.append(a.ctypes.data_as(C.c_void_p))
             else:
                 ptrs.append(None)
-        self._ck(self.lib.pe_gpu_set_state(self.h, *ptrs))
+        fn = self.lib.pe_gpu_set_state_f32 if f32 else self.lib.pe_gpu_set_state
+        self._ck(fn(self.h, *ptrs))
 
     def axes(self, n_scenes=1):
         out = np.zeros(n_scenes, np.int32)

@@ -461,3 +461,29 @@ def test_gpu_colored_tower_stays_physical():
     r = g.results()
     depth = [r["slots"][i, :n, 12].min() for i, n in enumerate(r["point_size"]) if n]
     assert min(depth) > -0.05
+
+
+def test_gpu_state_single_precision_transfers():
+    """The float32 entry points (pe_gpu_get_state_f32 / pe_gpu_set_state_f32, the reference's default
+    pe::Real) carry an FP32 world's state exactly: a float32 read equals the float64 read, and
+    writing it back through the float32 path and stepping gives the same bits as the float64 path."""
+    scene = sc.pile(200, seed=6, real_bits=32)
+    a = pg.GpuWorld(scene, 32)
+    b = pg.GpuWorld(scene, 32)
+    for w in (a, b):
+        w.step(15, pg.COLORED)
+    io = ("origin", "basis", "lin_vel", "ang_vel")
+    s64 = a.state(fields=io)
+    s32 = a.state(fields=io, dtype=np.float32)
+    for f in io:
+        assert s32[f].dtype == np.float32
+        np.testing.assert_array_equal(s32[f].astype(np.float64), s64[f])
+    a.set_state(s32)
+    b.set_state(s64)
+    for w in (a, b):
+        w.step(10, pg.COLORED)
+    ra, rb = a.state(fields=io), b.state(fields=io)
+    for f in io:
+        np.testing.assert_array_equal(ra[f], rb[f])
+    with pytest.raises(ValueError):
+        a.state(fields=("origin",), dtype=np.int32)
