@@ -26,7 +26,7 @@ TABLE_DIR = Path(__file__).resolve().parent / "tuning"
 
 # candidate values per setting, tried in this order (defaults included)
 CANDIDATES = {
-    "sat_heavy_cost": [50000, 100000, 200000, 400000, 1000000],
+    "sat_heavy_cost": [50000, 100000, 200000, 400000, 1000000, 2000000, 4000000],
     "side_streams": [1, 2, 4],
     "small_island_items": [2, 4, 8, 16, 32],
     "color_block": [32, 64, 128, 256],
