@@ -310,6 +310,8 @@ private:
     int stream_of_[PC_COUNT] = {};
     void plan_streams(int* plan) const;
     int bp_count();                 // integrate's successor up to the pair count (waits for it)
+    void bp_count_enqueue();        // its launches, ending with the count's copy to the host
+    void run_head();                // integrate and bp_count_enqueue, replayed from a CUDA graph when enabled
     void prepare_tail(int P);       // every capacity the rest of the step needs, before any launch of it
     void bp_tail();                 // pair list, scene pair offsets, sweep axes
     void np_enqueue();              // narrowphase, no host waits
@@ -352,6 +354,11 @@ private:
     cudaGraphExec_t gexec_[2][2] = {};
     GraphSig gsig_[2][2];
     GraphSig last_sig_;     // the previous step's (a capture waits for one repeat)
+    cudaGraphExec_t ghead_ = nullptr;   // the head's graph (integrate and the broadphase up to the pair count)
+    GraphSig gsig_head_, last_sig_head_;
+    long long glaunch_head_ = 0;
+    template <class F>
+    void graph_run(cudaGraphExec_t& ex, GraphSig& held, long long& held_launches, GraphSig& last, const GraphSig& sig, F&& enqueue);
     long long glaunch_[2][2] = {};
     bool graphs_ = true, capturing_ = false;
     long long steps_since_plan_ = 0;

@@ -27,6 +27,8 @@ template <class R> World<R>::World(int device) : dev_(device) {
     PE_CK(cudaMemset(dcnt_.p, 0, DC_COUNT * sizeof(int)));
     std::memset(gsig_, 0, sizeof gsig_);
     std::memset(&last_sig_, 0xff, sizeof last_sig_);
+    std::memset(&gsig_head_, 0, sizeof gsig_head_);
+    std::memset(&last_sig_head_, 0xff, sizeof last_sig_head_);
     dstat_.ensure(HS_COUNT);
     PE_CK(cudaMallocHost(&hstat_, HS_COUNT * sizeof(int)));
     std::memset(hstat_, 0, HS_COUNT * sizeof(int));
@@ -38,6 +40,7 @@ template <class R> World<R>::~World() {
     if (stage_) cudaFreeHost(stage_);
     if (hstat_) cudaFreeHost(hstat_);
     for (auto& m : gexec_) for (auto& g : m) if (g) cudaGraphExecDestroy(g);
+    if (ghead_) cudaGraphExecDestroy(ghead_);
     for (auto& q : pending_) { cudaEventDestroy(q.e0); cudaEventDestroy(q.e1); }
     for (auto e : ev_pool_) cudaEventDestroy(e);
     for (auto& e : ev_) { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }

@@ -113,8 +113,16 @@ template <class R> void World<R>::integrate() {
 // Broadphase up to the pair count: sort, sweep counts, scan; the host waits for the count (the
 // pair capacity follows it).  The count also stays on the device for the kernels after it.
 template <class R> int World<R>::bp_count() {
+    if (N_ < 2) return P_;   // the reference leaves the pair list untouched below two bodies
+    bp_count_enqueue();
+    PE_CK(cudaStreamSynchronize(st_));
+    return hstat_[HS_P];
+}
+
+// the launches of bp_count, ending with the count's copy into page-locked memory (no wait)
+template <class R> void World<R>::bp_count_enqueue() {
     const int n = N_;
-    if (n < 2) return P_;   // the reference leaves the pair list untouched below two bodies
+    if (n < 2) return;
     for (int k = 0; k < 2; k++) { key_[k].ensure(n); key2_[k].ensure(n); val_[k].ensure(n); }
     smn_.ensure((size_t)3 * n); smx_.ensure((size_t)3 * n); sflag_.ensure(n); ssc_.ensure(n);
     count_.ensure(n + 1);
@@ -156,8 +164,6 @@ template <class R> int World<R>::bp_count() {
     aux_.ensure((n + 1 + 1023) / 1024 + 1);
     scan_async(count_.p, n + 1, dcnt_.p + DC_P);
     PE_CK(cudaMemcpyAsync(hstat_ + HS_P, dcnt_.p + DC_P, sizeof(int), cudaMemcpyDeviceToHost, st_));
-    PE_CK(cudaStreamSynchronize(st_));
-    return hstat_[HS_P];
 }
 
 // Every buffer the rest of the step writes, sized for P pairs before any of its launches, so that
@@ -534,36 +540,15 @@ template <class R> void World<R>::graph_sig(GraphSig& g) const {
     std::memcpy(&g.tun, &tun_, sizeof tun_);
 }
 
-// The step's device part after the pair count (pair list, narrowphase, solver): launched directly,
-// or captured once as a CUDA graph per solver mode and contact-distance generation and replayed
-// while nothing it holds fixed has changed.  The side-stream plan follows the last step's class
-// counts; it is revised every 64 steps (a changed plan is a new capture).
-template <class R> void World<R>::run_tail(int mode) {
-    auto enqueue = [&]() {
-        bp_tail();
-        ev_end(1);
-        ev_begin(2); np_enqueue(); ev_end(2);
-        ev_begin(3); solve_enqueue(mode); ev_end(3);
-        ev_end(4);
-    };
-    bool counted = false;
-    for (int c = 0; c < PC_COUNT; c++) counted |= h_cls_[c] > 0;
-    if (!graphs_ || prof_ || !counted) {   // no graph (or no class counts yet for the plan)
-        plan_streams(stream_of_);
-        enqueue();
-        return;
-    }
-    const int m = mode ? 1 : 0, d = cur_dist_;
-    cudaGraphExec_t& ex = gexec_[m][d];
-    if (!ex || ++steps_since_plan_ >= 64) {
-        steps_since_plan_ = 0;
-        plan_streams(stream_of_);
-    }
-    GraphSig sig;
-    graph_sig(sig);
-    const bool same_as_last = std::memcmp(&sig, &last_sig_, sizeof sig) == 0;
-    std::memcpy(&last_sig_, &sig, sizeof sig);
-    if (!ex || std::memcmp(&sig, &gsig_[m][d], sizeof sig) != 0) {
+// Replays `ex` if its signature `held` matches `sig`, else captures `enqueue` into it (updating the
+// executable graph in place when the topology allows) once a step repeats its predecessor's
+// signature `last`; until then `enqueue` launches directly.  Keeps the step's launch count.
+template <class R>
+template <class F>
+void World<R>::graph_run(cudaGraphExec_t& ex, GraphSig& held, long long& held_launches, GraphSig& last, const GraphSig& sig, F&& enqueue) {
+    const bool same_as_last = std::memcmp(&sig, &last, sizeof sig) == 0;
+    std::memcpy(&last, &sig, sizeof sig);
+    if (!ex || std::memcmp(&sig, &held, sizeof sig) != 0) {
         // a world that changes every step (a serving loop admitting and retiring scenes) would pay
         // a capture per step: capture only once the step has repeated its predecessor's settings
         if (!same_as_last) { enqueue(); return; }
@@ -595,21 +580,64 @@ template <class R> void World<R>::run_tail(int mode) {
         if (!ex) e = cudaGraphInstantiate(&ex, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) { ex = nullptr; PE_CK(e); }
-        std::memcpy(&gsig_[m][d], &sig, sizeof sig);
-        glaunch_[m][d] = step_launches_ - before;
+        std::memcpy(&held, &sig, sizeof sig);
+        held_launches = step_launches_ - before;
         step_launches_ = before;
     }
     PE_CK(cudaGraphLaunch(ex, st_));
-    step_launches_ += glaunch_[m][d];
+    step_launches_ += held_launches;
+}
+
+// The step's head (integration and the broadphase up to the pair count's copy to the host) as one
+// CUDA graph; the host then waits for the count.
+template <class R> void World<R>::run_head() {
+    auto enqueue = [&]() {
+        ev_begin(4);
+        ev_begin(0); integrate(); ev_end(0);
+        ev_begin(1);
+        bp_count_enqueue();
+    };
+    if (!graphs_ || prof_) { enqueue(); return; }
+    GraphSig sig;
+    graph_sig(sig);
+    graph_run(ghead_, gsig_head_, glaunch_head_, last_sig_head_, sig, enqueue);
+}
+
+// The step's device part after the pair count (pair list, narrowphase, solver): launched directly,
+// or captured once as a CUDA graph per solver mode and contact-distance generation and replayed
+// while nothing it holds fixed has changed.  The side-stream plan follows the last step's class
+// counts; it is revised every 64 steps (a changed plan is a new capture).
+template <class R> void World<R>::run_tail(int mode) {
+    auto enqueue = [&]() {
+        bp_tail();
+        ev_end(1);
+        ev_begin(2); np_enqueue(); ev_end(2);
+        ev_begin(3); solve_enqueue(mode); ev_end(3);
+        ev_end(4);
+    };
+    bool counted = false;
+    for (int c = 0; c < PC_COUNT; c++) counted |= h_cls_[c] > 0;
+    if (!graphs_ || prof_ || !counted) {   // no graph (or no class counts yet for the plan)
+        plan_streams(stream_of_);
+        enqueue();
+        return;
+    }
+    const int m = mode ? 1 : 0, d = cur_dist_;
+    if (!gexec_[m][d] || ++steps_since_plan_ >= 64) {
+        steps_since_plan_ = 0;
+        plan_streams(stream_of_);
+    }
+    GraphSig sig;
+    graph_sig(sig);
+    graph_run(gexec_[m][d], gsig_[m][d], glaunch_[m][d], last_sig_, sig, enqueue);
 }
 
 template <class R> void World<R>::step(int n, int mode) {
     for (int s = 0; s < n; s++) {
         step_launches_ = 0;
-        ev_begin(4);
-        ev_begin(0); integrate(); ev_end(0);
-        ev_begin(1);
-        const int P = bp_count();   // the first host wait
+        run_head();
+        PE_CK(cudaStreamSynchronize(st_));   // the first host wait: the pair count
+        const int P = N_ < 2 ? P_ : hstat_[HS_P];
         prepare_tail(P);
         P_ = P;
         cur_dist_ ^= 1;
