@@ -286,7 +286,6 @@ private:
                    const double* o, const double* b, const double* v, const double* w) const;
     Results<R> results();
     Rows<R> rows();
-    int scan(int* data, int n);   // exclusive scan in place; returns the total (synchronises)
     void scan_async(int* data, int n, int* total);   // exclusive scan in place, total to device memory
     DBuf<int> rows_total_;
 

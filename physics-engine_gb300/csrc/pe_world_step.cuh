@@ -18,22 +18,6 @@ template <class R> void World<R>::scan_async(int* data, int n, int* total) {
     }
 }
 
-template <class R> int World<R>::scan(int* data, int n) {
-    const int tiles = (n + 1023) / 1024;
-    if (tiles <= kSmallScanTiles) {   // small: one block scans in place (one launch instead of three)
-        launch(K_SCAN, 1, k_scan_aux, data, n, total_.p);
-    } else {
-        aux_.ensure(tiles + 1);
-        launch(K_SCAN, tiles, k_scan_tiles, data, n, aux_.p);
-        launch(K_SCAN, 1, k_scan_aux, aux_.p, tiles, total_.p);
-        launch(K_SCAN, tiles, k_scan_add, data, n, aux_.p);
-    }
-    int tot = 0;
-    PE_CK(cudaMemcpyAsync(&tot, total_.p, sizeof(int), cudaMemcpyDeviceToHost, st_));
-    PE_CK(cudaStreamSynchronize(st_));
-    return tot;
-}
-
 template <class R> void World<R>::radix_sort(int n, int scene_passes) {
     order_ = val_[radix_sort_keys(n, (int)sizeof(R), scene_passes)].p;
 }
