@@ -543,6 +543,22 @@ def cpu_baseline(scene, bits, offs=None, preroll=0, budget_s=20.0, sample=32, st
     return cpu_scenes_wall(scene, bits, offs, preroll, steps)
 
 
+# ------------------------------------------------------------------ replicas (one process per GPU)
+def max_over_ranks(x, dist, device=None):
+    """The largest value of x over the ranks: the timed region of N replicas ends with the slowest
+    (a CUDA tensor under NCCL, a host tensor under gloo)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(bodies_per_replica, steps, world, dev_ms):
+    """Whole-job body-steps/s of `world` replicas, each stepping its own copy of the workload: every
+    rank's bodies over the slowest rank's time (weak scaling)."""
+    return bodies_per_replica * steps * world / (dev_ms * 1e-3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -618,15 +634,12 @@ def main():
         return 0
     dev_ms = res["dev_ms"]
     if dist is not None:
-        import torch
-        t = torch.tensor([dev_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
+        dev_ms = max_over_ranks(dev_ms, dist, device=f"cuda:{local}")
         dist.barrier()
     if rank != 0:
         return 0
     per = sorted(res["per_step"] + res["lat"])
-    value = res["N"] * args.steps * world / (dev_ms * 1e-3)
+    value = replica_value(res["N"], args.steps, world, dev_ms)
     cfg = dict(res["cfg"], l2="flushed between timed steps (256 MiB memset)", pairs_last_step=res["counts"]["pairs"],
                contact_points_last_step=res["counts"]["rows"], colors_last_step=res["counts"]["colors"],
                p50_step_ms=per[len(per) // 2], p99_step_ms=per[min(len(per) - 1, int(0.99 * len(per)))],
