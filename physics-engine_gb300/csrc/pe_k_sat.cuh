@@ -243,8 +243,8 @@ template <class R, int G> __device__ __forceinline__ V3<R> group_bcast3(const V3
 // the queue length
 template <class R> constexpr int sat_scratch_reals(int G) { return G == 1 ? 0 : 2 * G + 4; }
 // candidate axes per thread of one pruning pass, and the queue of surviving axis indices after the
-// scratch area
-constexpr int kSatQ = 8;
+// scratch area (16: the batched step 0.27 ms faster than with 8, 4 slower)
+constexpr int kSatQ = 16;
 template <class R> constexpr int sat_queue_reals(int G) { return (kSatQ * 32 * G * (int)sizeof(int) + (int)sizeof(R) - 1) / (int)sizeof(R); }
 
 // Pruning bound of one shape along a world axis: lo <= the computed maximum of its projection
