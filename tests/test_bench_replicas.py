@@ -54,3 +54,11 @@ def test_replica_value_counts_every_rank():
     one = bench.replica_value(501361, 20, 1, 200.0)
     assert one == pytest.approx(501361 * 20 / 0.2)
     assert bench.replica_value(501361, 20, 4, 200.0) == pytest.approx(4 * one)
+
+
+def test_roofline_traffic_reads_the_committed_launch_list():
+    # roofline.traffic and phases_dram_bytes_ncu come from the committed ncu summary of one batched step
+    for phase in ("integrate", "broadphase", "narrowphase", "solver"):
+        v = bench.ncu_traffic(phase)
+        assert v is not None and v > 0, phase
+    assert bench.ncu_traffic("narrowphase") > bench.ncu_traffic("solver") > bench.ncu_traffic("integrate")
